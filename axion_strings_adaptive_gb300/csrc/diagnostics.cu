@@ -1,0 +1,443 @@
+// Fused diagnostics pass: plaquette windings + pierced list (string finder),
+// the 14 screened/unscreened energy sums, and gamma^2 v^2 at pierced corners,
+// in one sweep over the valid cells.
+//
+// Reference: StringFinder.hpp:45-122, PlaquetteWinding.hpp:24-51,
+// EnergyKernel.hpp:106-233, Energy.hpp:64-190, Masking.hpp:75-93,
+// VelocityKernel.hpp:37-141, Velocity.hpp:62-78.
+//
+// Windings follow the reference literally: double atan2 of the (double-cast)
+// field at each corner, fmod fold into (-pi, pi], lround of the sum / 2 pi.
+// Edges whose |dtheta| lies within 1e-12 of pi are counted as "near ties":
+// only there could a different correctly-rounded-to-1-ulp atan2 flip a fold.
+// All per-cell energy/velocity arithmetic is FP64 whatever the field
+// precision; sums go per thread -> warp shuffle -> block -> per-block partial
+// in scratch -> a single-block finalize in a fixed order (deterministic, no
+// floating-point atomics).
+#include <cmath>
+
+#include "axs_internal.cuh"
+
+namespace axs {
+
+struct DiagView {
+    const void *data;
+    int32_t dtype;
+    int nx, ny, nz;
+    int ox, oy, oz;          // offset of valid cell (0,0,0) in elements along each axis
+    int wx, wy, wz;          // 1: wrap indices periodically on that axis; 0: read ghosts
+    int64_t js, ks, cs;
+};
+
+struct DiagPartial {
+    double e[14];
+    double vsum;
+    long long cnt[4];  // n_p_plain, n_p_weighted, vel_count, near_tie
+    double pad;
+};
+static_assert(sizeof(DiagPartial) == 160, "partial layout");
+
+constexpr int kDiagThreads = 256;
+
+struct DiagConst {
+    double one_over_dx, R, lambda, RpR, m_r, threshold;
+    int scheme;
+    int want_energy, want_plaq, want_vel;
+};
+
+template <typename T>
+__device__ __forceinline__ double ld(const DiagView &v, int c, int i, int j, int k)
+{
+    if (v.wx) i = (i % v.nx + v.nx) % v.nx;
+    if (v.wy) j = (j % v.ny + v.ny) % v.ny;
+    if (v.wz) k = (k % v.nz + v.nz) % v.nz;
+    const T *p = static_cast<const T *>(v.data);
+    return (double)__ldg(p + c * v.cs + (int64_t)(i + v.ox) + (int64_t)(j + v.oy) * v.js + (int64_t)(k + v.oz) * v.ks);
+}
+
+// GRTeclyn diff1 (centred 4th order, weights 1/12 and 2/3, times 1/dx),
+// rounded to the field precision as d1_scalar returns amrex::Real.
+template <typename T>
+__device__ __forceinline__ double diff1(const DiagView &v, int c, int i, int j, int k, int dir, double inv_dx)
+{
+    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
+    const double wf = 8.33333333333333333333e-2, wn = 6.66666666666666666667e-1;
+    const double r = (wf * ld<T>(v, c, i - 2 * di, j - 2 * dj, k - 2 * dk) - wn * ld<T>(v, c, i - di, j - dj, k - dk) +
+                      wn * ld<T>(v, c, i + di, j + dj, k + dk) - wf * ld<T>(v, c, i + 2 * di, j + 2 * dj, k + 2 * dk)) *
+                     inv_dx;
+    return (double)(T)r;
+}
+
+__device__ __forceinline__ double wrap_diff(double d, int &near_tie)
+{
+    const double pi = 3.14159265358979323846;
+    const double two_pi = 2.0 * pi;
+    if (fabs(fabs(d) - pi) < 1e-12) near_tie = 1;
+    d = fmod(d, two_pi);
+    if (d <= -pi)
+        d = __dadd_rn(d, two_pi);
+    else if (d > pi)
+        d = __dsub_rn(d, two_pi);
+    return d;
+}
+
+__device__ __forceinline__ int winding4(double t1, double t2, double t3, double t4, int &ties)
+{
+    int n1 = 0, n2 = 0, n3 = 0, n4 = 0;
+    const double a = wrap_diff(__dsub_rn(t2, t1), n1);
+    const double b = wrap_diff(__dsub_rn(t3, t2), n2);
+    const double c = wrap_diff(__dsub_rn(t4, t3), n3);
+    const double d = wrap_diff(__dsub_rn(t1, t4), n4);
+    ties += n1 + n2 + n3 + n4;
+    const double total = __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d);
+    return (int)llround(__ddiv_rn(total, 2.0 * 3.14159265358979323846));
+}
+
+template <typename T>
+__device__ __forceinline__ double phase(const DiagView &v, int i, int j, int k)
+{
+    return atan2(ld<T>(v, 1, i, j, k), ld<T>(v, 0, i, j, k));
+}
+
+// gamma^2 v^2 at one vertex (VelocityKernel.hpp:525-539 + Velocity.hpp:62-78)
+template <typename T>
+__device__ __forceinline__ double gvv(const DiagView &v, const DiagConst &q, int i, int j, int k)
+{
+    const double psi1 = ld<T>(v, 0, i, j, k), psi2 = ld<T>(v, 1, i, j, k);
+    const double Pi1 = ld<T>(v, 2, i, j, k), Pi2 = ld<T>(v, 3, i, j, k);
+    const double phi1 = psi1 / q.R, phi2 = psi2 / q.R;
+    const double pd1 = (Pi1 - q.RpR * psi1) / (q.R * q.R);
+    const double pd2 = (Pi2 - q.RpR * psi2) / (q.R * q.R);
+    const double c1 = 0.41222, e1 = -0.025763;
+    const double phi_sq = phi1 * phi1 + phi2 * phi2;
+    const double pd_sq = pd1 * pd1 + pd2 * pd2;
+    const double re = phi1 * pd1 + phi2 * pd2;
+    const double m2 = q.m_r * q.m_r, c1s = c1 * c1;
+    const double term1 = (pd_sq / (2.0 * m2 * c1s)) * (1.0 - e1 * phi_sq / (c1 * c1s));
+    const double term2 = (e1 / (4.0 * m2 * c1s * c1s * c1)) * re * re;
+    return term1 - term2;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kDiagThreads) diag_kernel(const DiagView v, const DiagConst q,
+                                                            const uint8_t *__restrict__ mask,
+                                                            DiagPartial *__restrict__ partials,
+                                                            unsigned long long *__restrict__ list_counter,
+                                                            long long *__restrict__ list, long long capacity)
+{
+    double e[14];
+#pragma unroll
+    for (int s = 0; s < 14; ++s) e[s] = 0.0;
+    double vsum = 0.0;
+    long long cnt[4] = {0, 0, 0, 0};
+
+    const int64_t ncell = (int64_t)v.nx * v.ny * v.nz;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // Every thread runs the same number of iterations so the block-wide list
+    // compaction below can synchronise.
+    const int64_t iters = (ncell + stride - 1) / stride;
+    __shared__ int warp_tot[kDiagThreads / 32];
+    __shared__ unsigned long long block_base;
+    for (int64_t it = 0; it < iters; ++it) {
+        const int64_t cell = it * stride + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        const bool in = cell < ncell && (mask == nullptr || mask[cell] != 0);
+        int w[3] = {0, 0, 0};
+        if (in) {
+            const int i = (int)(cell % v.nx), j = (int)((cell / v.nx) % v.ny), k = (int)(cell / ((int64_t)v.nx * v.ny));
+            if (q.want_energy) {
+                const double psi1 = ld<T>(v, 0, i, j, k), psi2 = ld<T>(v, 1, i, j, k);
+                const double Pi1 = ld<T>(v, 2, i, j, k), Pi2 = ld<T>(v, 3, i, j, k);
+                const double psi_sq = psi1 * psi1 + psi2 * psi2;
+                double g1sq = 0.0, g2sq = 0.0, gtsq = 0.0;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const double g1 = diff1<T>(v, 0, i, j, k, d, q.one_over_dx);
+                    const double g2 = diff1<T>(v, 1, i, j, k, d, q.one_over_dx);
+                    g1sq += (double)((T)g1 * (T)g1);
+                    g2sq += (double)((T)g2 * (T)g2);
+                    const double dth = (psi_sq > 0.0) ? (psi1 * g2 - psi2 * g1) / psi_sq : 0.0;
+                    gtsq += dth * dth;
+                }
+                const double R = q.R, R2 = R * R, R4 = R2 * R2;
+                const double c1 = Pi1 - q.RpR * psi1, c2 = Pi2 - q.RpR * psi2;
+                const double dsq = psi_sq - R2;
+                const double pot = 0.25 * q.lambda * dsq * dsq;
+                const double rho = (c1 * c1 + c2 * c2 + (g1sq + g2sq) + pot) / R4;
+                const double thp = (psi_sq > 0.0) ? (psi1 * Pi2 - Pi1 * psi2) / psi_sq : 0.0;
+                const double fa = 1.4142135623730951;
+                const double adot = fa * thp / R;
+                const double akin = 0.5 * adot * adot;
+                const double agrad = 0.5 * fa * fa * gtsq / R2;
+                double rkin = 0.0;
+                if (psi_sq > 0.0) {
+                    const double rd = (psi1 * c1 + psi2 * c2) / sqrt(psi_sq);
+                    rkin = rd * rd / R4;
+                }
+                const double rgrad = (g1sq + g2sq - psi_sq * gtsq) / R4;
+                const double rmass = pot / R4;
+                double wgt = 1.0;
+                if (q.scheme != AXS_MASK_NONE) {
+                    const double mod = sqrt(psi_sq) / R;
+                    if (q.scheme == AXS_MASK_B) {
+                        wgt = (mod >= q.threshold) ? 1.0 : 0.0;
+                    } else {
+                        const double f = 1.0 + (mod - 1.0) / fa;
+                        wgt = f * f;
+                    }
+                }
+                e[0] += rho;   e[1] += rho * wgt;
+                e[2] += akin;  e[3] += akin * wgt;
+                e[4] += agrad; e[5] += agrad * wgt;
+                e[6] += rkin;  e[7] += rkin * wgt;
+                e[8] += rgrad; e[9] += rgrad * wgt;
+                e[10] += rmass; e[11] += rmass * wgt;
+                e[12] += wgt;  e[13] += 1.0;
+            }
+            if (q.want_plaq || q.want_vel) {
+                const double th000 = phase<T>(v, i, j, k), th100 = phase<T>(v, i + 1, j, k);
+                const double th110 = phase<T>(v, i + 1, j + 1, k), th010 = phase<T>(v, i, j + 1, k);
+                const double th001 = phase<T>(v, i, j, k + 1), th101 = phase<T>(v, i + 1, j, k + 1);
+                const double th011 = phase<T>(v, i, j + 1, k + 1);
+                int ties = 0;
+                w[0] = winding4(th000, th100, th110, th010, ties);
+                w[1] = winding4(th000, th010, th011, th001, ties);
+                w[2] = winding4(th000, th001, th101, th100, ties);
+                cnt[0] += (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
+                cnt[1] += abs(w[0]) + abs(w[1]) + abs(w[2]);
+                cnt[3] += ties;
+                if (q.want_vel && (w[0] | w[1] | w[2])) {
+                    double s = 0.0;
+                    long long c = 0;
+                    if (w[0]) {
+                        s += gvv<T>(v, q, i, j, k) + gvv<T>(v, q, i + 1, j, k) + gvv<T>(v, q, i + 1, j + 1, k) +
+                             gvv<T>(v, q, i, j + 1, k);
+                        c += 4;
+                    }
+                    if (w[1]) {
+                        s += gvv<T>(v, q, i, j, k) + gvv<T>(v, q, i, j + 1, k) + gvv<T>(v, q, i, j + 1, k + 1) +
+                             gvv<T>(v, q, i, j, k + 1);
+                        c += 4;
+                    }
+                    if (w[2]) {
+                        s += gvv<T>(v, q, i, j, k) + gvv<T>(v, q, i, j, k + 1) + gvv<T>(v, q, i + 1, j, k + 1) +
+                             gvv<T>(v, q, i + 1, j, k);
+                        c += 4;
+                    }
+                    vsum += s;
+                    cnt[2] += c;
+                }
+            }
+        }
+        // ---- compaction of the pierced plaquettes of this iteration ----
+        if (q.want_plaq && list != nullptr) {
+            const int mine = (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            int incl = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) warp_tot[warp] = incl;
+            __syncthreads();
+            int warp_off = 0, block_tot = 0;
+            for (int ww = 0; ww < kDiagThreads / 32; ++ww) {
+                if (ww < warp) warp_off += warp_tot[ww];
+                block_tot += warp_tot[ww];
+            }
+            if (threadIdx.x == 0) block_base = block_tot ? atomicAdd(list_counter, (unsigned long long)block_tot) : 0ull;
+            __syncthreads();
+            if (mine) {
+                long long pos = (long long)block_base + warp_off + incl - mine;
+                const long long base_entry = 4LL * cell;
+                for (int pl = 0; pl < 3; ++pl) {
+                    if (w[pl]) {
+                        if (pos < capacity) list[pos] = base_entry + pl;
+                        ++pos;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+
+    // ---- block reduction (fixed order) ----
+    __shared__ double red_d[kDiagThreads / 32][15];
+    __shared__ long long red_l[kDiagThreads / 32][4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < 14; ++s) {
+        double x = e[s];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red_d[warp][s] = x;
+    }
+    {
+        double x = vsum;
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red_d[warp][14] = x;
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        long long x = cnt[s];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red_l[warp][s] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 15) {
+        double x = 0.0;
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) x += red_d[ww][threadIdx.x];
+        if (threadIdx.x < 14)
+            partials[blockIdx.x].e[threadIdx.x] = x;
+        else
+            partials[blockIdx.x].vsum = x;
+    } else if (threadIdx.x >= 32 && threadIdx.x < 36) {
+        long long x = 0;
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) x += red_l[ww][threadIdx.x - 32];
+        partials[blockIdx.x].cnt[threadIdx.x - 32] = x;
+    }
+}
+
+// Sum the per-block partials in a fixed pairwise order and write the result.
+__global__ void diag_finalize_kernel(const DiagPartial *__restrict__ partials, int nblocks,
+                                     const unsigned long long *__restrict__ list_counter, long long capacity,
+                                     int want_list, axs_diag_result *__restrict__ out)
+{
+    __shared__ double sd[256];
+    __shared__ long long sl[256];
+    const int t = threadIdx.x;
+    for (int f = 0; f < 19; ++f) {
+        double xd = 0.0;
+        long long xl = 0;
+        for (int b = t; b < nblocks; b += 256) {
+            if (f < 14)
+                xd += partials[b].e[f];
+            else if (f == 14)
+                xd += partials[b].vsum;
+            else
+                xl += partials[b].cnt[f - 15];
+        }
+        sd[t] = xd;
+        sl[t] = xl;
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (t < o) {
+                sd[t] += sd[t + o];
+                sl[t] += sl[t + o];
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            if (f < 14)
+                out->energy_sums[f] = sd[0];
+            else if (f == 14)
+                out->vel_sum = sd[0];
+            else if (f == 15)
+                out->n_p_plain = sl[0];
+            else if (f == 16)
+                out->n_p_weighted = sl[0];
+            else if (f == 17)
+                out->vel_count = sl[0];
+            else
+                out->n_near_tie = sl[0];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const long long listed = want_list ? (long long)*list_counter : 0;
+        out->n_listed = listed < capacity ? listed : capacity;
+        out->status = (want_list && listed > capacity) ? AXS_ERR_CAPACITY : AXS_OK;
+    }
+}
+
+static int diag_grid(int64_t ncell)
+{
+    const int sms = device_sm_count();
+    int64_t g = (ncell + kDiagThreads - 1) / kDiagThreads;
+    const int64_t cap = (int64_t)(sms > 0 ? sms : 148) * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+static int64_t diag_scratch_bytes(int64_t ncell) { return 256 + (int64_t)diag_grid(ncell) * sizeof(DiagPartial); }
+
+static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *mask, axs_diag_result *out,
+                    int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, cudaStream_t st)
+{
+    AXS_REQUIRE(p != nullptr && out != nullptr, AXS_ERR_INVALID_ARGUMENT, "null params or result");
+    AXS_REQUIRE(p->dx > 0.0 && p->R > 0.0 && p->m_r > 0.0, AXS_ERR_INVALID_ARGUMENT,
+                "dx, R and m_r must be positive");
+    AXS_REQUIRE(p->masking_scheme >= AXS_MASK_NONE && p->masking_scheme <= AXS_MASK_B, AXS_ERR_INVALID_ARGUMENT,
+                "bad masking scheme %d", p->masking_scheme);
+    AXS_REQUIRE(capacity >= 0, AXS_ERR_INVALID_ARGUMENT, "negative list capacity");
+    AXS_REQUIRE(capacity == 0 || list != nullptr, AXS_ERR_INVALID_ARGUMENT, "null list with positive capacity");
+    const int64_t ncell = (int64_t)v.nx * v.ny * v.nz;
+    const int64_t need = diag_scratch_bytes(ncell);
+    AXS_REQUIRE(scratch != nullptr && scratch_bytes >= need, AXS_ERR_WORKSPACE,
+                "diagnostics scratch too small (%lld < %lld bytes)", (long long)scratch_bytes, (long long)need);
+    AXS_REQUIRE(((uintptr_t)scratch % 16) == 0, AXS_ERR_ALIGNMENT, "scratch must be 16-byte aligned");
+    DiagConst q{};
+    q.one_over_dx = 1.0 / p->dx;
+    q.R = p->R;
+    q.lambda = p->lambda;
+    q.RpR = p->R_prime_over_R;
+    q.m_r = p->m_r;
+    q.threshold = p->masking_threshold;
+    q.scheme = p->masking_scheme;
+    q.want_energy = p->want_energy != 0;
+    q.want_plaq = p->want_plaquettes != 0;
+    q.want_vel = p->want_velocity != 0;
+    auto *counter = static_cast<unsigned long long *>(scratch);
+    auto *partials = reinterpret_cast<DiagPartial *>(static_cast<char *>(scratch) + 256);
+    AXS_CUDA_CHECK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+    const int grid = diag_grid(ncell);
+    long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
+    if (v.dtype == AXS_F64)
+        diag_kernel<double><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity);
+    else
+        diag_kernel<float><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity);
+    int rc = launch_status("diagnostics");
+    if (rc) return rc;
+    diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
+    return launch_status("diagnostics finalize");
+}
+
+}  // namespace axs
+
+using namespace axs;
+
+extern "C" {
+
+int axs_diagnostics_scratch_bytes(int32_t nx, int32_t ny, int32_t nz, int64_t *bytes)
+{
+    AXS_REQUIRE(bytes != nullptr, AXS_ERR_INVALID_ARGUMENT, "null output");
+    AXS_REQUIRE(nx > 0 && ny > 0 && nz > 0, AXS_ERR_INVALID_ARGUMENT, "empty box");
+    *bytes = diag_scratch_bytes((int64_t)nx * ny * nz);
+    return AXS_OK;
+}
+
+int axs_diagnostics(const axs_fab *state, const axs_diag_params *p, const uint8_t *mask, axs_diag_result *out,
+                    int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, void *stream)
+{
+    AXS_REQUIRE(p != nullptr, AXS_ERR_INVALID_ARGUMENT, "null params");
+    const int periodic = p->boundary == AXS_BOUNDARY_PERIODIC;
+    AXS_REQUIRE(p->boundary == AXS_BOUNDARY_GHOSTS || periodic, AXS_ERR_INVALID_ARGUMENT, "bad boundary mode");
+    const int need_ng = periodic ? 0 : (p->want_energy ? 2 : 1);
+    int rc = validate_fab(state, "state", 4, need_ng);
+    if (rc) return rc;
+    DiagView v{state->data, state->dtype, state->nx, state->ny, state->nz, state->ng, state->ng, state->ng,
+               periodic, periodic, periodic, state->jstride, state->kstride, state->cstride};
+    return run_diag(v, p, mask, out, list, capacity, scratch, scratch_bytes, (cudaStream_t)stream);
+}
+
+int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const uint8_t *mask, axs_diag_result *out,
+                          int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, void *stream)
+{
+    axs_level_layout L;
+    AXS_REQUIRE(lv != nullptr && lv->state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null level");
+    int rc = axs_level_layout_for(lv->dtype, lv->nx, lv->ny, lv->nz, &L);
+    if (rc) return rc;
+    DiagView v{lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, 4, 2, 0, 0, 0, 1, L.jstride, L.kstride, L.cstride};
+    return run_diag(v, p, mask, out, list, capacity, scratch, scratch_bytes, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,303 @@
+// Drop-in kernels on AMReX-layout FABs: the per-stage RHS that replaces the
+// body of AxionStringsLevel::specific_eval_rhs, the periodic ghost fill, the
+// RK stage combinations, and copies between FABs and the fused-RK4 level
+// layout.
+#include "axs_internal.cuh"
+
+namespace axs {
+
+// Offset of cell (i,j,k) of component 0 in a FAB (i etc. may be negative ghosts).
+__host__ __device__ __forceinline__ int64_t fab_off(const axs_fab &f, int i, int j, int k)
+{
+    return (int64_t)(i + f.ng) + (int64_t)(j + f.ng) * f.jstride + (int64_t)(k + f.ng) * f.kstride;
+}
+
+// ---------------------------------------------------------------- RHS
+// AxionStringsRHS<FourthOrderDerivatives>::operator() (AxionStringsRHS.impl.hpp:25-60).
+// FP64: evaluated with the reference's expression order and explicit
+// round-to-nearest intrinsics (no FMA contraction), so it reproduces the
+// host evaluation of the same expressions bit for bit. Laplacian weights are
+// GRTeclyn's centred 4th-order diff2 (1/12, 4/3, 5/2) * 1/dx^2.
+__device__ __forceinline__ double diff2_exact(const double *__restrict__ p, int64_t s, double one_over_dx2)
+{
+    const double wf = 8.33333333333333333333e-2;
+    const double wn = 1.33333333333333333333e+0;
+    const double wl = 2.50000000000000000000e+0;
+    double r = __dmul_rn(-wf, __ldg(p - 2 * s));
+    r = __dadd_rn(r, __dmul_rn(wn, __ldg(p - s)));
+    r = __dsub_rn(r, __dmul_rn(wl, __ldg(p)));
+    r = __dadd_rn(r, __dmul_rn(wn, __ldg(p + s)));
+    r = __dsub_rn(r, __dmul_rn(wf, __ldg(p + 2 * s)));
+    return __dmul_rn(r, one_over_dx2);
+}
+
+__global__ void eval_rhs_f64_kernel(const axs_fab s, const axs_fab r, double one_over_dx2, double kappa,
+                                    double lambda, double R2)
+{
+    const double *__restrict__ sp = static_cast<const double *>(s.data);
+    double *__restrict__ rp = static_cast<double *>(r.data);
+    const int64_t n = (int64_t)s.nx * s.ny * s.nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % s.nx), j = (int)((q / s.nx) % s.ny), k = (int)(q / ((int64_t)s.nx * s.ny));
+        const int64_t o = fab_off(s, i, j, k);
+        const int64_t st[3] = {1, s.jstride, s.kstride};
+        double lap1 = 0.0, lap2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) lap1 = __dadd_rn(lap1, diff2_exact(sp + o, st[d], one_over_dx2));
+#pragma unroll
+        for (int d = 0; d < 3; ++d) lap2 = __dadd_rn(lap2, diff2_exact(sp + s.cstride + o, st[d], one_over_dx2));
+        const double psi1 = sp[o], psi2 = sp[s.cstride + o];
+        const double dsq = __dsub_rn(__dadd_rn(__dmul_rn(psi1, psi1), __dmul_rn(psi2, psi2)), R2);
+        const double pc = __dmul_rn(__dmul_rn(0.5, lambda), dsq);
+        const int64_t ro = fab_off(r, i, j, k);
+        rp[ro] = sp[2 * s.cstride + o];
+        rp[r.cstride + ro] = sp[3 * s.cstride + o];
+        rp[2 * r.cstride + ro] = __dsub_rn(__dadd_rn(lap1, __dmul_rn(kappa, psi1)), __dmul_rn(pc, psi1));
+        rp[3 * r.cstride + ro] = __dsub_rn(__dadd_rn(lap2, __dmul_rn(kappa, psi2)), __dmul_rn(pc, psi2));
+    }
+}
+
+// FP32 (the reference's default PRECISION=FLOAT build): single-precision
+// arithmetic throughout, contraction allowed.
+__global__ void eval_rhs_f32_kernel(const axs_fab s, const axs_fab r, float one_over_dx2, float kappa, float lambda,
+                                    float R2)
+{
+    const float *__restrict__ sp = static_cast<const float *>(s.data);
+    float *__restrict__ rp = static_cast<float *>(r.data);
+    const float wf = 8.33333333333333333333e-2f, wn = 1.33333333333333333333e+0f, wl = 2.5f;
+    const int64_t n = (int64_t)s.nx * s.ny * s.nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % s.nx), j = (int)((q / s.nx) % s.ny), k = (int)(q / ((int64_t)s.nx * s.ny));
+        const int64_t o = fab_off(s, i, j, k);
+        const int64_t st[3] = {1, s.jstride, s.kstride};
+        float lap[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const float *p = sp + c * s.cstride + o;
+            float acc = 0.f;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int64_t t = st[d];
+                acc += (-wf * __ldg(p - 2 * t) + wn * __ldg(p - t) - wl * __ldg(p) + wn * __ldg(p + t) -
+                        wf * __ldg(p + 2 * t)) *
+                       one_over_dx2;
+            }
+            lap[c] = acc;
+        }
+        const float psi1 = sp[o], psi2 = sp[s.cstride + o];
+        const float pc = 0.5f * lambda * (psi1 * psi1 + psi2 * psi2 - R2);
+        const int64_t ro = fab_off(r, i, j, k);
+        rp[ro] = sp[2 * s.cstride + o];
+        rp[r.cstride + ro] = sp[3 * s.cstride + o];
+        rp[2 * r.cstride + ro] = lap[0] + kappa * psi1 - pc * psi1;
+        rp[3 * r.cstride + ro] = lap[1] + kappa * psi2 - pc * psi2;
+    }
+}
+
+// ---------------------------------------------------------------- ghost fill
+template <typename T>
+__global__ void fill_periodic_kernel(const axs_fab f)
+{
+    T *p = static_cast<T *>(f.data);
+    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng, gz = f.nz + 2 * f.ng;
+    const int64_t n = (int64_t)gx * gy * gz * f.ncomp;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % gx) - f.ng;
+        const int j = (int)((q / gx) % gy) - f.ng;
+        const int k = (int)((q / ((int64_t)gx * gy)) % gz) - f.ng;
+        const int c = (int)(q / ((int64_t)gx * gy * gz));
+        if (i >= 0 && i < f.nx && j >= 0 && j < f.ny && k >= 0 && k < f.nz) continue;
+        const int ii = ((i % f.nx) + f.nx) % f.nx, jj = ((j % f.ny) + f.ny) % f.ny, kk = ((k % f.nz) + f.nz) % f.nz;
+        p[c * f.cstride + fab_off(f, i, j, k)] = p[c * f.cstride + fab_off(f, ii, jj, kk)];
+    }
+}
+
+// ---------------------------------------------------------------- stage combinations
+template <typename T>
+__global__ void lincomb_kernel(const axs_fab d, const axs_fab x, T b, const axs_fab y, int ncomp)
+{
+    T *dp = static_cast<T *>(d.data);
+    const T *xp = static_cast<const T *>(x.data);
+    const T *yp = static_cast<const T *>(y.data);
+    const int64_t nc = (int64_t)d.nx * d.ny * d.nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nc * ncomp;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t cell = q % nc;
+        const int c = (int)(q / nc);
+        const int i = (int)(cell % d.nx), j = (int)((cell / d.nx) % d.ny), k = (int)(cell / ((int64_t)d.nx * d.ny));
+        const T xv = xp[c * x.cstride + fab_off(x, i, j, k)];
+        const T yv = yp[c * y.cstride + fab_off(y, i, j, k)];
+        dp[c * d.cstride + fab_off(d, i, j, k)] = xv + b * yv;
+    }
+}
+
+template <typename T>
+__global__ void rk4_combine_kernel(const axs_fab d, const axs_fab u, const axs_fab k1, const axs_fab k2,
+                                   const axs_fab k3, const axs_fab k4, T h6, int ncomp)
+{
+    const int64_t nc = (int64_t)d.nx * d.ny * d.nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nc * ncomp;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t cell = q % nc;
+        const int c = (int)(q / nc);
+        const int i = (int)(cell % d.nx), j = (int)((cell / d.nx) % d.ny), k = (int)(cell / ((int64_t)d.nx * d.ny));
+        auto at = [&](const axs_fab &f) { return static_cast<const T *>(f.data)[c * f.cstride + fab_off(f, i, j, k)]; };
+        static_cast<T *>(d.data)[c * d.cstride + fab_off(d, i, j, k)] =
+            at(u) + h6 * (at(k1) + T(2) * at(k2) + T(2) * at(k3) + at(k4));
+    }
+}
+
+// ---------------------------------------------------------------- level <-> FAB
+// Level layout: (x+4) + (y+2)*js + z*ks + c*cs (see axs_level_layout).
+template <typename T>
+__global__ void level_from_fab_kernel(T *lv, int64_t js, int64_t ks, int64_t cs, const axs_fab f, int to_level)
+{
+    T *fp = static_cast<T *>(f.data);
+    const int64_t nc = (int64_t)f.nx * f.ny * f.nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nc * 4; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t cell = q % nc;
+        const int c = (int)(q / nc);
+        const int i = (int)(cell % f.nx), j = (int)((cell / f.nx) % f.ny), k = (int)(cell / ((int64_t)f.nx * f.ny));
+        const int64_t lo = c * cs + (i + 4) + (int64_t)(j + 2) * js + (int64_t)k * ks;
+        const int64_t fo = c * f.cstride + fab_off(f, i, j, k);
+        if (to_level)
+            lv[lo] = fp[fo];
+        else
+            fp[fo] = lv[lo];
+    }
+}
+
+// Periodic copies in the x/y padding of `ncomp` level components (corners included).
+template <typename T>
+__global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs, int ncomp)
+{
+    const int px = nx + 8, py = ny + 4;
+    const int64_t n = (int64_t)px * py * nz * ncomp;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(q % px) - 4;
+        const int y = (int)((q / px) % py) - 2;
+        const int z = (int)((q / ((int64_t)px * py)) % nz);
+        const int c = (int)(q / ((int64_t)px * py * nz));
+        if (x >= 0 && x < nx && y >= 0 && y < ny) continue;
+        const int xx = ((x % nx) + nx) % nx, yy = ((y % ny) + ny) % ny;
+        T *base = lv + c * cs + (int64_t)z * ks;
+        base[(x + 4) + (int64_t)(y + 2) * js] = base[(xx + 4) + (int64_t)(yy + 2) * js];
+    }
+}
+
+static int grid_for(int64_t n)
+{
+    const int sms = device_sm_count();
+    int64_t g = (n + 255) / 256;
+    const int64_t cap = (int64_t)(sms > 0 ? sms : 148) * 16;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+static int same_shape(const axs_fab *a, const axs_fab *b, const char *what)
+{
+    AXS_REQUIRE(a->dtype == b->dtype && a->nx == b->nx && a->ny == b->ny && a->nz == b->nz, AXS_ERR_INVALID_ARGUMENT,
+                "%s: boxes differ in dtype or valid extent", what);
+    return AXS_OK;
+}
+
+int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
+                      int ncomp, cudaStream_t st)
+{
+    const int64_t n = (int64_t)(nx + 8) * (ny + 4) * nz * ncomp;
+    if (dtype == AXS_F64)
+        level_fill_ghosts_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(data), nx, ny, nz, js, ks, cs, ncomp);
+    else
+        level_fill_ghosts_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(data), nx, ny, nz, js, ks, cs, ncomp);
+    return launch_status("level_fill_ghosts");
+}
+
+int level_copy_fab(void *lv, int32_t dtype, int64_t js, int64_t ks, int64_t cs, const axs_fab &f, int to_level,
+                   cudaStream_t st)
+{
+    const int64_t n = (int64_t)f.nx * f.ny * f.nz * 4;
+    if (dtype == AXS_F64)
+        level_from_fab_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(lv), js, ks, cs, f, to_level);
+    else
+        level_from_fab_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(lv), js, ks, cs, f, to_level);
+    return launch_status("level_copy_fab");
+}
+
+}  // namespace axs
+
+using namespace axs;
+
+extern "C" {
+
+int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_rhs_coeffs *c, void *stream)
+{
+    int rc = validate_fab(soln, "soln", 4, 2);
+    if (rc) return rc;
+    if ((rc = validate_fab(rhs, "rhs", 4, 0))) return rc;
+    if ((rc = same_shape(soln, rhs, "eval_rhs"))) return rc;
+    AXS_REQUIRE(c != nullptr, AXS_ERR_INVALID_ARGUMENT, "null coefficients");
+    AXS_REQUIRE(dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
+    const int64_t n = (int64_t)soln->nx * soln->ny * soln->nz;
+    const double one_over_dx2 = 1.0 / (dx * dx);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (soln->dtype == AXS_F64)
+        eval_rhs_f64_kernel<<<grid_for(n), 256, 0, st>>>(*soln, *rhs, one_over_dx2, c->kappa, c->lambda, c->R2);
+    else
+        eval_rhs_f32_kernel<<<grid_for(n), 256, 0, st>>>(*soln, *rhs, (float)one_over_dx2, (float)c->kappa,
+                                                         (float)c->lambda, (float)c->R2);
+    return launch_status("eval_rhs");
+}
+
+int axs_fill_periodic_ghosts(const axs_fab *f, void *stream)
+{
+    int rc = validate_fab(f, "fab", 1, 0);
+    if (rc) return rc;
+    if (f->ng == 0) return AXS_OK;
+    AXS_REQUIRE(f->ng <= f->nx && f->ng <= f->ny && f->ng <= f->nz, AXS_ERR_UNSUPPORTED,
+                "periodic fill needs ng <= box extent");
+    const int64_t n = (int64_t)(f->nx + 2 * f->ng) * (f->ny + 2 * f->ng) * (f->nz + 2 * f->ng) * f->ncomp;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (f->dtype == AXS_F64)
+        fill_periodic_kernel<double><<<grid_for(n), 256, 0, st>>>(*f);
+    else
+        fill_periodic_kernel<float><<<grid_for(n), 256, 0, st>>>(*f);
+    return launch_status("fill_periodic_ghosts");
+}
+
+int axs_lincomb(const axs_fab *dst, const axs_fab *x, double b, const axs_fab *y, void *stream)
+{
+    int rc;
+    if ((rc = validate_fab(dst, "dst", 1, 0)) || (rc = validate_fab(x, "x", 1, 0)) || (rc = validate_fab(y, "y", 1, 0)))
+        return rc;
+    if ((rc = same_shape(dst, x, "lincomb")) || (rc = same_shape(dst, y, "lincomb"))) return rc;
+    const int nc = dst->ncomp < x->ncomp ? (dst->ncomp < y->ncomp ? dst->ncomp : y->ncomp)
+                                         : (x->ncomp < y->ncomp ? x->ncomp : y->ncomp);
+    const int64_t n = (int64_t)dst->nx * dst->ny * dst->nz * nc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dst->dtype == AXS_F64)
+        lincomb_kernel<double><<<grid_for(n), 256, 0, st>>>(*dst, *x, b, *y, nc);
+    else
+        lincomb_kernel<float><<<grid_for(n), 256, 0, st>>>(*dst, *x, (float)b, *y, nc);
+    return launch_status("lincomb");
+}
+
+int axs_rk4_combine(const axs_fab *dst, const axs_fab *uold, const axs_fab *k1, const axs_fab *k2, const axs_fab *k3,
+                    const axs_fab *k4, double dt, void *stream)
+{
+    const axs_fab *all[6] = {dst, uold, k1, k2, k3, k4};
+    const char *names[6] = {"dst", "uold", "k1", "k2", "k3", "k4"};
+    for (int q = 0; q < 6; ++q) {
+        int rc = validate_fab(all[q], names[q], 4, 0);
+        if (rc) return rc;
+        if (q && (rc = same_shape(dst, all[q], "rk4_combine"))) return rc;
+    }
+    const int64_t n = (int64_t)dst->nx * dst->ny * dst->nz * 4;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dst->dtype == AXS_F64)
+        rk4_combine_kernel<double><<<grid_for(n), 256, 0, st>>>(*dst, *uold, *k1, *k2, *k3, *k4, dt / 6.0, 4);
+    else
+        rk4_combine_kernel<float><<<grid_for(n), 256, 0, st>>>(*dst, *uold, *k1, *k2, *k3, *k4, (float)(dt / 6.0), 4);
+    return launch_status("rk4_combine");
+}
+
+}  // extern "C"

@@ -1,0 +1,266 @@
+/*
+ * axs.h -- C ABI of the GB300-native axion-string hot path.
+ *
+ * One shared library (libaxs_gb300.so, sm_103a) replaces the per-level hot
+ * path of the AMReX/GRTeclyn axion-string code:
+ *   (a) the complex-scalar RHS and its classic-RK4 time step,
+ *   (b) the plaquette-winding string finder (counts + compacted pierced list),
+ *   (c) the energy, string-velocity and xi reductions.
+ *
+ * Conventions
+ *   - Every entry point returns an axs_status (0 = AXS_OK). No C++ exception
+ *     crosses the ABI. axs_last_error() gives a message for the calling thread.
+ *   - The caller owns every buffer. Device pointers are plain CUDA device
+ *     addresses; `stream` is a cudaStream_t (NULL = legacy default stream).
+ *   - Device entry points are asynchronous on `stream` and never synchronise,
+ *     allocate or free, so they can be captured in a CUDA graph. Results that
+ *     the reference returned by value (plaquette counts, energy sums) are
+ *     written to caller-provided DEVICE memory.
+ *   - Arguments are validated on the host before anything is launched; a
+ *     failed validation launches nothing.
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the reference project root).
+ */
+#ifndef AXS_H
+#define AXS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AXS_ABI_VERSION 1
+
+typedef enum axs_status {
+    AXS_OK = 0,
+    AXS_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad enum */
+    AXS_ERR_UNSUPPORTED = 2,      /* shape / layout the kernels do not handle */
+    AXS_ERR_ALIGNMENT = 3,        /* pointer or stride not 16-byte aligned */
+    AXS_ERR_WORKSPACE = 4,        /* caller-provided scratch too small */
+    AXS_ERR_CUDA = 5,             /* a CUDA runtime/driver call failed */
+    AXS_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up */
+    AXS_ERR_CAPACITY = 7          /* pierced list truncated (counts stay exact) */
+} axs_status;
+
+typedef enum axs_dtype { AXS_F32 = 1, AXS_F64 = 2 } axs_dtype;
+
+/* Component order of the state (AxionStrings/StateVariables.hpp:9-17). */
+enum { AXS_C_PSI1 = 0, AXS_C_PSI2 = 1, AXS_C_PI1 = 2, AXS_C_PI2 = 3, AXS_NUM_VARS = 4 };
+
+/* One AMReX FArrayBox viewed through plain pointers: cell (i,j,k) of
+ * component c, i in [-ng, nx+ng) etc., lives at
+ *   data + (i+ng) + (j+ng)*jstride + (k+ng)*kstride + c*cstride   (elements).
+ * This is exactly amrex::Array4's layout (AxionStringsRHS.impl.hpp:29-36),
+ * so a box of a MultiFab maps with zero copies. */
+typedef struct axs_fab {
+    void *data;
+    int32_t dtype; /* axs_dtype */
+    int32_t nx, ny, nz, ng;
+    int32_t ncomp;
+    int64_t jstride, kstride, cstride;
+} axs_fab;
+
+/* RHS coefficients resolved on the host at one stage time
+ * (AxionStringsLevel.cpp:856-907; AxionStringsRHS.hpp:32-36). */
+typedef struct axs_rhs_coeffs {
+    double kappa;  /* curvature_term_coeff(tau) */
+    double lambda; /* lambda(tau) */
+    double R2;     /* R(tau)^2 */
+} axs_rhs_coeffs;
+
+/* Background models behind the coefficients: Background.hpp:21-134 (power
+ * law, c(tau) schedule with one switch), FlatBackground.hpp:26-44,
+ * PreEvolutionBackground.hpp:37-78, plus the optional post-handoff
+ * smoothstep blend of AxionStringsLevel.cpp:893-906. lambda_scale multiplies
+ * lambda (the reference fixes lambda0 = 1, Background.hpp:37; 1.0 reproduces it). */
+typedef enum axs_background_kind { AXS_BG_EXPANDING = 0, AXS_BG_FLAT = 1, AXS_BG_PRE_EVOLUTION = 2 } axs_background_kind;
+
+typedef struct axs_background {
+    int32_t kind; /* axs_background_kind */
+    int32_t has_switch;
+    double a_inv, c0, c1, tau_switch;
+    double lambda_scale;
+    double m_r;       /* flat: lambda = m_r^2 */
+    double gamma_pre; /* pre-evolution: constant m_r/H */
+    double blend_dtau, blend_tau_start, blend_lambda_start, blend_curv_start;
+} axs_background;
+
+typedef struct axs_background_values {
+    double R, R_prime, kappa, lambda, H, R2, m_r, R_prime_over_R;
+} axs_background_values;
+
+/* ---------------------------------------------------------------------------
+ * Host-side scalar models (no GPU needed)
+ * ------------------------------------------------------------------------- */
+
+/* Background::{R, R_prime, curvature_term_coeff, lambda, H} (Background.hpp:55-107)
+ * and the coefficient resolution of specific_eval_rhs (AxionStringsLevel.cpp:856-907). */
+int axs_background_eval(const axs_background *bg, double tau, axs_background_values *out);
+int axs_background_rhs_coeffs(const axs_background *bg, double tau, axs_rhs_coeffs *out);
+/* Background::tau_from_log_mr_over_h (Background.hpp:129-133). */
+int axs_background_tau_from_log_mr_over_h(const axs_background *bg, double log_mr_over_h, double *tau);
+
+/* XiFormula.hpp:33-59. */
+double axs_xi_from_comoving_length(double ell_comoving, double L_tilde, double a_inv, double tau);
+double axs_xi_from_plaquette_count(double N_p, double dx, double L_tilde, double a_inv, double tau);
+double axs_plaquette_count_for_target_xi(double xi_target, int N, double L_tilde, double a_inv, double tau);
+
+const char *axs_status_string(int status);
+const char *axs_last_error(void);
+int axs_abi_version(void);
+
+/* ---------------------------------------------------------------------------
+ * (a) RHS on AMReX FABs -- the drop-in for the level hook
+ * ------------------------------------------------------------------------- */
+
+/* Replaces the body of AxionStringsLevel::specific_eval_rhs
+ * (AxionStringsLevel.cpp:909-920): AxionStringsRHS<FourthOrderDerivatives>
+ * (AxionStringsRHS.impl.hpp:25-60) over the valid cells of one box.
+ * `soln` needs ng >= 2 filled ghost layers; rhs may have any ng. */
+int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_rhs_coeffs *c,
+                 void *stream);
+
+/* Replaces MultiFab::FillBoundary(periodicity) for a single-box periodic
+ * domain (AxionStringsLevel.cpp:820, :1255): fills every ghost cell. */
+int axs_fill_periodic_ghosts(const axs_fab *f, void *stream);
+
+/* dst = x + b*y over the valid cells of all components: the stage combination
+ * U_s = U_old + c_s dt k (AMReX MultiFab::LinComb in GRTeclyn's RK driver). */
+int axs_lincomb(const axs_fab *dst, const axs_fab *x, double b, const axs_fab *y, void *stream);
+
+/* Final classic-RK4 combination dst = uold + dt/6 (k1 + 2 k2 + 2 k3 + k4). */
+int axs_rk4_combine(const axs_fab *dst, const axs_fab *uold, const axs_fab *k1, const axs_fab *k2,
+                    const axs_fab *k3, const axs_fab *k4, double dt, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * (a) Fused RK4 on a periodic level (TMA-staged two-sweep scheme)
+ * ------------------------------------------------------------------------- */
+
+/* Device layout of a periodic single-box level: component-major SoA planes,
+ * x fastest, each plane padded by 4 columns on either side in x and 2 rows on
+ * either side in y (periodic copies kept current by the kernels), no z
+ * padding:  element (x,y,z,c) at (x+4) + (y+2)*jstride + z*kstride + c*cstride.
+ * `state` holds psi1, psi2, Pi1, Pi2; `work` holds 8 components of the same
+ * layout used between the two sweeps of a step, plus a 256-byte status block. */
+typedef struct axs_level_layout {
+    int64_t jstride, kstride, cstride; /* elements */
+    int64_t state_bytes;              /* 4 components */
+    int64_t work_bytes;               /* 8 components + status block */
+} axs_level_layout;
+
+typedef struct axs_level {
+    void *state;
+    void *work;
+    int32_t dtype; /* axs_dtype */
+    int32_t nx, ny, nz;
+    double dx;
+} axs_level;
+
+int axs_level_layout_for(int32_t dtype, int32_t nx, int32_t ny, int32_t nz, axs_level_layout *out);
+
+/* Periodic ghost columns/rows of the 4 state components (call after writing
+ * the state's valid cells by any other means). */
+int axs_level_fill_ghosts(const axs_level *lv, void *stream);
+
+/* Copy between an AMReX FAB (any ng) and the level layout, valid cells only.
+ * import also refreshes the level's ghosts. */
+int axs_level_import_fab(const axs_level *lv, const axs_fab *src, void *stream);
+int axs_level_export_fab(const axs_level *lv, const axs_fab *dst, void *stream);
+
+/* Replaces GRTeclyn's RK4 level advance (docs/conventions.md:239-245, driver
+ * absent from the reference tree) together with nsteps x 4 calls of
+ * specific_eval_rhs: advances the state by nsteps classic-RK4 steps of size
+ * dt from t0, coefficients from `bg` at tau = tau_i + t_stage. Two sweeps
+ * per step; async on `stream`. */
+int axs_level_rk4_advance(const axs_level *lv, const axs_background *bg, double tau_i, double t0,
+                          double dt, int32_t nsteps, void *stream);
+
+/* One of the two sweeps of the step starting at time t (sweep 0 = A: reads the
+ * state, writes the between-sweep components; sweep 1 = B: reads those, writes
+ * the state). Sweep A then sweep B equals one axs_level_rk4_advance step; this
+ * entry point lets a caller time or interleave the sweeps. */
+int axs_level_rk4_sweep(const axs_level *lv, const axs_background *bg, double tau_i, double t, double dt,
+                        int32_t sweep, void *stream);
+
+/* Synchronises `stream` and reports (and clears) the level's device status
+ * word: AXS_OK or AXS_ERR_DEVICE_TIMEOUT. */
+int axs_level_device_status(const axs_level *lv, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * (b)+(c) Fused diagnostics pass
+ * ------------------------------------------------------------------------- */
+
+typedef enum axs_masking_scheme { AXS_MASK_NONE = 0, AXS_MASK_A = 1, AXS_MASK_B = 2 } axs_masking_scheme;
+typedef enum axs_boundary { AXS_BOUNDARY_GHOSTS = 0, AXS_BOUNDARY_PERIODIC = 1 } axs_boundary;
+
+typedef struct axs_diag_params {
+    double dx;
+    double R, lambda, R_prime_over_R, m_r; /* host-resolved at the snapshot tau */
+    int32_t masking_scheme;                /* axs_masking_scheme (Masking.hpp:39-53) */
+    double masking_threshold;
+    int32_t boundary;                      /* axs_boundary */
+    int32_t want_energy, want_plaquettes, want_velocity;
+} axs_diag_params;
+
+/* Written to device memory by the diagnostics pass. */
+typedef struct axs_diag_result {
+    double energy_sums[14]; /* EnergyKernel.hpp:196-199 order: rho, rho w, a_kin, a_kin w,
+                               a_grad, a_grad w, r_kin, r_kin w, r_grad, r_grad w,
+                               r_mass, r_mass w, w, n_cells */
+    double vel_sum;         /* VelocityKernel.hpp: sum of gamma^2 v^2 at pierced corners */
+    int64_t vel_count;      /* corners counted (4 per pierced plaquette) */
+    int64_t n_p_plain;      /* StringFinder.hpp:76-122 */
+    int64_t n_p_weighted;
+    int64_t n_listed;       /* entries written to the pierced list (<= capacity) */
+    int64_t n_near_tie;     /* plaquette edges with | |dtheta| - pi | < 1e-12: the
+                               only edges where a different atan2 could round the
+                               other way (bit-exactness caveat) */
+    int64_t status;         /* AXS_OK or AXS_ERR_CAPACITY */
+} axs_diag_result;
+
+/* Scratch (device) bytes the diagnostics pass needs for a box of this size. */
+int axs_diagnostics_scratch_bytes(int32_t nx, int32_t ny, int32_t nz, int64_t *bytes);
+
+/* One pass over the valid cells computing, as requested:
+ *   - count_plaquettes (StringFinder.hpp:76-122, windings of
+ *     plaquette_windings_at :45-68 / PlaquetteWinding.hpp:42-51) and a
+ *     compacted list of pierced plaquettes, entry = 4*(i + nx*(j + ny*k)) + plane
+ *     (plane 0 = xy, 1 = yz, 2 = zx), order unspecified;
+ *   - compute_total_energy_sums (EnergyKernel.hpp:106-233);
+ *   - compute_velocity_at_pierced_corners (VelocityKernel.hpp:37-141).
+ * `mask` (nullable, nx*ny*nz bytes, 1 = include) is the composite coverage mask.
+ * Sums are accumulated in FP64, deterministically (fixed tree, no float atomics). */
+int axs_diagnostics(const axs_fab *state, const axs_diag_params *p, const uint8_t *mask,
+                    axs_diag_result *result_dev, int64_t *pierced_dev, int64_t pierced_capacity,
+                    void *scratch_dev, int64_t scratch_bytes, void *stream);
+
+/* Same pass on a fused-RK4 level (periodic wrap in z, ghost copies in x/y). */
+int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const uint8_t *mask,
+                          axs_diag_result *result_dev, int64_t *pierced_dev,
+                          int64_t pierced_capacity, void *scratch_dev, int64_t scratch_bytes,
+                          void *stream);
+
+/* plaquette_winding (PlaquetteWinding.hpp:42-51) on n device quadruples
+ * theta[4*q .. 4*q+3] -> w[q]: the device winding kernel on caller-chosen
+ * phases (known-answer tests). */
+int axs_plaquette_winding_batch(const double *theta_dev, int64_t n, int32_t *w_dev, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Initial data
+ * ------------------------------------------------------------------------- */
+
+/* FourierIC::generate's spectral fill (FourierIC.hpp:82-116) on the device:
+ * the R2C half spectrum (nz, ny, nx/2+1) of interleaved (re, im) doubles with
+ * hash-seeded Gaussian modes for 0 < k^2 <= k_max_cells^2. The inverse real
+ * FFT and the rescale to the target mean square follow on the caller's side. */
+int axs_fourier_spectrum(double *spec_dev, int32_t nx, int32_t ny, int32_t nz, double k_max_cells,
+                         uint64_t seed, int32_t comp_seed_offset, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXS_H */

@@ -1,0 +1,161 @@
+"""GPU parity of the fused diagnostics pass (string finder, energy sums,
+velocities) and the small device entry points, through the C ABI, against the
+reference-generated golden fixtures and the CPU oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return t if dtype is None else t.to(dtype)
+
+
+def _run_diag(axs, fab_t, ng, params, mask=None, capacity=None):
+    L = axs._lib
+    f = axs.fab(fab_t, ng)
+    ncell = f.nx * f.ny * f.nz
+    scratch = torch.zeros(axs.level.scratch_bytes(f.nx, f.ny, f.nz), dtype=torch.uint8, device="cuda")
+    res = torch.zeros(C.sizeof(L.DiagResult), dtype=torch.uint8, device="cuda")
+    cap = 3 * ncell if capacity is None else capacity
+    lst = torch.full((max(cap, 1),), -1, dtype=torch.int64, device="cuda")
+    m = None if mask is None else _dev(mask.astype(np.uint8)).reshape(-1)
+    L.call("axs_diagnostics", C.byref(f), C.byref(params), None if m is None else m.data_ptr(), res.data_ptr(),
+           lst.data_ptr(), cap, scratch.data_ptr(), scratch.numel(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    r = L.DiagResult.from_buffer_copy(res.cpu().numpy().tobytes())
+    return r, lst[: min(r.n_listed, cap)].cpu().numpy()
+
+
+def _params(axs, g, scheme, boundary, want=(1, 1, 1)):
+    dx, kappa, lam, R2, R, RpR, m_r = g["params"]
+    return axs._lib.DiagParams(dx, R, lam, RpR, m_r, scheme, 0.8, boundary, *want)
+
+
+def _pierced_from_windings(w):
+    nz, ny, nx, _ = w.shape
+    cells = np.arange(nx * ny * nz).reshape(nz, ny, nx)
+    out = []
+    for pl in range(3):
+        out.append(4 * cells[w[..., pl] != 0] + pl)
+    return np.sort(np.concatenate(out))
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("box", ["rand", "ic"])
+@pytest.mark.parametrize("boundary", ["ghosts", "periodic"])
+def test_diagnostics_vs_reference(axs, golden, prec, box, boundary):
+    g = golden(f"fields_{prec}.npz")
+    dt = torch.float64 if prec == "f64" else torch.float32
+    st = g[f"{box}_state"]
+    c, nz, ny, nx = st.shape
+    ng = 2 if boundary == "ghosts" else 0
+    t = axs.new_fab((nx, ny, nz), ng, dtype=dt)
+    axs.valid(t, ng).copy_(_dev(st, dt))
+    if ng:
+        axs.fill_periodic_ghosts(t, ng)
+    bmode = axs._lib.BOUNDARY_GHOSTS if ng else axs._lib.BOUNDARY_PERIODIC
+    for scheme in range(3):
+        r, lst = _run_diag(axs, t, ng, _params(axs, g, scheme, bmode))
+        assert r.status == 0 and r.n_near_tie == 0
+        assert (r.n_p_plain, r.n_p_weighted) == tuple(g[f"{box}_counts"])
+        np.testing.assert_array_equal(np.sort(lst), _pierced_from_windings(g[f"{box}_windings"]))
+        np.testing.assert_allclose(list(r.energy_sums), g[f"{box}_energy_sums"][scheme], rtol=1e-12, atol=1e-300)
+        vs, vc = g[f"{box}_velocity"]
+        if prec == "f64":  # the FLOAT build recomputes windings with float atan2 (VelocityKernel.hpp:66-69)
+            assert r.vel_count == int(vc)
+            assert r.vel_sum == pytest.approx(vs, rel=1e-12)
+    # coverage mask
+    r, _ = _run_diag(axs, t, ng, _params(axs, g, 1, bmode), mask=g[f"{box}_mask"])
+    assert (r.n_p_plain, r.n_p_weighted) == tuple(g[f"{box}_counts_masked"])
+    np.testing.assert_allclose(list(r.energy_sums), g[f"{box}_energy_sums_masked"], rtol=1e-12, atol=1e-300)
+
+
+def test_velocity_matches_oracle_f32(axs, orc, golden):
+    g = golden("fields_f32.npz")
+    dx, kappa, lam, R2, R, RpR, m_r = g["params"]
+    st = g["ic_state"]
+    fab = orc.to_fab(st, 2)
+    # oracle with the GPU's phase precision (double atan2) for the pierced set
+    from oracle.oracle import velocity
+    vs_native, vc_native = velocity(fab, 2, R, RpR, m_r)
+    t = axs.new_fab(st.shape[1:][::-1], 2, dtype=torch.float32)
+    axs.valid(t, 2).copy_(_dev(st))
+    axs.fill_periodic_ghosts(t, 2)
+    r, _ = _run_diag(axs, t, 2, _params(axs, g, 1, axs._lib.BOUNDARY_GHOSTS))
+    # smooth field: float and double atan2 agree on every winding here
+    assert r.vel_count == vc_native
+    assert r.vel_sum == pytest.approx(vs_native, rel=1e-12)
+
+
+def test_level_diagnostics_matches_oracle(axs, orc):
+    n, dx = 24, 0.5
+    v = orc.fourier_ic_state(n, 5.0, seed=99)
+    v[2:] = 0.3 * np.random.default_rng(1).standard_normal((2, n, n, n))
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    bgo = orc.background(a_inv=2.0, c0=1.0, lambda_scale=2.0)
+    tau = 1.7
+    lvl = axs.PeriodicLevel(n, dx, dtype=torch.float64)
+    lvl.set_state(_dev(v))
+    d = lvl.diagnostics(bg, tau)
+    ref = orc.level_diagnostics(v, dx, bgo, tau)
+    assert (d.n_p_plain, d.n_p_weighted) == (ref.n_p_plain, ref.n_p_weighted)
+    np.testing.assert_allclose(d.energy_sums, ref.energy_sums, rtol=1e-12)
+    assert d.xi_plain == pytest.approx(ref.xi_plain, rel=1e-14)
+    assert d.vel_count == ref.vel_count
+    assert d.mean_gamma_sq_v_sq == pytest.approx(ref.mean_gamma_sq_v_sq, rel=1e-12)
+    assert d.energy["rho_tot_unscreened"] == pytest.approx(ref.energy[0], rel=1e-12)
+    assert d.energy["rho_tot_screened"] == pytest.approx(ref.energy[1], rel=1e-12)
+
+
+def test_pierced_list_capacity(axs, golden):
+    g = golden("fields_f64.npz")
+    st = g["rand_state"]
+    c, nz, ny, nx = st.shape
+    t = axs.new_fab((nx, ny, nz), 0, dtype=torch.float64)
+    t.copy_(_dev(st))
+    r, lst = _run_diag(axs, t, 0, _params(axs, g, 1, axs._lib.BOUNDARY_PERIODIC), capacity=10)
+    assert r.status == axs._lib.AXS_ERR_CAPACITY
+    assert r.n_listed == 10 and r.n_p_plain == g["rand_counts"][0]  # counts stay exact
+    full = set(_pierced_from_windings(g["rand_windings"]).tolist())
+    assert set(lst.tolist()) <= full
+
+
+def test_winding_kats_on_device(axs, golden):
+    g = golden("kats.npz")
+    th = _dev(g["winding_theta"]).contiguous()
+    w = torch.zeros(th.shape[0], dtype=torch.int32, device="cuda")
+    axs._lib.call("axs_plaquette_winding_batch", th.data_ptr(), th.shape[0], w.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream)
+    np.testing.assert_array_equal(w.cpu().numpy(), g["winding_w"])
+
+
+def test_fourier_spectrum_and_ic(axs, orc, golden):
+    from axion_strings_adaptive_gb300 import ic
+    for (nx, ny, nz, kmax, seed, comp) in ((16, 16, 16, 4.0, 4242, 0), (12, 10, 8, 3.2, 99, 1),
+                                          (32, 32, 32, ic.strict_cutoff(8), 7, 1)):
+        ref = orc.fourier_spectrum(nx, ny, nz, kmax, seed, comp)
+        spec = torch.zeros((nz, ny, nx // 2 + 1, 2), dtype=torch.float64, device="cuda")
+        axs._lib.call("axs_fourier_spectrum", spec.data_ptr(), nx, ny, nz, kmax, seed, comp,
+                      torch.cuda.current_stream().cuda_stream)
+        got = spec.cpu().numpy()
+        np.testing.assert_allclose(got[..., 0] + 1j * got[..., 1], ref, rtol=0, atol=5e-15)
+    gf = golden("fourier_ic.npz")
+    nx, ny, nz, kmax, seed, comp = gf["a_args"]
+    f = ic.fourier_component((int(nx), int(ny), int(nz)), kmax, int(seed), int(comp))
+    np.testing.assert_allclose(f.cpu().numpy(), gf["a_field"], rtol=0, atol=1e-13)
+
+
+def test_rejects_bad_arguments_without_launching(axs):
+    L = axs._lib
+    f = L.Fab(None, L.AXS_F64, 8, 8, 8, 2, 4, 12, 144, 1728)
+    c = L.RhsCoeffs(0.0, 1.0, 1.0)
+    assert L.lib().axs_eval_rhs(C.byref(f), C.byref(f), 0.5, C.byref(c), None) == L.AXS_ERR_INVALID_ARGUMENT
+    t = axs.new_fab((8, 8, 8), 1, dtype=torch.float64)
+    assert L.lib().axs_eval_rhs(C.byref(axs.fab(t, 1)), C.byref(axs.fab(t, 1)), 0.5, C.byref(c),
+                                None) == L.AXS_ERR_INVALID_ARGUMENT  # needs 2 ghosts
+    assert b"ghost" in L.lib().axs_last_error()
