@@ -332,7 +332,7 @@ int axs_fourier_spectrum(double *spec, int32_t nx, int32_t ny, int32_t nz, doubl
 {
     AXS_REQUIRE(spec != nullptr, AXS_ERR_INVALID_ARGUMENT, "null spectrum");
     AXS_REQUIRE(nx > 0 && ny > 0 && nz > 0, AXS_ERR_INVALID_ARGUMENT, "empty box");
-    const uint64_t full_seed = seed ^ ((uint64_t)(uint32_t)comp_seed_offset << 32);
+    const uint64_t full_seed = seed ^ ((uint64_t)(int64_t)comp_seed_offset << 32);
     const int sms = device_sm_count();
     AXS_REQUIRE(sms > 0, AXS_ERR_CUDA, "no CUDA device");
     fourier_spectrum_kernel<<<sms * 8, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<double2 *>(spec), nx, ny,

@@ -62,10 +62,13 @@ __device__ __forceinline__ double diff1(const DiagView &v, int c, int i, int j, 
 {
     const int di = dir == 0, dj = dir == 1, dk = dir == 2;
     const double wf = 8.33333333333333333333e-2, wn = 6.66666666666666666667e-1;
-    const double r = (wf * ld<T>(v, c, i - 2 * di, j - 2 * dj, k - 2 * dk) - wn * ld<T>(v, c, i - di, j - dj, k - dk) +
-                      wn * ld<T>(v, c, i + di, j + dj, k + dk) - wf * ld<T>(v, c, i + 2 * di, j + 2 * dj, k + 2 * dk)) *
-                     inv_dx;
-    return (double)(T)r;
+    // reference expression order, no contraction: the result is rounded to the
+    // field precision, so a fused multiply-add could move it by one ulp
+    double r = __dmul_rn(wf, ld<T>(v, c, i - 2 * di, j - 2 * dj, k - 2 * dk));
+    r = __dsub_rn(r, __dmul_rn(wn, ld<T>(v, c, i - di, j - dj, k - dk)));
+    r = __dadd_rn(r, __dmul_rn(wn, ld<T>(v, c, i + di, j + dj, k + dk)));
+    r = __dsub_rn(r, __dmul_rn(wf, ld<T>(v, c, i + 2 * di, j + 2 * dj, k + 2 * dk)));
+    return (double)(T)__dmul_rn(r, inv_dx);
 }
 
 __device__ __forceinline__ double wrap_diff(double d, int &near_tie)
@@ -436,7 +439,9 @@ int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const u
     AXS_REQUIRE(lv != nullptr && lv->state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null level");
     int rc = axs_level_layout_for(lv->dtype, lv->nx, lv->ny, lv->nz, &L);
     if (rc) return rc;
-    DiagView v{lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, 4, 2, 0, 0, 0, 1, L.jstride, L.kstride, L.cstride};
+    // indices wrap on every axis: the sweeps keep the x/y padding current but
+    // not its corners, which the xy plaquette at (nx-1, ny-1) would read
+    DiagView v{lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, 4, 2, 0, 1, 1, 1, L.jstride, L.kstride, L.cstride};
     return run_diag(v, p, mask, out, list, capacity, scratch, scratch_bytes, (cudaStream_t)stream);
 }
 

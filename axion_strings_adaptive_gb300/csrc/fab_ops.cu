@@ -113,6 +113,14 @@ __global__ void fill_periodic_kernel(const axs_fab f)
 }
 
 // ---------------------------------------------------------------- stage combinations
+// Evaluated with explicit round-to-nearest operations in the host's
+// expression order (no contraction), so the per-stage drop-in path reproduces
+// a CPU evaluation of the same RK4 bit for bit.
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+
 template <typename T>
 __global__ void lincomb_kernel(const axs_fab d, const axs_fab x, T b, const axs_fab y, int ncomp)
 {
@@ -127,7 +135,7 @@ __global__ void lincomb_kernel(const axs_fab d, const axs_fab x, T b, const axs_
         const int i = (int)(cell % d.nx), j = (int)((cell / d.nx) % d.ny), k = (int)(cell / ((int64_t)d.nx * d.ny));
         const T xv = xp[c * x.cstride + fab_off(x, i, j, k)];
         const T yv = yp[c * y.cstride + fab_off(y, i, j, k)];
-        dp[c * d.cstride + fab_off(d, i, j, k)] = xv + b * yv;
+        dp[c * d.cstride + fab_off(d, i, j, k)] = rn_add(xv, rn_mul(b, yv));
     }
 }
 
@@ -142,8 +150,8 @@ __global__ void rk4_combine_kernel(const axs_fab d, const axs_fab u, const axs_f
         const int c = (int)(q / nc);
         const int i = (int)(cell % d.nx), j = (int)((cell / d.nx) % d.ny), k = (int)(cell / ((int64_t)d.nx * d.ny));
         auto at = [&](const axs_fab &f) { return static_cast<const T *>(f.data)[c * f.cstride + fab_off(f, i, j, k)]; };
-        static_cast<T *>(d.data)[c * d.cstride + fab_off(d, i, j, k)] =
-            at(u) + h6 * (at(k1) + T(2) * at(k2) + T(2) * at(k3) + at(k4));
+        const T sum = rn_add(rn_add(rn_add(at(k1), rn_mul(T(2), at(k2))), rn_mul(T(2), at(k3))), at(k4));
+        static_cast<T *>(d.data)[c * d.cstride + fab_off(d, i, j, k)] = rn_add(at(u), rn_mul(h6, sum));
     }
 }
 

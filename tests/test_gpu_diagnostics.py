@@ -31,8 +31,10 @@ def _run_diag(axs, fab_t, ng, params, mask=None, capacity=None):
     return r, lst[: min(r.n_listed, cap)].cpu().numpy()
 
 
-def _params(axs, g, scheme, boundary, want=(1, 1, 1)):
+def _params(axs, g, scheme, boundary, want=(1, 1, 1), prec="f64"):
     dx, kappa, lam, R2, R, RpR, m_r = g["params"]
+    if prec == "f32":  # the FLOAT build receives R, lambda, R'/R, m_r as amrex::Real (EnergyKernel.hpp:107-109)
+        dx, lam, R, RpR, m_r = (float(np.float32(x)) for x in (dx, lam, R, RpR, m_r))
     return axs._lib.DiagParams(dx, R, lam, RpR, m_r, scheme, 0.8, boundary, *want)
 
 
@@ -60,7 +62,7 @@ def test_diagnostics_vs_reference(axs, golden, prec, box, boundary):
         axs.fill_periodic_ghosts(t, ng)
     bmode = axs._lib.BOUNDARY_GHOSTS if ng else axs._lib.BOUNDARY_PERIODIC
     for scheme in range(3):
-        r, lst = _run_diag(axs, t, ng, _params(axs, g, scheme, bmode))
+        r, lst = _run_diag(axs, t, ng, _params(axs, g, scheme, bmode, prec=prec))
         assert r.status == 0 and r.n_near_tie == 0
         assert (r.n_p_plain, r.n_p_weighted) == tuple(g[f"{box}_counts"])
         np.testing.assert_array_equal(np.sort(lst), _pierced_from_windings(g[f"{box}_windings"]))
@@ -70,14 +72,14 @@ def test_diagnostics_vs_reference(axs, golden, prec, box, boundary):
             assert r.vel_count == int(vc)
             assert r.vel_sum == pytest.approx(vs, rel=1e-12)
     # coverage mask
-    r, _ = _run_diag(axs, t, ng, _params(axs, g, 1, bmode), mask=g[f"{box}_mask"])
+    r, _ = _run_diag(axs, t, ng, _params(axs, g, 1, bmode, prec=prec), mask=g[f"{box}_mask"])
     assert (r.n_p_plain, r.n_p_weighted) == tuple(g[f"{box}_counts_masked"])
     np.testing.assert_allclose(list(r.energy_sums), g[f"{box}_energy_sums_masked"], rtol=1e-12, atol=1e-300)
 
 
 def test_velocity_matches_oracle_f32(axs, orc, golden):
     g = golden("fields_f32.npz")
-    dx, kappa, lam, R2, R, RpR, m_r = g["params"]
+    dx, kappa, lam, R2, R, RpR, m_r = (float(np.float32(x)) for x in g["params"])
     st = g["ic_state"]
     fab = orc.to_fab(st, 2)
     # oracle with the GPU's phase precision (double atan2) for the pierced set
@@ -86,7 +88,7 @@ def test_velocity_matches_oracle_f32(axs, orc, golden):
     t = axs.new_fab(st.shape[1:][::-1], 2, dtype=torch.float32)
     axs.valid(t, 2).copy_(_dev(st))
     axs.fill_periodic_ghosts(t, 2)
-    r, _ = _run_diag(axs, t, 2, _params(axs, g, 1, axs._lib.BOUNDARY_GHOSTS))
+    r, _ = _run_diag(axs, t, 2, _params(axs, g, 1, axs._lib.BOUNDARY_GHOSTS, prec="f32"))
     # smooth field: float and double atan2 agree on every winding here
     assert r.vel_count == vc_native
     assert r.vel_sum == pytest.approx(vs_native, rel=1e-12)
