@@ -1,0 +1,130 @@
+"""C-ABI checks that need no GPU: the library loads, exports exactly the entry
+points include/axs.h declares, and its host-side scalar models (background
+coefficients, xi) reproduce the reference-generated golden vectors. Argument
+validation happens before any CUDA call, so bad descriptors are rejected here
+too."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "axs.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(axs_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from axion_strings_adaptive_gb300 import _build, _lib
+    _build.build()
+    return _lib
+
+
+def test_every_declared_symbol_is_exported(L):
+    lib = L.lib()
+    names = _declared()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in axs.h but not exported"
+    # and the Python binding covers every declaration
+    assert set(names) == set(L.SIGNATURES), set(names) ^ set(L.SIGNATURES)
+
+
+def test_abi_version_and_status_strings(L):
+    lib = L.lib()
+    assert lib.axs_abi_version() == 1
+    for s in range(8):
+        assert lib.axs_status_string(s)
+
+
+def test_background_matches_reference(L, golden):
+    from axion_strings_adaptive_gb300 import Background
+    g = golden("kats.npz")
+    for cfg, rows in zip(g["bg_cfg"], g["bg_out"]):
+        bg = Background.expanding(cfg[0], cfg[1], c1=cfg[2], tau_switch=cfg[3], has_switch=bool(cfg[4]))
+        for tau, row in zip(g["bg_tau"], rows):
+            v = bg.values(tau)
+            np.testing.assert_allclose([v.R, v.R_prime, v.kappa, v.lambda_, v.H], row[:5], rtol=2e-15)
+            assert v.H / v.m_r == pytest.approx(row[5], rel=1e-14)
+    for (a_inv, c0, l), tau in zip(g["bg_log_in"], g["bg_log_tau"]):
+        assert Background.expanding(a_inv, c0).tau_from_log_mr_over_h(l) == pytest.approx(tau, rel=1e-15)
+    for a, m in enumerate((1.0, 2.3, 0.7)):
+        v = Background.flat(m).values(1.0)
+        np.testing.assert_array_equal([v.R, v.R_prime, v.kappa, v.lambda_], g["flat_out"][a, 0])
+    for a, gp in enumerate((0.5, 1.0, 3.0)):
+        for b, t in enumerate((-2.0, -0.3, 0.0, 0.7, 4.0)):
+            v = Background.pre_evolution(gp).values(t)
+            np.testing.assert_allclose([v.R, v.R_prime, v.kappa, v.lambda_], g["pre_out"][a, b, :4], rtol=1e-15)
+
+
+def test_lambda_scale_and_handoff_blend(L):
+    from axion_strings_adaptive_gb300 import Background
+    b1 = Background.expanding(2.0, 1.0)
+    b2 = Background.expanding(2.0, 1.0, lambda0=2.0)
+    for tau in (1.0, 2.5, 7.0):
+        assert b2.lambda_(tau) == pytest.approx(2.0 * b1.lambda_(tau), rel=1e-15)
+    # smoothstep blend away from frozen pre-evolution values (AxionStringsLevel.cpp:893-906)
+    import dataclasses
+    bb = dataclasses.replace(b1, blend_dtau=2.0, blend_tau_start=1.0, blend_lambda_start=5.0, blend_curv_start=0.3)
+    c0 = bb.rhs_coeffs(1.0)
+    assert c0.lambda_ == pytest.approx(5.0) and c0.kappa == pytest.approx(0.3)
+    cm = bb.rhs_coeffs(2.0)  # t = 0.5 -> s = 0.5
+    assert cm.lambda_ == pytest.approx(0.5 * 5.0 + 0.5 * b1.lambda_(2.0))
+    c1 = bb.rhs_coeffs(3.5)
+    assert c1.lambda_ == pytest.approx(b1.lambda_(3.5), rel=1e-15)
+
+
+def test_xi_matches_reference(L, golden):
+    from axion_strings_adaptive_gb300 import (plaquette_count_for_target_xi, xi_from_comoving_length,
+                                              xi_from_plaquette_count)
+    g = golden("kats.npz")
+    for x, xi, xil, inv in zip(g["xi_in"], g["xi_out"], g["xi_len_out"], g["xi_inv_out"]):
+        assert xi_from_plaquette_count(*x) == xi
+        assert xi_from_comoving_length((2 / 3) * x[0] * x[1], *x[2:]) == xil
+        assert plaquette_count_for_target_xi(0.7, 64, x[2], x[3], x[4]) == inv
+
+
+def test_validation_rejects_bad_input_without_gpu(L):
+    lib = L.lib()
+    c = L.RhsCoeffs(0.0, 1.0, 1.0)
+    f = L.Fab(None, L.AXS_F64, 8, 8, 8, 2, 4, 12, 144, 1728)
+    assert lib.axs_eval_rhs(C.byref(f), C.byref(f), 0.5, C.byref(c), None) == L.AXS_ERR_INVALID_ARGUMENT
+    assert b"null data" in lib.axs_last_error()
+    f2 = L.Fab(C.c_void_p(256), L.AXS_F64, 8, 8, 8, 2, 4, 11, 144, 1728)  # jstride too small
+    assert lib.axs_eval_rhs(C.byref(f2), C.byref(f2), 0.5, C.byref(c), None) == L.AXS_ERR_INVALID_ARGUMENT
+    assert b"strides" in lib.axs_last_error()
+    f3 = L.Fab(C.c_void_p(256), 7, 8, 8, 8, 2, 4, 12, 144, 1728)
+    assert lib.axs_eval_rhs(C.byref(f3), C.byref(f3), 0.5, C.byref(c), None) == L.AXS_ERR_INVALID_ARGUMENT
+    lay = L.LevelLayout()
+    assert lib.axs_level_layout_for(L.AXS_F32, 6, 8, 8, C.byref(lay)) == L.AXS_ERR_UNSUPPORTED  # nx % 4
+    assert lib.axs_level_layout_for(L.AXS_F32, 8, 1, 8, C.byref(lay)) == L.AXS_ERR_UNSUPPORTED  # ny >= 2
+    assert lib.axs_level_layout_for(L.AXS_F64, 6, 8, 8, C.byref(lay)) == L.AXS_OK
+    assert lay.jstride == 14 and lay.kstride == 14 * 12 and lay.cstride == 14 * 12 * 8
+    assert lay.state_bytes == 4 * lay.cstride * 8 and lay.work_bytes == 8 * lay.cstride * 8 + 256
+    lv = L.LevelC(None, None, L.AXS_F32, 8, 8, 8, 0.5)
+    bg = L.BackgroundC(0, 0, 2.0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0)
+    assert lib.axs_level_rk4_advance(C.byref(lv), C.byref(bg), 1.0, 0.0, 0.1, 1, None) == L.AXS_ERR_INVALID_ARGUMENT
+    lv2 = L.LevelC(C.c_void_p(4096), C.c_void_p(8192), L.AXS_F32, 8, 8, 8, 0.5)
+    assert lib.axs_level_rk4_advance(C.byref(lv2), C.byref(bg), 1.0, 0.0, -0.1, 1, None) == L.AXS_ERR_INVALID_ARGUMENT
+    bad_bg = L.BackgroundC(0, 0, 0.5, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0)  # a_inv <= 1
+    assert lib.axs_level_rk4_advance(C.byref(lv2), C.byref(bad_bg), 1.0, 0.0, 0.1, 1, None) == \
+        L.AXS_ERR_INVALID_ARGUMENT
+    assert lib.axs_level_rk4_advance(C.byref(lv2), C.byref(bg), 1.0, 0.0, 0.1, 0, None) == L.AXS_OK  # no-op
+    b = C.c_int64()
+    assert lib.axs_diagnostics_scratch_bytes(0, 8, 8, C.byref(b)) == L.AXS_ERR_INVALID_ARGUMENT
+    assert lib.axs_plaquette_winding_batch(None, -1, None, None) == L.AXS_ERR_INVALID_ARGUMENT
+    assert lib.axs_plaquette_winding_batch(None, 0, None, None) == L.AXS_OK
+
+
+def test_package_refuses_cpu_tensors():
+    import torch
+
+    import axion_strings_adaptive_gb300 as A
+    with pytest.raises(ValueError, match="CUDA"):
+        A.fab(torch.zeros((4, 8, 8, 8)), 2)
