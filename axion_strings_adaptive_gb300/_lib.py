@@ -96,6 +96,7 @@ SIGNATURES = {
     "axs_diagnostics": (_i32, [C.POINTER(Fab), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr, _i64, _ptr]),
     "axs_level_diagnostics": (_i32, [C.POINTER(LevelC), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr, _i64,
                                      _ptr]),
+    "axs_diagnostics_static_scratch": (_i32, [C.POINTER(Fab), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr]),
     "axs_plaquette_winding_batch": (_i32, [_ptr, _i64, _ptr, _ptr]),
     "axs_fourier_spectrum": (_i32, [_ptr, _i32, _i32, _i32, _dbl, _u64, _i32, _ptr]),
 }

@@ -15,6 +15,7 @@
 // in scratch -> a single-block finalize in a fixed order (deterministic, no
 // floating-point atomics).
 #include <cmath>
+#include <mutex>
 
 #include "axs_internal.cuh"
 
@@ -443,6 +444,68 @@ int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const u
     // not its corners, which the xy plaquette at (nx-1, ny-1) would read
     DiagView v{lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, 4, 2, 0, 1, 1, 1, L.jstride, L.kstride, L.cstride};
     return run_diag(v, p, mask, out, list, capacity, scratch, scratch_bytes, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Diagnostics without caller-provided scratch.
+//
+// Some host codes cannot hand this library any extra device memory: an AMReX
+// application, for instance, gives most of the GPU to its own arena at start-up
+// and expects plugins to work inside the buffers they are passed, and other
+// callers run under a fixed device-memory budget where a cudaMalloc from a
+// plugin is not allowed. For them the diagnostics pass can use the scratch
+// array below, a file-scope device array that every GPU loading this library
+// holds until the process exits. Its size caps the per-block partials the pass
+// needs (256 bytes of header + 160 bytes per block); on a 152-SM GB300 a pass
+// uses at most 1216 blocks, i.e. about 195 KB of the 256 KiB.
+namespace axs {
+constexpr size_t kStaticDiagScratchBytes = 256 * 1024;
+static __device__ __align__(256) unsigned char g_static_diag_scratch[kStaticDiagScratchBytes];
+
+// Device address of g_static_diag_scratch, looked up once per device with that
+// device current (host code must not use the symbol itself as an address).
+static int static_scratch_address(void **out)
+{
+    constexpr int kMaxDevices = 64;
+    static void *addr[kMaxDevices] = {};
+    static std::mutex mu;
+    int dev = 0;
+    AXS_CUDA_CHECK(cudaGetDevice(&dev));
+    AXS_REQUIRE(dev >= 0 && dev < kMaxDevices, AXS_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (addr[dev] == nullptr) {
+        void *p = nullptr;
+        AXS_CUDA_CHECK(cudaGetSymbolAddress(&p, g_static_diag_scratch));
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return AXS_OK;
+}
+}  // namespace axs
+
+extern "C" {
+
+int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *p, const uint8_t *mask,
+                                   axs_diag_result *result_dev, int64_t *pierced_dev, int64_t pierced_capacity,
+                                   void *stream)
+{
+    AXS_REQUIRE(state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null state");
+    const int64_t ncell = (int64_t)state->nx * state->ny * state->nz;
+    AXS_REQUIRE(ncell > 0, AXS_ERR_INVALID_ARGUMENT, "empty box");
+    const int64_t need = diag_scratch_bytes(ncell);
+    AXS_REQUIRE(need <= (int64_t)kStaticDiagScratchBytes, AXS_ERR_WORKSPACE,
+                "diagnostics needs %lld scratch bytes on this device, more than the %lld-byte static array; "
+                "use axs_diagnostics with caller-provided scratch",
+                (long long)need, (long long)kStaticDiagScratchBytes);
+    void *scratch = nullptr;
+    int rc = static_scratch_address(&scratch);
+    if (rc) return rc;
+    // run_diag clears the list counter in the array before the pass; the
+    // per-block partials are overwritten in full.
+    return axs_diagnostics(state, p, mask, result_dev, pierced_dev, pierced_capacity, scratch,
+                           (int64_t)kStaticDiagScratchBytes, stream);
 }
 
 }  // extern "C"

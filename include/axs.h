@@ -243,6 +243,19 @@ int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const u
                           int64_t pierced_capacity, void *scratch_dev, int64_t scratch_bytes,
                           void *stream);
 
+/* axs_diagnostics for callers that cannot give this library device memory
+ * (no counterpart in the reference, which has no GPU path): the per-block
+ * partials live in a 256 KiB static device array inside the library instead of
+ * caller scratch, and the call allocates nothing. Boxes whose pass would need
+ * more than that array are rejected with AXS_ERR_WORKSPACE. The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture on the device. All calls
+ * share the one array, so calls whose work overlaps on the GPU (different
+ * streams or threads) race: serialise them. */
+int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *p, const uint8_t *mask,
+                                   axs_diag_result *result_dev, int64_t *pierced_dev, int64_t pierced_capacity,
+                                   void *stream);
+
 /* plaquette_winding (PlaquetteWinding.hpp:42-51) on n device quadruples
  * theta[4*q .. 4*q+3] -> w[q]: the device winding kernel on caller-chosen
  * phases (known-answer tests). */
