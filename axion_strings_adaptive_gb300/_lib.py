@@ -50,13 +50,13 @@ class BackgroundValues(C.Structure):
 
 
 class LevelLayout(C.Structure):
-    _fields_ = [("jstride", _i64), ("kstride", _i64), ("cstride", _i64), ("state_bytes", _i64),
-                ("work_bytes", _i64)]
+    _fields_ = [("jstride", _i64), ("kstride", _i64), ("cstride", _i64), ("x_offset", _i32), ("y_offset", _i32),
+                ("state_bytes", _i64), ("work_bytes", _i64)]
 
 
 class LevelC(C.Structure):
     _fields_ = [("state", _ptr), ("work", _ptr), ("dtype", _i32), ("nx", _i32), ("ny", _i32), ("nz", _i32),
-                ("dx", _dbl)]
+                ("dx", _dbl), ("tile_config", _i32)]
 
 
 class DiagParams(C.Structure):
@@ -86,6 +86,8 @@ SIGNATURES = {
     "axs_lincomb": (_i32, [C.POINTER(Fab), C.POINTER(Fab), _dbl, C.POINTER(Fab), _ptr]),
     "axs_rk4_combine": (_i32, [C.POINTER(Fab)] * 6 + [_dbl, _ptr]),
     "axs_level_layout_for": (_i32, [_i32, _i32, _i32, _i32, C.POINTER(LevelLayout)]),
+    "axs_level_tile_config_count": (C.c_int, [_i32]),
+    "axs_level_tile_config_name": (C.c_char_p, [_i32, _i32]),
     "axs_level_fill_ghosts": (_i32, [C.POINTER(LevelC), _ptr]),
     "axs_level_import_fab": (_i32, [C.POINTER(LevelC), C.POINTER(Fab), _ptr]),
     "axs_level_export_fab": (_i32, [C.POINTER(LevelC), C.POINTER(Fab), _ptr]),

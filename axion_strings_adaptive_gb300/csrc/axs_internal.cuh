@@ -47,6 +47,15 @@ inline size_t dtype_size(int32_t dt) { return dt == AXS_F64 ? 8 : (dt == AXS_F32
 int device_sm_count();
 int validate_fab(const axs_fab *f, const char *name, int min_comp, int min_ng);
 
+// Geometry of the fused-RK4 level layout (see axs_level_layout in axs.h):
+// element (x,y,z,c) at (x + ox) + (y + oy)*js + z*ks + c*cs. ox puts x = 0
+// on a 128-byte boundary; js is a multiple of 128 bytes.
+struct LevelGeom {
+    int64_t js, ks, cs;
+    int ox, oy;
+};
+int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g);
+
 // Background model (host), shared by the C ABI and the RK4 driver.
 void background_values(const axs_background &bg, double tau, axs_background_values &v);
 void rhs_coeffs(const axs_background &bg, double tau, axs_rhs_coeffs &c);
@@ -65,6 +74,45 @@ template <> struct Vec<double> {
     using type = double2;
     static constexpr int N = 2;
 };
+
+// V consecutive elements of T moved as one vector access (4, 8 or 16 bytes).
+template <typename T, int V> struct VecN;
+template <> struct VecN<float, 1> { using type = float; };
+template <> struct VecN<float, 2> { using type = float2; };
+template <> struct VecN<float, 4> { using type = float4; };
+template <> struct VecN<double, 1> { using type = double; };
+template <> struct VecN<double, 2> { using type = double2; };
+
+template <typename T, int V>
+__device__ __forceinline__ void ldv(const T *p, T *out)
+{
+    using VT = typename VecN<T, V>::type;
+    const VT v = *reinterpret_cast<const VT *>(p);
+    const T *e = reinterpret_cast<const T *>(&v);
+#pragma unroll
+    for (int i = 0; i < V; ++i) out[i] = e[i];
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void ldv_nc(const T *p, T *out)
+{
+    using VT = typename VecN<T, V>::type;
+    const VT v = __ldg(reinterpret_cast<const VT *>(p));
+    const T *e = reinterpret_cast<const T *>(&v);
+#pragma unroll
+    for (int i = 0; i < V; ++i) out[i] = e[i];
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void stv(T *p, const T *in)
+{
+    using VT = typename VecN<T, V>::type;
+    VT v;
+    T *e = reinterpret_cast<T *>(&v);
+#pragma unroll
+    for (int i = 0; i < V; ++i) e[i] = in[i];
+    *reinterpret_cast<VT *>(p) = v;
+}
 
 template <typename T>
 __device__ __forceinline__ void load_vec(const T *p, T *out)

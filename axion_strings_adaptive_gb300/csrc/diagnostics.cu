@@ -14,8 +14,11 @@
 // precision; sums go per thread -> warp shuffle -> block -> per-block partial
 // in scratch -> a single-block finalize in a fixed order (deterministic, no
 // floating-point atomics).
+#include <climits>
 #include <cmath>
 #include <mutex>
+
+#include <algorithm>
 
 #include "axs_internal.cuh"
 
@@ -42,34 +45,24 @@ constexpr int kDiagThreads = 256;
 
 struct DiagConst {
     double one_over_dx, R, lambda, RpR, m_r, threshold;
+    double R2, inv_R, inv_R2, inv_R4;
     int scheme;
     int want_energy, want_plaq, want_vel;
 };
 
 template <typename T>
-__device__ __forceinline__ double ld(const DiagView &v, int c, int i, int j, int k)
+__device__ __forceinline__ int64_t view_off(const DiagView &v, int c, int i, int j, int k)
 {
     if (v.wx) i = (i % v.nx + v.nx) % v.nx;
     if (v.wy) j = (j % v.ny + v.ny) % v.ny;
     if (v.wz) k = (k % v.nz + v.nz) % v.nz;
-    const T *p = static_cast<const T *>(v.data);
-    return (double)__ldg(p + c * v.cs + (int64_t)(i + v.ox) + (int64_t)(j + v.oy) * v.js + (int64_t)(k + v.oz) * v.ks);
+    return c * v.cs + (int64_t)(i + v.ox) + (int64_t)(j + v.oy) * v.js + (int64_t)(k + v.oz) * v.ks;
 }
 
-// GRTeclyn diff1 (centred 4th order, weights 1/12 and 2/3, times 1/dx),
-// rounded to the field precision as d1_scalar returns amrex::Real.
 template <typename T>
-__device__ __forceinline__ double diff1(const DiagView &v, int c, int i, int j, int k, int dir, double inv_dx)
+__device__ __forceinline__ double ld(const DiagView &v, int c, int i, int j, int k)
 {
-    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
-    const double wf = 8.33333333333333333333e-2, wn = 6.66666666666666666667e-1;
-    // reference expression order, no contraction: the result is rounded to the
-    // field precision, so a fused multiply-add could move it by one ulp
-    double r = __dmul_rn(wf, ld<T>(v, c, i - 2 * di, j - 2 * dj, k - 2 * dk));
-    r = __dsub_rn(r, __dmul_rn(wn, ld<T>(v, c, i - di, j - dj, k - dk)));
-    r = __dadd_rn(r, __dmul_rn(wn, ld<T>(v, c, i + di, j + dj, k + dk)));
-    r = __dsub_rn(r, __dmul_rn(wf, ld<T>(v, c, i + 2 * di, j + 2 * dj, k + 2 * dk)));
-    return (double)(T)__dmul_rn(r, inv_dx);
+    return (double)__ldg(static_cast<const T *>(v.data) + view_off<T>(v, c, i, j, k));
 }
 
 __device__ __forceinline__ double wrap_diff(double d, int &near_tie)
@@ -85,6 +78,7 @@ __device__ __forceinline__ double wrap_diff(double d, int &near_tie)
     return d;
 }
 
+// PlaquetteWinding.hpp:42-51 literally, on double phases.
 __device__ __forceinline__ int winding4(double t1, double t2, double t3, double t4, int &ties)
 {
     int n1 = 0, n2 = 0, n3 = 0, n4 = 0;
@@ -97,10 +91,25 @@ __device__ __forceinline__ int winding4(double t1, double t2, double t3, double 
     return (int)llround(__ddiv_rn(total, 2.0 * 3.14159265358979323846));
 }
 
-template <typename T>
-__device__ __forceinline__ double phase(const DiagView &v, int i, int j, int k)
+// Winding from single-precision phases. With every edge difference at least
+// 1e-5 away from +-pi the fold decisions of the reference's double arithmetic
+// are forced (the phases here are within ~1e-6 of the double ones), and the
+// winding is #(d <= -pi) - #(d > pi). Returns false when an edge is inside
+// that band: the caller then redoes the plaquette in double.
+__device__ __forceinline__ bool winding4_fast(float t1, float t2, float t3, float t4, int &w)
 {
-    return atan2(ld<T>(v, 1, i, j, k), ld<T>(v, 0, i, j, k));
+    const float pi = 3.14159265f, band = 1e-5f;
+    const float d[4] = {t2 - t1, t3 - t2, t4 - t3, t1 - t4};
+    int up = 0, down = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const float a = fabsf(d[e]);
+        if (fabsf(a - pi) < band) return false;
+        up += d[e] < -pi;
+        down += d[e] > pi;
+    }
+    w = up - down;
+    return true;
 }
 
 // gamma^2 v^2 at one vertex (VelocityKernel.hpp:525-539 + Velocity.hpp:62-78)
@@ -122,182 +131,288 @@ __device__ __forceinline__ double gvv(const DiagView &v, const DiagConst &q, int
     return term1 - term2;
 }
 
+// GRTeclyn diff1 (centred 4th order: weights 1/12, 2/3, times 1/dx) from
+// the four neighbours, rounded to the field precision as d1_scalar returns
+// amrex::Real. FP32 fields: the reference's expression order with explicit
+// round-to-nearest double operations, since a fused multiply-add could move
+// the rounded float by one ulp. FP64 fields: contraction allowed.
 template <typename T>
-__global__ void __launch_bounds__(kDiagThreads) diag_kernel(const DiagView v, const DiagConst q,
-                                                            const uint8_t *__restrict__ mask,
-                                                            DiagPartial *__restrict__ partials,
-                                                            unsigned long long *__restrict__ list_counter,
-                                                            long long *__restrict__ list, long long capacity)
+__device__ __forceinline__ double diff1_vals(double m2, double m1, double p1, double p2, double inv_dx)
 {
+    const double wf = 8.33333333333333333333e-2, wn = 6.66666666666666666667e-1;
+    if constexpr (sizeof(T) == 4) {
+        double r = __dmul_rn(wf, m2);
+        r = __dsub_rn(r, __dmul_rn(wn, m1));
+        r = __dadd_rn(r, __dmul_rn(wn, p1));
+        r = __dsub_rn(r, __dmul_rn(wf, p2));
+        return (double)(float)__dmul_rn(r, inv_dx);
+    } else {
+        return (wf * m2 - wn * m1 + wn * p1 - wf * p2) * inv_dx;
+    }
+}
+
+// Tiled diagnostics pass. A block owns a DTX x DTY tile of cells and marches
+// in z over a chunk; psi1/psi2 of five planes (tile plus a 2-cell halo) sit in
+// a shared ring for the gradient stencil, and single-precision phases of two
+// vertex planes sit beside them for the windings.
+constexpr int DTX = 32, DTY = 8, DHX = DTX + 4, DHY = DTY + 4;
+static_assert(DTX * DTY == kDiagThreads, "one cell per thread");
+
+template <typename T>
+__global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v, const DiagConst q,
+                                                               const uint8_t *__restrict__ mask,
+                                                               DiagPartial *__restrict__ partials,
+                                                               unsigned long long *__restrict__ list_counter,
+                                                               long long *__restrict__ list, long long capacity,
+                                                               int tiles_x, int ntiles, int zchunk, long long n_items)
+{
+    __shared__ T ps[5][2][DHY][DHX];
+    __shared__ float th[2][DTY + 1][DTX + 1];
+    __shared__ unsigned char thok[2][DTY + 1][DTX + 1];
+    __shared__ int warp_tot[kDiagThreads / 32];
+    __shared__ unsigned long long block_base;
+
     double e[14];
 #pragma unroll
     for (int s = 0; s < 14; ++s) e[s] = 0.0;
     double vsum = 0.0;
     long long cnt[4] = {0, 0, 0, 0};
 
-    const int64_t ncell = (int64_t)v.nx * v.ny * v.nz;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    // Every thread runs the same number of iterations so the block-wide list
-    // compaction below can synchronise.
-    const int64_t iters = (ncell + stride - 1) / stride;
-    __shared__ int warp_tot[kDiagThreads / 32];
-    __shared__ unsigned long long block_base;
-    for (int64_t it = 0; it < iters; ++it) {
-        const int64_t cell = it * stride + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-        const bool in = cell < ncell && (mask == nullptr || mask[cell] != 0);
-        int w[3] = {0, 0, 0};
-        if (in) {
-            const int i = (int)(cell % v.nx), j = (int)((cell / v.nx) % v.ny), k = (int)(cell / ((int64_t)v.nx * v.ny));
-            if (q.want_energy) {
-                const double psi1 = ld<T>(v, 0, i, j, k), psi2 = ld<T>(v, 1, i, j, k);
-                const double Pi1 = ld<T>(v, 2, i, j, k), Pi2 = ld<T>(v, 3, i, j, k);
-                const double psi_sq = psi1 * psi1 + psi2 * psi2;
-                double g1sq = 0.0, g2sq = 0.0, gtsq = 0.0;
+    const int tid = threadIdx.x;
+    const int lx = tid % DTX, ly = tid / DTX;
+    // the allocated extent along each axis (ghost reads stay inside it)
+    const int lo_x = v.wx ? INT_MIN / 2 : -v.ox, hi_x = v.wx ? INT_MAX / 2 : v.nx + v.ox;
+    const int lo_y = v.wy ? INT_MIN / 2 : -v.oy, hi_y = v.wy ? INT_MAX / 2 : v.ny + v.oy;
+
+    for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const int tile = (int)(item % ntiles);
+        const int chunk = (int)(item / ntiles);
+        const int x0 = (tile % tiles_x) * DTX, y0 = (tile / tiles_x) * DTY;
+        const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
+
+        auto load_plane = [&](int z) {
+            const int slot = ((z - za + 2) % 5 + 5) % 5;
+            // planes beyond the allocated ghosts are never needed by a valid
+            // result (the caller's ng covers what it asked for): read zeros
+            const bool zin = v.wz || (z >= -v.oz && z < v.nz + v.oz);
+            for (int idx = tid; idx < 2 * DHX * DHY; idx += kDiagThreads) {
+                const int c = idx / (DHX * DHY);
+                const int r = idx % (DHX * DHY);
+                const int hy = r / DHX, hx = r % DHX;
+                const int xx = x0 - 2 + hx, yy = y0 - 2 + hy;
+                T val = T(0);
+                if (zin && xx >= lo_x && xx < hi_x && yy >= lo_y && yy < hi_y && xx < v.nx + 2 && yy < v.ny + 2)
+                    val = __ldg(static_cast<const T *>(v.data) + view_off<T>(v, c, xx, yy, z));
+                ps[slot][c][hy][hx] = val;
+            }
+        };
+        // single-precision phase of the (DTX+1) x (DTY+1) vertices of plane z
+        auto phases = [&](int z) {
+            const int slot = ((z - za + 2) % 5 + 5) % 5;
+            const int ts = (z - za) & 1;
+            for (int idx = tid; idx < (DTX + 1) * (DTY + 1); idx += kDiagThreads) {
+                const int vy = idx / (DTX + 1), vx = idx % (DTX + 1);
+                const T a = ps[slot][0][vy + 2][vx + 2], b = ps[slot][1][vy + 2][vx + 2];
+                const double m = fmax(fabs((double)a), fabs((double)b));
+                // float conversion keeps the angle to ~1e-7 only away from under/overflow
+                thok[ts][vy][vx] = (m > 1e-30 && m < 1e30) ? 1 : 0;
+                th[ts][vy][vx] = atan2f((float)b, (float)a);
+            }
+        };
+
+        for (int p = -2; p <= 1; ++p) load_plane(za + p);
+        __syncthreads();
+        phases(za);
+
+        for (int m = 0; m < len; ++m) {
+            const int z = za + m;
+            load_plane(z + 2);
+            __syncthreads();
+            phases(z + 1);
+            __syncthreads();
+
+            const int x = x0 + lx, y = y0 + ly;
+            const int64_t cell = (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
+            const bool in = x < v.nx && y < v.ny && (mask == nullptr || mask[cell] != 0);
+            int w[3] = {0, 0, 0};
+            if (in) {
+                const int s0 = ((m + 2) % 5);
+                const int sm1 = (m + 1) % 5, sp1 = (m + 3) % 5, sm2 = m % 5, sp2 = (m + 4) % 5;
+                const int hx = lx + 2, hy = ly + 2;
+                if (q.want_energy) {
+                    const double psi1 = ps[s0][0][hy][hx], psi2 = ps[s0][1][hy][hx];
+                    const double Pi1 = ld<T>(v, 2, x, y, z), Pi2 = ld<T>(v, 3, x, y, z);
+                    const double psi_sq = psi1 * psi1 + psi2 * psi2;
+                    double g[2][3];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const double g1 = diff1<T>(v, 0, i, j, k, d, q.one_over_dx);
-                    const double g2 = diff1<T>(v, 1, i, j, k, d, q.one_over_dx);
-                    g1sq += (double)((T)g1 * (T)g1);
-                    g2sq += (double)((T)g2 * (T)g2);
-                    const double dth = (psi_sq > 0.0) ? (psi1 * g2 - psi2 * g1) / psi_sq : 0.0;
-                    gtsq += dth * dth;
-                }
-                const double R = q.R, R2 = R * R, R4 = R2 * R2;
-                const double c1 = Pi1 - q.RpR * psi1, c2 = Pi2 - q.RpR * psi2;
-                const double dsq = psi_sq - R2;
-                const double pot = 0.25 * q.lambda * dsq * dsq;
-                const double rho = (c1 * c1 + c2 * c2 + (g1sq + g2sq) + pot) / R4;
-                const double thp = (psi_sq > 0.0) ? (psi1 * Pi2 - Pi1 * psi2) / psi_sq : 0.0;
-                const double fa = 1.4142135623730951;
-                const double adot = fa * thp / R;
-                const double akin = 0.5 * adot * adot;
-                const double agrad = 0.5 * fa * fa * gtsq / R2;
-                double rkin = 0.0;
-                if (psi_sq > 0.0) {
-                    const double rd = (psi1 * c1 + psi2 * c2) / sqrt(psi_sq);
-                    rkin = rd * rd / R4;
-                }
-                const double rgrad = (g1sq + g2sq - psi_sq * gtsq) / R4;
-                const double rmass = pot / R4;
-                double wgt = 1.0;
-                if (q.scheme != AXS_MASK_NONE) {
-                    const double mod = sqrt(psi_sq) / R;
-                    if (q.scheme == AXS_MASK_B) {
-                        wgt = (mod >= q.threshold) ? 1.0 : 0.0;
-                    } else {
-                        const double f = 1.0 + (mod - 1.0) / fa;
-                        wgt = f * f;
+                    for (int c = 0; c < 2; ++c) {
+                        g[c][0] = diff1_vals<T>(ps[s0][c][hy][hx - 2], ps[s0][c][hy][hx - 1], ps[s0][c][hy][hx + 1],
+                                                ps[s0][c][hy][hx + 2], q.one_over_dx);
+                        g[c][1] = diff1_vals<T>(ps[s0][c][hy - 2][hx], ps[s0][c][hy - 1][hx], ps[s0][c][hy + 1][hx],
+                                                ps[s0][c][hy + 2][hx], q.one_over_dx);
+                        g[c][2] = diff1_vals<T>(ps[sm2][c][hy][hx], ps[sm1][c][hy][hx], ps[sp1][c][hy][hx],
+                                                ps[sp2][c][hy][hx], q.one_over_dx);
                     }
-                }
-                e[0] += rho;   e[1] += rho * wgt;
-                e[2] += akin;  e[3] += akin * wgt;
-                e[4] += agrad; e[5] += agrad * wgt;
-                e[6] += rkin;  e[7] += rkin * wgt;
-                e[8] += rgrad; e[9] += rgrad * wgt;
-                e[10] += rmass; e[11] += rmass * wgt;
-                e[12] += wgt;  e[13] += 1.0;
-            }
-            if (q.want_plaq || q.want_vel) {
-                const double th000 = phase<T>(v, i, j, k), th100 = phase<T>(v, i + 1, j, k);
-                const double th110 = phase<T>(v, i + 1, j + 1, k), th010 = phase<T>(v, i, j + 1, k);
-                const double th001 = phase<T>(v, i, j, k + 1), th101 = phase<T>(v, i + 1, j, k + 1);
-                const double th011 = phase<T>(v, i, j + 1, k + 1);
-                int ties = 0;
-                w[0] = winding4(th000, th100, th110, th010, ties);
-                w[1] = winding4(th000, th010, th011, th001, ties);
-                w[2] = winding4(th000, th001, th101, th100, ties);
-                cnt[0] += (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
-                cnt[1] += abs(w[0]) + abs(w[1]) + abs(w[2]);
-                cnt[3] += ties;
-                if (q.want_vel && (w[0] | w[1] | w[2])) {
-                    double s = 0.0;
-                    long long c = 0;
-                    if (w[0]) {
-                        s += gvv<T>(v, q, i, j, k) + gvv<T>(v, q, i + 1, j, k) + gvv<T>(v, q, i + 1, j + 1, k) +
-                             gvv<T>(v, q, i, j + 1, k);
-                        c += 4;
-                    }
-                    if (w[1]) {
-                        s += gvv<T>(v, q, i, j, k) + gvv<T>(v, q, i, j + 1, k) + gvv<T>(v, q, i, j + 1, k + 1) +
-                             gvv<T>(v, q, i, j, k + 1);
-                        c += 4;
-                    }
-                    if (w[2]) {
-                        s += gvv<T>(v, q, i, j, k) + gvv<T>(v, q, i, j, k + 1) + gvv<T>(v, q, i + 1, j, k + 1) +
-                             gvv<T>(v, q, i + 1, j, k);
-                        c += 4;
-                    }
-                    vsum += s;
-                    cnt[2] += c;
-                }
-            }
-        }
-        // ---- compaction of the pierced plaquettes of this iteration ----
-        if (q.want_plaq && list != nullptr) {
-            const int mine = (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
-            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-            int incl = mine;
+                    double g1sq = 0.0, g2sq = 0.0, cross2 = 0.0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            if (lane == 31) warp_tot[warp] = incl;
-            __syncthreads();
-            int warp_off = 0, block_tot = 0;
-            for (int ww = 0; ww < kDiagThreads / 32; ++ww) {
-                if (ww < warp) warp_off += warp_tot[ww];
-                block_tot += warp_tot[ww];
-            }
-            if (threadIdx.x == 0) block_base = block_tot ? atomicAdd(list_counter, (unsigned long long)block_tot) : 0ull;
-            __syncthreads();
-            if (mine) {
-                long long pos = (long long)block_base + warp_off + incl - mine;
-                const long long base_entry = 4LL * cell;
-                for (int pl = 0; pl < 3; ++pl) {
-                    if (w[pl]) {
-                        if (pos < capacity) list[pos] = base_entry + pl;
-                        ++pos;
+                    for (int d = 0; d < 3; ++d) {
+                        g1sq += (double)((T)g[0][d] * (T)g[0][d]);
+                        g2sq += (double)((T)g[1][d] * (T)g[1][d]);
+                        const double cr = psi1 * g[1][d] - psi2 * g[0][d];
+                        cross2 += cr * cr;
+                    }
+                    const double inv_psq = psi_sq > 0.0 ? 1.0 / psi_sq : 0.0;
+                    const double gtsq = cross2 * inv_psq * inv_psq;
+                    const double c1 = Pi1 - q.RpR * psi1, c2 = Pi2 - q.RpR * psi2;
+                    const double dsq = psi_sq - q.R2;
+                    const double pot = 0.25 * q.lambda * dsq * dsq;
+                    const double rho = (c1 * c1 + c2 * c2 + (g1sq + g2sq) + pot) * q.inv_R4;
+                    const double thp = (psi1 * Pi2 - Pi1 * psi2) * inv_psq;
+                    const double fa = 1.4142135623730951;
+                    const double akin = 0.5 * (fa * thp * q.inv_R) * (fa * thp * q.inv_R);
+                    const double agrad = 0.5 * fa * fa * gtsq * q.inv_R2;
+                    const double rdot = psi1 * c1 + psi2 * c2;
+                    const double rkin = rdot * rdot * inv_psq * q.inv_R4;
+                    const double rgrad = (g1sq + g2sq - psi_sq * gtsq) * q.inv_R4;
+                    const double rmass = pot * q.inv_R4;
+                    double wgt = 1.0;
+                    if (q.scheme != AXS_MASK_NONE) {
+                        const double mod = sqrt(psi_sq) * q.inv_R;
+                        if (q.scheme == AXS_MASK_B) {
+                            wgt = (mod >= q.threshold) ? 1.0 : 0.0;
+                        } else {
+                            const double f = 1.0 + (mod - 1.0) / fa;
+                            wgt = f * f;
+                        }
+                    }
+                    e[0] += rho;   e[1] += rho * wgt;
+                    e[2] += akin;  e[3] += akin * wgt;
+                    e[4] += agrad; e[5] += agrad * wgt;
+                    e[6] += rkin;  e[7] += rkin * wgt;
+                    e[8] += rgrad; e[9] += rgrad * wgt;
+                    e[10] += rmass; e[11] += rmass * wgt;
+                    e[12] += wgt;  e[13] += 1.0;
+                }
+                if (q.want_plaq || q.want_vel) {
+                    const int t0 = m & 1, t1 = (m + 1) & 1;
+                    // corner phases (x, y, z offsets) in the reference's order
+                    const float f000 = th[t0][ly][lx], f100 = th[t0][ly][lx + 1], f110 = th[t0][ly + 1][lx + 1];
+                    const float f010 = th[t0][ly + 1][lx], f001 = th[t1][ly][lx], f101 = th[t1][ly][lx + 1];
+                    const float f011 = th[t1][ly + 1][lx];
+                    const bool ok = thok[t0][ly][lx] & thok[t0][ly][lx + 1] & thok[t0][ly + 1][lx + 1] &
+                                    thok[t0][ly + 1][lx] & thok[t1][ly][lx] & thok[t1][ly][lx + 1] &
+                                    thok[t1][ly + 1][lx];
+                    bool fast = ok;
+                    if (fast) fast = winding4_fast(f000, f100, f110, f010, w[0]);
+                    if (fast) fast = winding4_fast(f000, f010, f011, f001, w[1]);
+                    if (fast) fast = winding4_fast(f000, f001, f101, f100, w[2]);
+                    if (!fast) {
+                        // near the branch cut or outside the float range: the reference's
+                        // double arithmetic for this cell's three plaquettes
+                        const int sz1 = (m + 3) % 5;
+                        auto dph = [&](int slot, int ox_, int oy_) {
+                            return atan2((double)ps[slot][1][hy + oy_][hx + ox_], (double)ps[slot][0][hy + oy_][hx + ox_]);
+                        };
+                        const double d000 = dph(s0, 0, 0), d100 = dph(s0, 1, 0), d110 = dph(s0, 1, 1);
+                        const double d010 = dph(s0, 0, 1), d001 = dph(sz1, 0, 0), d101 = dph(sz1, 1, 0);
+                        const double d011 = dph(sz1, 0, 1);
+                        int ties = 0;
+                        w[0] = winding4(d000, d100, d110, d010, ties);
+                        w[1] = winding4(d000, d010, d011, d001, ties);
+                        w[2] = winding4(d000, d001, d101, d100, ties);
+                        cnt[3] += ties;
+                    }
+                    cnt[0] += (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
+                    cnt[1] += abs(w[0]) + abs(w[1]) + abs(w[2]);
+                    if (q.want_vel && (w[0] | w[1] | w[2])) {
+                        double s = 0.0;
+                        long long c = 0;
+                        if (w[0]) {
+                            s += gvv<T>(v, q, x, y, z) + gvv<T>(v, q, x + 1, y, z) + gvv<T>(v, q, x + 1, y + 1, z) +
+                                 gvv<T>(v, q, x, y + 1, z);
+                            c += 4;
+                        }
+                        if (w[1]) {
+                            s += gvv<T>(v, q, x, y, z) + gvv<T>(v, q, x, y + 1, z) + gvv<T>(v, q, x, y + 1, z + 1) +
+                                 gvv<T>(v, q, x, y, z + 1);
+                            c += 4;
+                        }
+                        if (w[2]) {
+                            s += gvv<T>(v, q, x, y, z) + gvv<T>(v, q, x, y, z + 1) + gvv<T>(v, q, x + 1, y, z + 1) +
+                                 gvv<T>(v, q, x + 1, y, z);
+                            c += 4;
+                        }
+                        vsum += s;
+                        cnt[2] += c;
                     }
                 }
             }
-            __syncthreads();
+            // ---- compaction of the pierced plaquettes of this plane ----
+            if (q.want_plaq && list != nullptr) {
+                const int mine = (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
+                const int lane = tid & 31, warp = tid >> 5;
+                int incl = mine;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int yv = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += yv;
+                }
+                if (lane == 31) warp_tot[warp] = incl;
+                __syncthreads();
+                int warp_off = 0, block_tot = 0;
+                for (int ww = 0; ww < kDiagThreads / 32; ++ww) {
+                    if (ww < warp) warp_off += warp_tot[ww];
+                    block_tot += warp_tot[ww];
+                }
+                if (tid == 0) block_base = block_tot ? atomicAdd(list_counter, (unsigned long long)block_tot) : 0ull;
+                __syncthreads();
+                if (mine) {
+                    long long pos = (long long)block_base + warp_off + incl - mine;
+                    for (int pl = 0; pl < 3; ++pl) {
+                        if (w[pl]) {
+                            if (pos < capacity) list[pos] = 4LL * cell + pl;
+                            ++pos;
+                        }
+                    }
+                }
+            }
+            __syncthreads();  // ring slots and phase planes are rewritten next plane
         }
     }
 
     // ---- block reduction (fixed order) ----
     __shared__ double red_d[kDiagThreads / 32][15];
     __shared__ long long red_l[kDiagThreads / 32][4];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int s = 0; s < 14; ++s) {
-        double x = e[s];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) red_d[warp][s] = x;
+        double xv = e[s];
+        for (int o = 16; o > 0; o >>= 1) xv += __shfl_down_sync(0xffffffffu, xv, o);
+        if (lane == 0) red_d[warp][s] = xv;
     }
     {
-        double x = vsum;
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) red_d[warp][14] = x;
+        double xv = vsum;
+        for (int o = 16; o > 0; o >>= 1) xv += __shfl_down_sync(0xffffffffu, xv, o);
+        if (lane == 0) red_d[warp][14] = xv;
     }
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        long long x = cnt[s];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) red_l[warp][s] = x;
+        long long xv = cnt[s];
+        for (int o = 16; o > 0; o >>= 1) xv += __shfl_down_sync(0xffffffffu, xv, o);
+        if (lane == 0) red_l[warp][s] = xv;
     }
     __syncthreads();
-    if (threadIdx.x < 15) {
-        double x = 0.0;
-        for (int ww = 0; ww < kDiagThreads / 32; ++ww) x += red_d[ww][threadIdx.x];
-        if (threadIdx.x < 14)
-            partials[blockIdx.x].e[threadIdx.x] = x;
+    if (tid < 15) {
+        double xv = 0.0;
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red_d[ww][tid];
+        if (tid < 14)
+            partials[blockIdx.x].e[tid] = xv;
         else
-            partials[blockIdx.x].vsum = x;
-    } else if (threadIdx.x >= 32 && threadIdx.x < 36) {
-        long long x = 0;
-        for (int ww = 0; ww < kDiagThreads / 32; ++ww) x += red_l[ww][threadIdx.x - 32];
-        partials[blockIdx.x].cnt[threadIdx.x - 32] = x;
+            partials[blockIdx.x].vsum = xv;
+    } else if (tid >= 32 && tid < 36) {
+        long long xv = 0;
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red_l[ww][tid - 32];
+        partials[blockIdx.x].cnt[tid - 32] = xv;
     }
 }
 
@@ -353,6 +468,7 @@ __global__ void diag_finalize_kernel(const DiagPartial *__restrict__ partials, i
     }
 }
 
+// Upper bound on the blocks a pass launches (the scratch is sized for it).
 static int diag_grid(int64_t ncell)
 {
     const int sms = device_sm_count();
@@ -360,6 +476,23 @@ static int diag_grid(int64_t ncell)
     const int64_t cap = (int64_t)(sms > 0 ? sms : 148) * 8;
     if (g > cap) g = cap;
     return (int)(g < 1 ? 1 : g);
+}
+
+// Work items (tile, z-chunk), tile fastest; chunks long enough to amortise
+// the 4 warm-up planes while giving every resident block several items.
+static void diag_plan(const DiagView &v, int max_grid, int &tiles_x, int &ntiles, int &zchunk, long long &items,
+                      int &grid)
+{
+    tiles_x = (v.nx + DTX - 1) / DTX;
+    ntiles = tiles_x * ((v.ny + DTY - 1) / DTY);
+    const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
+    const long long resident = 2LL * sms;
+    int nch = (int)std::max<long long>(1, (4 * resident + ntiles - 1) / ntiles);
+    zchunk = std::max(1, (v.nz + nch - 1) / nch);
+    if (zchunk < 16 && v.nz >= 16) zchunk = 16;
+    if (zchunk > v.nz) zchunk = v.nz;
+    items = (long long)ntiles * ((v.nz + zchunk - 1) / zchunk);
+    grid = (int)std::min<long long>(std::min<long long>(items, resident), max_grid);
 }
 
 static int64_t diag_scratch_bytes(int64_t ncell) { return 256 + (int64_t)diag_grid(ncell) * sizeof(DiagPartial); }
@@ -382,6 +515,10 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     DiagConst q{};
     q.one_over_dx = 1.0 / p->dx;
     q.R = p->R;
+    q.R2 = p->R * p->R;
+    q.inv_R = 1.0 / p->R;
+    q.inv_R2 = 1.0 / q.R2;
+    q.inv_R4 = q.inv_R2 * q.inv_R2;
     q.lambda = p->lambda;
     q.RpR = p->R_prime_over_R;
     q.m_r = p->m_r;
@@ -393,12 +530,16 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     auto *counter = static_cast<unsigned long long *>(scratch);
     auto *partials = reinterpret_cast<DiagPartial *>(static_cast<char *>(scratch) + 256);
     AXS_CUDA_CHECK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
-    const int grid = diag_grid(ncell);
+    int tiles_x, ntiles, zchunk, grid;
+    long long items;
+    diag_plan(v, diag_grid(ncell), tiles_x, ntiles, zchunk, items, grid);
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
     if (v.dtype == AXS_F64)
-        diag_kernel<double><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity);
+        diag_kernel<double><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
+                                                           ntiles, zchunk, items);
     else
-        diag_kernel<float><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity);
+        diag_kernel<float><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
+                                                          ntiles, zchunk, items);
     int rc = launch_status("diagnostics");
     if (rc) return rc;
     diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
@@ -436,13 +577,13 @@ int axs_diagnostics(const axs_fab *state, const axs_diag_params *p, const uint8_
 int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const uint8_t *mask, axs_diag_result *out,
                           int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, void *stream)
 {
-    axs_level_layout L;
+    LevelGeom g;
     AXS_REQUIRE(lv != nullptr && lv->state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null level");
-    int rc = axs_level_layout_for(lv->dtype, lv->nx, lv->ny, lv->nz, &L);
+    int rc = level_geom(lv->dtype, lv->nx, lv->ny, lv->nz, g);
     if (rc) return rc;
     // indices wrap on every axis: the sweeps keep the x/y padding current but
     // not its corners, which the xy plaquette at (nx-1, ny-1) would read
-    DiagView v{lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, 4, 2, 0, 1, 1, 1, L.jstride, L.kstride, L.cstride};
+    DiagView v{lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g.ox, g.oy, 0, 1, 1, 1, g.js, g.ks, g.cs};
     return run_diag(v, p, mask, out, list, capacity, scratch, scratch_bytes, (cudaStream_t)stream);
 }
 

@@ -156,9 +156,9 @@ __global__ void rk4_combine_kernel(const axs_fab d, const axs_fab u, const axs_f
 }
 
 // ---------------------------------------------------------------- level <-> FAB
-// Level layout: (x+4) + (y+2)*js + z*ks + c*cs (see axs_level_layout).
+// Level layout: (x + ox) + (y + oy)*js + z*ks + c*cs (see axs_level_layout).
 template <typename T>
-__global__ void level_from_fab_kernel(T *lv, int64_t js, int64_t ks, int64_t cs, const axs_fab f, int to_level)
+__global__ void level_from_fab_kernel(T *lv, LevelGeom g, const axs_fab f, int to_level)
 {
     T *fp = static_cast<T *>(f.data);
     const int64_t nc = (int64_t)f.nx * f.ny * f.nz;
@@ -166,7 +166,7 @@ __global__ void level_from_fab_kernel(T *lv, int64_t js, int64_t ks, int64_t cs,
         const int64_t cell = q % nc;
         const int c = (int)(q / nc);
         const int i = (int)(cell % f.nx), j = (int)((cell / f.nx) % f.ny), k = (int)(cell / ((int64_t)f.nx * f.ny));
-        const int64_t lo = c * cs + (i + 4) + (int64_t)(j + 2) * js + (int64_t)k * ks;
+        const int64_t lo = c * g.cs + (i + g.ox) + (int64_t)(j + g.oy) * g.js + (int64_t)k * g.ks;
         const int64_t fo = c * f.cstride + fab_off(f, i, j, k);
         if (to_level)
             lv[lo] = fp[fo];
@@ -175,9 +175,10 @@ __global__ void level_from_fab_kernel(T *lv, int64_t js, int64_t ks, int64_t cs,
     }
 }
 
-// Periodic copies in the x/y padding of `ncomp` level components (corners included).
+// Periodic copies in the 4-column x and 2-row y padding of `ncomp` level
+// components (corners included).
 template <typename T>
-__global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs, int ncomp)
+__global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, LevelGeom g, int ncomp)
 {
     const int px = nx + 8, py = ny + 4;
     const int64_t n = (int64_t)px * py * nz * ncomp;
@@ -188,8 +189,8 @@ __global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, int64_t 
         const int c = (int)(q / ((int64_t)px * py * nz));
         if (x >= 0 && x < nx && y >= 0 && y < ny) continue;
         const int xx = ((x % nx) + nx) % nx, yy = ((y % ny) + ny) % ny;
-        T *base = lv + c * cs + (int64_t)z * ks;
-        base[(x + 4) + (int64_t)(y + 2) * js] = base[(xx + 4) + (int64_t)(yy + 2) * js];
+        T *base = lv + c * g.cs + (int64_t)z * g.ks;
+        base[(x + g.ox) + (int64_t)(y + g.oy) * g.js] = base[(xx + g.ox) + (int64_t)(yy + g.oy) * g.js];
     }
 }
 
@@ -209,25 +210,24 @@ static int same_shape(const axs_fab *a, const axs_fab *b, const char *what)
     return AXS_OK;
 }
 
-int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
-                      int ncomp, cudaStream_t st)
+int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, int ncomp,
+                      cudaStream_t st)
 {
     const int64_t n = (int64_t)(nx + 8) * (ny + 4) * nz * ncomp;
     if (dtype == AXS_F64)
-        level_fill_ghosts_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(data), nx, ny, nz, js, ks, cs, ncomp);
+        level_fill_ghosts_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(data), nx, ny, nz, g, ncomp);
     else
-        level_fill_ghosts_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(data), nx, ny, nz, js, ks, cs, ncomp);
+        level_fill_ghosts_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(data), nx, ny, nz, g, ncomp);
     return launch_status("level_fill_ghosts");
 }
 
-int level_copy_fab(void *lv, int32_t dtype, int64_t js, int64_t ks, int64_t cs, const axs_fab &f, int to_level,
-                   cudaStream_t st)
+int level_copy_fab(void *lv, int32_t dtype, const LevelGeom &g, const axs_fab &f, int to_level, cudaStream_t st)
 {
     const int64_t n = (int64_t)f.nx * f.ny * f.nz * 4;
     if (dtype == AXS_F64)
-        level_from_fab_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(lv), js, ks, cs, f, to_level);
+        level_from_fab_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(lv), g, f, to_level);
     else
-        level_from_fab_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(lv), js, ks, cs, f, to_level);
+        level_from_fab_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(lv), g, f, to_level);
     return launch_status("level_copy_fab");
 }
 

@@ -5,9 +5,9 @@
 // (AxionStringsRHS.impl.hpp:44-59) has stage states whose psi parts are
 //   psi_n, psi_n + h/2 Pi_n, psi_n + h/2 Pi_n + h^2/4 F1, psi_n + h Pi_n + h^2/2 F2
 // so the four stage RHS evaluations pair up:
-//   sweep A reads (psi_n, Pi_n)   and evaluates F1 = F(t, psi_n),
-//                                               F2 = F(t+h/2, psi_n + h/2 Pi_n);
-//   sweep B reads (S3, S4)        and evaluates F3 = F(t+h/2, S3), F4 = F(t+h, S4),
+//   sweep A reads (psi_n, Pi_n) and evaluates F1 = F(t, psi_n),
+//                                             F2 = F(t+h/2, psi_n + h/2 Pi_n);
+//   sweep B reads (S3, S4)      and evaluates F3 = F(t+h/2, S3), F4 = F(t+h, S4),
 // with S3 = psi_n + h/2 Pi_n + h^2/4 F1, S4 = psi_n + h Pi_n + h^2/2 F2 and
 //   psi_{n+1} = S4 + h^2/6 (F1 - 2 F2 + F3),
 //   Pi_{n+1}  = [Pi_n + h/6 F1 + h/3 F2] + h/3 F3 + h/6 F4,
@@ -20,11 +20,11 @@
 // one 4D TMA load per plane ({x, y, z, component} box of (TX+8) x (TY+4) x 1 x 4,
 // the 4 stencil components at once) into an NS-slot shared-memory ring,
 // completion signalled through an mbarrier per slot; all waits are bounded.
-// Periodic halos in x/y come from padding columns/rows that every sweep
-// rewrites when it writes a boundary site; z wraps by plane index. Work items
-// (tile, z-chunk) are numbered tile-fastest so the blocks resident at any
-// moment work on neighbouring tiles of the same z range and share halo
-// planes in L2.
+// Each thread owns V consecutive x sites of one row. Periodic halos in x/y
+// come from padding columns/rows that every sweep rewrites when it writes a
+// boundary site; z wraps by plane index. Work items (tile, z-chunk) are
+// numbered tile-fastest so the blocks resident at any moment work on
+// neighbouring tiles of the same z range.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -33,10 +33,9 @@
 
 namespace axs {
 
-int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
-                      int ncomp, cudaStream_t st);
-int level_copy_fab(void *lv, int32_t dtype, int64_t js, int64_t ks, int64_t cs, const axs_fab &f, int to_level,
-                   cudaStream_t st);
+int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, int ncomp,
+                      cudaStream_t st);
+int level_copy_fab(void *lv, int32_t dtype, const LevelGeom &g, const axs_fab &f, int to_level, cudaStream_t st);
 
 template <typename T> struct StageCoef {
     T kappa, hlam, R2;  // kappa, lambda/2, R^2 at one stage time
@@ -47,6 +46,7 @@ template <typename T> struct SweepArgs {
     int tiles_x, ntiles, zchunk;
     int64_t n_items;
     int64_t js, ks, cs;
+    int ox;                     // x offset of the valid region in a padded row
     T wA, wB, wC;               // lap = wA*S1 + wB*S2 + wC*f0 (S1/S2: sums of +-1 / +-2 neighbours)
     StageCoef<T> ca, cb;        // sweep A: F1, F2; sweep B: F3, F4
     T h, h_half, h2_quarter, h2_half, h_sixth, h_third, h2_sixth;
@@ -55,8 +55,7 @@ template <typename T> struct SweepArgs {
     unsigned *status;
 };
 
-template <typename T, int TX, int TY> struct SweepShape {
-    static constexpr int V = Vec<T>::N;
+template <typename T, int V, int TX, int TY> struct SweepShape {
     static constexpr int NTX = TX / V;
     static constexpr int NT = NTX * TY;
     static constexpr int BX = TX + 8;
@@ -64,29 +63,30 @@ template <typename T, int TX, int TY> struct SweepShape {
     static constexpr int TILE = BX * BY;
     static constexpr int SLOT = 4 * TILE;
     static constexpr uint32_t SLOT_BYTES = SLOT * sizeof(T);
-    static_assert(TX % V == 0, "tile width must hold whole vectors");
+    static constexpr int PRE = (2 + V - 1) / V;  // vectors left/right of the centre that cover +-2
+    static constexpr int NROW = 2 * PRE + 1;
+    static_assert(TX % V == 0 && 4 % V == 0, "tile width and halo must hold whole vectors");
     static_assert((BX * sizeof(T)) % 16 == 0, "TMA box row must be a multiple of 16 bytes");
     static_assert(SLOT_BYTES % 128 == 0, "ring slots must stay 128-byte aligned");
     static_assert(BX <= 256 && BY <= 256, "TMA box extent limit");
 };
 
-template <typename T>
+template <typename T, int V>
 __device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
                                                   const T *v)
 {
-    store_vec(base + off, v);
-    if (x < 4) store_vec(base + off + nx, v);
-    if (x >= nx - 4) store_vec(base + off - nx, v);
-    if (y < 2) store_vec(base + off + (int64_t)ny * js, v);
-    if (y >= ny - 2) store_vec(base + off - (int64_t)ny * js, v);
+    stv<T, V>(base + off, v);
+    if (x < 4) stv<T, V>(base + off + nx, v);
+    if (x >= nx - 4) stv<T, V>(base + off - nx, v);
+    if (y < 2) stv<T, V>(base + off + (int64_t)ny * js, v);
+    if (y >= ny - 2) stv<T, V>(base + off - (int64_t)ny * js, v);
 }
 
-template <typename T, int TX, int TY, int NS, int SWEEP>
-__global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
+template <typename T, int V, int TX, int TY, int NS, int MINB, int SWEEP>
+__global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     rk4_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
 {
-    using S = SweepShape<T, TX, TY>;
-    constexpr int V = S::V;
+    using S = SweepShape<T, V, TX, TY>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *ring = reinterpret_cast<T *>(smem_raw);
     __shared__ uint64_t full[NS];
@@ -117,8 +117,9 @@ __global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
         if (zp < 0) zp += a.nz;
         const int slot = (int)(q_issued % NS);
         mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
-        tma_load_4d(ring + (size_t)slot * S::SLOT, &tmap, (tile % a.tiles_x) * TX, (tile / a.tiles_x) * TY, zp, 0,
-                    &full[slot]);
+        // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned)
+        tma_load_4d(ring + (size_t)slot * S::SLOT, &tmap, a.ox - 4 + (tile % a.tiles_x) * TX,
+                    (tile / a.tiles_x) * TY, zp, 0, &full[slot]);
         ++q_issued;
         if (++p_k == len + 4) {
             p_k = 0;
@@ -143,18 +144,36 @@ __global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
         const int x = (tile % a.tiles_x) * TX + V * tx;
         const int y = (tile / a.tiles_x) * TY + ty;
         const bool active = (x < a.nx) && (y < a.ny);
+        // sweep B: the pointwise increments (G, P) of the next plane are loaded
+        // one iteration ahead, so their latency hides behind a whole plane of work
+        T gn[2][V], pn[2][V];
+        if constexpr (SWEEP == 1) {
+            if (active) {
+                const int64_t off0 = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)za * a.ks;
+                ldv_nc<T, V>(a.work + 4 * a.cs + off0, gn[0]);
+                ldv_nc<T, V>(a.work + 5 * a.cs + off0, gn[1]);
+                ldv_nc<T, V>(a.work + 6 * a.cs + off0, pn[0]);
+                ldv_nc<T, V>(a.work + 7 * a.cs + off0, pn[1]);
+            }
+        }
         for (int m = 0; m < len; ++m) {
             const int z = za + m;
-            const int64_t off = (int64_t)(x + 4) + (int64_t)(y + 2) * a.js + (int64_t)z * a.ks;
+            const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)z * a.ks;
 
-            // sweep B: pointwise increments, issued before the wait to overlap latency
             T gq[2][V], pq[2][V];
             if constexpr (SWEEP == 1) {
-                if (active) {
-                    load_vec_global_nc(a.work + 4 * a.cs + off, gq[0]);
-                    load_vec_global_nc(a.work + 5 * a.cs + off, gq[1]);
-                    load_vec_global_nc(a.work + 6 * a.cs + off, pq[0]);
-                    load_vec_global_nc(a.work + 7 * a.cs + off, pq[1]);
+#pragma unroll
+                for (int i = 0; i < 2; ++i)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        gq[i][v] = gn[i][v];
+                        pq[i][v] = pn[i][v];
+                    }
+                if (active && m + 1 < len) {
+                    ldv_nc<T, V>(a.work + 4 * a.cs + off + a.ks, gn[0]);
+                    ldv_nc<T, V>(a.work + 5 * a.cs + off + a.ks, gn[1]);
+                    ldv_nc<T, V>(a.work + 6 * a.cs + off + a.ks, pn[0]);
+                    ldv_nc<T, V>(a.work + 7 * a.cs + off + a.ks, pn[1]);
                 }
             }
 
@@ -177,23 +196,23 @@ __global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     const T *P0 = sl[2] + c * S::TILE;
-                    T row[3 * V], ym1[V], yp1[V], ym2[V], yp2[V], zm1[V], zp1[V], zm2[V], zp2[V];
-                    load_vec(P0 + yl * S::BX + xl - V, row);
-                    load_vec(P0 + yl * S::BX + xl, row + V);
-                    load_vec(P0 + yl * S::BX + xl + V, row + 2 * V);
-                    load_vec(P0 + (yl - 1) * S::BX + xl, ym1);
-                    load_vec(P0 + (yl + 1) * S::BX + xl, yp1);
-                    load_vec(P0 + (yl - 2) * S::BX + xl, ym2);
-                    load_vec(P0 + (yl + 2) * S::BX + xl, yp2);
-                    load_vec(sl[1] + c * S::TILE + yl * S::BX + xl, zm1);
-                    load_vec(sl[3] + c * S::TILE + yl * S::BX + xl, zp1);
-                    load_vec(sl[0] + c * S::TILE + yl * S::BX + xl, zm2);
-                    load_vec(sl[4] + c * S::TILE + yl * S::BX + xl, zp2);
+                    T row[S::NROW * V], ym1[V], yp1[V], ym2[V], yp2[V], zm1[V], zp1[V], zm2[V], zp2[V];
+#pragma unroll
+                    for (int r = 0; r < S::NROW; ++r) ldv<T, V>(P0 + yl * S::BX + xl + (r - S::PRE) * V, row + r * V);
+                    ldv<T, V>(P0 + (yl - 1) * S::BX + xl, ym1);
+                    ldv<T, V>(P0 + (yl + 1) * S::BX + xl, yp1);
+                    ldv<T, V>(P0 + (yl - 2) * S::BX + xl, ym2);
+                    ldv<T, V>(P0 + (yl + 2) * S::BX + xl, yp2);
+                    ldv<T, V>(sl[1] + c * S::TILE + yl * S::BX + xl, zm1);
+                    ldv<T, V>(sl[3] + c * S::TILE + yl * S::BX + xl, zp1);
+                    ldv<T, V>(sl[0] + c * S::TILE + yl * S::BX + xl, zm2);
+                    ldv<T, V>(sl[4] + c * S::TILE + yl * S::BX + xl, zp2);
 #pragma unroll
                     for (int v = 0; v < V; ++v) {
-                        const T f0 = row[V + v];
-                        const T s1 = (row[V + v - 1] + row[V + v + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
-                        const T s2 = (row[V + v - 2] + row[V + v + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
+                        const int ci = S::PRE * V + v;
+                        const T f0 = row[ci];
+                        const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
+                        const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
                         lap[c][v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
                         ctr[c][v] = f0;
                     }
@@ -213,20 +232,20 @@ __global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
                         const T k2 = fma(-a.cb.hlam, fma(c1, c1, c2 * c2) - a.cb.R2, a.cb.kappa);
                         const T f21 = fma(k2, c1, fma(a.h_half, lap[2][v], lap[0][v]));
                         const T f22 = fma(k2, c2, fma(a.h_half, lap[3][v], lap[1][v]));
-                        o[0][v] = fma(a.h2_quarter, f11, c1);                // S3
+                        o[0][v] = fma(a.h2_quarter, f11, c1);                     // S3
                         o[1][v] = fma(a.h2_quarter, f12, c2);
-                        o[2][v] = fma(a.h2_half, f21, fma(a.h, q1, p1));    // S4
+                        o[2][v] = fma(a.h2_half, f21, fma(a.h, q1, p1));          // S4
                         o[3][v] = fma(a.h2_half, f22, fma(a.h, q2, p2));
-                        o[4][v] = fma(T(-2), f21, f11);                    // G = F1 - 2 F2
+                        o[4][v] = fma(T(-2), f21, f11);                          // G = F1 - 2 F2
                         o[5][v] = fma(T(-2), f22, f12);
                         o[6][v] = fma(a.h_third, f21, fma(a.h_sixth, f11, q1));  // P = Pi + h/6 F1 + h/3 F2
                         o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
                     }
 #pragma unroll
                     for (int c = 0; c < 4; ++c)
-                        store_with_copies(a.work + c * a.cs, off, x, y, a.nx, a.ny, a.js, o[c]);
+                        store_with_copies<T, V>(a.work + c * a.cs, off, x, y, a.nx, a.ny, a.js, o[c]);
 #pragma unroll
-                    for (int c = 4; c < 8; ++c) store_vec(a.work + c * a.cs + off, o[c]);
+                    for (int c = 4; c < 8; ++c) stv<T, V>(a.work + c * a.cs + off, o[c]);
                 } else {
                     T o[4][V];
 #pragma unroll
@@ -245,7 +264,7 @@ __global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
                     }
 #pragma unroll
                     for (int c = 0; c < 4; ++c)
-                        store_with_copies(a.state + c * a.cs, off, x, y, a.nx, a.ny, a.js, o[c]);
+                        store_with_copies<T, V>(a.state + c * a.cs, off, x, y, a.nx, a.ny, a.js, o[c]);
                 }
             }
 
@@ -272,11 +291,7 @@ __global__ void __launch_bounds__(SweepShape<T, TX, TY>::NT, 1)
 }
 
 // ---------------------------------------------------------------- host side
-struct LevelGeom {
-    int64_t js, ks, cs;
-};
-
-static int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g)
+int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g)
 {
     AXS_REQUIRE(dtype == AXS_F32 || dtype == AXS_F64, AXS_ERR_INVALID_ARGUMENT, "bad dtype %d", dtype);
     AXS_REQUIRE(nx > 0 && ny > 0 && nz > 0, AXS_ERR_INVALID_ARGUMENT, "empty level %dx%dx%d", nx, ny, nz);
@@ -284,7 +299,10 @@ static int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g)
     AXS_REQUIRE(nx % V == 0 && nx >= 4, AXS_ERR_UNSUPPORTED, "level nx must be a multiple of %d and >= 4 (got %d)", V,
                 nx);
     AXS_REQUIRE(ny >= 2, AXS_ERR_UNSUPPORTED, "level ny must be >= 2 (got %d)", ny);
-    g.js = nx + 8;
+    const int line = 128 / (int)dtype_size(dtype);  // elements per 128-byte line
+    g.ox = line;                                     // x = 0 starts a line; 4 periodic columns sit left of it
+    g.oy = 2;
+    g.js = ((int64_t)nx + g.ox + 4 + line - 1) / line * line;
     g.ks = g.js * (ny + 4);
     g.cs = g.ks * nz;
     return AXS_OK;
@@ -297,8 +315,8 @@ static int validate_level(const axs_level *lv, LevelGeom &g)
     int rc = level_geom(lv->dtype, lv->nx, lv->ny, lv->nz, g);
     if (rc) return rc;
     AXS_REQUIRE(lv->dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
-    AXS_REQUIRE(((uintptr_t)lv->state % 16) == 0 && ((uintptr_t)lv->work % 16) == 0, AXS_ERR_ALIGNMENT,
-                "level buffers must be 16-byte aligned");
+    AXS_REQUIRE(((uintptr_t)lv->state % 128) == 0 && ((uintptr_t)lv->work % 128) == 0, AXS_ERR_ALIGNMENT,
+                "level buffers must be 128-byte aligned");
     return AXS_OK;
 }
 
@@ -308,58 +326,68 @@ static unsigned *level_status_word(const axs_level *lv, const LevelGeom &g)
     return reinterpret_cast<unsigned *>(static_cast<char *>(lv->work) + 8 * g.cs * es);
 }
 
-template <typename T, int TX, int TY, int NS> struct SweepConfig {
-    using S = SweepShape<T, TX, TY>;
+struct SweepRunArgs {
+    const axs_level *lv;
+    const LevelGeom *g;
+    const axs_background *bg;
+    double tau_i, t0, dt;
+    int nsteps;
+    int sweep_mask;
+    cudaStream_t st;
+};
+
+// Pick the z-chunk length: balance the last wave against the 4 warm-up
+// planes each chunk costs, and keep the SMs busy.
+static void plan_chunks(int ntiles, int nz, int grid_cap, int &zchunk, int64_t &items, int &grid)
+{
+    double best = -1.0;
+    zchunk = nz;
+    for (int nch = 1; nch <= nz; ++nch) {
+        const int lz = (nz + nch - 1) / nch;
+        if ((nz + lz - 1) / lz != nch) continue;
+        const int64_t it = (int64_t)ntiles * nch;
+        const int g = (int)std::min<int64_t>(it, grid_cap);
+        const int64_t waves = (it + g - 1) / g;
+        const double fill = (double)it / (double)(waves * g);
+        const double warm = (double)lz / (double)(lz + 4);
+        const double par = (double)g / (double)grid_cap;
+        const double score = fill * warm * std::min(1.0, par * 1.25);
+        if (score > best + 1e-9) {
+            best = score;
+            zchunk = lz;
+        }
+    }
+    items = (int64_t)ntiles * ((nz + zchunk - 1) / zchunk);
+    grid = (int)std::min<int64_t>(items, grid_cap);
+}
+
+template <typename T, int V, int TX, int TY, int NS, int MINB> struct SweepConfig {
+    using S = SweepShape<T, V, TX, TY>;
     static size_t smem() { return (size_t)NS * S::SLOT_BYTES; }
 
     static int prepare(int &blocks_per_sm)
     {
         static int cached = -1;
         if (cached < 0) {
-            AXS_CUDA_CHECK(cudaFuncSetAttribute(rk4_sweep_kernel<T, TX, TY, NS, 0>,
+            AXS_CUDA_CHECK(cudaFuncSetAttribute(rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 0>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
-            AXS_CUDA_CHECK(cudaFuncSetAttribute(rk4_sweep_kernel<T, TX, TY, NS, 1>,
+            AXS_CUDA_CHECK(cudaFuncSetAttribute(rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 1>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
             int b0 = 0, b1 = 0;
-            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, rk4_sweep_kernel<T, TX, TY, NS, 0>,
-                                                                         S::NT, smem()));
-            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, rk4_sweep_kernel<T, TX, TY, NS, 1>,
-                                                                         S::NT, smem()));
+            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &b0, rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 0>, S::NT, smem()));
+            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &b1, rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 1>, S::NT, smem()));
             cached = std::max(1, std::min(b0, b1));
         }
         blocks_per_sm = cached;
         return AXS_OK;
     }
 
-    // Pick the z-chunk length: balance the last wave against the 4 warm-up
-    // planes each chunk costs.
-    static void plan(int ntiles, int nz, int grid_cap, int &zchunk, int64_t &items, int &grid)
+    static int run(const SweepRunArgs &r)
     {
-        double best = -1.0;
-        zchunk = nz;
-        for (int nch = 1; nch <= nz; ++nch) {
-            const int lz = (nz + nch - 1) / nch;
-            const int real_nch = (nz + lz - 1) / lz;
-            if (real_nch != nch) continue;
-            const int64_t it = (int64_t)ntiles * nch;
-            const int g = (int)std::min<int64_t>(it, grid_cap);
-            const int64_t waves = (it + g - 1) / g;
-            const double fill = (double)it / (double)(waves * g);
-            const double warm = (double)lz / (double)(lz + 4);
-            const double par = (double)g / (double)grid_cap;  // idle SM slots cost too
-            const double score = fill * warm * std::min(1.0, par * 1.25);
-            if (score > best + 1e-9) {
-                best = score;
-                zchunk = lz;
-            }
-        }
-        items = (int64_t)ntiles * ((nz + zchunk - 1) / zchunk);
-        grid = (int)std::min<int64_t>(items, grid_cap);
-    }
-
-    static int run(const axs_level *lv, const LevelGeom &g, const axs_background &bg, double tau_i, double t0,
-                   double dt, int nsteps, cudaStream_t st, int sweep_mask = 3)
-    {
+        const axs_level *lv = r.lv;
+        const LevelGeom &g = *r.g;
         int bps = 0;
         int rc = prepare(bps);
         if (rc) return rc;
@@ -373,15 +401,16 @@ template <typename T, int TX, int TY, int NS> struct SweepConfig {
         a.tiles_x = tiles_x;
         a.ntiles = tiles_x * tiles_y;
         int grid = 0;
-        plan(a.ntiles, lv->nz, bps * sms, a.zchunk, a.n_items, grid);
+        plan_chunks(a.ntiles, lv->nz, bps * sms, a.zchunk, a.n_items, grid);
         a.js = g.js;
         a.ks = g.ks;
         a.cs = g.cs;
+        a.ox = g.ox;
         const double inv_dx2 = 1.0 / (lv->dx * lv->dx);
         a.wA = T((4.0 / 3.0) * inv_dx2);
         a.wB = T((-1.0 / 12.0) * inv_dx2);
         a.wC = T(-7.5 * inv_dx2);
-        const double h = dt;
+        const double h = r.dt;
         a.h = T(h);
         a.h_half = T(0.5 * h);
         a.h2_quarter = T(0.25 * h * h);
@@ -395,33 +424,33 @@ template <typename T, int TX, int TY, int NS> struct SweepConfig {
 
         const size_t es = sizeof(T);
         CUtensorMap map_state, map_work;
-        rc = make_tensor_map_4d(&map_state, lv->state, lv->dtype, lv->nx + 8, lv->ny + 4, lv->nz, 4, g.js * es,
-                                g.ks * es, g.cs * es, S::BX, S::BY, 1, 4);
+        rc = make_tensor_map_4d(&map_state, lv->state, lv->dtype, g.js, lv->ny + 4, lv->nz, 4, g.js * es, g.ks * es,
+                                g.cs * es, S::BX, S::BY, 1, 4);
         if (rc) return rc;
-        rc = make_tensor_map_4d(&map_work, lv->work, lv->dtype, lv->nx + 8, lv->ny + 4, lv->nz, 4, g.js * es,
-                                g.ks * es, g.cs * es, S::BX, S::BY, 1, 4);
+        rc = make_tensor_map_4d(&map_work, lv->work, lv->dtype, g.js, lv->ny + 4, lv->nz, 4, g.js * es, g.ks * es,
+                                g.cs * es, S::BX, S::BY, 1, 4);
         if (rc) return rc;
 
         auto coef = [&](double tau) {
             axs_rhs_coeffs c;
-            rhs_coeffs(bg, tau, c);
+            rhs_coeffs(*r.bg, tau, c);
             return StageCoef<T>{T(c.kappa), T(0.5 * c.lambda), T(c.R2)};
         };
-        for (int s = 0; s < nsteps; ++s) {
-            const double t = t0 + s * dt;
-            if (sweep_mask & 1) {
+        for (int s = 0; s < r.nsteps; ++s) {
+            const double t = r.t0 + s * r.dt;
+            if (r.sweep_mask & 1) {
                 SweepArgs<T> aa = a;
-                aa.ca = coef(tau_i + t);
-                aa.cb = coef(tau_i + t + 0.5 * dt);
-                rk4_sweep_kernel<T, TX, TY, NS, 0><<<grid, S::NT, smem(), st>>>(map_state, aa);
+                aa.ca = coef(r.tau_i + t);
+                aa.cb = coef(r.tau_i + t + 0.5 * r.dt);
+                rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 0><<<grid, S::NT, smem(), r.st>>>(map_state, aa);
                 rc = launch_status("rk4 sweep A");
                 if (rc) return rc;
             }
-            if (sweep_mask & 2) {
+            if (r.sweep_mask & 2) {
                 SweepArgs<T> ab = a;
-                ab.ca = coef(tau_i + t + 0.5 * dt);
-                ab.cb = coef(tau_i + t + dt);
-                rk4_sweep_kernel<T, TX, TY, NS, 1><<<grid, S::NT, smem(), st>>>(map_work, ab);
+                ab.ca = coef(r.tau_i + t + 0.5 * r.dt);
+                ab.cb = coef(r.tau_i + t + r.dt);
+                rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 1><<<grid, S::NT, smem(), r.st>>>(map_work, ab);
                 rc = launch_status("rk4 sweep B");
                 if (rc) return rc;
             }
@@ -430,8 +459,53 @@ template <typename T, int TX, int TY, int NS> struct SweepConfig {
     }
 };
 
-using SweepF32 = SweepConfig<float, 32, 16, 8>;
-using SweepF64 = SweepConfig<double, 32, 8, 6>;
+// Tile configurations (vector width, tile, ring depth, expected blocks/SM).
+// Entry 0 of each table is the default (tile_config = 0).
+struct TileConfigEntry {
+    const char *name;
+    int (*run)(const SweepRunArgs &);
+};
+
+static const TileConfigEntry kF32Configs[] = {
+    {"f32 v2 64x8 ring8", &SweepConfig<float, 2, 64, 8, 8, 2>::run},
+    {"f32 v2 32x16 ring8", &SweepConfig<float, 2, 32, 16, 8, 2>::run},
+    {"f32 v4 32x16 ring8", &SweepConfig<float, 4, 32, 16, 8, 2>::run},
+    {"f32 v2 32x8 ring8", &SweepConfig<float, 2, 32, 8, 8, 3>::run},
+    {"f32 v1 32x8 ring8", &SweepConfig<float, 1, 32, 8, 8, 3>::run},
+    {"f32 v2 64x8 ring10", &SweepConfig<float, 2, 64, 8, 10, 1>::run},
+    {"f32 v4 64x16 ring6", &SweepConfig<float, 4, 64, 16, 6, 1>::run},
+    {"f32 v2 32x16 ring6", &SweepConfig<float, 2, 32, 16, 6, 2>::run},
+    {"f32 v1 32x16 ring7", &SweepConfig<float, 1, 32, 16, 7, 2>::run},
+};
+static const TileConfigEntry kF64Configs[] = {
+    {"f64 v1 32x8 ring6", &SweepConfig<double, 1, 32, 8, 6, 2>::run},
+    {"f64 v2 32x8 ring6", &SweepConfig<double, 2, 32, 8, 6, 2>::run},
+    {"f64 v2 32x16 ring6", &SweepConfig<double, 2, 32, 16, 6, 1>::run},
+    {"f64 v1 32x4 ring7", &SweepConfig<double, 1, 32, 4, 7, 3>::run},
+};
+
+static int config_count(int32_t dtype)
+{
+    return dtype == AXS_F64 ? (int)(sizeof(kF64Configs) / sizeof(kF64Configs[0]))
+                            : (int)(sizeof(kF32Configs) / sizeof(kF32Configs[0]));
+}
+
+static const TileConfigEntry *config_for(int32_t dtype, int32_t id)
+{
+    const TileConfigEntry *tab = dtype == AXS_F64 ? kF64Configs : kF32Configs;
+    if (id < 0 || id > config_count(dtype)) return nullptr;
+    return &tab[id == 0 ? 0 : id - 1];
+}
+
+static int run_sweeps(const axs_level *lv, const LevelGeom &g, const axs_background *bg, double tau_i, double t0,
+                      double dt, int nsteps, int mask, cudaStream_t st)
+{
+    const TileConfigEntry *cfg = config_for(lv->dtype, lv->tile_config);
+    AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "tile_config %d out of range (0..%d)", lv->tile_config,
+                config_count(lv->dtype));
+    SweepRunArgs r{lv, &g, bg, tau_i, t0, dt, nsteps, mask, st};
+    return cfg->run(r);
+}
 
 }  // namespace axs
 
@@ -449,9 +523,24 @@ int axs_level_layout_for(int32_t dtype, int32_t nx, int32_t ny, int32_t nz, axs_
     out->jstride = g.js;
     out->kstride = g.ks;
     out->cstride = g.cs;
+    out->x_offset = g.ox;
+    out->y_offset = g.oy;
     out->state_bytes = 4 * g.cs * es;
     out->work_bytes = 8 * g.cs * es + 256;
     return AXS_OK;
+}
+
+int axs_level_tile_config_count(int32_t dtype)
+{
+    if (dtype != AXS_F32 && dtype != AXS_F64) return 0;
+    return config_count(dtype);
+}
+
+const char *axs_level_tile_config_name(int32_t dtype, int32_t id)
+{
+    if (dtype != AXS_F32 && dtype != AXS_F64) return nullptr;
+    const TileConfigEntry *c = config_for(dtype, id);
+    return c ? c->name : nullptr;
 }
 
 int axs_level_fill_ghosts(const axs_level *lv, void *stream)
@@ -459,7 +548,7 @@ int axs_level_fill_ghosts(const axs_level *lv, void *stream)
     LevelGeom g;
     int rc = validate_level(lv, g);
     if (rc) return rc;
-    return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g.js, g.ks, g.cs, 4, (cudaStream_t)stream);
+    return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g, 4, (cudaStream_t)stream);
 }
 
 int axs_level_import_fab(const axs_level *lv, const axs_fab *src, void *stream)
@@ -470,9 +559,9 @@ int axs_level_import_fab(const axs_level *lv, const axs_fab *src, void *stream)
     if ((rc = validate_fab(src, "src", 4, 0))) return rc;
     AXS_REQUIRE(src->dtype == lv->dtype && src->nx == lv->nx && src->ny == lv->ny && src->nz == lv->nz,
                 AXS_ERR_INVALID_ARGUMENT, "FAB and level differ in dtype or extent");
-    rc = level_copy_fab(lv->state, lv->dtype, g.js, g.ks, g.cs, *src, 1, (cudaStream_t)stream);
+    rc = level_copy_fab(lv->state, lv->dtype, g, *src, 1, (cudaStream_t)stream);
     if (rc) return rc;
-    return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g.js, g.ks, g.cs, 4, (cudaStream_t)stream);
+    return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g, 4, (cudaStream_t)stream);
 }
 
 int axs_level_export_fab(const axs_level *lv, const axs_fab *dst, void *stream)
@@ -483,7 +572,7 @@ int axs_level_export_fab(const axs_level *lv, const axs_fab *dst, void *stream)
     if ((rc = validate_fab(dst, "dst", 4, 0))) return rc;
     AXS_REQUIRE(dst->dtype == lv->dtype && dst->nx == lv->nx && dst->ny == lv->ny && dst->nz == lv->nz,
                 AXS_ERR_INVALID_ARGUMENT, "FAB and level differ in dtype or extent");
-    return level_copy_fab(lv->state, lv->dtype, g.js, g.ks, g.cs, *dst, 0, (cudaStream_t)stream);
+    return level_copy_fab(lv->state, lv->dtype, g, *dst, 0, (cudaStream_t)stream);
 }
 
 int axs_level_rk4_advance(const axs_level *lv, const axs_background *bg, double tau_i, double t0, double dt,
@@ -500,9 +589,7 @@ int axs_level_rk4_advance(const axs_level *lv, const axs_background *bg, double 
         AXS_REQUIRE(tau_i + t0 > 0.0, AXS_ERR_INVALID_ARGUMENT, "conformal time must stay positive");
     }
     if (nsteps == 0) return AXS_OK;
-    cudaStream_t st = (cudaStream_t)stream;
-    if (lv->dtype == AXS_F32) return SweepF32::run(lv, g, *bg, tau_i, t0, dt, nsteps, st);
-    return SweepF64::run(lv, g, *bg, tau_i, t0, dt, nsteps, st);
+    return run_sweeps(lv, g, bg, tau_i, t0, dt, nsteps, 3, (cudaStream_t)stream);
 }
 
 int axs_level_rk4_sweep(const axs_level *lv, const axs_background *bg, double tau_i, double t, double dt,
@@ -514,10 +601,7 @@ int axs_level_rk4_sweep(const axs_level *lv, const axs_background *bg, double ta
     AXS_REQUIRE(bg != nullptr, AXS_ERR_INVALID_ARGUMENT, "null background");
     AXS_REQUIRE(sweep == 0 || sweep == 1, AXS_ERR_INVALID_ARGUMENT, "sweep must be 0 (A) or 1 (B)");
     AXS_REQUIRE(std::isfinite(dt) && dt > 0.0, AXS_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
-    cudaStream_t st = (cudaStream_t)stream;
-    const int mask = sweep == 0 ? 1 : 2;
-    if (lv->dtype == AXS_F32) return SweepF32::run(lv, g, *bg, tau_i, t, dt, 1, st, mask);
-    return SweepF64::run(lv, g, *bg, tau_i, t, dt, 1, st, mask);
+    return run_sweeps(lv, g, bg, tau_i, t, dt, 1, sweep == 0 ? 1 : 2, (cudaStream_t)stream);
 }
 
 int axs_level_device_status(const axs_level *lv, void *stream)

@@ -1,0 +1,333 @@
+// Generic TMA-staged stencil sweep over a periodic level (sm_103a).
+//
+// A sweep reads four components of one level-layout array with the 13-point
+// 4th-order star (their Laplacians and centre values) plus up to 12 components
+// of other level-layout arrays pointwise, and hands both to a per-site
+// operation that writes its outputs. The forward RK4 sweeps and the two
+// adjoint sweeps are such operations (rk4_level.cu, adjoint.cu).
+//
+// Pipeline: a block owns a TX x TY tile of the xy plane over a chunk of z
+// planes and marches in z. One elected thread issues one 4D TMA load per plane
+// ({x, y, z, component} box of (TX+8) x (TY+4) x 1 x 4) into an NS-slot
+// shared-memory ring; completion is signalled through one mbarrier per slot and
+// every wait is bounded. Pointwise components are loaded one plane ahead into
+// registers. Work items (tile, z-chunk) are numbered tile-fastest so the blocks
+// resident at any moment work on neighbouring tiles of the same z range.
+#pragma once
+
+#include <algorithm>
+
+#include "axs_internal.cuh"
+
+namespace axs {
+
+template <typename T> struct StageCoef {
+    T kappa, hlam, R2;  // kappa, lambda/2, R^2 at one stage time
+};
+
+constexpr int kMaxPointwise = 12;
+
+template <typename T> struct SweepArgs {
+    int nx, ny, nz;
+    int tiles_x, ntiles, zchunk;
+    int64_t n_items;
+    int64_t js, ks, cs;
+    int ox;                      // x offset of the valid region in a padded row
+    T wA, wB, wC;                // lap = wA*S1 + wB*S2 + wC*f0 (S1/S2: sums of +-1 / +-2 neighbours)
+    StageCoef<T> c1, c2, c4;     // stage coefficients at t, t + h/2, t + h
+    T h, h_half, h2_quarter, h2_half, h_sixth, h_third, h2_sixth;
+    const T *pt[kMaxPointwise];  // pointwise input components (level layout)
+    T *out[8];                   // output components (level layout)
+    double inv_lambda0;          // adjoint: dlambda_s/dlambda0 = lambda_s / lambda0
+    double *lam_partial;         // adjoint: one lambda0-gradient partial per block
+    unsigned *status;
+};
+
+template <typename T, int V, int TX, int TY> struct SweepShape {
+    static constexpr int NTX = TX / V;
+    static constexpr int NT = NTX * TY;
+    static constexpr int BX = TX + 8;
+    static constexpr int BY = TY + 4;
+    static constexpr int TILE = BX * BY;
+    static constexpr int SLOT = 4 * TILE;
+    static constexpr uint32_t SLOT_BYTES = SLOT * sizeof(T);
+    static constexpr int PRE = (2 + V - 1) / V;  // vectors left/right of the centre that cover +-2
+    static constexpr int NROW = 2 * PRE + 1;
+    static_assert(TX % V == 0 && 4 % V == 0, "tile width and halo must hold whole vectors");
+    static_assert((BX * sizeof(T)) % 16 == 0, "TMA box row must be a multiple of 16 bytes");
+    static_assert(SLOT_BYTES % 128 == 0, "ring slots must stay 128-byte aligned");
+    static_assert(BX <= 256 && BY <= 256, "TMA box extent limit");
+};
+
+// Store V sites and, for sites next to the domain edge, their periodic copies
+// in the x/y padding (4 columns, 2 rows).
+template <typename T, int V>
+__device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
+                                                  const T *v)
+{
+    stv<T, V>(base + off, v);
+    if (x < 4) stv<T, V>(base + off + nx, v);
+    if (x >= nx - 4) stv<T, V>(base + off - nx, v);
+    if (y < 2) stv<T, V>(base + off + (int64_t)ny * js, v);
+    if (y >= ny - 2) stv<T, V>(base + off - (int64_t)ny * js, v);
+}
+
+// F(u) = lap + (kappa - lambda/2 (|u|^2 - R^2)) u, one component pair.
+template <typename T>
+__device__ __forceinline__ void rhs_pair(const StageCoef<T> &c, T u1, T u2, T l1, T l2, T &f1, T &f2)
+{
+    const T k = fma(-c.hlam, fma(u1, u1, u2 * u2) - c.R2, c.kappa);
+    f1 = fma(k, u1, l1);
+    f2 = fma(k, u2, l2);
+}
+
+// J_F(u)^T a = lap(a) + kappa a - lambda/2 [(|u|^2 - R^2) a + 2 u (u . a)]
+template <typename T>
+__device__ __forceinline__ void rhs_adjoint_pair(const StageCoef<T> &c, T u1, T u2, T a1, T a2, T la1, T la2, T &o1,
+                                                 T &o2)
+{
+    const T m = fma(u1, u1, u2 * u2) - c.R2;
+    const T k = fma(-c.hlam, m, c.kappa);
+    const T ua = T(2) * c.hlam * fma(u1, a1, u2 * a2);
+    o1 = fma(k, a1, la1) - ua * u1;
+    o2 = fma(k, a2, la2) - ua * u2;
+}
+
+template <typename T, int V, int TX, int TY, int NS, int MINB, class Op>
+__global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
+    stencil_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
+{
+    using S = SweepShape<T, V, TX, TY>;
+    constexpr int NPT = Op::kPointwise;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T *ring = reinterpret_cast<T *>(smem_raw);
+    __shared__ uint64_t full[NS];
+    __shared__ int abort_flag;
+    __shared__ double lam_red[S::NT / 32];
+
+    const int tid = threadIdx.x;
+    const int tx = tid % S::NTX, ty = tid / S::NTX;
+    double lam_acc = 0.0;
+
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+        prefetch_tensormap(&tmap);
+    }
+    __syncthreads();
+
+    // ---- producer cursor (thread 0 only) ----
+    int64_t p_item = blockIdx.x;
+    int p_k = 0;
+    int64_t q_issued = 0;
+    auto issue_one = [&]() -> bool {
+        if (p_item >= a.n_items) return false;
+        const int tile = (int)(p_item % a.ntiles);
+        const int chunk = (int)(p_item / a.ntiles);
+        const int za = chunk * a.zchunk;
+        const int len = min(a.zchunk, a.nz - za);
+        int zp = (za - 2 + p_k) % a.nz;
+        if (zp < 0) zp += a.nz;
+        const int slot = (int)(q_issued % NS);
+        mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
+        // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned)
+        tma_load_4d(ring + (size_t)slot * S::SLOT, &tmap, a.ox - 4 + (tile % a.tiles_x) * TX,
+                    (tile / a.tiles_x) * TY, zp, 0, &full[slot]);
+        ++q_issued;
+        if (++p_k == len + 4) {
+            p_k = 0;
+            p_item += gridDim.x;
+        }
+        return true;
+    };
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s)
+            if (!issue_one()) break;
+    }
+
+    int64_t q_base = 0, q_waited = 0;
+    bool aborted = false;
+    const int xl = 4 + V * tx;  // tile-local column of this thread's first site
+    const int yl = 2 + ty;
+    for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+        const int tile = (int)(item % a.ntiles);
+        const int chunk = (int)(item / a.ntiles);
+        const int za = chunk * a.zchunk;
+        const int len = min(a.zchunk, a.nz - za);
+        const int x = (tile % a.tiles_x) * TX + V * tx;
+        const int y = (tile / a.tiles_x) * TY + ty;
+        const bool active = (x < a.nx) && (y < a.ny);
+        // pointwise components of the next plane, loaded one iteration ahead
+        T pn[NPT > 0 ? NPT : 1][V];
+        if constexpr (NPT > 0) {
+            if (active) {
+                const int64_t off0 = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)za * a.ks;
+#pragma unroll
+                for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off0, pn[c]);
+            }
+        }
+        for (int m = 0; m < len; ++m) {
+            const int z = za + m;
+            const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)z * a.ks;
+
+            T pq[NPT > 0 ? NPT : 1][V];
+            if constexpr (NPT > 0) {
+#pragma unroll
+                for (int c = 0; c < NPT; ++c)
+#pragma unroll
+                    for (int v = 0; v < V; ++v) pq[c][v] = pn[c][v];
+                if (active && m + 1 < len) {
+#pragma unroll
+                    for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off + a.ks, pn[c]);
+                }
+            }
+
+            const int64_t need = q_base + m + 4;
+            while (q_waited <= need) {
+                const int slot = (int)(q_waited % NS);
+                if (!mbar_wait_bounded(&full[slot], (uint32_t)((q_waited / NS) & 1))) {
+                    atomicOr(a.status, kDevTimeout);
+                    abort_flag = 1;
+                }
+                ++q_waited;
+            }
+
+            const T *sl[5];
+#pragma unroll
+            for (int d = 0; d < 5; ++d) sl[d] = ring + (size_t)((q_base + m + d) % NS) * S::SLOT;
+
+            if (active) {
+                T lap[4][V], ctr[4][V];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const T *P0 = sl[2] + c * S::TILE;
+                    T row[S::NROW * V], ym1[V], yp1[V], ym2[V], yp2[V], zm1[V], zp1[V], zm2[V], zp2[V];
+#pragma unroll
+                    for (int r = 0; r < S::NROW; ++r) ldv<T, V>(P0 + yl * S::BX + xl + (r - S::PRE) * V, row + r * V);
+                    ldv<T, V>(P0 + (yl - 1) * S::BX + xl, ym1);
+                    ldv<T, V>(P0 + (yl + 1) * S::BX + xl, yp1);
+                    ldv<T, V>(P0 + (yl - 2) * S::BX + xl, ym2);
+                    ldv<T, V>(P0 + (yl + 2) * S::BX + xl, yp2);
+                    ldv<T, V>(sl[1] + c * S::TILE + yl * S::BX + xl, zm1);
+                    ldv<T, V>(sl[3] + c * S::TILE + yl * S::BX + xl, zp1);
+                    ldv<T, V>(sl[0] + c * S::TILE + yl * S::BX + xl, zm2);
+                    ldv<T, V>(sl[4] + c * S::TILE + yl * S::BX + xl, zp2);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) {
+                        const int ci = S::PRE * V + v;
+                        const T f0 = row[ci];
+                        const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
+                        const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
+                        lap[c][v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
+                        ctr[c][v] = f0;
+                    }
+                }
+                Op::template apply<T, V>(a, lap, ctr, pq, off, x, y, lam_acc);
+            }
+
+            __syncthreads();  // everyone is done with the oldest plane of this window
+            if (abort_flag) {
+                aborted = true;
+                break;
+            }
+            const int64_t next_needed = (m + 1 < len) ? (q_base + m + 1) : (q_base + len + 4);
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                while (q_issued < next_needed + NS && issue_one()) {
+                }
+            }
+        }
+        if (aborted) break;
+        q_base += len + 4;
+    }
+    // A wait expired: make sure no bulk copy is still landing in shared memory
+    // before the block exits (bounded as well).
+    if (aborted && tid == 0) {
+        for (int64_t q = q_waited; q < q_issued; ++q) mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 1u << 20);
+    }
+    if constexpr (Op::kLambdaGrad) {
+        // fixed-order block reduction of the lambda0-gradient contributions
+        for (int o = 16; o > 0; o >>= 1) lam_acc += __shfl_down_sync(0xffffffffu, lam_acc, o);
+        if ((tid & 31) == 0) lam_red[tid >> 5] = lam_acc;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0.0;
+            for (int w = 0; w < S::NT / 32; ++w) s += lam_red[w];
+            a.lam_partial[blockIdx.x] = s;
+        }
+    }
+}
+
+// Host: chunk length balancing the last wave against the 4 warm-up planes
+// each chunk costs, while keeping the SMs busy.
+inline void plan_chunks(int ntiles, int nz, int grid_cap, int &zchunk, int64_t &items, int &grid)
+{
+    double best = -1.0;
+    zchunk = nz;
+    for (int nch = 1; nch <= nz; ++nch) {
+        const int lz = (nz + nch - 1) / nch;
+        if ((nz + lz - 1) / lz != nch) continue;
+        const int64_t it = (int64_t)ntiles * nch;
+        const int g = (int)std::min<int64_t>(it, grid_cap);
+        const int64_t waves = (it + g - 1) / g;
+        const double fill = (double)it / (double)(waves * g);
+        const double warm = (double)lz / (double)(lz + 4);
+        const double par = (double)g / (double)grid_cap;
+        const double score = fill * warm * std::min(1.0, par * 1.25);
+        if (score > best + 1e-9) {
+            best = score;
+            zchunk = lz;
+        }
+    }
+    items = (int64_t)ntiles * ((nz + zchunk - 1) / zchunk);
+    grid = (int)std::min<int64_t>(items, grid_cap);
+}
+
+// One tiling of one sweep operation: occupancy, chunk plan and launch.
+template <typename T, int V, int TX, int TY, int NS, int MINB, class Op> struct SweepLauncher {
+    using S = SweepShape<T, V, TX, TY>;
+    static size_t smem() { return (size_t)NS * S::SLOT_BYTES; }
+
+    static int blocks_per_sm(int &bps)
+    {
+        static int cached = -1;
+        if (cached < 0) {
+            auto kern = stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op>;
+            AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
+            int b = 0;
+            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, S::NT, smem()));
+            cached = std::max(1, b);
+        }
+        bps = cached;
+        return AXS_OK;
+    }
+
+    // Fill the geometry part of `a` and return the grid size.
+    static int plan(SweepArgs<T> &a, int nx, int ny, int nz, int &grid)
+    {
+        int bps = 0;
+        int rc = blocks_per_sm(bps);
+        if (rc) return rc;
+        const int sms = device_sm_count();
+        AXS_REQUIRE(sms > 0, AXS_ERR_CUDA, "no CUDA device");
+        a.nx = nx;
+        a.ny = ny;
+        a.nz = nz;
+        a.tiles_x = (nx + TX - 1) / TX;
+        a.ntiles = a.tiles_x * ((ny + TY - 1) / TY);
+        plan_chunks(a.ntiles, nz, bps * sms, a.zchunk, a.n_items, grid);
+        return AXS_OK;
+    }
+
+    static int launch(const CUtensorMap &map, const SweepArgs<T> &a, int grid, cudaStream_t st)
+    {
+        stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op><<<grid, S::NT, smem(), st>>>(map, a);
+        return launch_status("stencil sweep");
+    }
+
+    static uint32_t box_x() { return S::BX; }
+    static uint32_t box_y() { return S::BY; }
+};
+
+}  // namespace axs

@@ -150,21 +150,25 @@ def scratch_bytes(nx: int, ny: int, nz: int) -> int:
 class PeriodicLevel:
     """One periodic box in the fused-RK4 layout (see axs_level_layout in include/axs.h).
 
-    ``state`` is (4, nz, ny+4, nx+8); the valid cells are ``state[:, :, 2:-2, 4:-4]``.
-    ``work`` holds the 8 between-sweep components and the device status word.
+    ``state`` is (4, nz, ny+4, jstride); the valid cells are
+    ``state[:, :, y_offset:y_offset+ny, x_offset:x_offset+nx]``, with x = 0 on a
+    128-byte boundary. ``work`` holds the 8 between-sweep components and the
+    device status word.
     """
 
-    def __init__(self, n, dx: float, dtype=torch.float32, device="cuda", pierced_capacity: int | None = None):
+    def __init__(self, n, dx: float, dtype=torch.float32, device="cuda", pierced_capacity: int | None = None,
+                 tile_config: int = 0):
         nx, ny, nz = (n, n, n) if isinstance(n, int) else n
         self.nx, self.ny, self.nz, self.dx, self.dtype = nx, ny, nz, float(dx), dtype
         lay = L.LevelLayout()
         L.call("axs_level_layout_for", _DT[dtype], nx, ny, nz, C.byref(lay))
         self.layout = lay
         es = torch.finfo(dtype).bits // 8
-        self.state = torch.zeros((4, nz, ny + 4, nx + 8), dtype=dtype, device=device)
+        self.state = torch.zeros((4, nz, ny + 4, lay.jstride), dtype=dtype, device=device)
         assert self.state.numel() * es == lay.state_bytes
         self.work = torch.zeros(lay.work_bytes, dtype=torch.uint8, device=device)
-        self.c = L.LevelC(self.state.data_ptr(), self.work.data_ptr(), _DT[dtype], nx, ny, nz, self.dx)
+        self.c = L.LevelC(self.state.data_ptr(), self.work.data_ptr(), _DT[dtype], nx, ny, nz, self.dx,
+                          int(tile_config))
         # diagnostics buffers (allocated once; the pass itself allocates nothing)
         self._scratch = torch.zeros(scratch_bytes(nx, ny, nz), dtype=torch.uint8, device=device)
         self._result = torch.zeros(C.sizeof(L.DiagResult), dtype=torch.uint8, device=device)
@@ -180,7 +184,49 @@ class PeriodicLevel:
         return self.nx * self.dx
 
     def valid_view(self) -> torch.Tensor:
-        return self.state[:, :, 2:2 + self.ny, 4:4 + self.nx]
+        ox, oy = self.layout.x_offset, self.layout.y_offset
+        return self.state[:, :, oy:oy + self.ny, ox:ox + self.nx]
+
+    @property
+    def tile_config(self) -> int:
+        return self.c.tile_config
+
+    @tile_config.setter
+    def tile_config(self, v: int) -> None:
+        self.c.tile_config = int(v)
+
+    def tile_configs(self) -> list:
+        """(id, name) of every sweep tiling compiled for this level's dtype."""
+        lib = L.lib()
+        d = _DT[self.dtype]
+        return [(i, lib.axs_level_tile_config_name(d, i).decode()) for i in range(1, lib.axs_level_tile_config_count(d) + 1)]
+
+    def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 3, repeats: int = 2,
+                 stream=None) -> dict:
+        """Time every compiled sweep tiling on this level (full RK4 steps, CUDA
+        events) and keep the fastest. The state is saved and restored, so the
+        level's contents are unchanged. Returns {name: ms_per_step}."""
+        saved = self.state.clone()
+        timings = {}
+        best = (float("inf"), self.c.tile_config)
+        for cid, name in self.tile_configs():
+            self.c.tile_config = cid
+            self.advance(bg, tau_i, 0.0, dt, 1, stream)  # warm-up (sets up the kernel)
+            ms = float("inf")
+            for _ in range(repeats):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                self.advance(bg, tau_i, 0.0, dt, steps, stream)
+                e1.record()
+                e1.synchronize()
+                ms = min(ms, e0.elapsed_time(e1) / steps)
+            timings[name] = ms
+            if ms < best[0]:
+                best = (ms, cid)
+        self.c.tile_config = best[1]
+        self.state.copy_(saved)
+        self.device_status(stream)
+        return timings
 
     def set_state(self, valid_cells: torch.Tensor, stream=None) -> None:
         """Copy (4, nz, ny, nx) valid cells in and refresh the periodic padding."""

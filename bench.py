@@ -224,8 +224,12 @@ def run_native(args):
         return ms, a, b, clocks
 
     # ---------------- FP32 (headline)
-    lv32 = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev)
+    lv32 = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev, pierced_capacity=1024)
     lv32.set_state(ic64.float())
+    tune32 = None
+    if not args.no_autotune:
+        tune32 = lv32.autotune(bg, TAU_I, DT)
+    cfg32 = dict(lv32.tile_configs())[lv32.tile_config] if lv32.tile_config else "default"
     ms, msA, msB, clocks = timed_run(lv32, args.steps, args.warmup, sample_clocks=True)
     ms_max = allmax(ms)
     value = ws * n ** 3 * args.steps / (ms_max * 1e-3)
@@ -255,17 +259,43 @@ def run_native(args):
                 "sweep_ms": {"A": msA, "B": msB},
                 "frac_of_nominal_8TBs": achieved / 8000.0}
 
+    # ---------------- fused diagnostics pass (string finder + energies + velocities) on the FP32 box
+    diag = None
+    if not args.no_diag:
+        t_ev = []
+        tau_d = TAU_I + (args.warmup + args.steps) * DT
+        bv = bg.values(tau_d)
+        params = A._lib.DiagParams(DX, bv.R, bv.lambda_, bv.R_prime_over_R, bv.m_r, A._lib.MASK_A, 0.8,
+                                   A._lib.BOUNDARY_PERIODIC, 1, 1, 1)
+        import ctypes as _C
+        for r in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            A._lib.call("axs_level_diagnostics", _C.byref(lv32.c), _C.byref(params), None, lv32._result.data_ptr(),
+                        lv32._pierced.data_ptr(), lv32._pierced.numel(), lv32._scratch.data_ptr(),
+                        lv32._scratch.numel(), torch.cuda.current_stream().cuda_stream)
+            e1.record()
+            e1.synchronize()
+            t_ev.append(e0.elapsed_time(e1))
+        ms_d = min(t_ev)
+        res = A.level._result_from_bytes(lv32._result)
+        diag = {"ms": ms_d, "read_gbps": 16 * n ** 3 / (ms_d * 1e-3) / 1e9, "n_p_plain": res.n_p_plain,
+                "n_near_tie": res.n_near_tie, "fields": "fp32", "per_cell_math": "fp64"}
+
     # ---------------- FP64 path on the same box
     fp64 = None
     if not args.no_fp64:
         del lv32
         torch.cuda.empty_cache()
-        lv64 = A.PeriodicLevel(n, DX, dtype=torch.float64, device=dev)
+        lv64 = A.PeriodicLevel(n, DX, dtype=torch.float64, device=dev, pierced_capacity=1024)
         lv64.set_state(ic64)
+        tune64 = None if args.no_autotune else lv64.autotune(bg, TAU_I, DT, steps=2, repeats=1)
         k64 = max(2, args.steps // 4)
         ms64, a64, b64, _ = timed_run(lv64, k64, 1)
         v64 = ws * n ** 3 * k64 / (allmax(ms64) * 1e-3)
-        fp64 = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "sweep_ms": {"A": a64, "B": b64}}
+        fp64 = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "sweep_ms": {"A": a64, "B": b64},
+                "tile_config": dict(lv64.tile_configs())[lv64.tile_config] if lv64.tile_config else "default",
+                "autotune_ms_per_step": tune64}
         del lv64
         torch.cuda.empty_cache()
 
@@ -337,7 +367,8 @@ def run_native(args):
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": _config(n), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clocks, "gpu_launches": 2 * args.steps, "fp64": fp64,
+                "clocks": clocks, "gpu_launches": 2 * args.steps, "tile_config": cfg32,
+                "autotune_ms_per_step": tune32, "diagnostics": diag, "fp64": fp64,
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision}
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -358,6 +389,8 @@ def main():
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-diag", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3

@@ -140,13 +140,19 @@ int axs_rk4_combine(const axs_fab *dst, const axs_fab *uold, const axs_fab *k1, 
  * ------------------------------------------------------------------------- */
 
 /* Device layout of a periodic single-box level: component-major SoA planes,
- * x fastest, each plane padded by 4 columns on either side in x and 2 rows on
- * either side in y (periodic copies kept current by the kernels), no z
- * padding:  element (x,y,z,c) at (x+4) + (y+2)*jstride + z*kstride + c*cstride.
- * `state` holds psi1, psi2, Pi1, Pi2; `work` holds 8 components of the same
- * layout used between the two sweeps of a step, plus a 256-byte status block. */
+ * x fastest, each xy plane padded in x and by 2 rows on either side in y, no
+ * z padding. Element (x,y,z,c) sits at
+ *   (x + x_offset) + (y + y_offset)*jstride + z*kstride + c*cstride.
+ * x_offset puts x = 0 on a 128-byte boundary (32 floats / 16 doubles) and
+ * jstride is a multiple of 128 bytes, so every row of valid cells starts a
+ * cache line; the 4 columns left of x = 0 and right of x = nx-1 and the 2 rows
+ * outside y hold periodic copies that the kernels keep current (padding
+ * corners excepted). `state` holds psi1, psi2, Pi1, Pi2; `work` holds 8
+ * components of the same layout used between the two sweeps of a step, plus
+ * a 256-byte status block. Both must be 128-byte aligned. */
 typedef struct axs_level_layout {
     int64_t jstride, kstride, cstride; /* elements */
+    int32_t x_offset, y_offset;       /* elements */
     int64_t state_bytes;              /* 4 components */
     int64_t work_bytes;               /* 8 components + status block */
 } axs_level_layout;
@@ -157,9 +163,16 @@ typedef struct axs_level {
     int32_t dtype; /* axs_dtype */
     int32_t nx, ny, nz;
     double dx;
+    int32_t tile_config; /* 0 = default sweep tiling for the dtype; 1..N = axs_level_tile_config_name(dtype, id) */
 } axs_level;
 
 int axs_level_layout_for(int32_t dtype, int32_t nx, int32_t ny, int32_t nz, axs_level_layout *out);
+
+/* Sweep tilings compiled into the library (vector width, tile, ring depth):
+ * ids 1..axs_level_tile_config_count(dtype); id 0 names the default. An
+ * autotuner can time each on the caller's level and set axs_level.tile_config. */
+int axs_level_tile_config_count(int32_t dtype);
+const char *axs_level_tile_config_name(int32_t dtype, int32_t id);
 
 /* Periodic ghost columns/rows of the 4 state components (call after writing
  * the state's valid cells by any other means). */

@@ -105,17 +105,26 @@ def test_validation_rejects_bad_input_without_gpu(L):
     assert lib.axs_level_layout_for(L.AXS_F32, 6, 8, 8, C.byref(lay)) == L.AXS_ERR_UNSUPPORTED  # nx % 4
     assert lib.axs_level_layout_for(L.AXS_F32, 8, 1, 8, C.byref(lay)) == L.AXS_ERR_UNSUPPORTED  # ny >= 2
     assert lib.axs_level_layout_for(L.AXS_F64, 6, 8, 8, C.byref(lay)) == L.AXS_OK
-    assert lay.jstride == 14 and lay.kstride == 14 * 12 and lay.cstride == 14 * 12 * 8
+    # x = 0 on a 128-byte line (16 doubles), rows a whole number of lines
+    assert lay.x_offset == 16 and lay.y_offset == 2 and lay.jstride == 32
+    assert lay.kstride == 32 * 12 and lay.cstride == 32 * 12 * 8
     assert lay.state_bytes == 4 * lay.cstride * 8 and lay.work_bytes == 8 * lay.cstride * 8 + 256
-    lv = L.LevelC(None, None, L.AXS_F32, 8, 8, 8, 0.5)
+    assert lib.axs_level_layout_for(L.AXS_F32, 512, 512, 512, C.byref(lay)) == L.AXS_OK
+    assert lay.x_offset == 32 and lay.jstride == 576 and (lay.jstride * 4) % 128 == 0
+    assert lib.axs_level_tile_config_count(L.AXS_F32) >= 1 and lib.axs_level_tile_config_count(L.AXS_F64) >= 1
+    assert lib.axs_level_tile_config_name(L.AXS_F32, 0) == lib.axs_level_tile_config_name(L.AXS_F32, 1)
+    assert lib.axs_level_tile_config_name(L.AXS_F32, 99) is None
+    lv = L.LevelC(None, None, L.AXS_F32, 8, 8, 8, 0.5, 0)
     bg = L.BackgroundC(0, 0, 2.0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0)
     assert lib.axs_level_rk4_advance(C.byref(lv), C.byref(bg), 1.0, 0.0, 0.1, 1, None) == L.AXS_ERR_INVALID_ARGUMENT
-    lv2 = L.LevelC(C.c_void_p(4096), C.c_void_p(8192), L.AXS_F32, 8, 8, 8, 0.5)
+    lv2 = L.LevelC(C.c_void_p(4096), C.c_void_p(8192), L.AXS_F32, 8, 8, 8, 0.5, 0)
     assert lib.axs_level_rk4_advance(C.byref(lv2), C.byref(bg), 1.0, 0.0, -0.1, 1, None) == L.AXS_ERR_INVALID_ARGUMENT
     bad_bg = L.BackgroundC(0, 0, 0.5, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0)  # a_inv <= 1
     assert lib.axs_level_rk4_advance(C.byref(lv2), C.byref(bad_bg), 1.0, 0.0, 0.1, 1, None) == \
         L.AXS_ERR_INVALID_ARGUMENT
     assert lib.axs_level_rk4_advance(C.byref(lv2), C.byref(bg), 1.0, 0.0, 0.1, 0, None) == L.AXS_OK  # no-op
+    lv3 = L.LevelC(C.c_void_p(4096 + 16), C.c_void_p(8192), L.AXS_F32, 8, 8, 8, 0.5, 0)
+    assert lib.axs_level_rk4_advance(C.byref(lv3), C.byref(bg), 1.0, 0.0, 0.1, 1, None) == L.AXS_ERR_ALIGNMENT
     b = C.c_int64()
     assert lib.axs_diagnostics_scratch_bytes(0, 8, 8, C.byref(b)) == L.AXS_ERR_INVALID_ARGUMENT
     assert lib.axs_plaquette_winding_batch(None, -1, None, None) == L.AXS_ERR_INVALID_ARGUMENT

@@ -168,6 +168,17 @@ def test_homogeneous_solution_is_exact(axs, dtype, tol):
     assert float(s[1].abs().max()) == 0.0 and float(s[3].abs().max()) == 0.0
 
 
+def _check_padding(lv, val):
+    """The 4 columns either side in x and 2 rows either side in y hold periodic copies."""
+    st = lv.state.cpu().numpy()
+    ox, oy, nx, ny = lv.layout.x_offset, lv.layout.y_offset, lv.nx, lv.ny
+    rows = st[:, :, oy:oy + ny]
+    np.testing.assert_array_equal(rows[..., ox - 4:ox], val[..., nx - 4:nx])
+    np.testing.assert_array_equal(rows[..., ox + nx:ox + nx + 4], val[..., :4])
+    np.testing.assert_array_equal(st[:, :, oy - 2:oy, ox:ox + nx], val[:, :, ny - 2:ny, :])
+    np.testing.assert_array_equal(st[:, :, oy + ny:oy + ny + 2, ox:ox + nx], val[:, :, :2, :])
+
+
 def test_level_fab_round_trip(axs):
     rng = np.random.default_rng(3)
     v = rng.standard_normal((4, 9, 10, 12))
@@ -179,11 +190,7 @@ def test_level_fab_round_trip(axs):
     lv.export_fab(out, 1)
     np.testing.assert_array_equal(axs.valid(out, 1).cpu().numpy(), v)
     # padding holds periodic copies
-    st = lv.state.cpu().numpy()
-    np.testing.assert_array_equal(st[:, :, 2:-2, 0:4], v[:, :, :, -4:])
-    np.testing.assert_array_equal(st[:, :, 2:-2, -4:], v[:, :, :, :4])
-    np.testing.assert_array_equal(st[:, :, 0:2, 4:-4], v[:, :, -2:, :])
-    np.testing.assert_array_equal(st[:, :, -2:, 4:-4], v[:, :, :2, :])
+    _check_padding(lv, v)
 
 
 def test_fused_rk4_keeps_padding_current(axs):
@@ -192,9 +199,4 @@ def test_fused_rk4_keeps_padding_current(axs):
     lv = axs.PeriodicLevel((8, 6, 8), 0.5, dtype=torch.float64)
     lv.set_state(_to_dev(v))
     lv.advance(axs.Background.flat(1.0), 0.0, 0.0, 0.05, 3)
-    st = lv.state.cpu().numpy()
-    val = st[:, :, 2:-2, 4:-4]
-    np.testing.assert_array_equal(st[:, :, 2:-2, 0:4], val[:, :, :, -4:])
-    np.testing.assert_array_equal(st[:, :, 2:-2, -4:], val[:, :, :, :4])
-    np.testing.assert_array_equal(st[:, :, 0:2, 4:-4], val[:, :, -2:, :])
-    np.testing.assert_array_equal(st[:, :, -2:, 4:-4], val[:, :, :2, :])
+    _check_padding(lv, lv.get_state().cpu().numpy())
