@@ -46,6 +46,7 @@ constexpr int kDiagThreads = 256;
 struct DiagConst {
     double one_over_dx, R, lambda, RpR, m_r, threshold;
     double R2, inv_R, inv_R2, inv_R4;
+    double vel_a, vel_b, vel_c;  // gamma^2 v^2 = |phi'|^2 vel_a (1 - vel_b |phi|^2) - vel_c (phi . phi')^2
     int scheme;
     int want_energy, want_plaq, want_vel;
 };
@@ -112,25 +113,6 @@ __device__ __forceinline__ bool winding4_fast(float t1, float t2, float t3, floa
     return true;
 }
 
-// gamma^2 v^2 at one vertex (VelocityKernel.hpp:525-539 + Velocity.hpp:62-78)
-template <typename T>
-__device__ __forceinline__ double gvv(const DiagView &v, const DiagConst &q, int i, int j, int k)
-{
-    const double psi1 = ld<T>(v, 0, i, j, k), psi2 = ld<T>(v, 1, i, j, k);
-    const double Pi1 = ld<T>(v, 2, i, j, k), Pi2 = ld<T>(v, 3, i, j, k);
-    const double phi1 = psi1 / q.R, phi2 = psi2 / q.R;
-    const double pd1 = (Pi1 - q.RpR * psi1) / (q.R * q.R);
-    const double pd2 = (Pi2 - q.RpR * psi2) / (q.R * q.R);
-    const double c1 = 0.41222, e1 = -0.025763;
-    const double phi_sq = phi1 * phi1 + phi2 * phi2;
-    const double pd_sq = pd1 * pd1 + pd2 * pd2;
-    const double re = phi1 * pd1 + phi2 * pd2;
-    const double m2 = q.m_r * q.m_r, c1s = c1 * c1;
-    const double term1 = (pd_sq / (2.0 * m2 * c1s)) * (1.0 - e1 * phi_sq / (c1 * c1s));
-    const double term2 = (e1 / (4.0 * m2 * c1s * c1s * c1)) * re * re;
-    return term1 - term2;
-}
-
 // GRTeclyn diff1 (centred 4th order: weights 1/12, 2/3, times 1/dx) from
 // the four neighbours, rounded to the field precision as d1_scalar returns
 // amrex::Real. FP32 fields: the reference's expression order with explicit
@@ -152,11 +134,27 @@ __device__ __forceinline__ double diff1_vals(double m2, double m1, double p1, do
 }
 
 // Tiled diagnostics pass. A block owns a DTX x DTY tile of cells and marches
-// in z over a chunk; psi1/psi2 of five planes (tile plus a 2-cell halo) sit in
-// a shared ring for the gradient stencil, and single-precision phases of two
-// vertex planes sit beside them for the windings.
-constexpr int DTX = 32, DTY = 8, DHX = DTX + 4, DHY = DTY + 4;
+// in z over a chunk. Shared memory holds psi1/psi2 of five planes (tile plus a
+// 2-cell halo) for the gradient stencil, and for the two vertex planes z and
+// z+1 ((DTX+1) x (DTY+1) vertices): Pi1/Pi2, single-precision phases, and
+// gamma^2 v^2, each computed once per vertex. Plane loads use element offsets
+// precomputed per work item, so the march needs no index division.
+constexpr int DTX = 32, DTY = 8, DHX = DTX + 4, DHY = DTY + 4, DVX = DTX + 1, DVY = DTY + 1;
 static_assert(DTX * DTY == kDiagThreads, "one cell per thread");
+constexpr int kPsiPts = DHX * DHY, kVtxPts = DVX * DVY;
+constexpr int kPsiPer = (2 * kPsiPts + kDiagThreads - 1) / kDiagThreads;  // psi loads per thread per plane
+constexpr int kPiPer = (2 * kVtxPts + kDiagThreads - 1) / kDiagThreads;   // Pi loads per thread per plane
+constexpr int kVtxPer = (kVtxPts + kDiagThreads - 1) / kDiagThreads;      // vertices per thread per plane
+
+template <typename T> struct DiagSmem {
+    T ps[5][2][DHY][DHX];
+    T pi[2][2][DVY][DVX];
+    double gv[2][DVY][DVX];
+    float th[2][DVY][DVX];
+    unsigned char ok[2][DVY][DVX];
+};
+
+__device__ __forceinline__ int wrap_or_self(int i, int n, int wrap) { return wrap ? (i % n + n) % n : i; }
 
 template <typename T>
 __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v, const DiagConst q,
@@ -166,11 +164,11 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                                                                long long *__restrict__ list, long long capacity,
                                                                int tiles_x, int ntiles, int zchunk, long long n_items)
 {
-    __shared__ T ps[5][2][DHY][DHX];
-    __shared__ float th[2][DTY + 1][DTX + 1];
-    __shared__ unsigned char thok[2][DTY + 1][DTX + 1];
+    extern __shared__ __align__(16) unsigned char diag_smem_raw[];
+    DiagSmem<T> &sm = *reinterpret_cast<DiagSmem<T> *>(diag_smem_raw);
     __shared__ int warp_tot[kDiagThreads / 32];
     __shared__ unsigned long long block_base;
+    const T *__restrict__ base = static_cast<const T *>(v.data);
 
     double e[14];
 #pragma unroll
@@ -180,9 +178,6 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
 
     const int tid = threadIdx.x;
     const int lx = tid % DTX, ly = tid / DTX;
-    // the allocated extent along each axis (ghost reads stay inside it)
-    const int lo_x = v.wx ? INT_MIN / 2 : -v.ox, hi_x = v.wx ? INT_MAX / 2 : v.nx + v.ox;
-    const int lo_y = v.wy ? INT_MIN / 2 : -v.oy, hi_y = v.wy ? INT_MAX / 2 : v.ny + v.oy;
 
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
         const int tile = (int)(item % ntiles);
@@ -190,45 +185,90 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
         const int x0 = (tile % tiles_x) * DTX, y0 = (tile / tiles_x) * DTY;
         const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
 
-        auto load_plane = [&](int z) {
-            const int slot = ((z - za + 2) % 5 + 5) % 5;
-            // planes beyond the allocated ghosts are never needed by a valid
-            // result (the caller's ng covers what it asked for): read zeros
-            const bool zin = v.wz || (z >= -v.oz && z < v.nz + v.oz);
-            for (int idx = tid; idx < 2 * DHX * DHY; idx += kDiagThreads) {
-                const int c = idx / (DHX * DHY);
-                const int r = idx % (DHX * DHY);
-                const int hy = r / DHX, hx = r % DHX;
-                const int xx = x0 - 2 + hx, yy = y0 - 2 + hy;
-                T val = T(0);
-                if (zin && xx >= lo_x && xx < hi_x && yy >= lo_y && yy < hi_y && xx < v.nx + 2 && yy < v.ny + 2)
-                    val = __ldg(static_cast<const T *>(v.data) + view_off<T>(v, c, xx, yy, z));
-                ps[slot][c][hy][hx] = val;
+        // ---- per-item load plan: in-plane element offsets (wrapped or ghost) ----
+        int64_t psi_off[kPsiPer];  // component + in-plane element offset
+        bool psi_ok[kPsiPer];
+#pragma unroll
+        for (int u = 0; u < kPsiPer; ++u) {
+            const int idx = tid + u * kDiagThreads;
+            const int c = idx / kPsiPts, r = idx % kPsiPts;
+            const int xx = x0 - 2 + r % DHX, yy = y0 - 2 + r / DHX;
+            psi_ok[u] = idx < 2 * kPsiPts && xx < v.nx + 2 && yy < v.ny + 2 && (v.wx || (xx >= -v.ox && xx < v.nx + v.ox)) &&
+                        (v.wy || (yy >= -v.oy && yy < v.ny + v.oy));
+            psi_off[u] = c * v.cs + (int64_t)(wrap_or_self(xx, v.nx, v.wx) + v.ox) +
+                         (int64_t)(wrap_or_self(yy, v.ny, v.wy) + v.oy) * v.js;
+        }
+        int64_t pi_off[kPiPer];
+        bool pi_ok[kPiPer];
+#pragma unroll
+        for (int u = 0; u < kPiPer; ++u) {
+            const int idx = tid + u * kDiagThreads;
+            const int c = idx / kVtxPts, r = idx % kVtxPts;
+            const int xx = x0 + r % DVX, yy = y0 + r / DVX;
+            pi_ok[u] = idx < 2 * kVtxPts && xx <= v.nx && yy <= v.ny && (v.wx || xx < v.nx + v.ox) &&
+                       (v.wy || yy < v.ny + v.oy);
+            pi_off[u] = (2 + c) * v.cs + (int64_t)(wrap_or_self(xx, v.nx, v.wx) + v.ox) +
+                        (int64_t)(wrap_or_self(yy, v.ny, v.wy) + v.oy) * v.js;
+        }
+        auto plane_off = [&](int z, bool &zin) -> int64_t {
+            zin = v.wz || (z >= -v.oz && z < v.nz + v.oz);
+            return (int64_t)(wrap_or_self(z, v.nz, v.wz) + v.oz) * v.ks;
+        };
+        auto load_psi = [&](int z) {
+            bool zin;
+            const int64_t po = plane_off(z, zin);
+            T *dst = &sm.ps[((z - za + 2) % 5 + 5) % 5][0][0][0];
+#pragma unroll
+            for (int u = 0; u < kPsiPer; ++u) {
+                const int idx = tid + u * kDiagThreads;
+                if (idx < 2 * kPsiPts) dst[idx] = (zin && psi_ok[u]) ? __ldg(base + psi_off[u] + po) : T(0);
             }
         };
-        // single-precision phase of the (DTX+1) x (DTY+1) vertices of plane z
-        auto phases = [&](int z) {
-            const int slot = ((z - za + 2) % 5 + 5) % 5;
+        // vertex plane z: Pi, phases and gamma^2 v^2 (psi already in the ring)
+        auto vertex_plane = [&](int z) {
+            bool zin;
+            const int64_t po = plane_off(z, zin);
             const int ts = (z - za) & 1;
-            for (int idx = tid; idx < (DTX + 1) * (DTY + 1); idx += kDiagThreads) {
-                const int vy = idx / (DTX + 1), vx = idx % (DTX + 1);
-                const T a = ps[slot][0][vy + 2][vx + 2], b = ps[slot][1][vy + 2][vx + 2];
+            T *pdst = &sm.pi[ts][0][0][0];
+#pragma unroll
+            for (int u = 0; u < kPiPer; ++u) {
+                const int idx = tid + u * kDiagThreads;
+                if (idx < 2 * kVtxPts) pdst[idx] = (zin && pi_ok[u]) ? __ldg(base + pi_off[u] + po) : T(0);
+            }
+            const int slot = ((z - za + 2) % 5 + 5) % 5;
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < kVtxPer; ++u) {
+                const int idx = tid + u * kDiagThreads;
+                if (idx >= kVtxPts) break;
+                const int vy = idx / DVX, vx = idx % DVX;
+                const T a = sm.ps[slot][0][vy + 2][vx + 2], b = sm.ps[slot][1][vy + 2][vx + 2];
                 const double m = fmax(fabs((double)a), fabs((double)b));
                 // float conversion keeps the angle to ~1e-7 only away from under/overflow
-                thok[ts][vy][vx] = (m > 1e-30 && m < 1e30) ? 1 : 0;
-                th[ts][vy][vx] = atan2f((float)b, (float)a);
+                sm.ok[ts][vy][vx] = (m > 1e-30 && m < 1e30) ? 1 : 0;
+                sm.th[ts][vy][vx] = atan2f((float)b, (float)a);
+                if (q.want_vel) {
+                    const double psi1 = a, psi2 = b, Pi1 = sm.pi[ts][0][vy][vx], Pi2 = sm.pi[ts][1][vy][vx];
+                    const double phi1 = psi1 * q.inv_R, phi2 = psi2 * q.inv_R;
+                    const double pd1 = (Pi1 - q.RpR * psi1) * q.inv_R2, pd2 = (Pi2 - q.RpR * psi2) * q.inv_R2;
+                    const double phi_sq = phi1 * phi1 + phi2 * phi2;
+                    const double pd_sq = pd1 * pd1 + pd2 * pd2;
+                    const double re = phi1 * pd1 + phi2 * pd2;
+                    // Velocity.hpp:62-78 with the constant prefactors folded on the host
+                    sm.gv[ts][vy][vx] = pd_sq * q.vel_a * (1.0 - q.vel_b * phi_sq) - q.vel_c * re * re;
+                }
             }
         };
 
-        for (int p = -2; p <= 1; ++p) load_plane(za + p);
+        for (int p = -2; p <= 1; ++p) load_psi(za + p);
         __syncthreads();
-        phases(za);
+        vertex_plane(za);
 
         for (int m = 0; m < len; ++m) {
             const int z = za + m;
-            load_plane(z + 2);
+            load_psi(z + 2);
             __syncthreads();
-            phases(z + 1);
+            vertex_plane(z + 1);
             __syncthreads();
 
             const int x = x0 + lx, y = y0 + ly;
@@ -236,22 +276,23 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             const bool in = x < v.nx && y < v.ny && (mask == nullptr || mask[cell] != 0);
             int w[3] = {0, 0, 0};
             if (in) {
-                const int s0 = ((m + 2) % 5);
+                const int s0 = (m + 2) % 5;
                 const int sm1 = (m + 1) % 5, sp1 = (m + 3) % 5, sm2 = m % 5, sp2 = (m + 4) % 5;
+                const int t0 = m & 1, t1 = (m + 1) & 1;
                 const int hx = lx + 2, hy = ly + 2;
                 if (q.want_energy) {
-                    const double psi1 = ps[s0][0][hy][hx], psi2 = ps[s0][1][hy][hx];
-                    const double Pi1 = ld<T>(v, 2, x, y, z), Pi2 = ld<T>(v, 3, x, y, z);
+                    const double psi1 = sm.ps[s0][0][hy][hx], psi2 = sm.ps[s0][1][hy][hx];
+                    const double Pi1 = sm.pi[t0][0][ly][lx], Pi2 = sm.pi[t0][1][ly][lx];
                     const double psi_sq = psi1 * psi1 + psi2 * psi2;
                     double g[2][3];
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
-                        g[c][0] = diff1_vals<T>(ps[s0][c][hy][hx - 2], ps[s0][c][hy][hx - 1], ps[s0][c][hy][hx + 1],
-                                                ps[s0][c][hy][hx + 2], q.one_over_dx);
-                        g[c][1] = diff1_vals<T>(ps[s0][c][hy - 2][hx], ps[s0][c][hy - 1][hx], ps[s0][c][hy + 1][hx],
-                                                ps[s0][c][hy + 2][hx], q.one_over_dx);
-                        g[c][2] = diff1_vals<T>(ps[sm2][c][hy][hx], ps[sm1][c][hy][hx], ps[sp1][c][hy][hx],
-                                                ps[sp2][c][hy][hx], q.one_over_dx);
+                        g[c][0] = diff1_vals<T>(sm.ps[s0][c][hy][hx - 2], sm.ps[s0][c][hy][hx - 1],
+                                                sm.ps[s0][c][hy][hx + 1], sm.ps[s0][c][hy][hx + 2], q.one_over_dx);
+                        g[c][1] = diff1_vals<T>(sm.ps[s0][c][hy - 2][hx], sm.ps[s0][c][hy - 1][hx],
+                                                sm.ps[s0][c][hy + 1][hx], sm.ps[s0][c][hy + 2][hx], q.one_over_dx);
+                        g[c][2] = diff1_vals<T>(sm.ps[sm2][c][hy][hx], sm.ps[sm1][c][hy][hx], sm.ps[sp1][c][hy][hx],
+                                                sm.ps[sp2][c][hy][hx], q.one_over_dx);
                     }
                     double g1sq = 0.0, g2sq = 0.0, cross2 = 0.0;
 #pragma unroll
@@ -268,9 +309,8 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     const double pot = 0.25 * q.lambda * dsq * dsq;
                     const double rho = (c1 * c1 + c2 * c2 + (g1sq + g2sq) + pot) * q.inv_R4;
                     const double thp = (psi1 * Pi2 - Pi1 * psi2) * inv_psq;
-                    const double fa = 1.4142135623730951;
-                    const double akin = 0.5 * (fa * thp * q.inv_R) * (fa * thp * q.inv_R);
-                    const double agrad = 0.5 * fa * fa * gtsq * q.inv_R2;
+                    const double akin = thp * thp * q.inv_R2;  // 1/2 (sqrt(2) theta'/R)^2
+                    const double agrad = gtsq * q.inv_R2;      // 1/2 sqrt(2)^2 |grad theta|^2 / R^2
                     const double rdot = psi1 * c1 + psi2 * c2;
                     const double rkin = rdot * rdot * inv_psq * q.inv_R4;
                     const double rgrad = (g1sq + g2sq - psi_sq * gtsq) * q.inv_R4;
@@ -281,7 +321,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                         if (q.scheme == AXS_MASK_B) {
                             wgt = (mod >= q.threshold) ? 1.0 : 0.0;
                         } else {
-                            const double f = 1.0 + (mod - 1.0) / fa;
+                            const double f = 1.0 + (mod - 1.0) * 0.70710678118654752440;  // 1 + r / f_a
                             wgt = f * f;
                         }
                     }
@@ -294,14 +334,13 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     e[12] += wgt;  e[13] += 1.0;
                 }
                 if (q.want_plaq || q.want_vel) {
-                    const int t0 = m & 1, t1 = (m + 1) & 1;
                     // corner phases (x, y, z offsets) in the reference's order
-                    const float f000 = th[t0][ly][lx], f100 = th[t0][ly][lx + 1], f110 = th[t0][ly + 1][lx + 1];
-                    const float f010 = th[t0][ly + 1][lx], f001 = th[t1][ly][lx], f101 = th[t1][ly][lx + 1];
-                    const float f011 = th[t1][ly + 1][lx];
-                    const bool ok = thok[t0][ly][lx] & thok[t0][ly][lx + 1] & thok[t0][ly + 1][lx + 1] &
-                                    thok[t0][ly + 1][lx] & thok[t1][ly][lx] & thok[t1][ly][lx + 1] &
-                                    thok[t1][ly + 1][lx];
+                    const float f000 = sm.th[t0][ly][lx], f100 = sm.th[t0][ly][lx + 1];
+                    const float f110 = sm.th[t0][ly + 1][lx + 1], f010 = sm.th[t0][ly + 1][lx];
+                    const float f001 = sm.th[t1][ly][lx], f101 = sm.th[t1][ly][lx + 1], f011 = sm.th[t1][ly + 1][lx];
+                    const bool ok = sm.ok[t0][ly][lx] & sm.ok[t0][ly][lx + 1] & sm.ok[t0][ly + 1][lx + 1] &
+                                    sm.ok[t0][ly + 1][lx] & sm.ok[t1][ly][lx] & sm.ok[t1][ly][lx + 1] &
+                                    sm.ok[t1][ly + 1][lx];
                     bool fast = ok;
                     if (fast) fast = winding4_fast(f000, f100, f110, f010, w[0]);
                     if (fast) fast = winding4_fast(f000, f010, f011, f001, w[1]);
@@ -309,13 +348,13 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     if (!fast) {
                         // near the branch cut or outside the float range: the reference's
                         // double arithmetic for this cell's three plaquettes
-                        const int sz1 = (m + 3) % 5;
                         auto dph = [&](int slot, int ox_, int oy_) {
-                            return atan2((double)ps[slot][1][hy + oy_][hx + ox_], (double)ps[slot][0][hy + oy_][hx + ox_]);
+                            return atan2((double)sm.ps[slot][1][hy + oy_][hx + ox_],
+                                         (double)sm.ps[slot][0][hy + oy_][hx + ox_]);
                         };
                         const double d000 = dph(s0, 0, 0), d100 = dph(s0, 1, 0), d110 = dph(s0, 1, 1);
-                        const double d010 = dph(s0, 0, 1), d001 = dph(sz1, 0, 0), d101 = dph(sz1, 1, 0);
-                        const double d011 = dph(sz1, 0, 1);
+                        const double d010 = dph(s0, 0, 1), d001 = dph(sp1, 0, 0), d101 = dph(sp1, 1, 0);
+                        const double d011 = dph(sp1, 0, 1);
                         int ties = 0;
                         w[0] = winding4(d000, d100, d110, d010, ties);
                         w[1] = winding4(d000, d010, d011, d001, ties);
@@ -325,23 +364,15 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     cnt[0] += (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
                     cnt[1] += abs(w[0]) + abs(w[1]) + abs(w[2]);
                     if (q.want_vel && (w[0] | w[1] | w[2])) {
+                        const double g000 = sm.gv[t0][ly][lx], g100 = sm.gv[t0][ly][lx + 1];
+                        const double g110 = sm.gv[t0][ly + 1][lx + 1], g010 = sm.gv[t0][ly + 1][lx];
+                        const double g001 = sm.gv[t1][ly][lx], g101 = sm.gv[t1][ly][lx + 1];
+                        const double g011 = sm.gv[t1][ly + 1][lx];
                         double s = 0.0;
                         long long c = 0;
-                        if (w[0]) {
-                            s += gvv<T>(v, q, x, y, z) + gvv<T>(v, q, x + 1, y, z) + gvv<T>(v, q, x + 1, y + 1, z) +
-                                 gvv<T>(v, q, x, y + 1, z);
-                            c += 4;
-                        }
-                        if (w[1]) {
-                            s += gvv<T>(v, q, x, y, z) + gvv<T>(v, q, x, y + 1, z) + gvv<T>(v, q, x, y + 1, z + 1) +
-                                 gvv<T>(v, q, x, y, z + 1);
-                            c += 4;
-                        }
-                        if (w[2]) {
-                            s += gvv<T>(v, q, x, y, z) + gvv<T>(v, q, x, y, z + 1) + gvv<T>(v, q, x + 1, y, z + 1) +
-                                 gvv<T>(v, q, x + 1, y, z);
-                            c += 4;
-                        }
+                        if (w[0]) { s += g000 + g100 + g110 + g010; c += 4; }
+                        if (w[1]) { s += g000 + g010 + g011 + g001; c += 4; }
+                        if (w[2]) { s += g000 + g001 + g101 + g100; c += 4; }
                         vsum += s;
                         cnt[2] += c;
                     }
@@ -376,7 +407,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     }
                 }
             }
-            __syncthreads();  // ring slots and phase planes are rewritten next plane
+            __syncthreads();  // ring slots and vertex planes are rewritten next plane
         }
     }
 
@@ -519,6 +550,14 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     q.inv_R = 1.0 / p->R;
     q.inv_R2 = 1.0 / q.R2;
     q.inv_R4 = q.inv_R2 * q.inv_R2;
+    {
+        // Velocity.hpp:62-78: term1 = |phi'|^2/(2 m^2 c1^2) (1 - e1 |phi|^2/c1^3),
+        //                     term2 = e1/(4 m^2 c1^5) (phi . phi')^2
+        const double c1 = 0.41222, e1 = -0.025763, m2 = p->m_r * p->m_r, c1s = c1 * c1;
+        q.vel_a = 1.0 / (2.0 * m2 * c1s);
+        q.vel_b = e1 / (c1 * c1s);
+        q.vel_c = e1 / (4.0 * m2 * c1s * c1s * c1);
+    }
     q.lambda = p->lambda;
     q.RpR = p->R_prime_over_R;
     q.m_r = p->m_r;
@@ -534,12 +573,17 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     long long items;
     diag_plan(v, diag_grid(ncell), tiles_x, ntiles, zchunk, items, grid);
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
-    if (v.dtype == AXS_F64)
-        diag_kernel<double><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
+    if (v.dtype == AXS_F64) {
+        const size_t sm = sizeof(DiagSmem<double>);
+        AXS_CUDA_CHECK(cudaFuncSetAttribute(diag_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        diag_kernel<double><<<grid, kDiagThreads, sm, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
+                                                            ntiles, zchunk, items);
+    } else {
+        const size_t sm = sizeof(DiagSmem<float>);
+        AXS_CUDA_CHECK(cudaFuncSetAttribute(diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        diag_kernel<float><<<grid, kDiagThreads, sm, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
                                                            ntiles, zchunk, items);
-    else
-        diag_kernel<float><<<grid, kDiagThreads, 0, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
-                                                          ntiles, zchunk, items);
+    }
     int rc = launch_status("diagnostics");
     if (rc) return rc;
     diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);

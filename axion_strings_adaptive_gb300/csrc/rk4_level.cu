@@ -29,7 +29,7 @@
 #include <cmath>
 #include <vector>
 
-#include "axs_internal.cuh"
+#include "sweep.cuh"
 
 namespace axs {
 
@@ -37,258 +37,62 @@ int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const L
                       cudaStream_t st);
 int level_copy_fab(void *lv, int32_t dtype, const LevelGeom &g, const axs_fab &f, int to_level, cudaStream_t st);
 
-template <typename T> struct StageCoef {
-    T kappa, hlam, R2;  // kappa, lambda/2, R^2 at one stage time
+// Sweep A: stencil on (psi_n, Pi_n); writes S3, S4 (with periodic copies) and G, P.
+struct ForwardA {
+    static constexpr int kPointwise = 0;
+    static constexpr bool kLambdaGrad = false;
+    template <typename T, int V, typename PQ>
+    __device__ static void apply(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V], const PQ &,
+                                 int64_t off, int x, int y, double &)
+    {
+        T o[8][V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const T p1 = ctr[0][v], p2 = ctr[1][v], q1 = ctr[2][v], q2 = ctr[3][v];
+            T f11, f12, f21, f22;
+            rhs_pair(a.c1, p1, p2, lap[0][v], lap[1][v], f11, f12);  // F1 = F(t, psi_n)
+            // F2 = F(t + h/2, chi), chi = psi_n + h/2 Pi_n, lap(chi) = lap(psi) + h/2 lap(Pi)
+            const T c1 = fma(a.h_half, q1, p1), c2 = fma(a.h_half, q2, p2);
+            rhs_pair(a.c2, c1, c2, fma(a.h_half, lap[2][v], lap[0][v]), fma(a.h_half, lap[3][v], lap[1][v]), f21, f22);
+            o[0][v] = fma(a.h2_quarter, f11, c1);                     // S3
+            o[1][v] = fma(a.h2_quarter, f12, c2);
+            o[2][v] = fma(a.h2_half, f21, fma(a.h, q1, p1));          // S4
+            o[3][v] = fma(a.h2_half, f22, fma(a.h, q2, p2));
+            o[4][v] = fma(T(-2), f21, f11);                          // G = F1 - 2 F2
+            o[5][v] = fma(T(-2), f22, f12);
+            o[6][v] = fma(a.h_third, f21, fma(a.h_sixth, f11, q1));  // P = Pi + h/6 F1 + h/3 F2
+            o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, o[c]);
+#pragma unroll
+        for (int c = 4; c < 8; ++c) stv<T, V>(a.out[c] + off, o[c]);
+    }
 };
 
-template <typename T> struct SweepArgs {
-    int nx, ny, nz;
-    int tiles_x, ntiles, zchunk;
-    int64_t n_items;
-    int64_t js, ks, cs;
-    int ox;                     // x offset of the valid region in a padded row
-    T wA, wB, wC;               // lap = wA*S1 + wB*S2 + wC*f0 (S1/S2: sums of +-1 / +-2 neighbours)
-    StageCoef<T> ca, cb;        // sweep A: F1, F2; sweep B: F3, F4
-    T h, h_half, h2_quarter, h2_half, h_sixth, h_third, h2_sixth;
-    T *state;                   // sweep B output (4 comps, padded copies kept current)
-    T *work;                    // sweep A output (8 comps); sweep B pointwise input (comps 4..7)
-    unsigned *status;
+// Sweep B: stencil on (S3, S4), pointwise (G, P); writes psi_{n+1}, Pi_{n+1}.
+struct ForwardB {
+    static constexpr int kPointwise = 4;
+    static constexpr bool kLambdaGrad = false;
+    template <typename T, int V, typename PQ>
+    __device__ static void apply(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V], const PQ &pq,
+                                 int64_t off, int x, int y, double &)
+    {
+        T o[4][V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            T f31, f32, f41, f42;
+            rhs_pair(a.c2, ctr[0][v], ctr[1][v], lap[0][v], lap[1][v], f31, f32);  // F3 = F(t + h/2, S3)
+            rhs_pair(a.c4, ctr[2][v], ctr[3][v], lap[2][v], lap[3][v], f41, f42);  // F4 = F(t + h, S4)
+            o[0][v] = fma(a.h2_sixth, pq[0][v] + f31, ctr[2][v]);
+            o[1][v] = fma(a.h2_sixth, pq[1][v] + f32, ctr[3][v]);
+            o[2][v] = fma(a.h_sixth, f41, fma(a.h_third, f31, pq[2][v]));
+            o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[3][v]));
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, o[c]);
+    }
 };
-
-template <typename T, int V, int TX, int TY> struct SweepShape {
-    static constexpr int NTX = TX / V;
-    static constexpr int NT = NTX * TY;
-    static constexpr int BX = TX + 8;
-    static constexpr int BY = TY + 4;
-    static constexpr int TILE = BX * BY;
-    static constexpr int SLOT = 4 * TILE;
-    static constexpr uint32_t SLOT_BYTES = SLOT * sizeof(T);
-    static constexpr int PRE = (2 + V - 1) / V;  // vectors left/right of the centre that cover +-2
-    static constexpr int NROW = 2 * PRE + 1;
-    static_assert(TX % V == 0 && 4 % V == 0, "tile width and halo must hold whole vectors");
-    static_assert((BX * sizeof(T)) % 16 == 0, "TMA box row must be a multiple of 16 bytes");
-    static_assert(SLOT_BYTES % 128 == 0, "ring slots must stay 128-byte aligned");
-    static_assert(BX <= 256 && BY <= 256, "TMA box extent limit");
-};
-
-template <typename T, int V>
-__device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
-                                                  const T *v)
-{
-    stv<T, V>(base + off, v);
-    if (x < 4) stv<T, V>(base + off + nx, v);
-    if (x >= nx - 4) stv<T, V>(base + off - nx, v);
-    if (y < 2) stv<T, V>(base + off + (int64_t)ny * js, v);
-    if (y >= ny - 2) stv<T, V>(base + off - (int64_t)ny * js, v);
-}
-
-template <typename T, int V, int TX, int TY, int NS, int MINB, int SWEEP>
-__global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
-    rk4_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
-{
-    using S = SweepShape<T, V, TX, TY>;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    T *ring = reinterpret_cast<T *>(smem_raw);
-    __shared__ uint64_t full[NS];
-    __shared__ int abort_flag;
-
-    const int tid = threadIdx.x;
-    const int tx = tid % S::NTX, ty = tid / S::NTX;
-
-    if (tid == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
-        fence_mbar_init();
-        abort_flag = 0;
-        prefetch_tensormap(&tmap);
-    }
-    __syncthreads();
-
-    // ---- producer cursor (thread 0 only) ----
-    int64_t p_item = blockIdx.x;
-    int p_k = 0;
-    int64_t q_issued = 0;
-    auto issue_one = [&]() -> bool {
-        if (p_item >= a.n_items) return false;
-        const int tile = (int)(p_item % a.ntiles);
-        const int chunk = (int)(p_item / a.ntiles);
-        const int za = chunk * a.zchunk;
-        const int len = min(a.zchunk, a.nz - za);
-        int zp = (za - 2 + p_k) % a.nz;
-        if (zp < 0) zp += a.nz;
-        const int slot = (int)(q_issued % NS);
-        mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
-        // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned)
-        tma_load_4d(ring + (size_t)slot * S::SLOT, &tmap, a.ox - 4 + (tile % a.tiles_x) * TX,
-                    (tile / a.tiles_x) * TY, zp, 0, &full[slot]);
-        ++q_issued;
-        if (++p_k == len + 4) {
-            p_k = 0;
-            p_item += gridDim.x;
-        }
-        return true;
-    };
-    if (tid == 0) {
-        for (int s = 0; s < NS; ++s)
-            if (!issue_one()) break;
-    }
-
-    int64_t q_base = 0, q_waited = 0;
-    bool aborted = false;
-    const int xl = 4 + V * tx;  // tile-local column of this thread's first site
-    const int yl = 2 + ty;
-    for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-        const int tile = (int)(item % a.ntiles);
-        const int chunk = (int)(item / a.ntiles);
-        const int za = chunk * a.zchunk;
-        const int len = min(a.zchunk, a.nz - za);
-        const int x = (tile % a.tiles_x) * TX + V * tx;
-        const int y = (tile / a.tiles_x) * TY + ty;
-        const bool active = (x < a.nx) && (y < a.ny);
-        // sweep B: the pointwise increments (G, P) of the next plane are loaded
-        // one iteration ahead, so their latency hides behind a whole plane of work
-        T gn[2][V], pn[2][V];
-        if constexpr (SWEEP == 1) {
-            if (active) {
-                const int64_t off0 = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)za * a.ks;
-                ldv_nc<T, V>(a.work + 4 * a.cs + off0, gn[0]);
-                ldv_nc<T, V>(a.work + 5 * a.cs + off0, gn[1]);
-                ldv_nc<T, V>(a.work + 6 * a.cs + off0, pn[0]);
-                ldv_nc<T, V>(a.work + 7 * a.cs + off0, pn[1]);
-            }
-        }
-        for (int m = 0; m < len; ++m) {
-            const int z = za + m;
-            const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)z * a.ks;
-
-            T gq[2][V], pq[2][V];
-            if constexpr (SWEEP == 1) {
-#pragma unroll
-                for (int i = 0; i < 2; ++i)
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        gq[i][v] = gn[i][v];
-                        pq[i][v] = pn[i][v];
-                    }
-                if (active && m + 1 < len) {
-                    ldv_nc<T, V>(a.work + 4 * a.cs + off + a.ks, gn[0]);
-                    ldv_nc<T, V>(a.work + 5 * a.cs + off + a.ks, gn[1]);
-                    ldv_nc<T, V>(a.work + 6 * a.cs + off + a.ks, pn[0]);
-                    ldv_nc<T, V>(a.work + 7 * a.cs + off + a.ks, pn[1]);
-                }
-            }
-
-            const int64_t need = q_base + m + 4;
-            while (q_waited <= need) {
-                const int slot = (int)(q_waited % NS);
-                if (!mbar_wait_bounded(&full[slot], (uint32_t)((q_waited / NS) & 1))) {
-                    atomicOr(a.status, kDevTimeout);
-                    abort_flag = 1;
-                }
-                ++q_waited;
-            }
-
-            const T *sl[5];
-#pragma unroll
-            for (int d = 0; d < 5; ++d) sl[d] = ring + (size_t)((q_base + m + d) % NS) * S::SLOT;
-
-            if (active) {
-                T lap[4][V], ctr[4][V];
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const T *P0 = sl[2] + c * S::TILE;
-                    T row[S::NROW * V], ym1[V], yp1[V], ym2[V], yp2[V], zm1[V], zp1[V], zm2[V], zp2[V];
-#pragma unroll
-                    for (int r = 0; r < S::NROW; ++r) ldv<T, V>(P0 + yl * S::BX + xl + (r - S::PRE) * V, row + r * V);
-                    ldv<T, V>(P0 + (yl - 1) * S::BX + xl, ym1);
-                    ldv<T, V>(P0 + (yl + 1) * S::BX + xl, yp1);
-                    ldv<T, V>(P0 + (yl - 2) * S::BX + xl, ym2);
-                    ldv<T, V>(P0 + (yl + 2) * S::BX + xl, yp2);
-                    ldv<T, V>(sl[1] + c * S::TILE + yl * S::BX + xl, zm1);
-                    ldv<T, V>(sl[3] + c * S::TILE + yl * S::BX + xl, zp1);
-                    ldv<T, V>(sl[0] + c * S::TILE + yl * S::BX + xl, zm2);
-                    ldv<T, V>(sl[4] + c * S::TILE + yl * S::BX + xl, zp2);
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        const int ci = S::PRE * V + v;
-                        const T f0 = row[ci];
-                        const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
-                        const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
-                        lap[c][v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
-                        ctr[c][v] = f0;
-                    }
-                }
-
-                if constexpr (SWEEP == 0) {
-                    T o[8][V];
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        const T p1 = ctr[0][v], p2 = ctr[1][v], q1 = ctr[2][v], q2 = ctr[3][v];
-                        // F1 = F(t, psi_n)
-                        const T k1 = fma(-a.ca.hlam, fma(p1, p1, p2 * p2) - a.ca.R2, a.ca.kappa);
-                        const T f11 = fma(k1, p1, lap[0][v]);
-                        const T f12 = fma(k1, p2, lap[1][v]);
-                        // F2 = F(t + h/2, chi), chi = psi_n + h/2 Pi_n, lap(chi) = lap(psi) + h/2 lap(Pi)
-                        const T c1 = fma(a.h_half, q1, p1), c2 = fma(a.h_half, q2, p2);
-                        const T k2 = fma(-a.cb.hlam, fma(c1, c1, c2 * c2) - a.cb.R2, a.cb.kappa);
-                        const T f21 = fma(k2, c1, fma(a.h_half, lap[2][v], lap[0][v]));
-                        const T f22 = fma(k2, c2, fma(a.h_half, lap[3][v], lap[1][v]));
-                        o[0][v] = fma(a.h2_quarter, f11, c1);                     // S3
-                        o[1][v] = fma(a.h2_quarter, f12, c2);
-                        o[2][v] = fma(a.h2_half, f21, fma(a.h, q1, p1));          // S4
-                        o[3][v] = fma(a.h2_half, f22, fma(a.h, q2, p2));
-                        o[4][v] = fma(T(-2), f21, f11);                          // G = F1 - 2 F2
-                        o[5][v] = fma(T(-2), f22, f12);
-                        o[6][v] = fma(a.h_third, f21, fma(a.h_sixth, f11, q1));  // P = Pi + h/6 F1 + h/3 F2
-                        o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
-                    }
-#pragma unroll
-                    for (int c = 0; c < 4; ++c)
-                        store_with_copies<T, V>(a.work + c * a.cs, off, x, y, a.nx, a.ny, a.js, o[c]);
-#pragma unroll
-                    for (int c = 4; c < 8; ++c) stv<T, V>(a.work + c * a.cs + off, o[c]);
-                } else {
-                    T o[4][V];
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        const T s31 = ctr[0][v], s32 = ctr[1][v], s41 = ctr[2][v], s42 = ctr[3][v];
-                        const T k3 = fma(-a.ca.hlam, fma(s31, s31, s32 * s32) - a.ca.R2, a.ca.kappa);
-                        const T f31 = fma(k3, s31, lap[0][v]);
-                        const T f32 = fma(k3, s32, lap[1][v]);
-                        const T k4 = fma(-a.cb.hlam, fma(s41, s41, s42 * s42) - a.cb.R2, a.cb.kappa);
-                        const T f41 = fma(k4, s41, lap[2][v]);
-                        const T f42 = fma(k4, s42, lap[3][v]);
-                        o[0][v] = fma(a.h2_sixth, gq[0][v] + f31, s41);
-                        o[1][v] = fma(a.h2_sixth, gq[1][v] + f32, s42);
-                        o[2][v] = fma(a.h_sixth, f41, fma(a.h_third, f31, pq[0][v]));
-                        o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[1][v]));
-                    }
-#pragma unroll
-                    for (int c = 0; c < 4; ++c)
-                        store_with_copies<T, V>(a.state + c * a.cs, off, x, y, a.nx, a.ny, a.js, o[c]);
-                }
-            }
-
-            __syncthreads();  // everyone is done with the oldest plane of this window
-            if (abort_flag) {
-                aborted = true;
-                break;
-            }
-            const int64_t next_needed = (m + 1 < len) ? (q_base + m + 1) : (q_base + len + 4);
-            if (tid == 0) {
-                fence_proxy_async_smem();
-                while (q_issued < next_needed + NS && issue_one()) {
-                }
-            }
-        }
-        if (aborted) break;
-        q_base += len + 4;
-    }
-    // A wait expired: make sure no bulk copy is still landing in shared memory
-    // before the block exits (bounded as well).
-    if (aborted && tid == 0) {
-        for (int64_t q = q_waited; q < q_issued; ++q) mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 1u << 20);
-    }
-}
 
 // ---------------------------------------------------------------- host side
 int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g)
@@ -336,123 +140,82 @@ struct SweepRunArgs {
     cudaStream_t st;
 };
 
-// Pick the z-chunk length: balance the last wave against the 4 warm-up
-// planes each chunk costs, and keep the SMs busy.
-static void plan_chunks(int ntiles, int nz, int grid_cap, int &zchunk, int64_t &items, int &grid)
+// Fill the step-independent part of the sweep arguments.
+template <typename T>
+static void fill_step_constants(SweepArgs<T> &a, const axs_level *lv, const LevelGeom &g, double dt)
 {
-    double best = -1.0;
-    zchunk = nz;
-    for (int nch = 1; nch <= nz; ++nch) {
-        const int lz = (nz + nch - 1) / nch;
-        if ((nz + lz - 1) / lz != nch) continue;
-        const int64_t it = (int64_t)ntiles * nch;
-        const int g = (int)std::min<int64_t>(it, grid_cap);
-        const int64_t waves = (it + g - 1) / g;
-        const double fill = (double)it / (double)(waves * g);
-        const double warm = (double)lz / (double)(lz + 4);
-        const double par = (double)g / (double)grid_cap;
-        const double score = fill * warm * std::min(1.0, par * 1.25);
-        if (score > best + 1e-9) {
-            best = score;
-            zchunk = lz;
-        }
-    }
-    items = (int64_t)ntiles * ((nz + zchunk - 1) / zchunk);
-    grid = (int)std::min<int64_t>(items, grid_cap);
+    a.js = g.js;
+    a.ks = g.ks;
+    a.cs = g.cs;
+    a.ox = g.ox;
+    const double inv_dx2 = 1.0 / (lv->dx * lv->dx);
+    a.wA = T((4.0 / 3.0) * inv_dx2);
+    a.wB = T((-1.0 / 12.0) * inv_dx2);
+    a.wC = T(-7.5 * inv_dx2);
+    a.h = T(dt);
+    a.h_half = T(0.5 * dt);
+    a.h2_quarter = T(0.25 * dt * dt);
+    a.h2_half = T(0.5 * dt * dt);
+    a.h_sixth = T(dt / 6.0);
+    a.h_third = T(dt / 3.0);
+    a.h2_sixth = T(dt * dt / 6.0);
+    a.status = level_status_word(lv, g);
+}
+
+template <typename T> static StageCoef<T> stage_coef(const axs_background &bg, double tau)
+{
+    axs_rhs_coeffs c;
+    rhs_coeffs(bg, tau, c);
+    return StageCoef<T>{T(c.kappa), T(0.5 * c.lambda), T(c.R2)};
+}
+
+int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const LevelGeom &g, int ny, int nz,
+                   uint32_t box_x, uint32_t box_y)
+{
+    const uint64_t es = dtype_size(dtype);
+    return make_tensor_map_4d(map, base, dtype, g.js, ny + 4, nz, 4, g.js * es, g.ks * es, g.cs * es, box_x, box_y, 1,
+                              4);
 }
 
 template <typename T, int V, int TX, int TY, int NS, int MINB> struct SweepConfig {
-    using S = SweepShape<T, V, TX, TY>;
-    static size_t smem() { return (size_t)NS * S::SLOT_BYTES; }
-
-    static int prepare(int &blocks_per_sm)
-    {
-        static int cached = -1;
-        if (cached < 0) {
-            AXS_CUDA_CHECK(cudaFuncSetAttribute(rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 0>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
-            AXS_CUDA_CHECK(cudaFuncSetAttribute(rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 1>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
-            int b0 = 0, b1 = 0;
-            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &b0, rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 0>, S::NT, smem()));
-            AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &b1, rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 1>, S::NT, smem()));
-            cached = std::max(1, std::min(b0, b1));
-        }
-        blocks_per_sm = cached;
-        return AXS_OK;
-    }
+    using LA = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardA>;
+    using LB = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardB>;
 
     static int run(const SweepRunArgs &r)
     {
         const axs_level *lv = r.lv;
         const LevelGeom &g = *r.g;
-        int bps = 0;
-        int rc = prepare(bps);
-        if (rc) return rc;
-        const int sms = device_sm_count();
-        AXS_REQUIRE(sms > 0, AXS_ERR_CUDA, "no CUDA device");
-        const int tiles_x = (lv->nx + TX - 1) / TX, tiles_y = (lv->ny + TY - 1) / TY;
         SweepArgs<T> a{};
-        a.nx = lv->nx;
-        a.ny = lv->ny;
-        a.nz = lv->nz;
-        a.tiles_x = tiles_x;
-        a.ntiles = tiles_x * tiles_y;
-        int grid = 0;
-        plan_chunks(a.ntiles, lv->nz, bps * sms, a.zchunk, a.n_items, grid);
-        a.js = g.js;
-        a.ks = g.ks;
-        a.cs = g.cs;
-        a.ox = g.ox;
-        const double inv_dx2 = 1.0 / (lv->dx * lv->dx);
-        a.wA = T((4.0 / 3.0) * inv_dx2);
-        a.wB = T((-1.0 / 12.0) * inv_dx2);
-        a.wC = T(-7.5 * inv_dx2);
-        const double h = r.dt;
-        a.h = T(h);
-        a.h_half = T(0.5 * h);
-        a.h2_quarter = T(0.25 * h * h);
-        a.h2_half = T(0.5 * h * h);
-        a.h_sixth = T(h / 6.0);
-        a.h_third = T(h / 3.0);
-        a.h2_sixth = T(h * h / 6.0);
-        a.state = static_cast<T *>(lv->state);
-        a.work = static_cast<T *>(lv->work);
-        a.status = level_status_word(lv, g);
-
-        const size_t es = sizeof(T);
+        int grid = 0, grid_b = 0;
+        int rc = LA::plan(a, lv->nx, lv->ny, lv->nz, grid);
+        if (rc) return rc;
+        SweepArgs<T> tmp = a;
+        if ((rc = LB::plan(tmp, lv->nx, lv->ny, lv->nz, grid_b))) return rc;
+        fill_step_constants(a, lv, g, r.dt);
+        T *state = static_cast<T *>(lv->state), *work = static_cast<T *>(lv->work);
         CUtensorMap map_state, map_work;
-        rc = make_tensor_map_4d(&map_state, lv->state, lv->dtype, g.js, lv->ny + 4, lv->nz, 4, g.js * es, g.ks * es,
-                                g.cs * es, S::BX, S::BY, 1, 4);
-        if (rc) return rc;
-        rc = make_tensor_map_4d(&map_work, lv->work, lv->dtype, g.js, lv->ny + 4, lv->nz, 4, g.js * es, g.ks * es,
-                                g.cs * es, S::BX, S::BY, 1, 4);
-        if (rc) return rc;
-
-        auto coef = [&](double tau) {
-            axs_rhs_coeffs c;
-            rhs_coeffs(*r.bg, tau, c);
-            return StageCoef<T>{T(c.kappa), T(0.5 * c.lambda), T(c.R2)};
-        };
+        if ((rc = make_level_map(&map_state, state, lv->dtype, g, lv->ny, lv->nz, LA::box_x(), LA::box_y())))
+            return rc;
+        if ((rc = make_level_map(&map_work, work, lv->dtype, g, lv->ny, lv->nz, LB::box_x(), LB::box_y())))
+            return rc;
         for (int s = 0; s < r.nsteps; ++s) {
             const double t = r.t0 + s * r.dt;
             if (r.sweep_mask & 1) {
                 SweepArgs<T> aa = a;
-                aa.ca = coef(r.tau_i + t);
-                aa.cb = coef(r.tau_i + t + 0.5 * r.dt);
-                rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 0><<<grid, S::NT, smem(), r.st>>>(map_state, aa);
-                rc = launch_status("rk4 sweep A");
-                if (rc) return rc;
+                aa.c1 = stage_coef<T>(*r.bg, r.tau_i + t);
+                aa.c2 = stage_coef<T>(*r.bg, r.tau_i + t + 0.5 * r.dt);
+                for (int c = 0; c < 8; ++c) aa.out[c] = work + c * g.cs;
+                if ((rc = LA::launch(map_state, aa, grid, r.st))) return rc;
             }
             if (r.sweep_mask & 2) {
                 SweepArgs<T> ab = a;
-                ab.ca = coef(r.tau_i + t + 0.5 * r.dt);
-                ab.cb = coef(r.tau_i + t + r.dt);
-                rk4_sweep_kernel<T, V, TX, TY, NS, MINB, 1><<<grid, S::NT, smem(), r.st>>>(map_work, ab);
-                rc = launch_status("rk4 sweep B");
-                if (rc) return rc;
+                ab.n_items = tmp.n_items;
+                ab.zchunk = tmp.zchunk;
+                ab.c2 = stage_coef<T>(*r.bg, r.tau_i + t + 0.5 * r.dt);
+                ab.c4 = stage_coef<T>(*r.bg, r.tau_i + t + r.dt);
+                for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.cs;
+                for (int c = 0; c < 4; ++c) ab.out[c] = state + c * g.cs;
+                if ((rc = LB::launch(map_work, ab, grid_b, r.st))) return rc;
             }
         }
         return AXS_OK;

@@ -203,6 +203,34 @@ int axs_level_rk4_sweep(const axs_level *lv, const axs_background *bg, double ta
 int axs_level_device_status(const axs_level *lv, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Differentiation: discrete adjoint of the fused RK4 step (no counterpart in
+ * the reference, which has no gradient code)
+ * ------------------------------------------------------------------------- */
+
+/* Bytes of the adjoint workspace for a level: 8 components of the level
+ * layout (Fbar and the stage adjoints) plus per-block lambda0-gradient partials. */
+int axs_level_adjoint_work_bytes(int32_t dtype, int32_t nx, int32_t ny, int32_t nz, int64_t *bytes);
+
+/* Reverse one axs_level_rk4_advance step taken from time t: lv->state must
+ * hold the state y_n at the start of that step (lv->work is overwritten with
+ * its recomputed stage fields). `abar` (4 components, level layout, periodic
+ * padding current) holds dL/dy_{n+1} on entry and dL/dy_n on return;
+ * *lambda0_bar (device) is incremented by dL/dlambda0 through this step, where
+ * lambda0 = bg->lambda_scale. Asynchronous on `stream`. */
+int axs_level_rk4_adjoint_step(const axs_level *lv, void *abar, void *adj_work, int64_t adj_work_bytes,
+                               const axs_background *bg, double tau_i, double t, double dt, double *lambda0_bar,
+                               void *stream);
+
+/* Smooth string-core loss of the level's state:
+ *   L = sum_cells exp(-|psi/R|^2 / width) + mean_cells (theta'/R)^2,
+ * theta' = (psi1 Pi2 - Pi1 psi2)/|psi|^2 -- the second term is the unscreened
+ * axion kinetic energy density average (Energy.hpp:90-97). Writes L to
+ * *loss_dev and, if `grad` is not NULL, dL/d(psi1, psi2, Pi1, Pi2) in the
+ * level layout (padding filled). `scratch` needs 8 bytes x 4 x SMs. */
+int axs_level_string_core_loss(const axs_level *lv, double R, double width, double *loss_dev, void *grad,
+                               void *scratch, int64_t scratch_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
  * (b)+(c) Fused diagnostics pass
  * ------------------------------------------------------------------------- */
 

@@ -19,12 +19,14 @@ pytestmark = pytest.mark.gpu
 
 def straight_string_pair(n, nz, dx, R, m_r, RpR):
     """T1 initial data (AxionStringsLevel.cpp:384-476): vortex/antivortex along z,
-    separated by L/4 either side of the centre, offset half a cell from vertices."""
+    separated by L/4 either side of the centre. Samples sit at cell centres
+    (i + 1/2) dx, so the cores are put on cell corners -- the centres of
+    plaquettes -- to keep every sample off a (phase-undefined) core."""
     L = n * dx
     c = 0.5 * L
     sep = 0.25 * L
-    x1, y1 = c + 0.5 * dx - sep, c + 0.5 * dx
-    x2, y2 = c + 0.5 * dx + sep, c + 0.5 * dx
+    x1, y1 = c - sep, c
+    x2, y2 = c + sep, c
     x = (np.arange(n) + 0.5) * dx
     X, Y = np.meshgrid(x, x, indexing="xy")  # [y, x]
     rho1 = np.hypot(X - x1, Y - y1)
