@@ -62,10 +62,10 @@ struct AdjointB {
             uo[1][v] = u3b2;
             uo[2][v] = u4b1;
             uo[3][v] = u4b2;
-            const double m3 = (double)u31 * u31 + (double)u32 * u32 - (double)a.c2.R2;
-            const double m4 = (double)u41 * u41 + (double)u42 * u42 - (double)a.c4.R2;
-            lam -= (double)a.c2.hlam * a.inv_lambda0 * m3 * ((double)u31 * f3b1 + (double)u32 * f3b2);
-            lam -= (double)a.c4.hlam * a.inv_lambda0 * m4 * ((double)u41 * f4b1 + (double)u42 * f4b2);
+            // lambda0 gradient: per-site term in T, accumulated in double
+            const T m3 = fma(u31, u31, fma(u32, u32, -a.c2.R2));
+            const T m4 = fma(u41, u41, fma(u42, u42, -a.c4.R2));
+            lam -= (double)(fma(a.c2.hlam * m3, fma(u31, f3b1, u32 * f3b2), a.c4.hlam * m4 * fma(u41, f4b1, u42 * f4b2)));
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, fo[c]);
@@ -100,10 +100,9 @@ struct AdjointA {
             o[1][v] = qb2 + u1b2 + u2b2 + u4b2;
             o[2][v] = fma(a.h, u4b1, fma(a.h_half, u2b1, fma(a.h, qb1, pb1)));
             o[3][v] = fma(a.h, u4b2, fma(a.h_half, u2b2, fma(a.h, qb2, pb2)));
-            const double m1 = (double)p1 * p1 + (double)p2 * p2 - (double)a.c1.R2;
-            const double m2 = (double)u21 * u21 + (double)u22 * u22 - (double)a.c2.R2;
-            lam -= (double)a.c1.hlam * a.inv_lambda0 * m1 * ((double)p1 * f1b1 + (double)p2 * f1b2);
-            lam -= (double)a.c2.hlam * a.inv_lambda0 * m2 * ((double)u21 * f2b1 + (double)u22 * f2b2);
+            const T m1 = fma(p1, p1, fma(p2, p2, -a.c1.R2));
+            const T m2 = fma(u21, u21, fma(u22, u22, -a.c2.R2));
+            lam -= (double)(fma(a.c1.hlam * m1, fma(p1, f1b1, p2 * f1b2), a.c2.hlam * m2 * fma(u21, f2b1, u22 * f2b2)));
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, o[c]);

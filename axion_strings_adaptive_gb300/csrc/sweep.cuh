@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
         if (tid == 0) {
             double s = 0.0;
             for (int w = 0; w < S::NT / 32; ++w) s += lam_red[w];
-            a.lam_partial[blockIdx.x] = s;
+            a.lam_partial[blockIdx.x] = s * a.inv_lambda0;
         }
     }
 }

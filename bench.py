@@ -282,6 +282,37 @@ def run_native(args):
         diag = {"ms": ms_d, "read_gbps": 16 * n ** 3 / (ms_d * 1e-3) / 1e9, "n_p_plain": res.n_p_plain,
                 "n_near_tie": res.n_near_tie, "fields": "fp32", "per_cell_math": "fp64"}
 
+    # ---------------- adjoint step cost on the same FP32 box (recompute sweep A + adjoint sweeps B and A)
+    adj = None
+    if not args.no_adjoint:
+        from axion_strings_adaptive_gb300 import adjoint as ADJ
+        buf = ADJ.AdjointBuffers(lv32)
+        stored = lv32.state.clone()
+        tau_f = TAU_I + (args.warmup + args.steps) * DT
+        ADJ.loss_and_seed(lv32, buf, bg.values(tau_f).R, 0.1)
+        ka = max(3, args.steps // 4)
+        t_end = (args.warmup + args.steps) * DT
+        for w in range(2):
+            ADJ.adjoint_step(lv32, stored, buf, bg, TAU_I, t_end - (w + 1) * DT, DT)
+        torch.cuda.synchronize()
+        ea0, ea1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea0.record()
+        for s in range(ka):
+            ADJ.adjoint_step(lv32, stored, buf, bg, TAU_I, t_end - (s + 3) * DT, DT)
+        ea1.record()
+        torch.cuda.synchronize()
+        lv32.device_status()
+        ms_adj = allmax(ea0.elapsed_time(ea1)) / ka
+        fwd_ms = ms_max / args.steps
+        adj = {"ms_per_step": ms_adj, "forward_ms_per_step": fwd_ms, "adjoint_over_forward": ms_adj / fwd_ms,
+               "steps": ka, "dtype": "f32", "algorithmic_bytes_per_site": 48 * es32,
+               "achieved_gbs": 48 * es32 * n ** 3 / (ms_adj * 1e-3) / 1e9,
+               "kernels_per_step": ["rk4_sweep_A (recompute u3,u4)", "adjoint_sweep_B", "adjoint_sweep_A",
+                                    "lambda_bar_finalize"],
+               "finite": bool(torch.isfinite(buf.abar).all())}
+        del buf, stored
+        torch.cuda.empty_cache()
+
     # ---------------- FP64 path on the same box
     fp64 = None
     if not args.no_fp64:
@@ -299,29 +330,52 @@ def run_native(args):
         del lv64
         torch.cuda.empty_cache()
 
-    # ---------------- FP32 vs FP64 after a short evolution (both from the same IC)
+    # ---------------- precision: FP32 vs FP64 from the same IC, plus the FP64 evolution of the
+    # FP32-rounded IC (how far an FP64 run moves when its input is perturbed at FP32 roundoff:
+    # the conditioning floor of each observable)
     precision = None
     if not args.no_precision and args.precision_steps > 0:
         ps = args.precision_steps
+        marks = sorted({min(40, ps), ps})
+        legs = (("fp64", torch.float64, ic64), ("fp32", torch.float32, ic64.float()),
+                ("fp64_rounded_ic", torch.float64, ic64.float().double()))
         out = {}
-        for dt_, name in ((torch.float64, "fp64"), (torch.float32, "fp32")):
-            lv = A.PeriodicLevel(n, DX, dtype=dt_, device=dev)
-            lv.set_state(ic64.to(dt_))
-            lv.advance(bg, TAU_I, 0.0, DT, ps)
-            lv.device_status()
-            out[name] = lv.diagnostics(bg, TAU_I + ps * DT, want_list=False)
+        for name, dt_, s0 in legs:
+            lv = A.PeriodicLevel(n, DX, dtype=dt_, device=dev, pierced_capacity=3 * n ** 3 // 8)
+            lv.set_state(s0.to(dt_))
+            done = 0
+            for mk in marks:
+                lv.advance(bg, TAU_I, done * DT, DT, mk - done)
+                done = mk
+                lv.device_status()
+                d = lv.diagnostics(bg, TAU_I + mk * DT, want_list=True)
+                out[(name, mk)] = (d, torch.sort(d.pierced.to(torch.int64))[0])
             del lv
             torch.cuda.empty_cache()
-        d64, d32 = out["fp64"], out["fp32"]
-        errs = {}
-        for k, v in d64.energy.items():
-            if k.startswith("rho_") and v != 0.0:
-                errs[k] = abs(d32.energy[k] - v) / abs(v)
-        precision = {"steps": ps, "tau": TAU_I + ps * DT, "energy_rel_err": errs,
-                     "max_energy_rel_err": max(errs.values()),
-                     "xi_fp64": d64.xi_plain, "xi_rel_err": abs(d32.xi_plain - d64.xi_plain) / max(d64.xi_plain, 1e-300),
-                     "n_p_fp64": d64.n_p_plain, "n_p_fp32": d32.n_p_plain,
-                     "n_near_tie": [d64.n_near_tie, d32.n_near_tie]}
+
+        def compare(ref, oth):
+            (a, la), (b, lb) = ref, oth
+            errs = {k: abs(b.energy[k] - v) / abs(v) for k, v in a.energy.items() if k.startswith("rho_") and v != 0.0}
+            only_a = int((~torch.isin(la, lb)).sum())
+            only_b = int((~torch.isin(lb, la)).sum())
+            return {"energy_rel_err": errs, "max_energy_rel_err": max(errs.values()),
+                    "total_energy_rel_err": max(errs["rho_tot_unscreened"], errs["rho_tot_screened"]),
+                    "xi_rel_err": abs(b.xi_plain - a.xi_plain) / max(a.xi_plain, 1e-300),
+                    "n_p": [a.n_p_plain, b.n_p_plain], "pierced_only_in_fp64": only_a,
+                    "pierced_only_in_other": only_b, "n_near_tie": [a.n_near_tie, b.n_near_tie]}
+
+        precision = {"steps": ps, "workload": f"{n}^3 Moore c0=2 lambda0=2, same IC in both precisions",
+                     "by_step": {}}
+        for mk in marks:
+            ref = out[("fp64", mk)]
+            precision["by_step"][str(mk)] = {
+                "tau": TAU_I + mk * DT, "xi_fp64": ref[0].xi_plain, "n_p_fp64": ref[0].n_p_plain,
+                "fp32_vs_fp64": compare(ref, out[("fp32", mk)]),
+                "fp64_rounded_ic_vs_fp64": compare(ref, out[("fp64_rounded_ic", mk)])}
+        fin = precision["by_step"][str(ps)]["fp32_vs_fp64"]
+        precision["total_energy_rel_err"] = fin["total_energy_rel_err"]
+        precision["max_energy_rel_err"] = fin["max_energy_rel_err"]
+        del out
 
     # ---------------- end to end through the C ABI with host buffers
     e2e = None
@@ -369,7 +423,8 @@ def run_native(args):
                 "config": _config(n), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks, "gpu_launches": 2 * args.steps, "tile_config": cfg32,
                 "autotune_ms_per_step": tune32, "diagnostics": diag, "fp64": fp64,
-                "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision}
+                "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision,
+                "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -383,7 +438,7 @@ def main():
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--ref-n", type=int, default=256)
-    ap.add_argument("--precision-steps", type=int, default=40)
+    ap.add_argument("--precision-steps", type=int, default=400)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
@@ -391,6 +446,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-diag", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
