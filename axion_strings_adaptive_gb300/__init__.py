@@ -11,11 +11,12 @@ from ._build import build
 from ._lib import AxsError
 from .background import (Background, plaquette_count_for_target_xi, xi_from_comoving_length,
                          xi_from_plaquette_count)
+from .ensemble import Ensemble
 from .level import (AxionStringsLevel, Diagnostics, PeriodicLevel, eval_rhs, fab, fill_periodic_ghosts, lincomb,
                     new_fab, rk4_combine, valid)
 
 __all__ = [
-    "AxionStringsLevel", "AxsError", "Background", "Diagnostics", "PeriodicLevel", "build", "eval_rhs", "fab",
+    "AxionStringsLevel", "AxsError", "Background", "Diagnostics", "Ensemble", "PeriodicLevel", "build", "eval_rhs", "fab",
     "fill_periodic_ghosts", "lincomb", "new_fab", "plaquette_count_for_target_xi", "rk4_combine", "valid",
     "xi_from_comoving_length", "xi_from_plaquette_count",
 ]

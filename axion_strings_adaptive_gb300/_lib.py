@@ -62,12 +62,28 @@ class LevelC(C.Structure):
 class DiagParams(C.Structure):
     _fields_ = [("dx", _dbl), ("R", _dbl), ("lambda_", _dbl), ("R_prime_over_R", _dbl), ("m_r", _dbl),
                 ("masking_scheme", _i32), ("masking_threshold", _dbl), ("boundary", _i32),
-                ("want_energy", _i32), ("want_plaquettes", _i32), ("want_velocity", _i32)]
+                ("want_energy", _i32), ("want_plaquettes", _i32), ("want_velocity", _i32),
+                ("per_cell_fp32", _i32)]
 
 
 class DiagResult(C.Structure):
     _fields_ = [("energy_sums", _dbl * 14), ("vel_sum", _dbl), ("vel_count", _i64), ("n_p_plain", _i64),
                 ("n_p_weighted", _i64), ("n_listed", _i64), ("n_near_tie", _i64), ("status", _i64)]
+
+
+class EnsembleC(C.Structure):
+    _fields_ = [("dtype", _i32), ("nboxes", _i32), ("dims", C.POINTER(_i32)), ("dx", _dbl), ("state", _ptr),
+                ("work", _ptr), ("table", _ptr), ("state_bytes", _i64), ("work_bytes", _i64),
+                ("table_bytes", _i64)]
+
+
+class EnsembleBox(C.Structure):
+    _fields_ = [("base", _i64), ("jstride", _i64), ("kstride", _i64), ("x_offset", _i32), ("y_offset", _i32)]
+
+
+class EnsemblePlan(C.Structure):
+    _fields_ = [("tile_config", _i32), ("z_chunk", _i32), ("n_items", _i64), ("grid_a", _i32), ("grid_b", _i32),
+                ("plane_elems", _i64), ("key", _u64)]
 
 
 # name -> (restype, argtypes); every symbol here is declared in include/axs.h
@@ -103,6 +119,17 @@ SIGNATURES = {
     "axs_level_diagnostics": (_i32, [C.POINTER(LevelC), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr, _i64,
                                      _ptr]),
     "axs_diagnostics_static_scratch": (_i32, [C.POINTER(Fab), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr]),
+    "axs_ensemble_sizes": (_i32, [_i32, _i32, C.POINTER(_i32), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),
+    "axs_ensemble_box_layout": (_i32, [_i32, _i32, C.POINTER(_i32), _i32, C.POINTER(EnsembleBox)]),
+    "axs_ensemble_tile_config_count": (_i32, [_i32]),
+    "axs_ensemble_tile_config_name": (C.c_char_p, [_i32, _i32]),
+    "axs_ensemble_init": (_i32, [C.POINTER(EnsembleC), C.POINTER(EnsemblePlan), _ptr]),
+    "axs_ensemble_fill_ghosts": (_i32, [C.POINTER(EnsembleC), _ptr]),
+    "axs_ensemble_rk4_advance": (_i32, [C.POINTER(EnsembleC), C.POINTER(EnsemblePlan), C.POINTER(BackgroundC), _dbl,
+                                        _dbl, _dbl, _i32, _ptr]),
+    "axs_ensemble_diagnostics_scratch_bytes": (_i32, [_i32, C.POINTER(_i32), C.POINTER(_i64)]),
+    "axs_ensemble_diagnostics": (_i32, [C.POINTER(EnsembleC), C.POINTER(DiagParams), _ptr, _ptr, _i64, _ptr]),
+    "axs_ensemble_device_status": (_i32, [C.POINTER(EnsembleC), _ptr]),
     "axs_plaquette_winding_batch": (_i32, [_ptr, _i64, _ptr, _ptr]),
     "axs_fourier_spectrum": (_i32, [_ptr, _i32, _i32, _i32, _dbl, _u64, _i32, _ptr]),
 }

@@ -23,7 +23,7 @@
 // sweep A reads 4+12 and writes 4.
 #include <cmath>
 
-#include "sweep.cuh"
+#include "rk4_ops.cuh"
 
 namespace axs {
 
@@ -38,8 +38,8 @@ struct AdjointB {
     static constexpr int kPointwise = 4;
     static constexpr bool kLambdaGrad = true;
     template <typename T, int V, typename PQ>
-    __device__ static void apply(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V], const PQ &pq,
-                                 int64_t off, int x, int y, double &lam)
+    __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam)
     {
         T fo[4][V], uo[4][V];
 #pragma unroll
@@ -68,7 +68,7 @@ struct AdjointB {
             lam -= (double)(fma(a.c2.hlam * m3, fma(u31, f3b1, u32 * f3b2), a.c4.hlam * m4 * fma(u41, f4b1, u42 * f4b2)));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, fo[c]);
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, b.nx, b.ny, b.js, fo[c]);
 #pragma unroll
         for (int c = 0; c < 4; ++c) stv<T, V>(a.out[4 + c] + off, uo[c]);
     }
@@ -80,8 +80,8 @@ struct AdjointA {
     static constexpr int kPointwise = 12;
     static constexpr bool kLambdaGrad = true;
     template <typename T, int V, typename PQ>
-    __device__ static void apply(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V], const PQ &pq,
-                                 int64_t off, int x, int y, double &lam)
+    __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam)
     {
         T o[4][V];
 #pragma unroll
@@ -105,7 +105,7 @@ struct AdjointA {
             lam -= (double)(fma(a.c1.hlam * m1, fma(p1, f1b1, p2 * f1b2), a.c2.hlam * m2 * fma(u21, f2b1, u22 * f2b2)));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, o[c]);
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c]);
     }
 };
 
@@ -212,26 +212,11 @@ template <typename T> struct AdjointRunner {
         a.ks = g.ks;
         a.cs = g.cs;
         a.ox = g.ox;
-        const double inv_dx2 = 1.0 / (lv->dx * lv->dx);
-        a.wA = T((4.0 / 3.0) * inv_dx2);
-        a.wB = T((-1.0 / 12.0) * inv_dx2);
-        a.wC = T(-7.5 * inv_dx2);
-        a.h = T(dt);
-        a.h_half = T(0.5 * dt);
-        a.h2_quarter = T(0.25 * dt * dt);
-        a.h2_half = T(0.5 * dt * dt);
-        a.h_sixth = T(dt / 6.0);
-        a.h_third = T(dt / 3.0);
-        a.h2_sixth = T(dt * dt / 6.0);
+        fill_step_constants(a, lv->dx, dt);
         a.inv_lambda0 = 1.0 / bg.lambda_scale;
-        auto coef = [&](double tau) {
-            axs_rhs_coeffs c;
-            rhs_coeffs(bg, tau, c);
-            return StageCoef<T>{T(c.kappa), T(0.5 * c.lambda), T(c.R2)};
-        };
-        a.c1 = coef(tau_i + t);
-        a.c2 = coef(tau_i + t + 0.5 * dt);
-        a.c4 = coef(tau_i + t + dt);
+        a.c1 = stage_coef<T>(bg, tau_i + t);
+        a.c2 = stage_coef<T>(bg, tau_i + t + 0.5 * dt);
+        a.c4 = stage_coef<T>(bg, tau_i + t + dt);
         a.status = reinterpret_cast<unsigned *>(static_cast<char *>(lv->work) + 8 * g.cs * sizeof(T));
         const T *state = static_cast<const T *>(lv->state);
         const T *work = static_cast<const T *>(lv->work);

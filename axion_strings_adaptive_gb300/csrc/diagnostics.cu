@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "axs_internal.cuh"
 
@@ -49,6 +50,9 @@ struct DiagConst {
     double vel_a, vel_b, vel_c;  // gamma^2 v^2 = |phi'|^2 vel_a (1 - vel_b |phi|^2) - vel_c (phi . phi')^2
     int scheme;
     int want_energy, want_plaq, want_vel;
+    // single-precision copies for the per_cell_fp32 variant
+    float f_one_over_dx, f_R2, f_inv_R, f_inv_R2, f_inv_R4, f_lambda, f_RpR, f_threshold;
+    float f_vel_a, f_vel_b, f_vel_c;
 };
 
 template <typename T>
@@ -133,6 +137,58 @@ __device__ __forceinline__ double diff1_vals(double m2, double m1, double p1, do
     }
 }
 
+// The seven per-cell energy terms (EnergyKernel.hpp:130-190) and the masking
+// weight (Masking.hpp:75-93) from psi, Pi and the six diff1 values, in math
+// type M: double as the reference computes them, or float for the
+// per_cell_fp32 variant.
+template <typename M> struct CellConst {
+    M R2, inv_R, inv_R2, inv_R4, lambda, RpR, threshold;
+};
+
+template <typename M, typename T>
+__device__ __forceinline__ void cell_energy(const CellConst<M> &k, int scheme, M psi1, M psi2, M Pi1, M Pi2,
+                                            const M (&g)[2][3], M (&term)[6], M &wgt)
+{
+    const M psi_sq = psi1 * psi1 + psi2 * psi2;
+    M g1sq = 0, g2sq = 0, cross2 = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if constexpr (sizeof(M) == 8) {
+            // the reference squares the float diff1 values in float
+            g1sq += (M)((T)g[0][d] * (T)g[0][d]);
+            g2sq += (M)((T)g[1][d] * (T)g[1][d]);
+        } else {
+            g1sq += g[0][d] * g[0][d];
+            g2sq += g[1][d] * g[1][d];
+        }
+        const M cr = psi1 * g[1][d] - psi2 * g[0][d];
+        cross2 += cr * cr;
+    }
+    const M inv_psq = psi_sq > M(0) ? M(1) / psi_sq : M(0);
+    const M gtsq = cross2 * inv_psq * inv_psq;
+    const M c1 = Pi1 - k.RpR * psi1, c2 = Pi2 - k.RpR * psi2;
+    const M dsq = psi_sq - k.R2;
+    const M pot = M(0.25) * k.lambda * dsq * dsq;
+    term[0] = (c1 * c1 + c2 * c2 + (g1sq + g2sq) + pot) * k.inv_R4;  // rho
+    const M thp = (psi1 * Pi2 - Pi1 * psi2) * inv_psq;
+    term[1] = thp * thp * k.inv_R2;                                  // 1/2 (sqrt(2) theta'/R)^2
+    term[2] = gtsq * k.inv_R2;                                       // 1/2 sqrt(2)^2 |grad theta|^2 / R^2
+    const M rdot = psi1 * c1 + psi2 * c2;
+    term[3] = rdot * rdot * inv_psq * k.inv_R4;                      // radial kinetic
+    term[4] = (g1sq + g2sq - psi_sq * gtsq) * k.inv_R4;              // radial gradient
+    term[5] = pot * k.inv_R4;                                        // radial mass
+    wgt = M(1);
+    if (scheme != AXS_MASK_NONE) {
+        const M mod = sqrt(psi_sq) * k.inv_R;
+        if (scheme == AXS_MASK_B) {
+            wgt = (mod >= k.threshold) ? M(1) : M(0);
+        } else {
+            const M f = M(1) + (mod - M(1)) * M(0.70710678118654752440);  // 1 + r / f_a
+            wgt = f * f;
+        }
+    }
+}
+
 // Tiled diagnostics pass. A block owns a DTX x DTY tile of cells and marches
 // in z over a chunk. Shared memory holds psi1/psi2 of five planes (tile plus a
 // 2-cell halo) for the gradient stencil, and for the two vertex planes z and
@@ -146,17 +202,17 @@ constexpr int kPsiPer = (2 * kPsiPts + kDiagThreads - 1) / kDiagThreads;  // psi
 constexpr int kPiPer = (2 * kVtxPts + kDiagThreads - 1) / kDiagThreads;   // Pi loads per thread per plane
 constexpr int kVtxPer = (kVtxPts + kDiagThreads - 1) / kDiagThreads;      // vertices per thread per plane
 
-template <typename T> struct DiagSmem {
+template <typename T, bool FAST> struct DiagSmem {
     T ps[5][2][DHY][DHX];
     T pi[2][2][DVY][DVX];
-    double gv[2][DVY][DVX];
+    typename std::conditional<FAST, float, double>::type gv[2][DVY][DVX];
     float th[2][DVY][DVX];
     unsigned char ok[2][DVY][DVX];
 };
 
 __device__ __forceinline__ int wrap_or_self(int i, int n, int wrap) { return wrap ? (i % n + n) % n : i; }
 
-template <typename T>
+template <typename T, bool FAST>
 __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v, const DiagConst q,
                                                                const uint8_t *__restrict__ mask,
                                                                DiagPartial *__restrict__ partials,
@@ -165,7 +221,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                                                                int tiles_x, int ntiles, int zchunk, long long n_items)
 {
     extern __shared__ __align__(16) unsigned char diag_smem_raw[];
-    DiagSmem<T> &sm = *reinterpret_cast<DiagSmem<T> *>(diag_smem_raw);
+    DiagSmem<T, FAST> &sm = *reinterpret_cast<DiagSmem<T, FAST> *>(diag_smem_raw);
     __shared__ int warp_tot[kDiagThreads / 32];
     __shared__ unsigned long long block_base;
     const T *__restrict__ base = static_cast<const T *>(v.data);
@@ -173,6 +229,12 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
     double e[14];
 #pragma unroll
     for (int s = 0; s < 14; ++s) e[s] = 0.0;
+    // per_cell_fp32: one work item's cells are summed in float, then added to e
+    float ef[FAST ? 14 : 1];
+#pragma unroll
+    for (int s = 0; s < (FAST ? 14 : 1); ++s) ef[s] = 0.f;
+    const CellConst<double> kd{q.R2, q.inv_R, q.inv_R2, q.inv_R4, q.lambda, q.RpR, q.threshold};
+    const CellConst<float> kf{q.f_R2, q.f_inv_R, q.f_inv_R2, q.f_inv_R4, q.f_lambda, q.f_RpR, q.f_threshold};
     double vsum = 0.0;
     long long cnt[4] = {0, 0, 0, 0};
 
@@ -247,7 +309,15 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                 // float conversion keeps the angle to ~1e-7 only away from under/overflow
                 sm.ok[ts][vy][vx] = (m > 1e-30 && m < 1e30) ? 1 : 0;
                 sm.th[ts][vy][vx] = atan2f((float)b, (float)a);
-                if (q.want_vel) {
+                if (q.want_vel && FAST) {
+                    const float psi1 = a, psi2 = b, Pi1 = sm.pi[ts][0][vy][vx], Pi2 = sm.pi[ts][1][vy][vx];
+                    const float phi1 = psi1 * q.f_inv_R, phi2 = psi2 * q.f_inv_R;
+                    const float pd1 = (Pi1 - q.f_RpR * psi1) * q.f_inv_R2, pd2 = (Pi2 - q.f_RpR * psi2) * q.f_inv_R2;
+                    const float phi_sq = phi1 * phi1 + phi2 * phi2;
+                    const float pd_sq = pd1 * pd1 + pd2 * pd2;
+                    const float re = phi1 * pd1 + phi2 * pd2;
+                    sm.gv[ts][vy][vx] = pd_sq * q.f_vel_a * (1.f - q.f_vel_b * phi_sq) - q.f_vel_c * re * re;
+                } else if (q.want_vel) {
                     const double psi1 = a, psi2 = b, Pi1 = sm.pi[ts][0][vy][vx], Pi2 = sm.pi[ts][1][vy][vx];
                     const double phi1 = psi1 * q.inv_R, phi2 = psi2 * q.inv_R;
                     const double pd1 = (Pi1 - q.RpR * psi1) * q.inv_R2, pd2 = (Pi2 - q.RpR * psi2) * q.inv_R2;
@@ -281,57 +351,57 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                 const int t0 = m & 1, t1 = (m + 1) & 1;
                 const int hx = lx + 2, hy = ly + 2;
                 if (q.want_energy) {
-                    const double psi1 = sm.ps[s0][0][hy][hx], psi2 = sm.ps[s0][1][hy][hx];
-                    const double Pi1 = sm.pi[t0][0][ly][lx], Pi2 = sm.pi[t0][1][ly][lx];
-                    const double psi_sq = psi1 * psi1 + psi2 * psi2;
-                    double g[2][3];
+                    const T p1 = sm.ps[s0][0][hy][hx], p2 = sm.ps[s0][1][hy][hx];
+                    const T q1 = sm.pi[t0][0][ly][lx], q2 = sm.pi[t0][1][ly][lx];
+                    bool done = false;
+                    if constexpr (FAST) {
+                        const float psq = p1 * p1 + p2 * p2;
+                        // float keeps 1/|psi|^4 finite only away from the cores' exact zeros
+                        if (psq > 1e-15f && psq < 1e15f) {
+                            float g[2][3];
+                            const float wf = 0.0833333333f, wn = 0.666666667f;
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        g[c][0] = diff1_vals<T>(sm.ps[s0][c][hy][hx - 2], sm.ps[s0][c][hy][hx - 1],
-                                                sm.ps[s0][c][hy][hx + 1], sm.ps[s0][c][hy][hx + 2], q.one_over_dx);
-                        g[c][1] = diff1_vals<T>(sm.ps[s0][c][hy - 2][hx], sm.ps[s0][c][hy - 1][hx],
-                                                sm.ps[s0][c][hy + 1][hx], sm.ps[s0][c][hy + 2][hx], q.one_over_dx);
-                        g[c][2] = diff1_vals<T>(sm.ps[sm2][c][hy][hx], sm.ps[sm1][c][hy][hx], sm.ps[sp1][c][hy][hx],
-                                                sm.ps[sp2][c][hy][hx], q.one_over_dx);
-                    }
-                    double g1sq = 0.0, g2sq = 0.0, cross2 = 0.0;
+                            for (int c = 0; c < 2; ++c) {
+                                g[c][0] = (wf * (sm.ps[s0][c][hy][hx - 2] - sm.ps[s0][c][hy][hx + 2]) +
+                                           wn * (sm.ps[s0][c][hy][hx + 1] - sm.ps[s0][c][hy][hx - 1])) * q.f_one_over_dx;
+                                g[c][1] = (wf * (sm.ps[s0][c][hy - 2][hx] - sm.ps[s0][c][hy + 2][hx]) +
+                                           wn * (sm.ps[s0][c][hy + 1][hx] - sm.ps[s0][c][hy - 1][hx])) * q.f_one_over_dx;
+                                g[c][2] = (wf * (sm.ps[sm2][c][hy][hx] - sm.ps[sp2][c][hy][hx]) +
+                                           wn * (sm.ps[sp1][c][hy][hx] - sm.ps[sm1][c][hy][hx])) * q.f_one_over_dx;
+                            }
+                            float term[6], wgt;
+                            cell_energy<float, T>(kf, q.scheme, p1, p2, q1, q2, g, term, wgt);
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        g1sq += (double)((T)g[0][d] * (T)g[0][d]);
-                        g2sq += (double)((T)g[1][d] * (T)g[1][d]);
-                        const double cr = psi1 * g[1][d] - psi2 * g[0][d];
-                        cross2 += cr * cr;
-                    }
-                    const double inv_psq = psi_sq > 0.0 ? 1.0 / psi_sq : 0.0;
-                    const double gtsq = cross2 * inv_psq * inv_psq;
-                    const double c1 = Pi1 - q.RpR * psi1, c2 = Pi2 - q.RpR * psi2;
-                    const double dsq = psi_sq - q.R2;
-                    const double pot = 0.25 * q.lambda * dsq * dsq;
-                    const double rho = (c1 * c1 + c2 * c2 + (g1sq + g2sq) + pot) * q.inv_R4;
-                    const double thp = (psi1 * Pi2 - Pi1 * psi2) * inv_psq;
-                    const double akin = thp * thp * q.inv_R2;  // 1/2 (sqrt(2) theta'/R)^2
-                    const double agrad = gtsq * q.inv_R2;      // 1/2 sqrt(2)^2 |grad theta|^2 / R^2
-                    const double rdot = psi1 * c1 + psi2 * c2;
-                    const double rkin = rdot * rdot * inv_psq * q.inv_R4;
-                    const double rgrad = (g1sq + g2sq - psi_sq * gtsq) * q.inv_R4;
-                    const double rmass = pot * q.inv_R4;
-                    double wgt = 1.0;
-                    if (q.scheme != AXS_MASK_NONE) {
-                        const double mod = sqrt(psi_sq) * q.inv_R;
-                        if (q.scheme == AXS_MASK_B) {
-                            wgt = (mod >= q.threshold) ? 1.0 : 0.0;
-                        } else {
-                            const double f = 1.0 + (mod - 1.0) * 0.70710678118654752440;  // 1 + r / f_a
-                            wgt = f * f;
+                            for (int k = 0; k < 6; ++k) {
+                                ef[2 * k] += term[k];
+                                ef[2 * k + 1] += term[k] * wgt;
+                            }
+                            ef[12] += wgt;
+                            ef[13] += 1.f;
+                            done = true;
                         }
                     }
-                    e[0] += rho;   e[1] += rho * wgt;
-                    e[2] += akin;  e[3] += akin * wgt;
-                    e[4] += agrad; e[5] += agrad * wgt;
-                    e[6] += rkin;  e[7] += rkin * wgt;
-                    e[8] += rgrad; e[9] += rgrad * wgt;
-                    e[10] += rmass; e[11] += rmass * wgt;
-                    e[12] += wgt;  e[13] += 1.0;
+                    if (!done) {
+                        double g[2][3];
+#pragma unroll
+                        for (int c = 0; c < 2; ++c) {
+                            g[c][0] = diff1_vals<T>(sm.ps[s0][c][hy][hx - 2], sm.ps[s0][c][hy][hx - 1],
+                                                    sm.ps[s0][c][hy][hx + 1], sm.ps[s0][c][hy][hx + 2], q.one_over_dx);
+                            g[c][1] = diff1_vals<T>(sm.ps[s0][c][hy - 2][hx], sm.ps[s0][c][hy - 1][hx],
+                                                    sm.ps[s0][c][hy + 1][hx], sm.ps[s0][c][hy + 2][hx], q.one_over_dx);
+                            g[c][2] = diff1_vals<T>(sm.ps[sm2][c][hy][hx], sm.ps[sm1][c][hy][hx],
+                                                    sm.ps[sp1][c][hy][hx], sm.ps[sp2][c][hy][hx], q.one_over_dx);
+                        }
+                        double term[6], wgt;
+                        cell_energy<double, T>(kd, q.scheme, p1, p2, q1, q2, g, term, wgt);
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) {
+                            e[2 * k] += term[k];
+                            e[2 * k + 1] += term[k] * wgt;
+                        }
+                        e[12] += wgt;
+                        e[13] += 1.0;
+                    }
                 }
                 if (q.want_plaq || q.want_vel) {
                     // corner phases (x, y, z offsets) in the reference's order
@@ -408,6 +478,13 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                 }
             }
             __syncthreads();  // ring slots and vertex planes are rewritten next plane
+        }
+        if constexpr (FAST) {
+#pragma unroll
+            for (int k = 0; k < 14; ++k) {
+                e[k] += (double)ef[k];
+                ef[k] = 0.f;
+            }
         }
     }
 
@@ -566,6 +643,17 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     q.want_energy = p->want_energy != 0;
     q.want_plaq = p->want_plaquettes != 0;
     q.want_vel = p->want_velocity != 0;
+    q.f_one_over_dx = (float)q.one_over_dx;
+    q.f_R2 = (float)q.R2;
+    q.f_inv_R = (float)q.inv_R;
+    q.f_inv_R2 = (float)q.inv_R2;
+    q.f_inv_R4 = (float)q.inv_R4;
+    q.f_lambda = (float)q.lambda;
+    q.f_RpR = (float)q.RpR;
+    q.f_threshold = (float)q.threshold;
+    q.f_vel_a = (float)q.vel_a;
+    q.f_vel_b = (float)q.vel_b;
+    q.f_vel_c = (float)q.vel_c;
     auto *counter = static_cast<unsigned long long *>(scratch);
     auto *partials = reinterpret_cast<DiagPartial *>(static_cast<char *>(scratch) + 256);
     AXS_CUDA_CHECK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
@@ -573,22 +661,36 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     long long items;
     diag_plan(v, diag_grid(ncell), tiles_x, ntiles, zchunk, items, grid);
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
-    if (v.dtype == AXS_F64) {
-        const size_t sm = sizeof(DiagSmem<double>);
-        AXS_CUDA_CHECK(cudaFuncSetAttribute(diag_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        diag_kernel<double><<<grid, kDiagThreads, sm, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
-                                                            ntiles, zchunk, items);
-    } else {
-        const size_t sm = sizeof(DiagSmem<float>);
-        AXS_CUDA_CHECK(cudaFuncSetAttribute(diag_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        diag_kernel<float><<<grid, kDiagThreads, sm, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
-                                                           ntiles, zchunk, items);
-    }
+    int rc0 = AXS_OK;
+    auto launch = [&](auto kern, size_t smem) -> int {
+        AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid, kDiagThreads, smem, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x, ntiles, zchunk,
+                                               items);
+        return AXS_OK;
+    };
+    if (v.dtype == AXS_F64)
+        rc0 = launch(diag_kernel<double, false>, sizeof(DiagSmem<double, false>));
+    else if (p->per_cell_fp32)
+        rc0 = launch(diag_kernel<float, true>, sizeof(DiagSmem<float, true>));
+    else
+        rc0 = launch(diag_kernel<float, false>, sizeof(DiagSmem<float, false>));
+    if (rc0) return rc0;
     int rc = launch_status("diagnostics");
     if (rc) return rc;
     diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
     return launch_status("diagnostics finalize");
 }
+
+// One periodic box in level layout (an ensemble member), without the pierced list.
+int diag_level_box(const void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g,
+                   const axs_diag_params *p, axs_diag_result *out, void *scratch, int64_t scratch_bytes,
+                   cudaStream_t st)
+{
+    DiagView v{data, dtype, nx, ny, nz, g.ox, g.oy, 0, 1, 1, 1, g.js, g.ks, g.cs};
+    return run_diag(v, p, nullptr, out, nullptr, 0, scratch, scratch_bytes, st);
+}
+
+int64_t diag_scratch_bytes_for(int64_t ncell) { return diag_scratch_bytes(ncell); }
 
 }  // namespace axs
 

@@ -29,70 +29,13 @@
 #include <cmath>
 #include <vector>
 
-#include "sweep.cuh"
+#include "rk4_ops.cuh"
 
 namespace axs {
 
 int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, int ncomp,
                       cudaStream_t st);
 int level_copy_fab(void *lv, int32_t dtype, const LevelGeom &g, const axs_fab &f, int to_level, cudaStream_t st);
-
-// Sweep A: stencil on (psi_n, Pi_n); writes S3, S4 (with periodic copies) and G, P.
-struct ForwardA {
-    static constexpr int kPointwise = 0;
-    static constexpr bool kLambdaGrad = false;
-    template <typename T, int V, typename PQ>
-    __device__ static void apply(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V], const PQ &,
-                                 int64_t off, int x, int y, double &)
-    {
-        T o[8][V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const T p1 = ctr[0][v], p2 = ctr[1][v], q1 = ctr[2][v], q2 = ctr[3][v];
-            T f11, f12, f21, f22;
-            rhs_pair(a.c1, p1, p2, lap[0][v], lap[1][v], f11, f12);  // F1 = F(t, psi_n)
-            // F2 = F(t + h/2, chi), chi = psi_n + h/2 Pi_n, lap(chi) = lap(psi) + h/2 lap(Pi)
-            const T c1 = fma(a.h_half, q1, p1), c2 = fma(a.h_half, q2, p2);
-            rhs_pair(a.c2, c1, c2, fma(a.h_half, lap[2][v], lap[0][v]), fma(a.h_half, lap[3][v], lap[1][v]), f21, f22);
-            o[0][v] = fma(a.h2_quarter, f11, c1);                     // S3
-            o[1][v] = fma(a.h2_quarter, f12, c2);
-            o[2][v] = fma(a.h2_half, f21, fma(a.h, q1, p1));          // S4
-            o[3][v] = fma(a.h2_half, f22, fma(a.h, q2, p2));
-            o[4][v] = fma(T(-2), f21, f11);                          // G = F1 - 2 F2
-            o[5][v] = fma(T(-2), f22, f12);
-            o[6][v] = fma(a.h_third, f21, fma(a.h_sixth, f11, q1));  // P = Pi + h/6 F1 + h/3 F2
-            o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, o[c]);
-#pragma unroll
-        for (int c = 4; c < 8; ++c) stv<T, V>(a.out[c] + off, o[c]);
-    }
-};
-
-// Sweep B: stencil on (S3, S4), pointwise (G, P); writes psi_{n+1}, Pi_{n+1}.
-struct ForwardB {
-    static constexpr int kPointwise = 4;
-    static constexpr bool kLambdaGrad = false;
-    template <typename T, int V, typename PQ>
-    __device__ static void apply(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V], const PQ &pq,
-                                 int64_t off, int x, int y, double &)
-    {
-        T o[4][V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            T f31, f32, f41, f42;
-            rhs_pair(a.c2, ctr[0][v], ctr[1][v], lap[0][v], lap[1][v], f31, f32);  // F3 = F(t + h/2, S3)
-            rhs_pair(a.c4, ctr[2][v], ctr[3][v], lap[2][v], lap[3][v], f41, f42);  // F4 = F(t + h, S4)
-            o[0][v] = fma(a.h2_sixth, pq[0][v] + f31, ctr[2][v]);
-            o[1][v] = fma(a.h2_sixth, pq[1][v] + f32, ctr[3][v]);
-            o[2][v] = fma(a.h_sixth, f41, fma(a.h_third, f31, pq[2][v]));
-            o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[3][v]));
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, a.nx, a.ny, a.js, o[c]);
-    }
-};
 
 // ---------------------------------------------------------------- host side
 int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g)
@@ -140,33 +83,16 @@ struct SweepRunArgs {
     cudaStream_t st;
 };
 
-// Fill the step-independent part of the sweep arguments.
+// Step constants plus this level's strides and status word.
 template <typename T>
-static void fill_step_constants(SweepArgs<T> &a, const axs_level *lv, const LevelGeom &g, double dt)
+static void fill_level_constants(SweepArgs<T> &a, const axs_level *lv, const LevelGeom &g, double dt)
 {
+    fill_step_constants(a, lv->dx, dt);
     a.js = g.js;
     a.ks = g.ks;
     a.cs = g.cs;
     a.ox = g.ox;
-    const double inv_dx2 = 1.0 / (lv->dx * lv->dx);
-    a.wA = T((4.0 / 3.0) * inv_dx2);
-    a.wB = T((-1.0 / 12.0) * inv_dx2);
-    a.wC = T(-7.5 * inv_dx2);
-    a.h = T(dt);
-    a.h_half = T(0.5 * dt);
-    a.h2_quarter = T(0.25 * dt * dt);
-    a.h2_half = T(0.5 * dt * dt);
-    a.h_sixth = T(dt / 6.0);
-    a.h_third = T(dt / 3.0);
-    a.h2_sixth = T(dt * dt / 6.0);
     a.status = level_status_word(lv, g);
-}
-
-template <typename T> static StageCoef<T> stage_coef(const axs_background &bg, double tau)
-{
-    axs_rhs_coeffs c;
-    rhs_coeffs(bg, tau, c);
-    return StageCoef<T>{T(c.kappa), T(0.5 * c.lambda), T(c.R2)};
 }
 
 int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const LevelGeom &g, int ny, int nz,
@@ -191,7 +117,7 @@ template <typename T, int V, int TX, int TY, int NS, int MINB> struct SweepConfi
         if (rc) return rc;
         SweepArgs<T> tmp = a;
         if ((rc = LB::plan(tmp, lv->nx, lv->ny, lv->nz, grid_b))) return rc;
-        fill_step_constants(a, lv, g, r.dt);
+        fill_level_constants(a, lv, g, r.dt);
         T *state = static_cast<T *>(lv->state), *work = static_cast<T *>(lv->work);
         CUtensorMap map_state, map_work;
         if ((rc = make_level_map(&map_state, state, lv->dtype, g, lv->ny, lv->nz, LA::box_x(), LA::box_y())))

@@ -13,9 +13,16 @@
 // every wait is bounded. Pointwise components are loaded one plane ahead into
 // registers. Work items (tile, z-chunk) are numbered tile-fastest so the blocks
 // resident at any moment work on neighbouring tiles of the same z range.
+//
+// A work item belongs to a box: the one level of a single-level sweep, or one
+// of many independent levels packed component-major in one arena (an ensemble,
+// ensemble.cu), each box then having its own tensor map and offset in every
+// component plane. The work-item source is a template policy, so the
+// single-level kernel reads its geometry from the launch parameters.
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "axs_internal.cuh"
 
@@ -41,6 +48,51 @@ template <typename T> struct SweepArgs {
     double inv_lambda0;          // adjoint: dlambda_s/dlambda0 = lambda_s / lambda0
     double *lam_partial;         // adjoint: one lambda0-gradient partial per block
     unsigned *status;
+    // ensemble sweeps: box table, packed work items (box << 20 | item in box),
+    // two tensor maps per box (state, stage buffers) and which one this sweep reads
+    const struct EnsBoxDesc *boxes;
+    const uint32_t *items;
+    const CUtensorMap *maps;
+    int map_sel;
+};
+
+// One box of an ensemble (device table entry). Element offsets are relative to
+// the arena base of each component plane.
+struct EnsBoxDesc {
+    int nx, ny, nz;
+    int tiles_x, ntiles, zchunk;
+    int64_t js, ks;
+    int64_t base;  // element offset of the box's (padded) origin in every component plane
+};
+constexpr int kEnsItemBits = 20;  // work items per box < 2^20; boxes < 2^12
+
+// Geometry of the box a work item belongs to, and the item's number in it.
+struct BoxGeom {
+    int nx, ny, nz;
+    int tiles_x, ntiles, zchunk;
+    int64_t js, ks, base;
+    const CUtensorMap *map;
+    int64_t local;
+};
+
+// Work-item sources.
+struct SingleLevel {  // the one level described by the launch parameters
+    template <typename T>
+    __device__ __forceinline__ static BoxGeom item(const SweepArgs<T> &a, const CUtensorMap *map, int64_t it)
+    {
+        return BoxGeom{a.nx, a.ny, a.nz, a.tiles_x, a.ntiles, a.zchunk, a.js, a.ks, 0, map, it};
+    }
+};
+struct BoxTable {  // the boxes of an ensemble
+    template <typename T>
+    __device__ __forceinline__ static BoxGeom item(const SweepArgs<T> &a, const CUtensorMap *, int64_t it)
+    {
+        const uint32_t e = __ldg(a.items + it);
+        const int b = (int)(e >> kEnsItemBits);
+        const EnsBoxDesc &d = a.boxes[b];
+        return BoxGeom{d.nx, d.ny, d.nz, d.tiles_x, d.ntiles, d.zchunk, d.js, d.ks, d.base,
+                       a.maps + 2 * b + a.map_sel, (int64_t)(e & ((1u << kEnsItemBits) - 1))};
+    }
 };
 
 template <typename T, int V, int TX, int TY> struct SweepShape {
@@ -93,7 +145,7 @@ __device__ __forceinline__ void rhs_adjoint_pair(const StageCoef<T> &c, T u1, T 
     o2 = fma(k, a2, la2) - ua * u2;
 }
 
-template <typename T, int V, int TX, int TY, int NS, int MINB, class Op>
+template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel>
 __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     stencil_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
 {
@@ -113,35 +165,45 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         fence_mbar_init();
         abort_flag = 0;
-        prefetch_tensormap(&tmap);
+        if constexpr (std::is_same<Src, SingleLevel>::value) prefetch_tensormap(&tmap);
     }
     __syncthreads();
 
     // ---- producer cursor (thread 0 only) ----
     int64_t p_item = blockIdx.x;
-    int p_k = 0;
+    int p_k = 0, p_len = 0, p_za = 0, p_nz = 1, p_x = 0, p_y = 0;
+    const CUtensorMap *p_map = &tmap;
+    auto p_start = [&]() {
+        if (p_item >= a.n_items) return;
+        const BoxGeom b = Src::item(a, &tmap, p_item);
+        const int tile = (int)(b.local % b.ntiles);
+        p_za = (int)(b.local / b.ntiles) * b.zchunk;
+        p_len = min(b.zchunk, b.nz - p_za);
+        p_nz = b.nz;
+        p_x = (tile % b.tiles_x) * TX;
+        p_y = (tile / b.tiles_x) * TY;
+        p_map = b.map;
+        if constexpr (!std::is_same<Src, SingleLevel>::value) fence_tensormap_acquire(p_map);
+    };
     int64_t q_issued = 0;
     auto issue_one = [&]() -> bool {
         if (p_item >= a.n_items) return false;
-        const int tile = (int)(p_item % a.ntiles);
-        const int chunk = (int)(p_item / a.ntiles);
-        const int za = chunk * a.zchunk;
-        const int len = min(a.zchunk, a.nz - za);
-        int zp = (za - 2 + p_k) % a.nz;
-        if (zp < 0) zp += a.nz;
+        int zp = (p_za - 2 + p_k) % p_nz;
+        if (zp < 0) zp += p_nz;
         const int slot = (int)(q_issued % NS);
         mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
         // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned)
-        tma_load_4d(ring + (size_t)slot * S::SLOT, &tmap, a.ox - 4 + (tile % a.tiles_x) * TX,
-                    (tile / a.tiles_x) * TY, zp, 0, &full[slot]);
+        tma_load_4d(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y, zp, 0, &full[slot]);
         ++q_issued;
-        if (++p_k == len + 4) {
+        if (++p_k == p_len + 4) {
             p_k = 0;
             p_item += gridDim.x;
+            p_start();
         }
         return true;
     };
     if (tid == 0) {
+        p_start();
         for (int s = 0; s < NS; ++s)
             if (!issue_one()) break;
     }
@@ -151,25 +213,25 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     const int xl = 4 + V * tx;  // tile-local column of this thread's first site
     const int yl = 2 + ty;
     for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-        const int tile = (int)(item % a.ntiles);
-        const int chunk = (int)(item / a.ntiles);
-        const int za = chunk * a.zchunk;
-        const int len = min(a.zchunk, a.nz - za);
-        const int x = (tile % a.tiles_x) * TX + V * tx;
-        const int y = (tile / a.tiles_x) * TY + ty;
-        const bool active = (x < a.nx) && (y < a.ny);
+        const BoxGeom b = Src::item(a, &tmap, item);
+        const int tile = (int)(b.local % b.ntiles);
+        const int za = (int)(b.local / b.ntiles) * b.zchunk;
+        const int len = min(b.zchunk, b.nz - za);
+        const int x = (tile % b.tiles_x) * TX + V * tx;
+        const int y = (tile / b.tiles_x) * TY + ty;
+        const bool active = (x < b.nx) && (y < b.ny);
         // pointwise components of the next plane, loaded one iteration ahead
         T pn[NPT > 0 ? NPT : 1][V];
         if constexpr (NPT > 0) {
             if (active) {
-                const int64_t off0 = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)za * a.ks;
+                const int64_t off0 = b.base + (int64_t)(x + a.ox) + (int64_t)(y + 2) * b.js + (int64_t)za * b.ks;
 #pragma unroll
                 for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off0, pn[c]);
             }
         }
         for (int m = 0; m < len; ++m) {
             const int z = za + m;
-            const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + 2) * a.js + (int64_t)z * a.ks;
+            const int64_t off = b.base + (int64_t)(x + a.ox) + (int64_t)(y + 2) * b.js + (int64_t)z * b.ks;
 
             T pq[NPT > 0 ? NPT : 1][V];
             if constexpr (NPT > 0) {
@@ -179,7 +241,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                     for (int v = 0; v < V; ++v) pq[c][v] = pn[c][v];
                 if (active && m + 1 < len) {
 #pragma unroll
-                    for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off + a.ks, pn[c]);
+                    for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off + b.ks, pn[c]);
                 }
             }
 
@@ -217,13 +279,25 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                     for (int v = 0; v < V; ++v) {
                         const int ci = S::PRE * V + v;
                         const T f0 = row[ci];
-                        const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
-                        const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
-                        lap[c][v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
+                        if constexpr (std::is_same<T, float>::value) {
+                            // FP32: differences from the centre first (exact while a
+                            // neighbour lies within a factor 2 of f0), so the -30 f0
+                            // term of the 4th-order stencil does not cancel against
+                            // the neighbour sums: lap = wA sum(f+-1 - f0) + wB sum(f+-2 - f0)
+                            const T d1 = ((row[ci - 1] - f0) + (row[ci + 1] - f0)) + ((ym1[v] - f0) + (yp1[v] - f0)) +
+                                         ((zm1[v] - f0) + (zp1[v] - f0));
+                            const T d2 = ((row[ci - 2] - f0) + (row[ci + 2] - f0)) + ((ym2[v] - f0) + (yp2[v] - f0)) +
+                                         ((zm2[v] - f0) + (zp2[v] - f0));
+                            lap[c][v] = fma(a.wA, d1, a.wB * d2);
+                        } else {
+                            const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
+                            const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
+                            lap[c][v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
+                        }
                         ctr[c][v] = f0;
                     }
                 }
-                Op::template apply<T, V>(a, lap, ctr, pq, off, x, y, lam_acc);
+                Op::template apply<T, V>(a, b, lap, ctr, pq, off, x, y, lam_acc);
             }
 
             __syncthreads();  // everyone is done with the oldest plane of this window
@@ -285,7 +359,7 @@ inline void plan_chunks(int ntiles, int nz, int grid_cap, int &zchunk, int64_t &
 }
 
 // One tiling of one sweep operation: occupancy, chunk plan and launch.
-template <typename T, int V, int TX, int TY, int NS, int MINB, class Op> struct SweepLauncher {
+template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel> struct SweepLauncher {
     using S = SweepShape<T, V, TX, TY>;
     static size_t smem() { return (size_t)NS * S::SLOT_BYTES; }
 
@@ -293,7 +367,7 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, class Op> struct 
     {
         static int cached = -1;
         if (cached < 0) {
-            auto kern = stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op>;
+            auto kern = stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op, Src>;
             AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
             int b = 0;
             AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, S::NT, smem()));
@@ -322,7 +396,7 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, class Op> struct 
 
     static int launch(const CUtensorMap &map, const SweepArgs<T> &a, int grid, cudaStream_t st)
     {
-        stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op><<<grid, S::NT, smem(), st>>>(map, a);
+        stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op, Src><<<grid, S::NT, smem(), st>>>(map, a);
         return launch_status("stencil sweep");
     }
 

@@ -161,6 +161,150 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- differentiation configuration
+def differentiation_report(A, ic, dev, n=128, nsteps=200, ndir=16):
+    import torch
+    from axion_strings_adaptive_gb300.adjoint import EvolutionSpec, string_core_loss
+    spec = EvolutionSpec(dx=DX, dt=DT, nsteps=nsteps, tau_i=TAU_I, a_inv=A_INV, c0=1.0, width=0.1,
+                         checkpoint_every=20)
+    s0 = ic.fourier_state(n, ic.strict_cutoff(n / 4), seed=SEED + 4, dtype=torch.float64, device=dev)
+    res = {}
+    for dt_, name in ((torch.float32, "fp32"), (torch.float64, "fp64")):
+        x = s0.to(dt_).clone().requires_grad_(True)
+        lam = torch.tensor(LAMBDA0, dtype=dt_, requires_grad=True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        e0.record()
+        loss = string_core_loss(x, lam, spec)
+        e1.record()
+        loss.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        res[name] = {"loss": float(loss), "grad": x.grad.double(), "lambda_grad": float(lam.grad),
+                     "forward_ms": e0.elapsed_time(e1), "backward_ms": e1.elapsed_time(e2)}
+    g32, g64 = res["fp32"]["grad"], res["fp64"]["grad"]
+    lam64 = torch.tensor(LAMBDA0, dtype=torch.float64)
+    gen = torch.Generator(device=dev).manual_seed(SEED + 5)
+    eps = 1e-3
+    dirs = []
+    for _ in range(ndir):
+        d = torch.zeros_like(s0)
+        d[:2] = torch.randn(d[:2].shape, generator=gen, device=dev, dtype=torch.float64)
+        d /= d.norm()
+        fd = (float(string_core_loss(s0 + eps * d, lam64, spec)) -
+              float(string_core_loss(s0 - eps * d, lam64, spec))) / (2 * eps)
+        dirs.append({"fd": fd, "adjoint_fp32": float((g32 * d).sum()), "adjoint_fp64": float((g64 * d).sum())})
+    fd_l = (float(string_core_loss(s0, lam64 + eps, spec)) - float(string_core_loss(s0, lam64 - eps, spec))) / (2 * eps)
+    scale = float(g64[:2].norm())
+
+    def rel(a, b, floor=0.0):
+        return abs(a - b) / max(abs(b), floor, 1e-300)
+
+    out = {"config": f"{n}^3 FP32, c0=1, lambda0=2, {nsteps} RK4 steps, dx=0.5, dt=0.1, checkpoint every 20, "
+                     f"loss = sum exp(-|psi/R|^2/0.1) + <axion kinetic energy>, IC |n|<N/4, Pi=0",
+           "loss": {k: v["loss"] for k, v in res.items()},
+           "grad_psi_rel_err_fp32_vs_fp64": float((g32[:2] - g64[:2]).norm() / g64[:2].norm()),
+           "lambda_grad": {"fp32": res["fp32"]["lambda_grad"], "fp64": res["fp64"]["lambda_grad"], "fd": fd_l},
+           "lambda_grad_rel_err": {"fp32_vs_fd": rel(res["fp32"]["lambda_grad"], fd_l),
+                                   "fp64_vs_fd": rel(res["fp64"]["lambda_grad"], fd_l)},
+           "directions": len(dirs), "eps": eps,
+           "max_rel_err_fp32_vs_fd": max(rel(d["adjoint_fp32"], d["fd"], 1e-3 * scale) for d in dirs),
+           "max_rel_err_fp64_vs_fd": max(rel(d["adjoint_fp64"], d["fd"], 1e-3 * scale) for d in dirs),
+           "rel_err_floor": "1e-3 x |grad_psi| (directional derivatives near zero)",
+           "timing_ms": {k: {"forward": v["forward_ms"], "backward": v["backward_ms"],
+                             "backward_over_forward": v["backward_ms"] / v["forward_ms"]} for k, v in res.items()},
+           "directional": dirs}
+    return out
+
+
+# ---------------------------------------------------------------- batching configuration
+def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 64, 96, 128)):
+    """64 seeded boxes of sizes drawn uniformly from `sizes`, FP32, c0 = 1,
+    lambda0 = 2, IC |n| < N_box/4 (seed + box), 200 RK4 steps per box: one
+    persistent launch per sweep over all boxes, the whole run plus per-box
+    diagnostics captured as one CUDA graph; beside it the same boxes advanced
+    one level at a time."""
+    import numpy as np
+    import torch
+    rng = np.random.RandomState(SEED)
+    ns = [int(v) for v in rng.choice(sizes, size=nboxes)]
+    dims = [(n, n, n) for n in ns]
+    bg = A.Background.expanding(A_INV, 1.0, lambda0=LAMBDA0)
+    ens = A.Ensemble(dims, DX, dtype=torch.float32, device=dev)
+    ics = []
+    for b, n in enumerate(ns):
+        s0 = ic.fourier_state(n, ic.strict_cutoff(n / 4), seed=SEED + b, dtype=torch.float64, device=dev).float()
+        ens.set_box(b, s0)
+        ics.append(s0)
+    ens.fill_ghosts()
+    tune = ens.autotune(bg, TAU_I, DT, steps=3, repeats=1)
+    init = ens.state.clone()
+    sites = ens.n_sites
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    ens.advance(bg, TAU_I, 0.0, DT, 3)  # warm
+    ens.state.copy_(init)
+    ms_eager = timed(lambda: ens.advance(bg, TAU_I, 0.0, DT, nsteps))
+    ens.device_status()
+    eager_final = ens.state.clone()
+    ens.state.copy_(init)
+    graph = ens.capture(bg, TAU_I, 0.0, DT, nsteps, diagnostics=True)
+    graph.replay()  # warm replay
+    ens.state.copy_(init)
+    ms_graph = timed(graph.replay)
+    ens.device_status()
+    same = bool(torch.equal(ens.state, eager_final))
+    tau_f = TAU_I + nsteps * DT
+    res = ens.results(bg, tau_f)
+    cfg_name = dict(ens.tile_configs()).get(ens.plan.tile_config, "default")
+    plan = {"tile_config": cfg_name, "z_chunk": ens.plan.z_chunk or "auto", "work_items": ens.plan.n_items,
+            "grid": [ens.plan.grid_a, ens.plan.grid_b]}
+    del ens, graph, init, eager_final
+    torch.cuda.empty_cache()
+
+    # the same boxes, one level at a time (same kernels, one launch per box per sweep)
+    levels = []
+    for b, n in enumerate(ns):
+        lv = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev, pierced_capacity=1)
+        lv.set_state(ics[b])
+        levels.append(lv)
+    for lv in levels:
+        lv.advance(bg, TAU_I, 0.0, DT, 1)
+    for b, lv in enumerate(levels):
+        lv.set_state(ics[b])
+
+    def per_box():
+        for s in range(nsteps):
+            for lv in levels:
+                lv.advance(bg, TAU_I, s * DT, DT, 1)
+
+    ms_levels = timed(per_box)
+    del levels
+    torch.cuda.empty_cache()
+    words = 24  # compulsory words per site per RK4 step (two sweeps of 4+8 and 8+4)
+    return {"config": f"{nboxes} boxes, sizes uniform from {list(sizes)}^3 (seed {SEED}), FP32, c0=1, lambda0=2, "
+                      f"IC |n|<N/4 seed+box, {nsteps} RK4 steps, per-box energy + winding diagnostics",
+            "sizes": {str(k): ns.count(k) for k in sizes}, "sites": sites, "steps": nsteps,
+            "graph_ms": ms_graph, "graph_site_updates_per_s": sites * nsteps / (ms_graph * 1e-3),
+            "eager_ms": ms_eager, "eager_site_updates_per_s": sites * nsteps / (ms_eager * 1e-3),
+            "graph_equals_eager": same,
+            "hbm_frac_of_measured": words * 4 * sites * nsteps / (ms_eager * 1e-3) / 1e9 / hbm_peak,
+            "per_box_levels_ms": ms_levels, "speedup_vs_per_box_levels": ms_levels / ms_graph,
+            "plan": plan, "autotune_ms_per_step": tune,
+            "launches_per_step": 2, "graph_nodes": 2 * nsteps + 3 * nboxes,
+            "n_p_total": sum(r.n_p_plain for r in res),
+            "per_box": [{"n": n, "n_p": r.n_p_plain, "rho_tot": r.energy["rho_tot_unscreened"],
+                         "xi": r.xi_plain} for n, r in zip(ns, res)][:8]}
+
+
 # ---------------------------------------------------------------- native arm
 def run_native(args):
     import torch
@@ -262,25 +406,29 @@ def run_native(args):
     # ---------------- fused diagnostics pass (string finder + energies + velocities) on the FP32 box
     diag = None
     if not args.no_diag:
-        t_ev = []
         tau_d = TAU_I + (args.warmup + args.steps) * DT
         bv = bg.values(tau_d)
-        params = A._lib.DiagParams(DX, bv.R, bv.lambda_, bv.R_prime_over_R, bv.m_r, A._lib.MASK_A, 0.8,
-                                   A._lib.BOUNDARY_PERIODIC, 1, 1, 1)
         import ctypes as _C
-        for r in range(3):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            A._lib.call("axs_level_diagnostics", _C.byref(lv32.c), _C.byref(params), None, lv32._result.data_ptr(),
-                        lv32._pierced.data_ptr(), lv32._pierced.numel(), lv32._scratch.data_ptr(),
-                        lv32._scratch.numel(), torch.cuda.current_stream().cuda_stream)
-            e1.record()
-            e1.synchronize()
-            t_ev.append(e0.elapsed_time(e1))
-        ms_d = min(t_ev)
-        res = A.level._result_from_bytes(lv32._result)
-        diag = {"ms": ms_d, "read_gbps": 16 * n ** 3 / (ms_d * 1e-3) / 1e9, "n_p_plain": res.n_p_plain,
-                "n_near_tie": res.n_near_tie, "fields": "fp32", "per_cell_math": "fp64"}
+        diag = {"fields": "fp32", "read_bytes_per_cell": 16}
+        for mode, fp32 in (("per_cell_fp64", 0), ("per_cell_fp32", 1)):
+            params = A._lib.DiagParams(DX, bv.R, bv.lambda_, bv.R_prime_over_R, bv.m_r, A._lib.MASK_A, 0.8,
+                                       A._lib.BOUNDARY_PERIODIC, 1, 1, 1, fp32)
+            t_ev = []
+            for r in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                A._lib.call("axs_level_diagnostics", _C.byref(lv32.c), _C.byref(params), None,
+                            lv32._result.data_ptr(), lv32._pierced.data_ptr(), lv32._pierced.numel(),
+                            lv32._scratch.data_ptr(), lv32._scratch.numel(), torch.cuda.current_stream().cuda_stream)
+                e1.record()
+                e1.synchronize()
+                t_ev.append(e0.elapsed_time(e1))
+            ms_d = min(t_ev)
+            res = A.level._result_from_bytes(lv32._result)
+            diag[mode] = {"ms": ms_d, "read_gbps": 16 * n ** 3 / (ms_d * 1e-3) / 1e9, "n_p_plain": res.n_p_plain,
+                          "n_near_tie": res.n_near_tie, "rho_tot_sum": res.energy_sums[0]}
+        diag["rho_tot_rel_diff"] = abs(diag["per_cell_fp32"]["rho_tot_sum"] - diag["per_cell_fp64"]["rho_tot_sum"]) / \
+            abs(diag["per_cell_fp64"]["rho_tot_sum"])
 
     # ---------------- adjoint step cost on the same FP32 box (recompute sweep A + adjoint sweeps B and A)
     adj = None
@@ -377,6 +525,18 @@ def run_native(args):
         precision["max_energy_rel_err"] = fin["max_energy_rel_err"]
         del out
 
+    # ---------------- differentiation: 128^3 FP32, c0 = 1, lambda0 = 2, 200 steps, checkpoint every 20;
+    # gradients w.r.t. the initial psi and lambda0 against central differences (eps = 1e-3, FP64
+    # evolution) on 16 unit-norm random directions in psi, and against the FP64 adjoint
+    differentiation = None
+    if not args.no_differentiation:
+        differentiation = differentiation_report(A, ic, dev, args.diff_n, args.diff_steps, args.diff_directions)
+
+    # ---------------- batching: 64 uneven boxes, one persistent launch per sweep, one CUDA graph
+    batching = None
+    if not args.no_batching:
+        batching = batching_report(A, ic, dev, hbm_peak)
+
     # ---------------- end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
@@ -424,7 +584,8 @@ def run_native(args):
                 "clocks": clocks, "gpu_launches": 2 * args.steps, "tile_config": cfg32,
                 "autotune_ms_per_step": tune32, "diagnostics": diag, "fp64": fp64,
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision,
-                "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None}
+                "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None,
+                "differentiation": differentiation, "batching": batching}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -447,6 +608,11 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-diag", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-differentiation", action="store_true")
+    ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--diff-n", type=int, default=128)
+    ap.add_argument("--diff-steps", type=int, default=200)
+    ap.add_argument("--diff-directions", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3

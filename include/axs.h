@@ -244,6 +244,13 @@ typedef struct axs_diag_params {
     double masking_threshold;
     int32_t boundary;                      /* axs_boundary */
     int32_t want_energy, want_plaquettes, want_velocity;
+    int32_t per_cell_fp32;                 /* FP32 fields only: 0 = per-cell energy, masking and
+                                              gamma^2 v^2 in double as the reference computes them
+                                              (sums equal the reference's FLOAT build); 1 = per-cell
+                                              terms in FP32, summed per work item in FP32 and
+                                              across items in FP64 (about 1e-7 relative; ~10x
+                                              faster on GB300, whose FP64 rate is 1/64 of FP32).
+                                              Windings and counts are exact either way. */
 } axs_diag_params;
 
 /* Written to device memory by the diagnostics pass. */
@@ -301,6 +308,78 @@ int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *
  * theta[4*q .. 4*q+3] -> w[q]: the device winding kernel on caller-chosen
  * phases (known-answer tests). */
 int axs_plaquette_winding_batch(const double *theta_dev, int64_t n, int32_t *w_dev, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Ensembles: many independent periodic boxes of uneven sizes advanced together
+ * (no counterpart in the reference, which runs one box layout per process;
+ * each box evolves exactly as an axs_level of its size would, bit for bit).
+ *
+ * The boxes are packed component-major: component c of every box lives in one
+ * "component plane" of plane_elems elements; box b starts at element `base`
+ * of each plane and inside it has the axs_level layout of its size (x_offset,
+ * y_offset, jstride, kstride as axs_level_layout_for reports). The state arena
+ * holds 4 planes, the work arena 8; both and the table are caller-owned device
+ * memory, 128-byte aligned. axs_ensemble_init writes the device table (box
+ * descriptors, work items, two TMA descriptors per box) for one tiling; every
+ * RK4 sweep is then ONE persistent launch over the work items of all boxes.
+ * ------------------------------------------------------------------------- */
+typedef struct axs_ensemble {
+    int32_t dtype;
+    int32_t nboxes;
+    const int32_t *dims; /* host array, 3 per box: nx, ny, nz */
+    double dx;           /* grid spacing shared by all boxes */
+    void *state;         /* 4 component planes */
+    void *work;          /* 8 component planes */
+    void *table;         /* written by axs_ensemble_init */
+    int64_t state_bytes, work_bytes, table_bytes;
+} axs_ensemble;
+
+typedef struct axs_ensemble_box {
+    int64_t base;       /* element offset of the box in every component plane */
+    int64_t jstride, kstride;
+    int32_t x_offset, y_offset;
+} axs_ensemble_box;
+
+typedef struct axs_ensemble_plan {
+    int32_t tile_config; /* in: index from axs_ensemble_tile_config_name, 0 = default */
+    int32_t z_chunk;     /* in: target z planes per work item, 0 = automatic */
+    int64_t n_items;     /* out: work items of one sweep (all boxes) */
+    int32_t grid_a;      /* out: persistent grid of sweep A */
+    int32_t grid_b;      /* out: persistent grid of sweep B */
+    int64_t plane_elems; /* out */
+    uint64_t key;        /* out: ties the plan to the ensemble it was built for */
+} axs_ensemble_plan;
+
+int axs_ensemble_sizes(int32_t dtype, int32_t nboxes, const int32_t *dims, int64_t *state_bytes,
+                       int64_t *work_bytes, int64_t *table_bytes);
+int axs_ensemble_box_layout(int32_t dtype, int32_t nboxes, const int32_t *dims, int32_t box, axs_ensemble_box *out);
+int32_t axs_ensemble_tile_config_count(int32_t dtype);
+const char *axs_ensemble_tile_config_name(int32_t dtype, int32_t id);
+
+/* Build the device table for plan->tile_config / plan->z_chunk and fill the
+ * plan's outputs. Host-synchronous (it uploads the table and waits); call it
+ * before capturing axs_ensemble_rk4_advance in a CUDA graph. */
+int axs_ensemble_init(const axs_ensemble *e, axs_ensemble_plan *plan, void *stream);
+
+/* Periodic padding of every box (after the caller wrote the valid cells). */
+int axs_ensemble_fill_ghosts(const axs_ensemble *e, void *stream);
+
+/* nsteps classic-RK4 steps of every box: two persistent launches per step
+ * (sweeps A and B over all boxes' work items). Graph-capturable. The plan must
+ * be the one the last axs_ensemble_init on this table returned (checked on the
+ * host; a stale plan is rejected with AXS_ERR_INVALID_ARGUMENT). */
+int axs_ensemble_rk4_advance(const axs_ensemble *e, const axs_ensemble_plan *plan, const axs_background *bg,
+                             double tau_i, double t0, double dt, int32_t nsteps, void *stream);
+
+/* Per-box diagnostics (as axs_level_diagnostics, without the pierced list)
+ * into result_dev[0 .. nboxes-1]; scratch sized by
+ * axs_ensemble_diagnostics_scratch_bytes and reused box after box. */
+int axs_ensemble_diagnostics_scratch_bytes(int32_t nboxes, const int32_t *dims, int64_t *bytes);
+int axs_ensemble_diagnostics(const axs_ensemble *e, const axs_diag_params *p, axs_diag_result *result_dev,
+                             void *scratch, int64_t scratch_bytes, void *stream);
+
+/* Host-synchronous: AXS_ERR_DEVICE_TIMEOUT if a sweep's bounded wait gave up. */
+int axs_ensemble_device_status(const axs_ensemble *e, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Initial data

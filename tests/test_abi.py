@@ -137,3 +137,38 @@ def test_package_refuses_cpu_tensors():
     import axion_strings_adaptive_gb300 as A
     with pytest.raises(ValueError, match="CUDA"):
         A.fab(torch.zeros((4, 8, 8, 8)), 2)
+
+
+def test_ensemble_layout_and_validation(L):
+    lib = L.lib()
+    dims = [32, 32, 32, 48, 40, 24, 16, 16, 8]
+    arr = (C.c_int32 * len(dims))(*dims)
+    sb, wb, tb = C.c_int64(), C.c_int64(), C.c_int64()
+    L.call("axs_ensemble_sizes", L.AXS_F32, 3, arr, C.byref(sb), C.byref(wb), C.byref(tb))
+    plane = sb.value // 16
+    assert wb.value == 2 * sb.value and tb.value > 128
+    end = 0
+    for b in range(3):
+        lay = L.EnsembleBox()
+        L.call("axs_ensemble_box_layout", L.AXS_F32, 3, arr, b, C.byref(lay))
+        nx, ny, nz = dims[3 * b:3 * b + 3]
+        ref = L.LevelLayout()
+        L.call("axs_level_layout_for", L.AXS_F32, nx, ny, nz, C.byref(ref))
+        assert (lay.jstride, lay.kstride, lay.x_offset, lay.y_offset) == \
+               (ref.jstride, ref.kstride, ref.x_offset, ref.y_offset)
+        assert lay.base % 32 == 0 and lay.base >= end  # 128-byte aligned, no overlap
+        end = lay.base + nz * lay.kstride
+    assert end <= plane
+    assert lib.axs_ensemble_tile_config_count(L.AXS_F32) >= 3
+    assert lib.axs_ensemble_tile_config_name(L.AXS_F32, 0)
+    assert lib.axs_ensemble_tile_config_name(L.AXS_F32, 99) is None
+    # rejected before any CUDA call
+    bad = (C.c_int32 * 3)(30, 32, 32)  # nx not a multiple of 4 (FP32 rows)
+    assert lib.axs_ensemble_sizes(L.AXS_F32, 1, bad, C.byref(sb), C.byref(wb), C.byref(tb)) == L.AXS_ERR_UNSUPPORTED
+    assert lib.axs_ensemble_sizes(L.AXS_F32, 0, arr, C.byref(sb), C.byref(wb), C.byref(tb)) == \
+        L.AXS_ERR_INVALID_ARGUMENT
+    e = L.EnsembleC(L.AXS_F32, 3, arr, 0.5, None, None, None, 0, 0, 0)
+    plan = L.EnsemblePlan()
+    assert lib.axs_ensemble_init(C.byref(e), C.byref(plan), None) == L.AXS_ERR_INVALID_ARGUMENT
+    e2 = L.EnsembleC(L.AXS_F32, 3, arr, 0.5, 128, 128, 128, 16, 16, 16)  # buffers too small
+    assert lib.axs_ensemble_init(C.byref(e2), C.byref(plan), None) == L.AXS_ERR_WORKSPACE

@@ -161,3 +161,21 @@ def test_rejects_bad_arguments_without_launching(axs):
     assert L.lib().axs_eval_rhs(C.byref(axs.fab(t, 1)), C.byref(axs.fab(t, 1)), 0.5, C.byref(c),
                                 None) == L.AXS_ERR_INVALID_ARGUMENT  # needs 2 ghosts
     assert b"ghost" in L.lib().axs_last_error()
+
+
+def test_per_cell_fp32_variant(axs):
+    """per_cell_fp32 on FP32 fields: identical winding counts, pierced list and
+    velocity count; energy sums within 2e-6 relative of the double per-cell pass."""
+    from axion_strings_adaptive_gb300 import ic
+    n = 64
+    bg = axs.Background.expanding(2.0, 2.0, lambda0=2.0)
+    lv = axs.PeriodicLevel(n, 0.5, dtype=torch.float32)
+    lv.set_state(ic.fourier_state(n, ic.strict_cutoff(n / 8), seed=5).float())
+    lv.advance(bg, 1.0, 0.0, 0.1, 30)
+    lv.device_status()
+    ref = lv.diagnostics(bg, 4.0)
+    fast = lv.diagnostics(bg, 4.0, per_cell_fp32=True)
+    assert (fast.n_p_plain, fast.n_p_weighted, fast.vel_count) == (ref.n_p_plain, ref.n_p_weighted, ref.vel_count)
+    assert torch.equal(torch.sort(fast.pierced)[0], torch.sort(ref.pierced)[0])
+    np.testing.assert_allclose(fast.energy_sums, ref.energy_sums, rtol=2e-6)
+    assert fast.mean_gamma_sq_v_sq == pytest.approx(ref.mean_gamma_sq_v_sq, rel=1e-5)
