@@ -20,6 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include")
 LIB_NAME = "libaxs_gb300.so"
 LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
+HOST_DIR = os.path.join(PKG_DIR, "host")
+DEMO_PATH = os.path.join(PKG_DIR, "axs_level_demo")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing",
@@ -39,7 +41,8 @@ def _sources():
 
 def _fingerprint() -> str:
     h = hashlib.sha256()
-    for p in _sources() + sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + [os.path.join(INCLUDE, "axs.h")]:
+    extra = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + sorted(glob.glob(os.path.join(HOST_DIR, "*.*")))
+    for p in _sources() + extra + [os.path.join(INCLUDE, "axs.h")]:
         with open(p, "rb") as f:
             h.update(p.encode())
             h.update(f.read())
@@ -51,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     """Compile (if stale) and return the path of libaxs_gb300.so."""
     stamp = LIB_PATH + ".stamp"
     fp = _fingerprint()
-    if not force and os.path.exists(LIB_PATH) and os.path.exists(stamp):
+    if not force and os.path.exists(LIB_PATH) and os.path.exists(DEMO_PATH) and os.path.exists(stamp):
         with open(stamp) as f:
             if f.read().strip() == fp:
                 return LIB_PATH
@@ -77,9 +80,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB_PATH)
+    build_host_demo(cc)
     with open(stamp, "w") as f:
         f.write(fp)
     return LIB_PATH
+
+
+def build_host_demo(cc: str | None = None) -> str:
+    """The C++ host driver (host/level_demo.cpp over host/axs_level.hpp),
+    linked against libaxs_gb300.so next to it."""
+    cc = cc or nvcc()
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(cc)))
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, "-I", os.path.join(cuda, "include"), "-I", HOST_DIR,
+           os.path.join(HOST_DIR, "level_demo.cpp"), "-o", DEMO_PATH, "-L", PKG_DIR, "-laxs_gb300",
+           "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+           "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host demo build failed:\n{r.stdout}\n{r.stderr}")
+    return DEMO_PATH
 
 
 if __name__ == "__main__":

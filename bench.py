@@ -305,6 +305,29 @@ def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 
                          "xi": r.xi_plain} for n, r in zip(ns, res)][:8]}
 
 
+# ---------------------------------------------------------------- replicas (one independent box per rank)
+def replica_barrier(ws: int) -> None:
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def replica_max(x: float, ws: int, device) -> float:
+    """Max of a per-rank scalar (the slowest rank's time) over all ranks."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Each rank evolves its own seeded realisation (weak scaling, no data exchange)."""
+    return SEED + rank
+
+
 # ---------------------------------------------------------------- native arm
 def run_native(args):
     import torch
@@ -322,18 +345,13 @@ def run_native(args):
     A.lib()
     n = args.n
     bg = A.Background.expanding(A_INV, C0, lambda0=LAMBDA0)
-    ic64 = ic.fourier_state(n, ic.strict_cutoff(n / 8), seed=SEED + rank, dtype=torch.float64, device=dev)
+    ic64 = ic.fourier_state(n, ic.strict_cutoff(n / 8), seed=replica_seed(rank), dtype=torch.float64, device=dev)
 
     def barrier():
-        if ws > 1:
-            dist.barrier()
+        replica_barrier(ws)
 
     def allmax(x):
-        if ws == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_max(x, ws, dev)
 
     def timed_run(level, steps, warmup, t_start=0.0, sample_clocks=False):
         for w in range(warmup):

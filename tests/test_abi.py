@@ -172,3 +172,10 @@ def test_ensemble_layout_and_validation(L):
     assert lib.axs_ensemble_init(C.byref(e), C.byref(plan), None) == L.AXS_ERR_INVALID_ARGUMENT
     e2 = L.EnsembleC(L.AXS_F32, 3, arr, 0.5, 128, 128, 128, 16, 16, 16)  # buffers too small
     assert lib.axs_ensemble_init(C.byref(e2), C.byref(plan), None) == L.AXS_ERR_WORKSPACE
+
+
+def test_cpp_host_demo_is_built(L):
+    import subprocess
+    from axion_strings_adaptive_gb300 import _build
+    r = subprocess.run([_build.DEMO_PATH], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
