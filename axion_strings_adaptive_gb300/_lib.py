@@ -71,6 +71,11 @@ class DiagResult(C.Structure):
                 ("n_p_weighted", _i64), ("n_listed", _i64), ("n_near_tie", _i64), ("status", _i64)]
 
 
+class TagParams(C.Structure):
+    _fields_ = [("dx", _dbl), ("gradient_threshold", _dbl), ("radial_gradient_threshold", _dbl),
+                ("n_error_buf", _i32), ("block", _i32)]
+
+
 class EnsembleC(C.Structure):
     _fields_ = [("dtype", _i32), ("nboxes", _i32), ("dims", C.POINTER(_i32)), ("dx", _dbl), ("state", _ptr),
                 ("work", _ptr), ("table", _ptr), ("state_bytes", _i64), ("work_bytes", _i64),
@@ -119,6 +124,8 @@ SIGNATURES = {
     "axs_level_diagnostics": (_i32, [C.POINTER(LevelC), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr, _i64,
                                      _ptr]),
     "axs_diagnostics_static_scratch": (_i32, [C.POINTER(Fab), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr]),
+    "axs_tag_scratch_bytes": (_i32, [_i32, _i32, _i32, C.POINTER(_i64)]),
+    "axs_level_tag_cells": (_i32, [C.POINTER(LevelC), C.POINTER(TagParams), _ptr, _ptr, _ptr, _ptr, _i64, _ptr]),
     "axs_ensemble_sizes": (_i32, [_i32, _i32, C.POINTER(_i32), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),
     "axs_ensemble_box_layout": (_i32, [_i32, _i32, C.POINTER(_i32), _i32, C.POINTER(EnsembleBox)]),
     "axs_ensemble_tile_config_count": (_i32, [_i32]),

@@ -37,9 +37,10 @@ int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const Leve
 struct AdjointB {
     static constexpr int kPointwise = 4;
     static constexpr bool kLambdaGrad = true;
-    template <typename T, int V, typename PQ>
+    template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam)
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam,
+                                 uint64_t pol)
     {
         T fo[4][V], uo[4][V];
 #pragma unroll
@@ -68,9 +69,9 @@ struct AdjointB {
             lam -= (double)(fma(a.c2.hlam * m3, fma(u31, f3b1, u32 * f3b2), a.c4.hlam * m4 * fma(u41, f4b1, u42 * f4b2)));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, b.nx, b.ny, b.js, fo[c]);
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, fo[c], pol);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) stv<T, V>(a.out[4 + c] + off, uo[c]);
+        for (int c = 0; c < 4; ++c) st_out<T, V, HINT>(a.out[4 + c] + off, uo[c], pol);
     }
 };
 
@@ -79,9 +80,10 @@ struct AdjointB {
 struct AdjointA {
     static constexpr int kPointwise = 12;
     static constexpr bool kLambdaGrad = true;
-    template <typename T, int V, typename PQ>
+    template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam)
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam,
+                                 uint64_t pol)
     {
         T o[4][V];
 #pragma unroll
@@ -105,7 +107,7 @@ struct AdjointA {
             lam -= (double)(fma(a.c1.hlam * m1, fma(p1, f1b1, p2 * f1b2), a.c2.hlam * m2 * fma(u21, f2b1, u22 * f2b2)));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c]);
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol);
     }
 };
 

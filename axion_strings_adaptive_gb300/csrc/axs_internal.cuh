@@ -151,6 +151,71 @@ __device__ __forceinline__ void store_vec(T *p, const T *in)
     *reinterpret_cast<V *>(p) = v;
 }
 
+// ---------------------------------------------------------------- L2 cache policies
+// 64-bit L2 access policies (createpolicy) for loads and stores that carry an
+// .L2::cache_hint: evict_first for streams read or written once, evict_last
+// for data other blocks re-read soon (stencil halos).
+__device__ __forceinline__ uint64_t l2_policy_evict_first()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t l2_policy_evict_last()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// V-wide vector store / non-coherent load with an L2 policy.
+template <typename T, int V>
+__device__ __forceinline__ void stv_hint(T *p, const T *in, uint64_t pol)
+{
+    if constexpr (sizeof(T) == 4 && V == 1) {
+        asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(in[0]), "l"(pol) : "memory");
+    } else if constexpr (sizeof(T) == 4 && V == 2) {
+        asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(in[0]), "f"(in[1]),
+                     "l"(pol)
+                     : "memory");
+    } else if constexpr (sizeof(T) == 4 && V == 4) {
+        asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(in[0]),
+                     "f"(in[1]), "f"(in[2]), "f"(in[3]), "l"(pol)
+                     : "memory");
+    } else if constexpr (sizeof(T) == 8 && V == 1) {
+        asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(in[0]), "l"(pol) : "memory");
+    } else {
+        static_assert(sizeof(T) == 8 && V == 2, "unsupported vector");
+        asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(in[0]), "d"(in[1]),
+                     "l"(pol)
+                     : "memory");
+    }
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void ldv_nc_hint(const T *p, T *out, uint64_t pol)
+{
+    if constexpr (sizeof(T) == 4 && V == 1) {
+        asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(out[0]) : "l"(p), "l"(pol));
+    } else if constexpr (sizeof(T) == 4 && V == 2) {
+        asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+                     : "=f"(out[0]), "=f"(out[1])
+                     : "l"(p), "l"(pol));
+    } else if constexpr (sizeof(T) == 4 && V == 4) {
+        asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                     : "=f"(out[0]), "=f"(out[1]), "=f"(out[2]), "=f"(out[3])
+                     : "l"(p), "l"(pol));
+    } else if constexpr (sizeof(T) == 8 && V == 1) {
+        asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(out[0]) : "l"(p), "l"(pol));
+    } else {
+        static_assert(sizeof(T) == 8 && V == 2, "unsupported vector");
+        asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+                     : "=d"(out[0]), "=d"(out[1])
+                     : "l"(p), "l"(pol));
+    }
+}
+
 // ---------------------------------------------------------------- PTX: mbarrier + TMA
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
@@ -216,6 +281,16 @@ __device__ __forceinline__ void fence_tensormap_acquire(const CUtensorMap *map)
 {
     asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
                  : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d_hint(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                                 uint64_t *bar, uint64_t pol)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint "
+        "[%0], [%1, {%2, %3, %4, %5}], [%6], %7;" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar)), "l"(pol)
+        : "memory");
 }
 
 __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map)

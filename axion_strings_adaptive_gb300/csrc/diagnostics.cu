@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "axs_internal.cuh"
+#include "winding.cuh"
 
 namespace axs {
 
@@ -68,53 +69,6 @@ template <typename T>
 __device__ __forceinline__ double ld(const DiagView &v, int c, int i, int j, int k)
 {
     return (double)__ldg(static_cast<const T *>(v.data) + view_off<T>(v, c, i, j, k));
-}
-
-__device__ __forceinline__ double wrap_diff(double d, int &near_tie)
-{
-    const double pi = 3.14159265358979323846;
-    const double two_pi = 2.0 * pi;
-    if (fabs(fabs(d) - pi) < 1e-12) near_tie = 1;
-    d = fmod(d, two_pi);
-    if (d <= -pi)
-        d = __dadd_rn(d, two_pi);
-    else if (d > pi)
-        d = __dsub_rn(d, two_pi);
-    return d;
-}
-
-// PlaquetteWinding.hpp:42-51 literally, on double phases.
-__device__ __forceinline__ int winding4(double t1, double t2, double t3, double t4, int &ties)
-{
-    int n1 = 0, n2 = 0, n3 = 0, n4 = 0;
-    const double a = wrap_diff(__dsub_rn(t2, t1), n1);
-    const double b = wrap_diff(__dsub_rn(t3, t2), n2);
-    const double c = wrap_diff(__dsub_rn(t4, t3), n3);
-    const double d = wrap_diff(__dsub_rn(t1, t4), n4);
-    ties += n1 + n2 + n3 + n4;
-    const double total = __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d);
-    return (int)llround(__ddiv_rn(total, 2.0 * 3.14159265358979323846));
-}
-
-// Winding from single-precision phases. With every edge difference at least
-// 1e-5 away from +-pi the fold decisions of the reference's double arithmetic
-// are forced (the phases here are within ~1e-6 of the double ones), and the
-// winding is #(d <= -pi) - #(d > pi). Returns false when an edge is inside
-// that band: the caller then redoes the plaquette in double.
-__device__ __forceinline__ bool winding4_fast(float t1, float t2, float t3, float t4, int &w)
-{
-    const float pi = 3.14159265f, band = 1e-5f;
-    const float d[4] = {t2 - t1, t3 - t2, t4 - t3, t1 - t4};
-    int up = 0, down = 0;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const float a = fabsf(d[e]);
-        if (fabsf(a - pi) < band) return false;
-        up += d[e] < -pi;
-        down += d[e] > pi;
-    }
-    w = up - down;
-    return true;
 }
 
 // GRTeclyn diff1 (centred 4th order: weights 1/12, 2/3, times 1/dx) from

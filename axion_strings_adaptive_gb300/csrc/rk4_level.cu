@@ -103,9 +103,9 @@ int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const Leve
                               4);
 }
 
-template <typename T, int V, int TX, int TY, int NS, int MINB> struct SweepConfig {
-    using LA = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardA>;
-    using LB = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardB>;
+template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false> struct SweepConfig {
+    using LA = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardA, SingleLevel, HINT>;
+    using LB = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardB, SingleLevel, HINT>;
 
     static int run(const SweepRunArgs &r)
     {
@@ -165,12 +165,18 @@ static const TileConfigEntry kF32Configs[] = {
     {"f32 v4 64x16 ring6", &SweepConfig<float, 4, 64, 16, 6, 1>::run},
     {"f32 v2 32x16 ring6", &SweepConfig<float, 2, 32, 16, 6, 2>::run},
     {"f32 v1 32x16 ring7", &SweepConfig<float, 1, 32, 16, 7, 2>::run},
+    // L2 policies: stencil planes evict-last, pointwise inputs and outputs evict-first
+    {"f32 v2 64x8 ring8 l2", &SweepConfig<float, 2, 64, 8, 8, 2, true>::run},
+    {"f32 v2 32x16 ring8 l2", &SweepConfig<float, 2, 32, 16, 8, 2, true>::run},
+    {"f32 v2 32x8 ring8 l2", &SweepConfig<float, 2, 32, 8, 8, 3, true>::run},
+    {"f32 v4 64x16 ring6 l2", &SweepConfig<float, 4, 64, 16, 6, 1, true>::run},
 };
 static const TileConfigEntry kF64Configs[] = {
     {"f64 v1 32x8 ring6", &SweepConfig<double, 1, 32, 8, 6, 2>::run},
     {"f64 v2 32x8 ring6", &SweepConfig<double, 2, 32, 8, 6, 2>::run},
     {"f64 v2 32x16 ring6", &SweepConfig<double, 2, 32, 16, 6, 1>::run},
     {"f64 v1 32x4 ring7", &SweepConfig<double, 1, 32, 4, 7, 3>::run},
+    {"f64 v1 32x8 ring6 l2", &SweepConfig<double, 1, 32, 8, 6, 2, true>::run},
 };
 
 static int config_count(int32_t dtype)

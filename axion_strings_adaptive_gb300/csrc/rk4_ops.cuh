@@ -11,9 +11,10 @@ namespace axs {
 struct ForwardA {
     static constexpr int kPointwise = 0;
     static constexpr bool kLambdaGrad = false;
-    template <typename T, int V, typename PQ>
+    template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &, int64_t off, int x, int y, double &)
+                                 const T (&ctr)[4][V], const PQ &, int64_t off, int x, int y, double &,
+                                 uint64_t pol)
     {
         T o[8][V];
 #pragma unroll
@@ -34,9 +35,9 @@ struct ForwardA {
             o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c]);
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol);
 #pragma unroll
-        for (int c = 4; c < 8; ++c) stv<T, V>(a.out[c] + off, o[c]);
+        for (int c = 4; c < 8; ++c) st_out<T, V, HINT>(a.out[c] + off, o[c], pol);
     }
 };
 
@@ -44,9 +45,10 @@ struct ForwardA {
 struct ForwardB {
     static constexpr int kPointwise = 4;
     static constexpr bool kLambdaGrad = false;
-    template <typename T, int V, typename PQ>
+    template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &)
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &,
+                                 uint64_t pol)
     {
         T o[4][V];
 #pragma unroll
@@ -60,7 +62,7 @@ struct ForwardB {
             o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[3][v]));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c]);
+        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol);
     }
 };
 

@@ -111,17 +111,27 @@ template <typename T, int V, int TX, int TY> struct SweepShape {
     static_assert(BX <= 256 && BY <= 256, "TMA box extent limit");
 };
 
+// One output vector: a plain store, or (HINT) one with an L2 policy.
+template <typename T, int V, bool HINT>
+__device__ __forceinline__ void st_out(T *p, const T *v, uint64_t pol)
+{
+    if constexpr (HINT)
+        stv_hint<T, V>(p, v, pol);
+    else
+        stv<T, V>(p, v);
+}
+
 // Store V sites and, for sites next to the domain edge, their periodic copies
 // in the x/y padding (4 columns, 2 rows).
-template <typename T, int V>
+template <typename T, int V, bool HINT = false>
 __device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
-                                                  const T *v)
+                                                  const T *v, uint64_t pol = 0)
 {
-    stv<T, V>(base + off, v);
-    if (x < 4) stv<T, V>(base + off + nx, v);
-    if (x >= nx - 4) stv<T, V>(base + off - nx, v);
-    if (y < 2) stv<T, V>(base + off + (int64_t)ny * js, v);
-    if (y >= ny - 2) stv<T, V>(base + off - (int64_t)ny * js, v);
+    st_out<T, V, HINT>(base + off, v, pol);
+    if (x < 4) st_out<T, V, HINT>(base + off + nx, v, pol);
+    if (x >= nx - 4) st_out<T, V, HINT>(base + off - nx, v, pol);
+    if (y < 2) st_out<T, V, HINT>(base + off + (int64_t)ny * js, v, pol);
+    if (y >= ny - 2) st_out<T, V, HINT>(base + off - (int64_t)ny * js, v, pol);
 }
 
 // F(u) = lap + (kappa - lambda/2 (|u|^2 - R^2)) u, one component pair.
@@ -145,7 +155,7 @@ __device__ __forceinline__ void rhs_adjoint_pair(const StageCoef<T> &c, T u1, T 
     o2 = fma(k, a2, la2) - ua * u2;
 }
 
-template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel>
+template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel, bool HINT = false>
 __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     stencil_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
 {
@@ -160,6 +170,9 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     const int tid = threadIdx.x;
     const int tx = tid % S::NTX, ty = tid / S::NTX;
     double lam_acc = 0.0;
+    // HINT: stencil planes (re-read by neighbouring tiles) evict-last in L2,
+    // pointwise inputs and all outputs (touched once) evict-first
+    const uint64_t pol_first = HINT ? l2_policy_evict_first() : 0, pol_last = HINT ? l2_policy_evict_last() : 0;
 
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
@@ -193,7 +206,10 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
         const int slot = (int)(q_issued % NS);
         mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
         // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned)
-        tma_load_4d(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y, zp, 0, &full[slot]);
+        if constexpr (HINT)
+            tma_load_4d_hint(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y, zp, 0, &full[slot], pol_last);
+        else
+            tma_load_4d(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y, zp, 0, &full[slot]);
         ++q_issued;
         if (++p_k == p_len + 4) {
             p_k = 0;
@@ -226,7 +242,12 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
             if (active) {
                 const int64_t off0 = b.base + (int64_t)(x + a.ox) + (int64_t)(y + 2) * b.js + (int64_t)za * b.ks;
 #pragma unroll
-                for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off0, pn[c]);
+                for (int c = 0; c < NPT; ++c) {
+                    if constexpr (HINT)
+                        ldv_nc_hint<T, V>(a.pt[c] + off0, pn[c], pol_first);
+                    else
+                        ldv_nc<T, V>(a.pt[c] + off0, pn[c]);
+                }
             }
         }
         for (int m = 0; m < len; ++m) {
@@ -241,7 +262,12 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                     for (int v = 0; v < V; ++v) pq[c][v] = pn[c][v];
                 if (active && m + 1 < len) {
 #pragma unroll
-                    for (int c = 0; c < NPT; ++c) ldv_nc<T, V>(a.pt[c] + off + b.ks, pn[c]);
+                    for (int c = 0; c < NPT; ++c) {
+                        if constexpr (HINT)
+                            ldv_nc_hint<T, V>(a.pt[c] + off + b.ks, pn[c], pol_first);
+                        else
+                            ldv_nc<T, V>(a.pt[c] + off + b.ks, pn[c]);
+                    }
                 }
             }
 
@@ -297,7 +323,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                         ctr[c][v] = f0;
                     }
                 }
-                Op::template apply<T, V>(a, b, lap, ctr, pq, off, x, y, lam_acc);
+                Op::template apply<T, V, HINT>(a, b, lap, ctr, pq, off, x, y, lam_acc, pol_first);
             }
 
             __syncthreads();  // everyone is done with the oldest plane of this window
@@ -359,7 +385,8 @@ inline void plan_chunks(int ntiles, int nz, int grid_cap, int &zchunk, int64_t &
 }
 
 // One tiling of one sweep operation: occupancy, chunk plan and launch.
-template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel> struct SweepLauncher {
+template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel, bool HINT = false>
+struct SweepLauncher {
     using S = SweepShape<T, V, TX, TY>;
     static size_t smem() { return (size_t)NS * S::SLOT_BYTES; }
 
@@ -367,7 +394,7 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class S
     {
         static int cached = -1;
         if (cached < 0) {
-            auto kern = stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op, Src>;
+            auto kern = stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op, Src, HINT>;
             AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem()));
             int b = 0;
             AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, S::NT, smem()));
@@ -396,7 +423,7 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class S
 
     static int launch(const CUtensorMap &map, const SweepArgs<T> &a, int grid, cudaStream_t st)
     {
-        stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op, Src><<<grid, S::NT, smem(), st>>>(map, a);
+        stencil_sweep_kernel<T, V, TX, TY, NS, MINB, Op, Src, HINT><<<grid, S::NT, smem(), st>>>(map, a);
         return launch_status("stencil sweep");
     }
 

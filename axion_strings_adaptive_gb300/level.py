@@ -255,6 +255,30 @@ class PeriodicLevel:
     def device_status(self, stream=None) -> None:
         L.call("axs_level_device_status", C.byref(self.c), _stream_ptr(stream))
 
+    def tag_cells(self, gradient_threshold: float = 1.7976931348623157e308,
+                  radial_gradient_threshold: float = 1.7976931348623157e308, n_error_buf: int = 0,
+                  block: int = 0, stream=None):
+        """AxionStringsLevel::tag_cells' criterion (StringTagger) plus the
+        n_error_buf cube buffer. Returns (tags (nz, ny, nx) uint8 CUDA tensor,
+        n_tagged, block flags (nbz, nby, nbx) or None)."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        dev = self.state.device
+        if getattr(self, "_tag_scratch", None) is None:
+            b = C.c_int64()
+            L.call("axs_tag_scratch_bytes", nx, ny, nz, C.byref(b))
+            self._tag_scratch = torch.zeros(b.value, dtype=torch.uint8, device=dev)
+            self._n_tagged = torch.zeros(1, dtype=torch.int64, device=dev)
+        tags = torch.empty((nz, ny, nx), dtype=torch.uint8, device=dev)
+        flags = None
+        if block > 0:
+            flags = torch.empty((-(-nz // block), -(-ny // block), -(-nx // block)), dtype=torch.uint8, device=dev)
+        p = L.TagParams(self.dx, float(gradient_threshold), float(radial_gradient_threshold), int(n_error_buf),
+                        int(block))
+        L.call("axs_level_tag_cells", C.byref(self.c), C.byref(p), tags.data_ptr(),
+               flags.data_ptr() if flags is not None else None, self._n_tagged.data_ptr(),
+               self._tag_scratch.data_ptr(), self._tag_scratch.numel(), _stream_ptr(stream))
+        return tags, int(self._n_tagged.item()), flags
+
     def diagnostics_raw(self, params: L.DiagParams, mask: torch.Tensor | None = None, want_list: bool = True,
                         stream=None) -> L.DiagResult:
         mptr = None

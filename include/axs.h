@@ -310,6 +310,30 @@ int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *
 int axs_plaquette_winding_batch(const double *theta_dev, int64_t n, int32_t *w_dev, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Refinement tagging: StringTagger::operator() (StringTagger.hpp:117-151,
+ * called from AxionStringsLevel::tag_cells) on a periodic level, plus the
+ * buffer AMReX's TagBoxArray::buffer adds before clustering (amr.n_error_buf,
+ * StringTagger.hpp:60-66) and per-block flags for fixed-size patches.
+ * ------------------------------------------------------------------------- */
+typedef struct axs_tag_params {
+    double dx;
+    double gradient_threshold;        /* dx^2 |lap psi_i| > t tags (StringTaggerParams); >= DBL_MAX: off */
+    double radial_gradient_threshold; /* dx |grad |psi|| > t tags; >= DBL_MAX: off */
+    int32_t n_error_buf;              /* tag every cell within this many cells (a cube, periodic) of a tag */
+    int32_t block;                    /* > 0: flag each block^3 cell block that holds a tag */
+} axs_tag_params;
+
+int axs_tag_scratch_bytes(int32_t nx, int32_t ny, int32_t nz, int64_t *bytes);
+
+/* tags_dev: nx*ny*nz bytes (cell = i + nx*(j + ny*k)), 1 = tagged.
+ * block_flags_dev: ceil(nx/b)*ceil(ny/b)*ceil(nz/b) bytes when block = b > 0.
+ * n_tagged_dev (nullable): number of tagged cells after buffering.
+ * A cell is tagged when a plaquette at its low corner is pierced (the string
+ * finder's own winding test, bit-exact), or by the two optional criteria. */
+int axs_level_tag_cells(const axs_level *lv, const axs_tag_params *p, uint8_t *tags_dev, uint8_t *block_flags_dev,
+                        int64_t *n_tagged_dev, void *scratch, int64_t scratch_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Ensembles: many independent periodic boxes of uneven sizes advanced together
  * (no counterpart in the reference, which runs one box layout per process;
  * each box evolves exactly as an axs_level of its size would, bit for bit).

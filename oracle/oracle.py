@@ -92,6 +92,7 @@ def lib():
             f.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, C.POINTER(OrcBackground), _dbl, _dbl, _dbl, C.c_int]
             f.restype = C.c_int
             getattr(L, f"oracle_count_plaquettes_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr, C.POINTER(_i64), C.POINTER(_i64), _ptr]
+            getattr(L, f"oracle_tag_cells_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, C.c_int, _ptr]
             getattr(L, f"oracle_energy_sums_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl, C.c_int, _dbl, _ptr, _ptr]
             getattr(L, f"oracle_velocity_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _ptr, C.POINTER(_dbl), C.POINTER(_i64)]
         L.oracle_plaquette_winding.argtypes = [_dbl] * 4
@@ -140,6 +141,7 @@ def ref(prec: str = "f64"):
     L.ref_real_size.restype = C.c_int
     L.ref_rhs.argtypes = [_ptr, _ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl]
     L.ref_windings.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr]
+    L.ref_tag_cells.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _ptr]
     L.ref_count_plaquettes.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     L.ref_energy_sums.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl, C.c_int, _dbl, _ptr, _ptr]
     L.ref_total_energy.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl, C.c_int, _dbl, _ptr]
@@ -244,6 +246,17 @@ def count_plaquettes(state_fab: np.ndarray, ng: int, mask: np.ndarray | None = N
         _p(state_fab), nx, ny, nz, ng, None if m is None else _p(m), C.byref(plain),
         C.byref(weighted), None if w is None else _p(w))
     return (plain.value, weighted.value, w) if want_windings else (plain.value, weighted.value)
+
+
+def tag_cells(state_fab: np.ndarray, ng: int, dx: float, gradient_threshold: float = np.finfo(np.float64).max,
+              radial_gradient_threshold: float = np.finfo(np.float64).max, n_error_buf: int = 0) -> np.ndarray:
+    """StringTagger over the valid cells plus the periodic n_error_buf cube buffer:
+    (nz, ny, nx) uint8 tags (oracle_fields.h: oracle_tag_cells)."""
+    nx, ny, nz = _dims(state_fab, ng)
+    tags = np.zeros((nz, ny, nx), dtype=np.uint8)
+    getattr(lib(), f"oracle_tag_cells_{_sfx(state_fab)}")(
+        _p(state_fab), nx, ny, nz, ng, dx, gradient_threshold, radial_gradient_threshold, n_error_buf, _p(tags))
+    return tags
 
 
 def energy_sums(state_fab: np.ndarray, ng: int, dx: float, R: float, lam: float, RpR: float,

@@ -229,6 +229,82 @@ void FN(oracle_count_plaquettes)(const REAL *state, int nx, int ny, int nz, int 
     *n_weighted = weighted;
 }
 
+/* StringTagger::operator() (StringTagger.hpp:117-151): a cell is tagged when
+ * a plaquette at its low corner is pierced (plaquette_windings_at, the string
+ * finder's own test), or when dx^2 |lap psi_i| > gradient_threshold
+ * (scalar_laplacian, :159-177: sum over d of diff2 as amrex::Real, summed in
+ * double), or when dx |grad r| > radial_gradient_threshold (radial_gradient_sq,
+ * :187-217). Then the n_error_buf buffer AMReX's TagBoxArray::buffer applies
+ * before clustering: every cell within nbuf cells (a cube) of a tag is tagged,
+ * wrapping periodically on this one-box periodic domain. tags[cell] = 1/0,
+ * cell = i + nx*(j + ny*k). `state` needs >= 2 filled ghost layers. */
+void FN(oracle_tag_cells)(const REAL *state, int nx, int ny, int nz, int ng, double dx_d, double grad_thr,
+                          double rad_thr, int nbuf, uint8_t *tags)
+{
+    const FN(orc_box) b = FN(orc_make_box)(nx, ny, nz, ng);
+    const int64_t n = (int64_t)nx * ny * nz;
+    int8_t *w = (int8_t *)malloc((size_t)(3 * n));
+    int64_t np, nw;
+    FN(oracle_count_plaquettes)(state, nx, ny, nz, ng, NULL, &np, &nw, w);
+    const REAL dx = (REAL)dx_d;
+    const double dx2 = (double)(dx * dx);
+    const double one_over_dx2 = 1.0 / (dx_d * dx_d), one_over_dx = 1.0 / dx_d;
+    const int64_t strides[3] = {1, b.js, b.ks};
+    uint8_t *t0 = (uint8_t *)malloc((size_t)n);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int64_t cell = i + (int64_t)nx * (j + (int64_t)ny * k);
+                const int64_t o = FN(orc_idx)(&b, i, j, k);
+                uint8_t tag = (w[3 * cell] | w[3 * cell + 1] | w[3 * cell + 2]) != 0;
+                if (!tag) {
+                    double lap1 = 0.0, lap2 = 0.0;
+                    for (int d = 0; d < 3; ++d) {
+                        lap1 += (double)FN(orc_diff2)(state + o, strides[d], one_over_dx2);
+                        lap2 += (double)FN(orc_diff2)(state + b.cs + o, strides[d], one_over_dx2);
+                    }
+                    tag = dx2 * fabs(lap1) > grad_thr || dx2 * fabs(lap2) > grad_thr;
+                }
+                if (!tag) {
+                    const double psi1 = state[o], psi2 = state[b.cs + o];
+                    const double psi_sq = psi1 * psi1 + psi2 * psi2;
+                    double g1 = 0.0, g2 = 0.0, gt = 0.0;
+                    for (int d = 0; d < 3; ++d) {
+                        const double d1 = (double)FN(orc_diff1)(state + o, strides[d], one_over_dx);
+                        const double d2 = (double)FN(orc_diff1)(state + b.cs + o, strides[d], one_over_dx);
+                        g1 += d1 * d1;
+                        g2 += d2 * d2;
+                        const double dth = psi_sq > 0.0 ? (psi1 * d2 - psi2 * d1) / psi_sq : 0.0;
+                        gt += dth * dth;
+                    }
+                    tag = (double)dx * sqrt(g1 + g2 - psi_sq * gt) > rad_thr;
+                }
+                t0[cell] = tag;
+            }
+    free(w);
+    if (nbuf <= 0) {
+        memcpy(tags, t0, (size_t)n);
+        free(t0);
+        return;
+    }
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                uint8_t any = 0;
+                for (int dk = -nbuf; dk <= nbuf && !any; ++dk)
+                    for (int dj = -nbuf; dj <= nbuf && !any; ++dj)
+                        for (int di = -nbuf; di <= nbuf && !any; ++di) {
+                            const int ii = FN(orc_wrap)(i + di, nx), jj = FN(orc_wrap)(j + dj, ny),
+                                      kk = FN(orc_wrap)(k + dk, nz);
+                            any = t0[ii + (int64_t)nx * (jj + (int64_t)ny * kk)];
+                        }
+                tags[i + (int64_t)nx * (j + (int64_t)ny * k)] = any;
+            }
+    free(t0);
+}
+
 /* EnergyKernel.hpp:106-233 (compute_total_energy_sums): the 14 per-cell
  * sums {rho, rho w, a_kin, a_kin w, a_grad, a_grad w, r_kin, r_kin w,
  * r_grad, r_grad w, r_mass, r_mass w, w, 1} in that order, 4th-order diff1

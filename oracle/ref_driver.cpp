@@ -16,11 +16,13 @@
 #include "PlaquetteWinding.hpp"
 #include "PreEvolutionBackground.hpp"
 #include "StringFinder.hpp"
+#include "StringTagger.hpp"
 #include "Velocity.hpp"
 #include "VelocityKernel.hpp"
 #include "XiFormula.hpp"
 
 #include <cstdint>
+#include <vector>
 
 using amrex::Real;
 
@@ -57,6 +59,25 @@ void ref_rhs(const Real *soln, Real *rhs, int nx, int ny, int nz, int ng, double
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) op(i, j, k, ra, sa);
+}
+
+// StringTagger::operator() (StringTagger.hpp:117-151) over the valid cells,
+// as AxionStringsLevel::tag_cells launches it; tags[cell] = 1 where SET.
+void ref_tag_cells(const Real *state, int nx, int ny, int nz, int ng, double dx, double gradient_threshold,
+                   double radial_gradient_threshold, int8_t *tags)
+{
+    auto s = wrap_state(state, nx, ny, nz, ng);
+    const auto a = s.const_arrays()[0];
+    StringTaggerParams prm{};
+    prm.gradient_threshold = gradient_threshold;
+    prm.radial_gradient_threshold = radial_gradient_threshold;
+    const StringTagger tagger(static_cast<Real>(dx), prm);
+    std::vector<amrex::TagBox::TagType> t(size_t(nx) * ny * nz, amrex::TagBox::CLEAR);
+    const amrex::Array4<amrex::TagBox::TagType> ta(t.data(), amrex::Dim3{0, 0, 0}, amrex::Dim3{nx, ny, nz}, 1);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) tagger(i, j, k, a, ta);
+    for (size_t c = 0; c < t.size(); ++c) tags[c] = t[c] == amrex::TagBox::SET ? 1 : 0;
 }
 
 void ref_windings(const Real *state, int nx, int ny, int nz, int ng, int8_t *w)

@@ -95,6 +95,13 @@ template <class T> struct Array4
     CellData<T> cellData(int i, int j, int k) const { return CellData<T>{ptr(i, j, k), stride.a[2]}; }
 };
 
+// TagBox: only the tag type and values a tagging functor writes.
+struct TagBox
+{
+    using TagType = char;
+    static constexpr TagType CLEAR = 0, BUF = 1, SET = 2;
+};
+
 template <class T> struct MultiArray4
 {
     Array4<T> a;

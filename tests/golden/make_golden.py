@@ -18,6 +18,10 @@ Fixtures:
                   velocity sum/count -- on a seeded random box and a seeded
                   Fourier-IC box, in the PRECISION=DOUBLE and =FLOAT builds
   fourier_ic.npz  FourierIC::generate outputs for two boxes / seeds
+  tagging.npz     StringTagger::operator() tags (plaquette, Laplacian and radial-
+                  gradient criteria) on seeded boxes, both precision builds
+
+    python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
 from __future__ import annotations
 
@@ -196,17 +200,58 @@ def fourier() -> dict:
     return out
 
 
-def main() -> None:
+TAG_THRESHOLDS = [  # (gradient_threshold, radial_gradient_threshold); max = criterion off
+    (np.finfo(np.float64).max, np.finfo(np.float64).max),
+    (2.0, np.finfo(np.float64).max),
+    (np.finfo(np.float64).max, 1.0),
+    (4.0, 1.5),
+]
+
+
+def tagging() -> dict:
+    """StringTagger::operator() (StringTagger.hpp:117-151) on the fields boxes
+    of both precision builds, for the default (plaquette-only) criterion and
+    with the Laplacian / radial-gradient criteria switched on."""
+    out = {"thresholds": np.array(TAG_THRESHOLDS)}
+    for prec in ("f64", "f32"):
+        R = O.ref(prec)
+        dt = np.float64 if prec == "f64" else np.float32
+        rng = np.random.default_rng(91 if prec == "f64" else 92)
+        boxes = {
+            "rand": (rng.standard_normal((4, 10, 11, 12)) * np.array([1, 1, 0.3, 0.3])[:, None, None, None]).astype(dt),
+            "ic": np.concatenate([O.fourier_ic_state(16, 4.0, 515)[:2],
+                                  0.2 * rng.standard_normal((2, 16, 16, 16))]).astype(dt),
+        }
+        for name, valid in boxes.items():
+            _, nz, ny, nx = valid.shape
+            fab = O.to_fab(np.ascontiguousarray(valid), 2)
+            out[f"{prec}_{name}_state"] = valid
+            tags = np.zeros((len(TAG_THRESHOLDS), nz, ny, nx), dtype=np.int8)
+            for t, (g, r) in enumerate(TAG_THRESHOLDS):
+                R.ref_tag_cells(_p(fab), nx, ny, nz, 2, 0.5, g, r, _p(tags[t]))
+            out[f"{prec}_{name}_tags"] = tags
+    return out
+
+
+FIXTURES = {
+    "kats": lambda: kats(O.ref("f64")),
+    "fields_f64": lambda: fields("f64"),
+    "fields_f32": lambda: fields("f32"),
+    "fourier_ic": fourier,
+    "tagging": tagging,
+}
+
+
+def main(names=None) -> None:
+    """Write the named fixtures (all by default)."""
     if not (O.ref_available("f64") and O.ref_available("f32")):
         O.build()
     if not (O.ref_available("f64") and O.ref_available("f32")):
         raise SystemExit("reference-built checker unavailable (needs the reference tree)")
-    np.savez_compressed(os.path.join(HERE, "kats.npz"), **kats(O.ref("f64")))
-    np.savez_compressed(os.path.join(HERE, "fields_f64.npz"), **fields("f64"))
-    np.savez_compressed(os.path.join(HERE, "fields_f32.npz"), **fields("f32"))
-    np.savez_compressed(os.path.join(HERE, "fourier_ic.npz"), **fourier())
+    for name in names or FIXTURES:
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **FIXTURES[name]())
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -139,3 +139,32 @@ def test_fourier_ic(orc, golden):
     L = orc.lib()
     for x, h in zip(g["hash_in"], g["hash_out"]):
         assert L.oracle_hash_u64(int(x)) == int(h)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("box", ["rand", "ic"])
+def test_tagger_matches_reference(orc, golden, prec, box):
+    """StringTagger::operator() (StringTagger.hpp:117-151): plaquette, Laplacian and
+    radial-gradient criteria, restated in the oracle, against the reference's own
+    tagger on the same boxes."""
+    g = golden("tagging.npz")
+    fab = orc.to_fab(np.ascontiguousarray(g[f"{prec}_{box}_state"]), 2)
+    for t, (gt, rt) in enumerate(g["thresholds"]):
+        tags = orc.tag_cells(fab, 2, 0.5, gt, rt, 0)
+        np.testing.assert_array_equal(tags, g[f"{prec}_{box}_tags"][t].astype(np.uint8))
+
+
+def test_tag_buffer_is_a_periodic_cube(orc):
+    """n_error_buf: every cell within nbuf cells (a cube, periodic wrap) of a tag."""
+    rng = np.random.default_rng(4)
+    v = rng.standard_normal((4, 9, 10, 12))
+    fab = orc.to_fab(v, 2)
+    base = orc.tag_cells(fab, 2, 0.5, 1e300, 1e300, 0)
+    for nb in (1, 2):
+        got = orc.tag_cells(fab, 2, 0.5, 1e300, 1e300, nb)
+        ref = np.zeros_like(base)
+        for dz in range(-nb, nb + 1):
+            for dy in range(-nb, nb + 1):
+                for dx in range(-nb, nb + 1):
+                    ref |= np.roll(base, (dz, dy, dx), axis=(0, 1, 2))
+        np.testing.assert_array_equal(got, ref)
