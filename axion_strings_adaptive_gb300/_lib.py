@@ -124,6 +124,9 @@ SIGNATURES = {
     "axs_level_diagnostics": (_i32, [C.POINTER(LevelC), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr, _i64,
                                      _ptr]),
     "axs_diagnostics_static_scratch": (_i32, [C.POINTER(Fab), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr]),
+    "axs_level_masked_a_dot": (_i32, [C.POINTER(LevelC), _i32, _dbl, _dbl, _ptr, _ptr, _ptr, _i64, _ptr]),
+    "axs_spectrum_scratch_bytes": (_i32, [_i32, _i32, _i32, C.POINTER(_i64)]),
+    "axs_spectrum_bin": (_i32, [_ptr, _i32, _i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _i64, _ptr]),
     "axs_tag_scratch_bytes": (_i32, [_i32, _i32, _i32, C.POINTER(_i64)]),
     "axs_level_tag_cells": (_i32, [C.POINTER(LevelC), C.POINTER(TagParams), _ptr, _ptr, _ptr, _ptr, _i64, _ptr]),
     "axs_ensemble_sizes": (_i32, [_i32, _i32, C.POINTER(_i32), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),

@@ -310,6 +310,30 @@ int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *
 int axs_plaquette_winding_batch(const double *theta_dev, int64_t n, int32_t *w_dev, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Axion power spectrum (AxionStringsLevel.cpp:1583-1640): the masked a_dot
+ * buffer, a caller-run unnormalised forward R2C (cuFFT), then shell binning.
+ * ------------------------------------------------------------------------- */
+
+/* fill_masked_a_dot_buffer (MaskedFieldBuffer.hpp:15-35): buf_dev[cell] =
+ * masked_a_dot(psi, Pi, R) (Masking.hpp:96-118) in the level's precision,
+ * dense (nz, ny, nx), x fastest; *sum_sq_dev = sum of buf^2 (MultiFab::Dot).
+ * scratch: 8 bytes per block of the pass (axs_spectrum_scratch_bytes is enough). */
+int axs_level_masked_a_dot(const axs_level *lv, int32_t masking_scheme, double masking_threshold, double R,
+                           void *buf_dev, double *sum_sq_dev, void *scratch, int64_t scratch_bytes, void *stream);
+
+int axs_spectrum_scratch_bytes(int32_t nx, int32_t ny, int32_t nz, int64_t *bytes);
+
+/* compute_spectrum's binning (SpectrumKernel.hpp:77-153) of an R2C spectrum
+ * spec_dev (nz, ny, nx/2+1) of interleaved complex values of `dtype`:
+ * n_shells = max(nx, ny, nz)/2 + 1; shell_sum_dev[s] = sum of w 4 pi |p|^2 |X|^2
+ * and shell_count_dev[s] = sum of w over modes with floor(|p| + 1/2) = s and
+ * |p| < n_max/2 (w = 1 on the kx = 0 and kx = nx/2 planes, 2 elsewhere);
+ * totals_dev = {full-cube energy, inscribed-sphere energy}. Deterministic. */
+int axs_spectrum_bin(const void *spec_dev, int32_t dtype, int32_t nx, int32_t ny, int32_t nz, double *shell_sum_dev,
+                     int64_t *shell_count_dev, double *totals_dev, void *scratch, int64_t scratch_bytes,
+                     void *stream);
+
+/* ---------------------------------------------------------------------------
  * Refinement tagging: StringTagger::operator() (StringTagger.hpp:117-151,
  * called from AxionStringsLevel::tag_cells) on a periodic level, plus the
  * buffer AMReX's TagBoxArray::buffer adds before clustering (amr.n_error_buf,

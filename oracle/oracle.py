@@ -92,6 +92,7 @@ def lib():
             f.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, C.POINTER(OrcBackground), _dbl, _dbl, _dbl, C.c_int]
             f.restype = C.c_int
             getattr(L, f"oracle_count_plaquettes_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr, C.POINTER(_i64), C.POINTER(_i64), _ptr]
+            getattr(L, f"oracle_masked_a_dot_buffer_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _ptr]
             getattr(L, f"oracle_tag_cells_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, C.c_int, _ptr]
             getattr(L, f"oracle_energy_sums_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl, C.c_int, _dbl, _ptr, _ptr]
             getattr(L, f"oracle_velocity_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _ptr, C.POINTER(_dbl), C.POINTER(_i64)]
@@ -141,6 +142,7 @@ def ref(prec: str = "f64"):
     L.ref_real_size.restype = C.c_int
     L.ref_rhs.argtypes = [_ptr, _ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl]
     L.ref_windings.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr]
+    L.ref_spectrum.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _ptr, _ptr, _ptr, _ptr]
     L.ref_tag_cells.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _ptr]
     L.ref_count_plaquettes.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     L.ref_energy_sums.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl, C.c_int, _dbl, _ptr, _ptr]
@@ -246,6 +248,47 @@ def count_plaquettes(state_fab: np.ndarray, ng: int, mask: np.ndarray | None = N
         _p(state_fab), nx, ny, nz, ng, None if m is None else _p(m), C.byref(plain),
         C.byref(weighted), None if w is None else _p(w))
     return (plain.value, weighted.value, w) if want_windings else (plain.value, weighted.value)
+
+
+def masked_a_dot_buffer(state_fab: np.ndarray, ng: int, scheme: int, threshold: float, R: float) -> np.ndarray:
+    """fill_masked_a_dot_buffer (MaskedFieldBuffer.hpp:15-35): (nz, ny, nx) of the field precision."""
+    nx, ny, nz = _dims(state_fab, ng)
+    buf = np.zeros((nz, ny, nx), dtype=state_fab.dtype)
+    getattr(lib(), f"oracle_masked_a_dot_buffer_{_sfx(state_fab)}")(
+        _p(state_fab), nx, ny, nz, ng, scheme, threshold, R, _p(buf))
+    return buf
+
+
+def spectrum(buf: np.ndarray) -> dict:
+    """compute_spectrum (SpectrumKernel.hpp:53-153) of a real (nz, ny, nx) field:
+    unnormalised forward R2C (numpy's FFT in double; the reference's FFT runs in
+    the field precision), then the reference's binning -- kx = 0 and kx = nx/2
+    planes weight 1, others 2; shell = floor(|p| + 1/2) for |p| < n_max/2;
+    shells accumulate w 4 pi |p|^2 |X|^2 and w. Returns per-shell sums
+    (`shell_sum`, `shell_count`, index = shell) and the two totals."""
+    nz, ny, nx = buf.shape
+    X = np.fft.rfftn(buf.astype(np.float64), axes=(0, 1, 2))
+    if buf.dtype == np.float32:
+        X = X.astype(np.complex64).astype(np.complex128)
+    n_max = max(nx, ny, nz)
+    n_shells = n_max // 2 + 1
+    kx = np.arange(nx // 2 + 1)
+    ky = np.where(np.arange(ny) <= ny // 2, np.arange(ny), np.arange(ny) - ny)
+    kz = np.where(np.arange(nz) <= nz // 2, np.arange(nz), np.arange(nz) - nz)
+    KZ, KY, KX = np.meshgrid(kz, ky, kx, indexing="ij")
+    p_sq = (KX * KX + KY * KY + KZ * KZ).astype(np.float64)
+    p = np.sqrt(p_sq)
+    mag = X.real ** 2 + X.imag ** 2
+    w = np.where((KX == 0) | (KX == nx // 2), 1.0, 2.0)
+    full = float((w * mag).sum())
+    ins = p < n_max / 2.0
+    inscribed = float((w * mag)[ins].sum())
+    shell = np.floor(p + 0.5).astype(np.int64)
+    sel = ins & (shell < n_shells)
+    shell_sum = np.bincount(shell[sel], weights=(w * 4.0 * np.pi * p_sq * mag)[sel], minlength=n_shells)
+    shell_count = np.bincount(shell[sel], weights=w[sel], minlength=n_shells).astype(np.int64)
+    return {"shell_sum": shell_sum, "shell_count": shell_count, "full_cube_energy": full,
+            "inscribed_sphere_energy": inscribed}
 
 
 def tag_cells(state_fab: np.ndarray, ng: int, dx: float, gradient_threshold: float = np.finfo(np.float64).max,

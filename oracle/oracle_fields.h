@@ -229,6 +229,23 @@ void FN(oracle_count_plaquettes)(const REAL *state, int nx, int ny, int nz, int 
     *n_weighted = weighted;
 }
 
+/* fill_masked_a_dot_buffer (MaskedFieldBuffer.hpp:15-35): buf[cell] =
+ * (REAL) masked_a_dot(psi1, psi2, Pi1, Pi2, R), R passed as amrex::Real. */
+void FN(oracle_masked_a_dot_buffer)(const REAL *state, int nx, int ny, int nz, int ng, int scheme,
+                                    double threshold, double R_d, REAL *buf)
+{
+    const FN(orc_box) b = FN(orc_make_box)(nx, ny, nz, ng);
+    const double R = (double)(REAL)R_d;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int64_t o = FN(orc_idx)(&b, i, j, k);
+                buf[i + (int64_t)nx * (j + (int64_t)ny * k)] = (REAL)orc_masked_a_dot(
+                    scheme, threshold, state[o], state[b.cs + o], state[2 * b.cs + o], state[3 * b.cs + o], R);
+            }
+}
+
 /* StringTagger::operator() (StringTagger.hpp:117-151): a cell is tagged when
  * a plaquette at its low corner is pierced (plaquette_windings_at, the string
  * finder's own test), or when dx^2 |lap psi_i| > gradient_threshold

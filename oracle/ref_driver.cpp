@@ -17,6 +17,8 @@
 #include "PreEvolutionBackground.hpp"
 #include "StringFinder.hpp"
 #include "StringTagger.hpp"
+#include "MaskedFieldBuffer.hpp"
+#include "SpectrumKernel.hpp"
 #include "Velocity.hpp"
 #include "VelocityKernel.hpp"
 #include "XiFormula.hpp"
@@ -78,6 +80,33 @@ void ref_tag_cells(const Real *state, int nx, int ny, int nz, int ng, double dx,
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) tagger(i, j, k, a, ta);
     for (size_t c = 0; c < t.size(); ++c) tags[c] = t[c] == amrex::TagBox::SET ? 1 : 0;
+}
+
+// fill_masked_a_dot_buffer (MaskedFieldBuffer.hpp) then compute_spectrum
+// (SpectrumKernel.hpp:53-153) of the buffer, as specific_post_timestep
+// does (AxionStringsLevel.cpp:1583-1640). shell_average/count are indexed by
+// shell (0 where a shell is empty); out3 = {full_cube, inscribed_sphere,
+// sum of buffer^2}; the buffer is written to `buf` (nx*ny*nz).
+void ref_spectrum(const Real *state, int nx, int ny, int nz, int ng, int scheme, double threshold, double R,
+                  double *shell_average, long *shell_count, double *out3, Real *buf)
+{
+    auto s = wrap_state(state, nx, ny, nz, ng);
+    amrex::MultiFab b(amrex::BoxArray{amrex::Box{{nx, ny, nz}}}, amrex::DistributionMapping{}, 1, 0);
+    fill_masked_a_dot_buffer(b, s, masking(scheme, threshold), static_cast<Real>(R));
+    amrex::Geometry geom{amrex::Box{{nx, ny, nz}}};
+    const Spectrum sp = compute_spectrum(b, geom);
+    for (size_t q = 0; q < sp.p.size(); ++q) {
+        const int shell = int(sp.p[q]);
+        shell_average[shell] = sp.shell_average[q];
+        shell_count[shell] = sp.shell_count[q];
+    }
+    out3[0] = sp.full_cube_energy;
+    out3[1] = sp.inscribed_sphere_energy;
+    out3[2] = double(amrex::MultiFab::Dot(b, 0, b, 0, 1, 0));
+    const auto ba = b.array();
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) buf[i + size_t(nx) * (j + size_t(ny) * k)] = ba(i, j, k, 0);
 }
 
 void ref_windings(const Real *state, int nx, int ny, int nz, int ng, int8_t *w)

@@ -13,6 +13,7 @@
 // part of the kx = 0 and kx = nx/2 terms).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <complex>
@@ -112,6 +113,8 @@ struct IntVect
 {
     int v[3];
     explicit IntVect(int s = 0) : v{s, s, s} {}
+    IntVect(int a, int b, int c) : v{a, b, c} {}
+    int operator[](int d) const { return v[d]; }
 };
 
 struct Box
@@ -119,6 +122,8 @@ struct Box
     int n[3];
     int length(int d) const { return n[d]; }
     Long numPts() const { return Long(n[0]) * n[1] * n[2]; }
+    IntVect smallEnd() const { return IntVect(0); }
+    IntVect bigEnd() const { return IntVect(n[0] - 1, n[1] - 1, n[2] - 1); }
 };
 struct BoxArray
 {
@@ -151,7 +156,7 @@ template <class T> struct FabArrayShim
     FabArrayShim(const BoxArray &ba, const DistributionMapping &, int a_nc, int a_ng)
         : n{ba.box.n[0], ba.box.n[1], ba.box.n[2]}, ng(a_ng), nc(a_nc)
     {
-        owned.assign(size_t(n[0] + 2 * ng) * (n[1] + 2 * ng) * (n[2] + 2 * ng) * nc, T(0));
+        owned.assign(size_t(n[0] + 2 * ng) * (n[1] + 2 * ng) * (n[2] + 2 * ng) * nc, T{});
         data = owned.data();
     }
     Array4<T> array() const
@@ -160,6 +165,7 @@ template <class T> struct FabArrayShim
     }
     MultiArray4<T const> const_arrays() const { return MultiArray4<T const>{Array4<T const>(array())}; }
     MultiArray4<T> arrays() const { return MultiArray4<T>{array()}; }
+    template <class I> Array4<T const> const_array(const I &) const { return Array4<T const>(array()); }
     BoxArray boxArray() const { return BoxArray{Box{{n[0], n[1], n[2]}}}; }
     DistributionMapping DistributionMap() const { return {}; }
     void setVal(T v)
@@ -192,6 +198,34 @@ template <class T> struct FabArrayShim
 };
 using MultiFab = FabArrayShim<Real>;
 using iMultiFab = FabArrayShim<int>;
+
+// ParallelFor over the valid cells of a one-box FabArray (box number 0), in (k, j, i) order.
+template <class FA, class F> void ParallelFor(const FA &fa, F &&f)
+{
+    for (int k = 0; k < fa.n[2]; ++k)
+        for (int j = 0; j < fa.n[1]; ++j)
+            for (int i = 0; i < fa.n[0]; ++i) f(0, i, j, k);
+}
+
+namespace Gpu
+{
+inline void streamSynchronize() {}
+} // namespace Gpu
+
+// The single box of a one-box FabArray.
+struct MFIter
+{
+    Box box;
+    bool valid{true};
+    template <class FA> explicit MFIter(const FA &fa) : box{{fa.n[0], fa.n[1], fa.n[2]}} {}
+    bool isValid() const { return valid; }
+    MFIter &operator++()
+    {
+        valid = false;
+        return *this;
+    }
+    const Box &validbox() const { return box; }
+};
 
 struct ReduceOpSum
 {
@@ -226,6 +260,7 @@ template <std::size_t N, class... Ts> auto get(const std::tuple<Ts...> &t) { ret
 namespace ParallelDescriptor
 {
 inline void ReduceLongSum(long &) {}
+inline void ReduceLongSum(long *, int) {}
 inline void ReduceRealSum(double &) {}
 inline void ReduceRealSum(double *, int) {}
 inline void ReduceRealSum(float &) {}
@@ -237,6 +272,8 @@ template <class T> struct GpuComplex
     T re{0}, im{0};
     GpuComplex() = default;
     GpuComplex(T r, T i) : re(r), im(i) {}
+    T real() const { return re; }
+    T imag() const { return im; }
 };
 
 namespace FFT
@@ -245,7 +282,48 @@ namespace FFT
 template <class T> struct R2C
 {
     Box dom;
+    using cMF = FabArrayShim<GpuComplex<T>>;
     explicit R2C(const Box &d) : dom(d) {}
+    std::pair<BoxArray, DistributionMapping> getSpectralDataLayout() const
+    {
+        return {BoxArray{Box{{dom.n[0] / 2 + 1, dom.n[1], dom.n[2]}}}, DistributionMapping{}};
+    }
+    // Unnormalised forward transform, X_k = sum_x f(x) exp(-2 pi i k.x/N), kx >= 0 stored.
+    void forward(const FabArrayShim<T> &in, cMF &out)
+    {
+        const int nx = dom.n[0], ny = dom.n[1], nz = dom.n[2], nxh = nx / 2 + 1;
+        const double two_pi = 2.0 * 3.14159265358979323846;
+        auto a = in.array();
+        // x transform per (y, z) row, then (y, z) per kx
+        std::vector<std::complex<double>> row(size_t(nxh) * ny * nz);
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y)
+                for (int i = 0; i < nxh; ++i)
+                {
+                    std::complex<double> s = 0.0;
+                    for (int x = 0; x < nx; ++x)
+                    {
+                        const double ph = -two_pi * double(i) * x / nx;
+                        s += double(a(x, y, z, 0)) * std::complex<double>(std::cos(ph), std::sin(ph));
+                    }
+                    row[i + size_t(nxh) * (y + size_t(ny) * z)] = s;
+                }
+        auto o = out.array();
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nxh; ++i)
+                {
+                    std::complex<double> s = 0.0;
+                    for (int z = 0; z < nz; ++z)
+                        for (int y = 0; y < ny; ++y)
+                        {
+                            const double ph = -two_pi * (double(j) * y / ny + double(k) * z / nz);
+                            s += row[i + size_t(nxh) * (y + size_t(ny) * z)] *
+                                 std::complex<double>(std::cos(ph), std::sin(ph));
+                        }
+                    o(i, j, k, 0) = GpuComplex<T>(T(s.real()), T(s.imag()));
+                }
+    }
     template <class F> void forwardThenBackward(const MultiFab &, MultiFab &out, F fill)
     {
         const int nx = dom.n[0], ny = dom.n[1], nz = dom.n[2], nxh = nx / 2 + 1;

@@ -18,6 +18,7 @@ Fixtures:
                   velocity sum/count -- on a seeded random box and a seeded
                   Fourier-IC box, in the PRECISION=DOUBLE and =FLOAT builds
   fourier_ic.npz  FourierIC::generate outputs for two boxes / seeds
+  spectrum.npz    fill_masked_a_dot_buffer + compute_spectrum shells and totals
   tagging.npz     StringTagger::operator() tags (plaquette, Laplacian and radial-
                   gradient criteria) on seeded boxes, both precision builds
 
@@ -233,12 +234,40 @@ def tagging() -> dict:
     return out
 
 
+def spectrum() -> dict:
+    """fill_masked_a_dot_buffer + compute_spectrum (MaskedFieldBuffer.hpp,
+    SpectrumKernel.hpp:53-153) on seeded boxes, schemes None and B, both
+    precision builds (the shim's FFT is a direct DFT in double)."""
+    out = {}
+    for prec in ("f64", "f32"):
+        R = O.ref(prec)
+        dt = np.float64 if prec == "f64" else np.float32
+        rng = np.random.default_rng(61 if prec == "f64" else 62)
+        boxes = {"cube": (16, 16, 16), "odd": (12, 10, 8)}
+        for name, (nx, ny, nz) in boxes.items():
+            psi = [O.fourier_ic_component(nx, ny, nz, 3.0, 0.5, 808, c) for c in (0, 1)]
+            v = np.concatenate([np.stack(psi), 0.3 * rng.standard_normal((2, nz, ny, nx))]).astype(dt)
+            fab = O.to_fab(np.ascontiguousarray(v), 2)
+            out[f"{prec}_{name}_state"] = v
+            n_sh = max(nx, ny, nz) // 2 + 1
+            for scheme in (0, 2):
+                sa, sc, o3 = np.zeros(n_sh), np.zeros(n_sh, dtype=np.int64), np.zeros(3)
+                buf = np.zeros((nz, ny, nx), dtype=dt)
+                R.ref_spectrum(_p(fab), nx, ny, nz, 2, scheme, 0.8, 1.1, _p(sa), _p(sc), _p(o3), _p(buf))
+                out[f"{prec}_{name}_s{scheme}_shell_average"] = sa
+                out[f"{prec}_{name}_s{scheme}_shell_count"] = sc
+                out[f"{prec}_{name}_s{scheme}_totals"] = o3
+                out[f"{prec}_{name}_s{scheme}_buffer"] = buf
+    return out
+
+
 FIXTURES = {
     "kats": lambda: kats(O.ref("f64")),
     "fields_f64": lambda: fields("f64"),
     "fields_f32": lambda: fields("f32"),
     "fourier_ic": fourier,
     "tagging": tagging,
+    "spectrum": spectrum,
 }
 
 

@@ -28,8 +28,8 @@ def test_tagger_matches_reference(axs, golden, prec, box):
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 def test_buffer_counts_and_blocks_match_oracle(axs, orc, dtype):
     from axion_strings_adaptive_gb300 import ic
-    n, nbuf, block = 32, 3, 8
-    s = ic.fourier_state(n, 6.0, seed=8).to(dtype)
+    n, nbuf, block = 32, 2, 8
+    s = ic.fourier_state(n, 2.0, seed=8).to(dtype)  # ~1 % pierced cells, ~30 % after the buffer
     lv = axs.PeriodicLevel(n, 0.5, dtype=dtype)
     lv.set_state(s)
     tags, count, flags = lv.tag_cells(n_error_buf=nbuf, block=block)
