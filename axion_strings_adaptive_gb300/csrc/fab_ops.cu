@@ -120,6 +120,10 @@ __device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(
 __device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
 
 template <typename T>
 __global__ void lincomb_kernel(const axs_fab d, const axs_fab x, T b, const axs_fab y, int ncomp)
@@ -194,6 +198,29 @@ __global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, LevelGeo
     }
 }
 
+// Pre-evolution -> main handoff (AxionStringsLevel.cpp:2027-2132) on the valid
+// cells of a level, in the field precision with the reference's operation
+// order: kappa = R_main/R_pre, common = R_main' - kappa^2 R_pre',
+// psi <- kappa psi, Pi <- kappa^2 Pi + (psi/R_pre) common.
+template <typename T>
+__global__ void level_handoff_kernel(T *lv, int nx, int ny, int nz, LevelGeom g, T R_pre, T R_pre_prime, T R_main,
+                                     T R_main_prime)
+{
+    const T kappa = rn_div(R_main, R_pre);
+    const T kk = rn_mul(kappa, kappa);
+    const T common = rn_sub(R_main_prime, rn_mul(kk, R_pre_prime));
+    const int64_t n = (int64_t)nx * ny * nz;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(q % nx), y = (int)((q / nx) % ny), z = (int)(q / ((int64_t)nx * ny));
+        const int64_t o = (x + g.ox) + (int64_t)(y + g.oy) * g.js + (int64_t)z * g.ks;
+        const T p1 = lv[o], p2 = lv[g.cs + o], q1 = lv[2 * g.cs + o], q2 = lv[3 * g.cs + o];
+        lv[o] = rn_mul(kappa, p1);
+        lv[g.cs + o] = rn_mul(kappa, p2);
+        lv[2 * g.cs + o] = rn_add(rn_mul(kk, q1), rn_mul(rn_div(p1, R_pre), common));
+        lv[3 * g.cs + o] = rn_add(rn_mul(kk, q2), rn_mul(rn_div(p2, R_pre), common));
+    }
+}
+
 static int grid_for(int64_t n)
 {
     const int sms = device_sm_count();
@@ -236,6 +263,28 @@ int level_copy_fab(void *lv, int32_t dtype, const LevelGeom &g, const axs_fab &f
 using namespace axs;
 
 extern "C" {
+
+int axs_level_handoff_rescale(const axs_level *lv, double R_pre, double R_pre_prime, double R_main,
+                              double R_main_prime, void *stream)
+{
+    AXS_REQUIRE(lv != nullptr && lv->state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null level");
+    AXS_REQUIRE(R_pre != 0.0, AXS_ERR_INVALID_ARGUMENT, "R_pre must be nonzero");
+    LevelGeom g;
+    int rc = level_geom(lv->dtype, lv->nx, lv->ny, lv->nz, g);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n = (int64_t)lv->nx * lv->ny * lv->nz;
+    // the reference holds R and R' as amrex::Real
+    if (lv->dtype == AXS_F64)
+        level_handoff_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(lv->state), lv->nx, lv->ny,
+                                                                  lv->nz, g, R_pre, R_pre_prime, R_main, R_main_prime);
+    else
+        level_handoff_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(lv->state), lv->nx, lv->ny,
+                                                                 lv->nz, g, (float)R_pre, (float)R_pre_prime,
+                                                                 (float)R_main, (float)R_main_prime);
+    if ((rc = launch_status("handoff rescale"))) return rc;
+    return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g, 4, st);
+}
 
 int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_rhs_coeffs *c, void *stream)
 {

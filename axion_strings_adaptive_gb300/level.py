@@ -342,6 +342,33 @@ class AxionStringsLevel:
         self.level.advance(self.bg, self.tau_i, self.time, dt, nsteps, stream)
         self.time += nsteps * dt
 
+    # AxionStringsLevel::apply_pre_evolution_to_main_rescale (AxionStringsLevel.cpp:2027-2132)
+    def apply_pre_evolution_to_main_rescale(self, main_background: Background, tau_i_main: float,
+                                            transition_n_periods: float = 0.0, stream=None) -> None:
+        """End pre-evolution: this level has run on its pre-evolution background
+        with the pre-evolution clock (tau = time, tau_i = 0). Rescale psi, Pi onto
+        the main background at tau_i_main, switch to it, and shift tau_i so that
+        tau = tau_i + time equals tau_i_main now. With transition_n_periods > 0,
+        lambda and the curvature coefficient blend from their frozen
+        pre-evolution values over that many main-schedule core periods."""
+        import dataclasses
+        import math
+        pre = self.bg
+        tau_pre_end = self.time
+        vp, vm = pre.values(tau_pre_end), main_background.values(tau_i_main)
+        L.call("axs_level_handoff_rescale", C.byref(self.level.c), vp.R, vp.R_prime, vm.R, vm.R_prime,
+               _stream_ptr(stream))
+        bg = main_background
+        if transition_n_periods > 0.0:
+            lam_start = vp.lambda_
+            lam_main = vm.lambda_
+            m_r_period = math.sqrt(lam_main) if lam_main > 0.0 else math.sqrt(lam_start)
+            bg = dataclasses.replace(main_background, blend_dtau=transition_n_periods * 2.0 * math.pi / m_r_period,
+                                     blend_tau_start=tau_i_main, blend_lambda_start=lam_start,
+                                     blend_curv_start=vp.kappa)
+        self.bg = bg
+        self.tau_i = tau_i_main - tau_pre_end
+
     # AxionStringsLevel::specific_post_timestep's diagnostics (AxionStringsLevel.cpp:1256-1434)
     def specific_post_timestep(self, mask: torch.Tensor | None = None, want_list: bool = True) -> Diagnostics:
         return self.level.diagnostics(self.bg, self.tau, self.masking_scheme, self.masking_threshold, mask,

@@ -202,6 +202,15 @@ int axs_level_rk4_sweep(const axs_level *lv, const axs_background *bg, double ta
  * word: AXS_OK or AXS_ERR_DEVICE_TIMEOUT. */
 int axs_level_device_status(const axs_level *lv, void *stream);
 
+/* AxionStringsLevel::apply_pre_evolution_to_main_rescale (AxionStringsLevel.cpp:2027-2132):
+ * in place on the level, in the field precision, kappa = R_main/R_pre,
+ * psi <- kappa psi, Pi <- kappa^2 Pi + (psi/R_pre)(R_main' - kappa^2 R_pre'),
+ * with R_pre, R_pre' at the end of pre-evolution and R_main, R_main' at tau_i.
+ * The caller then shifts tau_i by -tau_pre_end and, optionally, sets the
+ * axs_background blend fields (handoff transition). */
+int axs_level_handoff_rescale(const axs_level *lv, double R_pre, double R_pre_prime, double R_main,
+                              double R_main_prime, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Differentiation: discrete adjoint of the fused RK4 step (no counterpart in
  * the reference, which has no gradient code)

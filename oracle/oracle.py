@@ -92,6 +92,7 @@ def lib():
             f.argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, C.POINTER(OrcBackground), _dbl, _dbl, _dbl, C.c_int]
             f.restype = C.c_int
             getattr(L, f"oracle_count_plaquettes_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _ptr, C.POINTER(_i64), C.POINTER(_i64), _ptr]
+            getattr(L, f"oracle_handoff_rescale_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl]
             getattr(L, f"oracle_masked_a_dot_buffer_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _ptr]
             getattr(L, f"oracle_tag_cells_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, C.c_int, _ptr]
             getattr(L, f"oracle_energy_sums_{sfx}").argtypes = [_ptr, C.c_int, C.c_int, C.c_int, C.c_int, _dbl, _dbl, _dbl, _dbl, C.c_int, _dbl, _ptr, _ptr]
@@ -248,6 +249,14 @@ def count_plaquettes(state_fab: np.ndarray, ng: int, mask: np.ndarray | None = N
         _p(state_fab), nx, ny, nz, ng, None if m is None else _p(m), C.byref(plain),
         C.byref(weighted), None if w is None else _p(w))
     return (plain.value, weighted.value, w) if want_windings else (plain.value, weighted.value)
+
+
+def handoff_rescale(state_fab: np.ndarray, ng: int, R_pre: float, R_pre_prime: float, R_main: float,
+                    R_main_prime: float) -> None:
+    """apply_pre_evolution_to_main_rescale on a FAB, in place (oracle_fields.h)."""
+    nx, ny, nz = _dims(state_fab, ng)
+    getattr(lib(), f"oracle_handoff_rescale_{_sfx(state_fab)}")(_p(state_fab), nx, ny, nz, ng, R_pre, R_pre_prime,
+                                                                  R_main, R_main_prime)
 
 
 def masked_a_dot_buffer(state_fab: np.ndarray, ng: int, scheme: int, threshold: float, R: float) -> np.ndarray:

@@ -229,6 +229,25 @@ void FN(oracle_count_plaquettes)(const REAL *state, int nx, int ny, int nz, int 
     *n_weighted = weighted;
 }
 
+/* AxionStringsLevel::apply_pre_evolution_to_main_rescale (AxionStringsLevel.cpp:2027-2132):
+ * in place over every cell including ghosts; R's and kappa as amrex::Real. */
+void FN(oracle_handoff_rescale)(REAL *state, int nx, int ny, int nz, int ng, double R_pre_d, double R_pre_prime_d,
+                                double R_main_d, double R_main_prime_d)
+{
+    const FN(orc_box) b = FN(orc_make_box)(nx, ny, nz, ng);
+    const REAL R_pre = (REAL)R_pre_d, R_pre_prime = (REAL)R_pre_prime_d;
+    const REAL R_main = (REAL)R_main_d, R_main_prime = (REAL)R_main_prime_d;
+    const REAL kappa = R_main / R_pre;
+    const REAL common_term = R_main_prime - kappa * kappa * R_pre_prime;
+    for (int64_t o = 0; o < b.cs; ++o) {
+        const REAL psi1 = state[o], psi2 = state[b.cs + o], Pi1 = state[2 * b.cs + o], Pi2 = state[3 * b.cs + o];
+        state[o] = kappa * psi1;
+        state[b.cs + o] = kappa * psi2;
+        state[2 * b.cs + o] = kappa * kappa * Pi1 + (psi1 / R_pre) * common_term;
+        state[3 * b.cs + o] = kappa * kappa * Pi2 + (psi2 / R_pre) * common_term;
+    }
+}
+
 /* fill_masked_a_dot_buffer (MaskedFieldBuffer.hpp:15-35): buf[cell] =
  * (REAL) masked_a_dot(psi1, psi2, Pi1, Pi2, R), R passed as amrex::Real. */
 void FN(oracle_masked_a_dot_buffer)(const REAL *state, int nx, int ny, int nz, int ng, int scheme,
