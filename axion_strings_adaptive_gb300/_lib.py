@@ -112,6 +112,8 @@ SIGNATURES = {
     "axs_level_fill_ghosts": (_i32, [C.POINTER(LevelC), _ptr]),
     "axs_level_import_fab": (_i32, [C.POINTER(LevelC), C.POINTER(Fab), _ptr]),
     "axs_level_export_fab": (_i32, [C.POINTER(LevelC), C.POINTER(Fab), _ptr]),
+    "axs_level_upload": (_i32, [C.POINTER(LevelC), _ptr, _ptr]),
+    "axs_level_download": (_i32, [C.POINTER(LevelC), _ptr, _ptr]),
     "axs_level_rk4_advance": (_i32, [C.POINTER(LevelC), C.POINTER(BackgroundC), _dbl, _dbl, _dbl, _i32, _ptr]),
     "axs_level_rk4_sweep": (_i32, [C.POINTER(LevelC), C.POINTER(BackgroundC), _dbl, _dbl, _dbl, _i32, _ptr]),
     "axs_level_device_status": (_i32, [C.POINTER(LevelC), _ptr]),

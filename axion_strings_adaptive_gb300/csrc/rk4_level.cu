@@ -270,6 +270,54 @@ int axs_level_export_fab(const axs_level *lv, const axs_fab *dst, void *stream)
     return level_copy_fab(lv->state, lv->dtype, g, *dst, 0, (cudaStream_t)stream);
 }
 
+// Host <-> level copies as one 3D copy each: the host array (4, nz, ny, nx) is
+// 4*nz slices of ny rows of nx elements; in the level a slice is kstride
+// elements (jstride * (ny + 4)) and the component stride is nz slices, so slice
+// c*nz + z lands on component c, plane z.
+static cudaMemcpy3DParms level_host_copy(const axs_level *lv, const LevelGeom &g, void *host, bool to_level)
+{
+    const size_t es = dtype_size(lv->dtype);
+    cudaMemcpy3DParms p{};
+    cudaPitchedPtr h = make_cudaPitchedPtr(host, (size_t)lv->nx * es, (size_t)lv->nx * es, (size_t)lv->ny);
+    cudaPitchedPtr d = make_cudaPitchedPtr(lv->state, (size_t)g.js * es, (size_t)lv->nx * es, (size_t)(lv->ny + 4));
+    const cudaPos at = make_cudaPos((size_t)g.ox * es, (size_t)g.oy, 0);
+    if (to_level) {
+        p.srcPtr = h;
+        p.dstPtr = d;
+        p.dstPos = at;
+        p.kind = cudaMemcpyHostToDevice;
+    } else {
+        p.srcPtr = d;
+        p.srcPos = at;
+        p.dstPtr = h;
+        p.kind = cudaMemcpyDeviceToHost;
+    }
+    p.extent = make_cudaExtent((size_t)lv->nx * es, (size_t)lv->ny, (size_t)4 * lv->nz);
+    return p;
+}
+
+int axs_level_upload(const axs_level *lv, const void *host_state, void *stream)
+{
+    LevelGeom g;
+    int rc = validate_level(lv, g);
+    if (rc) return rc;
+    AXS_REQUIRE(host_state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null host state");
+    cudaMemcpy3DParms p = level_host_copy(lv, g, const_cast<void *>(host_state), true);
+    AXS_CUDA_CHECK(cudaMemcpy3DAsync(&p, (cudaStream_t)stream));
+    return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g, 4, (cudaStream_t)stream);
+}
+
+int axs_level_download(const axs_level *lv, void *host_state, void *stream)
+{
+    LevelGeom g;
+    int rc = validate_level(lv, g);
+    if (rc) return rc;
+    AXS_REQUIRE(host_state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null host state");
+    cudaMemcpy3DParms p = level_host_copy(lv, g, host_state, false);
+    AXS_CUDA_CHECK(cudaMemcpy3DAsync(&p, (cudaStream_t)stream));
+    return AXS_OK;
+}
+
 int axs_level_rk4_advance(const axs_level *lv, const axs_background *bg, double tau_i, double t0, double dt,
                           int32_t nsteps, void *stream)
 {

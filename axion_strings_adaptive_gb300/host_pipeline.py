@@ -3,31 +3,37 @@
 A caller that keeps its fields in host memory (a CPU code handing boxes to the
 GPU, or a stream of independent realisations) pays a host->device copy of each
 input and a device->host copy of each result per call. :class:`HostStepPipeline`
-runs those copies on their own streams into rotating device staging buffers,
-so that the input of call s+1 and the result of call s-1 move while call s
-computes (H2D and D2H also overlap each other: the link is full duplex).
-Every call is: pinned host state -> H2D -> ``axs_level_import_fab`` ->
-``axs_level_rk4_advance`` -> ``axs_level_export_fab`` -> D2H.
+rotates over `depth` device levels: the upload of call s+1, the compute of call
+s and the download of call s-1 use different levels and run on three streams,
+so the two copy directions (the link is full duplex) and the compute overlap.
+Every call is: pinned host state -> ``axs_level_upload`` (one strided DMA copy
+into the level layout + periodic padding) -> ``axs_level_rk4_advance`` ->
+``axs_level_download`` -> pinned host result.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import torch
 
+from . import _lib as L
 from .background import Background
 from .level import PeriodicLevel
 
 
 class HostStepPipeline:
-    def __init__(self, level: PeriodicLevel, depth: int = 2):
+    def __init__(self, level: PeriodicLevel, depth: int = 3):
+        self.levels = [level]
+        for _ in range(max(1, int(depth)) - 1):
+            lv = PeriodicLevel((level.nx, level.ny, level.nz), level.dx, dtype=level.dtype, device=level.state.device,
+                               pierced_capacity=1, tile_config=level.tile_config)
+            self.levels.append(lv)
         dev = level.state.device
-        self.level = level
-        self.depth = max(1, int(depth))
-        shape = (4, level.nz, level.ny, level.nx)
-        self.staging = [torch.empty(shape, dtype=level.dtype, device=dev) for _ in range(self.depth)]
-        self.h2d, self.comp, self.d2h = (torch.cuda.Stream(device=dev) for _ in range(3))
-        self._h2d_done = [torch.cuda.Event() for _ in range(self.depth)]
+        self.depth = len(self.levels)
+        self.up, self.comp, self.down = (torch.cuda.Stream(device=dev) for _ in range(3))
+        self._up_done = [torch.cuda.Event() for _ in range(self.depth)]
         self._comp_done = [torch.cuda.Event() for _ in range(self.depth)]
-        self._d2h_done = [torch.cuda.Event() for _ in range(self.depth)]
+        self._down_done = [torch.cuda.Event() for _ in range(self.depth)]
         self._used = [False] * self.depth
         self._k = 0
 
@@ -36,26 +42,25 @@ class HostStepPipeline:
         """Queue one call: host_in (pinned, (4, nz, ny, nx)) advanced nsteps -> host_out (pinned)."""
         slot = self._k % self.depth
         self._k += 1
-        buf = self.staging[slot]
+        lv = self.levels[slot]
         if self._used[slot]:
-            self.h2d.wait_event(self._d2h_done[slot])  # the slot's previous result has left
+            self.up.wait_event(self._down_done[slot])  # the slot's previous result has left
         self._used[slot] = True
-        with torch.cuda.stream(self.h2d):
-            buf.copy_(host_in, non_blocking=True)
-            self._h2d_done[slot].record(self.h2d)
-        self.comp.wait_event(self._h2d_done[slot])
-        with torch.cuda.stream(self.comp):
-            self.level.import_fab(buf, 0, self.comp)
-            self.level.advance(bg, tau_i, t0, dt, nsteps, self.comp)
-            self.level.export_fab(buf, 0, self.comp)
-            self._comp_done[slot].record(self.comp)
-        self.d2h.wait_event(self._comp_done[slot])
-        with torch.cuda.stream(self.d2h):
-            host_out.copy_(buf, non_blocking=True)
-            self._d2h_done[slot].record(self.d2h)
+        L.call("axs_level_upload", C.byref(lv.c), C.c_void_p(host_in.data_ptr()), self.up.cuda_stream)
+        self._up_done[slot].record(self.up)
+        self.comp.wait_event(self._up_done[slot])
+        lv.advance(bg, tau_i, t0, dt, nsteps, self.comp)
+        self._comp_done[slot].record(self.comp)
+        self.down.wait_event(self._comp_done[slot])
+        L.call("axs_level_download", C.byref(lv.c), C.c_void_p(host_out.data_ptr()), self.down.cuda_stream)
+        self._down_done[slot].record(self.down)
 
     def join(self, stream: torch.cuda.Stream | None = None) -> None:
         """Make `stream` (default: the current stream) wait for everything queued."""
         s = stream or torch.cuda.current_stream()
-        for st in (self.h2d, self.comp, self.d2h):
+        for st in (self.up, self.comp, self.down):
             s.wait_stream(st)
+
+    def device_status(self) -> None:
+        for lv in self.levels:
+            lv.device_status()

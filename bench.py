@@ -566,7 +566,7 @@ def run_native(args):
         hin = [ic64.float().cpu().pin_memory(), (ic64.float() * 0.999).cpu().pin_memory()]
         hout = [torch.empty_like(hin[0]).pin_memory() for _ in range(2)]
         steps_e = max(4, args.steps // 2)
-        pipe = HostStepPipeline(lv, depth=2)
+        pipe = HostStepPipeline(lv, depth=3)
 
         def run(k, serial):
             for s_ in range(k):
@@ -590,16 +590,16 @@ def run_native(args):
 
         ems_serial = timed_e2e(True)
         ems = timed_e2e(False)
-        lv.device_status()
+        pipe.device_status()
         nbytes = hin[0].numel() * 4
         e2e = {"value": ws * n ** 3 * steps_e / (ems * 1e-3), "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "steps": steps_e, "ms_per_step": ems / steps_e,
                "serial_value": ws * n ** 3 * steps_e / (ems_serial * 1e-3), "serial_ms_per_step": ems_serial / steps_e,
                "link_gbs_per_direction": nbytes / (ems / steps_e * 1e-3) / 1e9,
-               "path": "pinned host state -> H2D -> axs_level_import_fab -> axs_level_rk4_advance(1 step) -> "
-                       "axs_level_export_fab -> D2H, copies of neighbouring steps overlapped with compute "
-                       "(HostStepPipeline, 2 staging buffers)"}
+               "path": "pinned host state -> axs_level_upload (strided DMA into the level layout) -> "
+                       "axs_level_rk4_advance(1 step) -> axs_level_download -> pinned host result; upload, compute "
+                       "and download of neighbouring steps overlap (HostStepPipeline, 3 levels, 3 streams)"}
         del lv, pipe, hin, hout
 
     cpu = None

@@ -183,6 +183,12 @@ int axs_level_fill_ghosts(const axs_level *lv, void *stream);
 int axs_level_import_fab(const axs_level *lv, const axs_fab *src, void *stream);
 int axs_level_export_fab(const axs_level *lv, const axs_fab *dst, void *stream);
 
+/* The level's valid cells from / to a HOST array (4, nz, ny, nx) of its dtype
+ * (pinned memory for asynchronous copies): one strided DMA copy each way, then
+ * (upload) the periodic padding. For callers whose fields live in host memory. */
+int axs_level_upload(const axs_level *lv, const void *host_state, void *stream);
+int axs_level_download(const axs_level *lv, void *host_state, void *stream);
+
 /* Replaces GRTeclyn's RK4 level advance (docs/conventions.md:239-245, driver
  * absent from the reference tree) together with nsteps x 4 calls of
  * specific_eval_rhs: advances the state by nsteps classic-RK4 steps of size
