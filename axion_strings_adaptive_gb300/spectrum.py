@@ -51,7 +51,7 @@ def spectrum_at(level: PeriodicLevel, R: float, H: float = 0.0, masking_scheme: 
     sums = torch.zeros(3, dtype=torch.float64, device=dev)  # sum_sq, full, inscribed
     L.call("axs_level_masked_a_dot", C.byref(level.c), int(masking_scheme), float(threshold), float(R),
            buf.data_ptr(), sums.data_ptr(), scratch.data_ptr(), scratch.numel(), _stream_ptr(stream))
-    X = torch.fft.rfftn(buf)
+    X = torch.fft.rfftn(buf).contiguous()  # cuFFT may hand back permuted strides
     S = max(nx, ny, nz) // 2 + 1
     shell_sum = torch.zeros(S, dtype=torch.float64, device=dev)
     shell_cnt = torch.zeros(S, dtype=torch.int64, device=dev)
