@@ -71,6 +71,25 @@ class DiagResult(C.Structure):
                 ("n_p_weighted", _i64), ("n_listed", _i64), ("n_near_tie", _i64), ("status", _i64)]
 
 
+class PatchLayout(C.Structure):
+    _fields_ = [("jstride", _i64), ("kstride", _i64), ("patch_elems", _i64), ("plane_elems", _i64),
+                ("x_offset", _i32), ("y_offset", _i32), ("z_offset", _i32), ("state_bytes", _i64),
+                ("work_bytes", _i64), ("table_bytes", _i64)]
+
+
+class PatchesC(C.Structure):
+    _fields_ = [("dtype", _i32), ("n", _i32), ("npatches", _i32), ("dx", _dbl), ("state", _ptr), ("work", _ptr),
+                ("table", _ptr), ("state_bytes", _i64), ("work_bytes", _i64), ("table_bytes", _i64)]
+
+
+class PatchPlan(C.Structure):
+    _fields_ = [("items_a", _i64), ("items_b", _i64), ("grid_a", _i32), ("grid_b", _i32)]
+
+
+class PatchMap(C.Structure):
+    _fields_ = [("patch_block", _ptr), ("block_patch", _ptr)]
+
+
 class TagParams(C.Structure):
     _fields_ = [("dx", _dbl), ("gradient_threshold", _dbl), ("radial_gradient_threshold", _dbl),
                 ("n_error_buf", _i32), ("block", _i32)]
@@ -127,6 +146,14 @@ SIGNATURES = {
     "axs_level_diagnostics": (_i32, [C.POINTER(LevelC), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr, _i64,
                                      _ptr]),
     "axs_diagnostics_static_scratch": (_i32, [C.POINTER(Fab), C.POINTER(DiagParams), _ptr, _ptr, _ptr, _i64, _ptr]),
+    "axs_patches_layout": (_i32, [_i32, _i32, _i32, C.POINTER(PatchLayout)]),
+    "axs_patches_init": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchPlan), _ptr]),
+    "axs_patches_fill": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchMap), C.POINTER(LevelC), C.POINTER(LevelC), _dbl,
+                                _dbl, _i32, _ptr]),
+    "axs_patches_rk4_step": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchPlan), C.POINTER(BackgroundC), _dbl, _dbl,
+                                    _dbl, _ptr]),
+    "axs_patches_average_down": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchMap), C.POINTER(LevelC), _ptr]),
+    "axs_patches_device_status": (_i32, [C.POINTER(PatchesC), _ptr]),
     "axs_level_masked_a_dot": (_i32, [C.POINTER(LevelC), _i32, _dbl, _dbl, _ptr, _ptr, _ptr, _i64, _ptr]),
     "axs_spectrum_scratch_bytes": (_i32, [_i32, _i32, _i32, C.POINTER(_i64)]),
     "axs_spectrum_bin": (_i32, [_ptr, _i32, _i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _i64, _ptr]),

@@ -1,0 +1,226 @@
+"""Two-level block-structured refinement on a periodic coarse level (the scale path).
+
+The coarse level is a :class:`~.level.PeriodicLevel`. The refinement tagger
+(``axs_level_tag_cells``: the StringTagger criteria plus an ``n_error_buf``
+buffer) flags block^3 blocks of coarse cells; every flagged block gets a patch
+of (2 block)^3 fine cells (:class:`Patches`, ``axs_patches_*``). One coarse
+step advances the coarse level by dt and then the patches by two fine steps of
+dt/2 (subcycling), each after refilling the patch ghost rings from neighbouring
+patches or, where none owns a ring cell, from the coarse level interpolated in
+space and time. As in the reference, the coarse level keeps evolving under the
+patches (nothing averages fine data down during the evolution);
+:meth:`TwoLevel.collapse_to_coarse` averages down on request, e.g. before a
+spectrum. :meth:`TwoLevel.diagnostics` is the composite of
+specific_post_timestep (AxionStringsLevel.cpp:1296-1350): the coarse level
+with its covered cells masked out plus every patch, string lengths weighted by
+dx, velocities by dx, energies by dx^3 (EnergyKernel.hpp:287-339).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .background import Background, xi_from_comoving_length
+from .level import _DT, PeriodicLevel, _stream_ptr
+
+
+class Patches:
+    """npatches refined patches of n^3 fine cells (spacing dx) with ghost rings."""
+
+    def __init__(self, n: int, npatches: int, dx: float, dtype=torch.float32, device="cuda"):
+        lay = L.PatchLayout()
+        L.call("axs_patches_layout", _DT[dtype], int(n), int(npatches), C.byref(lay))
+        self.layout, self.n, self.npatches, self.dx, self.dtype = lay, int(n), int(npatches), float(dx), dtype
+        self.state = torch.zeros((4, lay.plane_elems), dtype=dtype, device=device)
+        self.work = torch.zeros((8, lay.plane_elems), dtype=dtype, device=device)
+        self.table = torch.zeros(lay.table_bytes, dtype=torch.uint8, device=device)
+        self.c = L.PatchesC(_DT[dtype], self.n, self.npatches, self.dx, self.state.data_ptr(), self.work.data_ptr(),
+                            self.table.data_ptr(), lay.state_bytes, lay.work_bytes, lay.table_bytes)
+        self.plan = L.PatchPlan()
+        L.call("axs_patches_init", C.byref(self.c), C.byref(self.plan), None)
+
+    def box(self, q: int, arena: torch.Tensor | None = None) -> torch.Tensor:
+        """(ncomp, n+8, n+8, jstride) padded box of patch q."""
+        t = self.state if arena is None else arena
+        lay, n = self.layout, self.n
+        blk = t[:, q * lay.patch_elems:q * lay.patch_elems + (n + 8) * lay.kstride]
+        return blk.view(t.shape[0], n + 8, n + 8, lay.jstride)
+
+    def valid(self, q: int, arena: torch.Tensor | None = None) -> torch.Tensor:
+        lay, n = self.layout, self.n
+        return self.box(q, arena)[:, lay.z_offset:lay.z_offset + n, lay.y_offset:lay.y_offset + n,
+                                  lay.x_offset:lay.x_offset + n]
+
+    def step(self, bg: Background, tau_i: float, t: float, dt: float, stream=None) -> None:
+        L.call("axs_patches_rk4_step", C.byref(self.c), C.byref(self.plan), C.byref(bg.to_c()), float(tau_i),
+               float(t), float(dt), _stream_ptr(stream))
+
+    def device_status(self) -> None:
+        L.call("axs_patches_device_status", C.byref(self.c), None)
+
+    def fab(self, q: int) -> L.Fab:
+        """axs_fab view of patch q with 4 ghost layers (its ring), for the diagnostics pass."""
+        lay, es = self.layout, torch.finfo(self.dtype).bits // 8
+        ptr = self.state.data_ptr() + (q * lay.patch_elems + lay.x_offset - 4) * es
+        return L.Fab(ptr, _DT[self.dtype], self.n, self.n, self.n, 4, 4, lay.jstride, lay.kstride, lay.plane_elems)
+
+
+@dataclasses.dataclass
+class CompositeDiagnostics:
+    n_p_plain: int
+    n_p_weighted: int
+    xi_plain: float
+    xi_weighted: float
+    energy: dict
+    mean_gamma_sq_v_sq: float
+    vel_count: int
+    n_patches: int
+    refined_fraction: float
+
+
+class TwoLevel:
+    """A periodic coarse level plus 2x-refined patches on tagged block^3 blocks."""
+
+    ENERGY_NAMES = ["rho_tot", "rho_axion_kinetic", "rho_axion_gradient", "rho_radial_kinetic",
+                    "rho_radial_gradient", "rho_radial_mass"]
+
+    def __init__(self, coarse: PeriodicLevel, block: int = 32):
+        if coarse.nx % block or coarse.ny % block or coarse.nz % block:
+            raise ValueError("the coarse level must tile into blocks")
+        self.coarse, self.block = coarse, int(block)
+        self.nb = (coarse.nx // block, coarse.ny // block, coarse.nz // block)
+        self.old = PeriodicLevel((coarse.nx, coarse.ny, coarse.nz), coarse.dx, dtype=coarse.dtype,
+                                 device=coarse.state.device, pierced_capacity=1, tile_config=coarse.tile_config)
+        self.patches: Patches | None = None
+        self.blocks = np.zeros((0, 3), dtype=np.int32)
+        dev = coarse.state.device
+        self._block_patch = torch.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=torch.int32, device=dev)
+        self._patch_block = torch.zeros((1, 3), dtype=torch.int32, device=dev)
+
+    # ------------------------------------------------------------------ patch management
+    def _map(self) -> L.PatchMap:
+        return L.PatchMap(self._patch_block.data_ptr(), self._block_patch.data_ptr())
+
+    def set_blocks(self, blocks: np.ndarray) -> None:
+        """Refine exactly these blocks ((k, 3) block coordinates x, y, z): blocks
+        refined before keep their fine data, new ones interpolate the coarse level."""
+        blocks = np.asarray(blocks, dtype=np.int32).reshape(-1, 3)
+        dev = self.coarse.state.device
+        old_patches, old_blocks = self.patches, self.blocks
+        old_index = {tuple(b): q for q, b in enumerate(old_blocks)}
+        self.blocks = blocks
+        if len(blocks) == 0:
+            self.patches = None
+            self._block_patch.fill_(-1)
+            return
+        dt = self.coarse.dtype
+        self.patches = Patches(2 * self.block, len(blocks), 0.5 * self.coarse.dx, dtype=dt, device=dev)
+        self._patch_block = torch.from_numpy(blocks.copy()).to(dev)
+        bp = torch.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=torch.int32)
+        for q, (bx, by, bz) in enumerate(blocks):
+            bp[bz, by, bx] = q
+        self._block_patch = bp.to(dev)
+        L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c), None, 0.0,
+               0.0, 1, None)
+        if old_patches is not None:
+            for q, b in enumerate(blocks):
+                oq = old_index.get(tuple(b))
+                if oq is not None:
+                    self.patches.valid(q).copy_(old_patches.valid(oq))
+
+    def regrid(self, n_error_buf: int = 4, gradient_threshold: float = 1.7976931348623157e308,
+               radial_gradient_threshold: float = 1.7976931348623157e308) -> int:
+        """Tag the coarse level (StringTagger + buffer) and refine every block holding a tag."""
+        _, _, flags = self.coarse.tag_cells(gradient_threshold, radial_gradient_threshold, n_error_buf, self.block)
+        idx = torch.nonzero(flags.cpu()).numpy()  # (bz, by, bx)
+        self.set_blocks(idx[:, ::-1].astype(np.int32))
+        return len(idx)
+
+    # ------------------------------------------------------------------ evolution
+    def advance(self, bg: Background, tau_i: float, t0: float, dt: float, nsteps: int) -> None:
+        """nsteps coarse steps, each followed by two subcycled fine steps."""
+        for s in range(nsteps):
+            t = t0 + s * dt
+            if self.patches is None:
+                self.coarse.advance(bg, tau_i, t, dt, 1)
+                continue
+            self.old.state.copy_(self.coarse.state)
+            self.coarse.advance(bg, tau_i, t, dt, 1)
+            for f, theta in enumerate((0.0, 0.5)):
+                L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.old.c),
+                       C.byref(self.coarse.c), theta, dt, 0, None)
+                self.patches.step(bg, tau_i, t + f * 0.5 * dt, 0.5 * dt)
+
+    def device_status(self) -> None:
+        self.coarse.device_status()
+        if self.patches is not None:
+            self.patches.device_status()
+
+    def collapse_to_coarse(self) -> None:
+        """amrex::average_down of every patch onto the coarse level (in place)."""
+        if self.patches is not None:
+            L.call("axs_patches_average_down", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c),
+                   None)
+
+    # ------------------------------------------------------------------ composite diagnostics
+    def coverage_mask(self) -> torch.Tensor:
+        """uint8 (nz, ny, nx) over the coarse cells: 1 where no patch covers the cell."""
+        b = self.block
+        covered = (self._block_patch >= 0).to(torch.uint8)
+        covered = covered.repeat_interleave(b, 0).repeat_interleave(b, 1).repeat_interleave(b, 2)
+        return (1 - covered).contiguous()
+
+    def diagnostics(self, bg: Background, tau: float, masking_scheme: int = L.MASK_A,
+                    threshold: float = 0.8) -> CompositeDiagnostics:
+        v = bg.values(tau)
+        rpr = 0.0 if bg.kind == L.BG_FLAT else v.R_prime_over_R
+        levels = []
+        mask = self.coverage_mask().reshape(-1) if self.patches is not None else None
+        levels.append((self.coarse.diagnostics_raw(
+            L.DiagParams(self.coarse.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold, L.BOUNDARY_PERIODIC,
+                         1, 1, 1, 0), mask, want_list=False), self.coarse.dx))
+        if self.patches is not None:
+            p = self.patches
+            # rings at the current time: neighbours, else the (current) coarse level
+            L.call("axs_patches_fill", C.byref(p.c), C.byref(self._map()), C.byref(self.coarse.c), None, 0.0, 0.0, 0,
+                   None)
+            nbytes = C.c_int64()
+            L.call("axs_diagnostics_scratch_bytes", p.n, p.n, p.n, C.byref(nbytes))
+            dev = self.coarse.state.device
+            scratch = torch.zeros(nbytes.value, dtype=torch.uint8, device=dev)
+            res = torch.zeros((p.npatches, C.sizeof(L.DiagResult)), dtype=torch.uint8, device=dev)
+            prm = L.DiagParams(p.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold, L.BOUNDARY_GHOSTS, 1, 1,
+                               1, 0)
+            s = torch.cuda.current_stream().cuda_stream
+            for q in range(p.npatches):
+                L.call("axs_diagnostics", C.byref(p.fab(q)), C.byref(prm), None, res[q].data_ptr(), None, 0,
+                       scratch.data_ptr(), scratch.numel(), s)
+            host = res.cpu().numpy()
+            for q in range(p.npatches):
+                levels.append((L.DiagResult.from_buffer_copy(host[q].tobytes()), p.dx))
+        # composite combination (AxionStringsLevel.cpp:1302-1350, EnergyKernel.hpp:287-339)
+        n_p = sum(r.n_p_plain for r, _ in levels)
+        n_w = sum(r.n_p_weighted for r, _ in levels)
+        ell_p = sum((2.0 / 3.0) * r.n_p_plain * dx for r, dx in levels)
+        ell_w = sum((2.0 / 3.0) * r.n_p_weighted * dx for r, dx in levels)
+        vsum = sum(r.vel_sum * dx for r, dx in levels)
+        vcnt = sum(r.vel_count * dx for r, dx in levels)
+        acc = np.zeros(14)
+        for r, dx in levels:
+            acc += np.array(list(r.energy_sums)) * dx ** 3
+        n_total, n_unmasked = acc[13], acc[12]
+        energy = {"n_total": n_total, "n_unmasked": n_unmasked}
+        for q, name in enumerate(self.ENERGY_NAMES):
+            energy[name + "_unscreened"] = acc[2 * q] / n_total
+            energy[name + "_screened"] = acc[2 * q + 1] / n_unmasked if n_unmasked > 0.0 else 0.0
+        L_tilde = self.coarse.nx * self.coarse.dx
+        nref = 0 if self.patches is None else self.patches.npatches
+        return CompositeDiagnostics(
+            n_p_plain=n_p, n_p_weighted=n_w, xi_plain=xi_from_comoving_length(ell_p, L_tilde, bg.a_inv, tau),
+            xi_weighted=xi_from_comoving_length(ell_w, L_tilde, bg.a_inv, tau), energy=energy,
+            mean_gamma_sq_v_sq=vsum / vcnt if vcnt > 0 else 0.0, vel_count=sum(r.vel_count for r, _ in levels),
+            n_patches=nref, refined_fraction=nref / float(np.prod(self.nb)))

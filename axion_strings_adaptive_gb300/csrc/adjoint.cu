@@ -69,7 +69,8 @@ struct AdjointB {
             lam -= (double)(fma(a.c2.hlam * m3, fma(u31, f3b1, u32 * f3b2), a.c4.hlam * m4 * fma(u41, f4b1, u42 * f4b2)));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, fo[c], pol);
+        for (int c = 0; c < 4; ++c)
+            store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, fo[c], pol, b.periodic);
 #pragma unroll
         for (int c = 0; c < 4; ++c) st_out<T, V, HINT>(a.out[4 + c] + off, uo[c], pol);
     }
@@ -107,7 +108,8 @@ struct AdjointA {
             lam -= (double)(fma(a.c1.hlam * m1, fma(p1, f1b1, p2 * f1b2), a.c2.hlam * m2 * fma(u21, f2b1, u22 * f2b2)));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol);
+        for (int c = 0; c < 4; ++c)
+            store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol, b.periodic);
     }
 };
 

@@ -1,0 +1,541 @@
+// Refined patches over a periodic coarse level (the scale path's fine level).
+//
+// A patch refines one block^3 block of coarse cells by 2 in every direction:
+// n = 2*block fine cells per side, spacing dx/2, time step dt/2 (two fine steps
+// per coarse step). Patches are cubes of fine cells in a fixed-block layout,
+// so the patch that owns any fine cell is found by integer division.
+//
+// Patch layout: valid fine cell (0,0,0) sits at padded position (8, 4, 4);
+// every patch holds a ghost ring of 6 columns in x and 4 rows / planes in y
+// and z (plus 2 columns of slack on either side for the TMA boxes), rows are
+// padded to 128 bytes, and the patches are stacked along each component plane
+// as an ensemble's boxes are.
+//
+// One fine RK4 step of every patch is the two fused sweeps with explicit
+// ghost rings instead of periodic wrap: sweep A runs over the valid cells
+// plus a ring of 4 (x, keeping the TMA boxes 16-byte aligned) / 2 (y, z)
+// cells, reading psi, Pi on the 6 / 4-wide ring, so that sweep B over the
+// valid cells finds S3, S4 on its 2-wide stencil ring. The ring therefore has
+// to hold psi, Pi at the step's start time; it is filled first from the
+// neighbouring patches (same fine level, same time) and, where no patch owns
+// a ring cell, by interpolating the coarse level: quartic Lagrange
+// interpolation of coarse cell-centre values in each direction (the 5 coarse
+// cells around the fine cell's parent; fine centres sit at -1/4 and +1/4 of a
+// coarse cell), and in time between the coarse states at the start and end of
+// the coarse step -- cubic Hermite for psi (Pi = dpsi/dtau is its derivative)
+// and linear for Pi.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "rk4_ops.cuh"
+
+namespace axs {
+
+int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g);
+int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, int ncomp,
+                      cudaStream_t st);
+constexpr int kPatchOX = 8, kPatchRY = 4, kPatchRZ = 4;  // padded position of valid (0, 0, 0)
+constexpr int kRingX = 6, kRingYZ = 4;                    // ghost ring widths the step reads
+constexpr int64_t kPatchHeader = 128;
+
+struct PatchGeom {
+    int n;           // fine cells per side
+    int64_t js, ks;  // row and plane strides
+    int64_t box;     // elements of one patch in one component plane (128-byte multiple)
+    int64_t plane;   // elements of one component plane (all patches)
+};
+
+static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g)
+{
+    AXS_REQUIRE(dtype == AXS_F32 || dtype == AXS_F64, AXS_ERR_INVALID_ARGUMENT, "bad dtype %d", dtype);
+    AXS_REQUIRE(n >= 8 && n % 8 == 0 && n <= 256, AXS_ERR_UNSUPPORTED, "patch side %d must be a multiple of 8 in [8, 256]",
+                n);
+    AXS_REQUIRE(npatches > 0 && npatches < (1 << (32 - kEnsItemBits)) / 2, AXS_ERR_INVALID_ARGUMENT,
+                "patch count %d out of range", npatches);
+    const int64_t line = 128 / (int64_t)dtype_size(dtype);
+    g.n = n;
+    g.js = (kPatchOX + n + kRingX + 2 + line - 1) / line * line;
+    g.ks = g.js * (n + 2 * kPatchRY);
+    g.box = (g.ks * (n + 2 * kPatchRZ) + line - 1) / line * line;
+    g.plane = g.box * npatches;
+    return AXS_OK;
+}
+
+static int64_t patch_items_bound(const PatchGeom &g, int npatches)
+{
+    // sweep A domain (n+8) x (n+4) x (n+4) and sweep B n^3, tiles >= 16 x 8, chunks >= 1 plane
+    const int64_t a = (int64_t)((g.n + 8 + 15) / 16) * ((g.n + 4 + 7) / 8) * (g.n + 4);
+    const int64_t b = (int64_t)((g.n + 15) / 16) * ((g.n + 7) / 8) * g.n;
+    return (a + b) * npatches;
+}
+
+static int64_t patch_table_bytes(const PatchGeom &g, int npatches)
+{
+    return kPatchHeader + (int64_t)npatches * 2 * sizeof(CUtensorMap) + (int64_t)npatches * 2 * sizeof(EnsBoxDesc) +
+           4 * patch_items_bound(g, npatches);
+}
+
+static int validate_patches(const axs_patches *p, PatchGeom &g)
+{
+    AXS_REQUIRE(p != nullptr, AXS_ERR_INVALID_ARGUMENT, "null patches");
+    int rc = patch_geom(p->dtype, p->n, p->npatches, g);
+    if (rc) return rc;
+    AXS_REQUIRE(p->dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
+    AXS_REQUIRE(p->state && p->work && p->table, AXS_ERR_INVALID_ARGUMENT, "null patch buffer");
+    AXS_REQUIRE(((uintptr_t)p->state % 128) == 0 && ((uintptr_t)p->work % 128) == 0 && ((uintptr_t)p->table % 128) == 0,
+                AXS_ERR_ALIGNMENT, "patch buffers must be 128-byte aligned");
+    const int64_t es = (int64_t)dtype_size(p->dtype);
+    AXS_REQUIRE(p->state_bytes >= 4 * g.plane * es && p->work_bytes >= 8 * g.plane * es &&
+                    p->table_bytes >= patch_table_bytes(g, p->npatches),
+                AXS_ERR_WORKSPACE, "patch buffer too small");
+    return AXS_OK;
+}
+
+// ---------------------------------------------------------------- the two sweeps
+template <typename T> struct PatchTilings {
+    // sweep A: domain x in [-4, n+4) (tiles start on 16-byte boundaries), y, z in [-2, n+2)
+    using LA = SweepLauncher<T, 2, 24, 16, 8, 2, ForwardA, BoxTable, true>;
+    // sweep B: the valid cells
+    using LB = SweepLauncher<T, 2, 32, 16, 8, 2, ForwardB, BoxTable, true>;
+    static constexpr int TXA = 24, TYA = 16, TXB = 32, TYB = 16;
+};
+
+struct PatchTableOut {
+    int64_t items_a, items_b;
+    int grid_a, grid_b;
+};
+
+template <typename T> static int build_patch_table(const axs_patches *p, const PatchGeom &g, cudaStream_t st,
+                                                   PatchTableOut &out)
+{
+    using PT = PatchTilings<T>;
+    int ba = 0, bb = 0;
+    int rc = PT::LA::blocks_per_sm(ba);
+    if (rc) return rc;
+    if ((rc = PT::LB::blocks_per_sm(bb))) return rc;
+    const int sms = device_sm_count();
+    AXS_REQUIRE(sms > 0, AXS_ERR_CUDA, "no CUDA device");
+    const int np = p->npatches, n = g.n;
+    std::vector<EnsBoxDesc> desc(2 * (size_t)np);
+    std::vector<uint32_t> items_a, items_b;
+    auto fill = [&](EnsBoxDesc &d, int map_box, int lo_x, int lo_yz, int ext_x, int ext_yz, int tx, int ty,
+                    int zchunk) {
+        d.nx = ext_x;
+        d.ny = ext_yz;
+        d.nz = ext_yz;
+        d.tiles_x = (ext_x + tx - 1) / tx;
+        d.ntiles = d.tiles_x * ((ext_yz + ty - 1) / ty);
+        d.zchunk = zchunk;
+        d.js = g.js;
+        d.ks = g.ks;
+        d.base = (int64_t)map_box * g.box;
+        d.xlo = lo_x;
+        d.ylo = d.zlo = lo_yz;
+        d.oy = kPatchRY;
+        d.oz = kPatchRZ;
+        d.periodic = 0;
+        d.map_box = map_box;
+        d.pad = 0;
+    };
+    // chunk length: about 4 chunks per patch side, at least 8 planes
+    const int zc_a = std::max(8, (n + 4 + 3) / 4), zc_b = std::max(8, (n + 3) / 4);
+    for (int q = 0; q < np; ++q) {
+        fill(desc[q], q, -4, -2, n + 8, n + 4, PT::TXA, PT::TYA, zc_a);
+        fill(desc[np + q], q, 0, 0, n, n, PT::TXB, PT::TYB, zc_b);
+    }
+    for (int q = 0; q < np; ++q) {
+        const EnsBoxDesc &da = desc[q], &db = desc[np + q];
+        const int64_t na = (int64_t)da.ntiles * ((da.nz + da.zchunk - 1) / da.zchunk);
+        const int64_t nb = (int64_t)db.ntiles * ((db.nz + db.zchunk - 1) / db.zchunk);
+        for (int64_t i = 0; i < na; ++i) items_a.push_back(((uint32_t)q << kEnsItemBits) | (uint32_t)i);
+        for (int64_t i = 0; i < nb; ++i) items_b.push_back(((uint32_t)(np + q) << kEnsItemBits) | (uint32_t)i);
+    }
+    const size_t maps_off = kPatchHeader, desc_off = maps_off + 2 * sizeof(CUtensorMap) * np,
+                 items_off = desc_off + sizeof(EnsBoxDesc) * 2 * np;
+    std::vector<unsigned char> img(items_off + 4 * (items_a.size() + items_b.size()), 0);
+    const int64_t es = (int64_t)dtype_size(p->dtype);
+    for (int q = 0; q < np; ++q) {
+        auto *maps = reinterpret_cast<CUtensorMap *>(img.data() + maps_off) + 2 * q;
+        const char *sb = static_cast<const char *>(p->state) + (int64_t)q * g.box * es;
+        const char *wb = static_cast<const char *>(p->work) + (int64_t)q * g.box * es;
+        // sweep A boxes are TXA+8 x TYA+4, sweep B boxes TXB+8 x TYB+4: one map each
+        if ((rc = make_tensor_map_4d(&maps[0], sb, p->dtype, g.js, n + 2 * kPatchRY, n + 2 * kPatchRZ, 4, g.js * es,
+                                     g.ks * es, g.plane * es, PT::TXA + 8, PT::TYA + 4, 1, 4)))
+            return rc;
+        if ((rc = make_tensor_map_4d(&maps[1], wb, p->dtype, g.js, n + 2 * kPatchRY, n + 2 * kPatchRZ, 4, g.js * es,
+                                     g.ks * es, g.plane * es, PT::TXB + 8, PT::TYB + 4, 1, 4)))
+            return rc;
+    }
+    std::memcpy(img.data() + desc_off, desc.data(), sizeof(EnsBoxDesc) * desc.size());
+    std::memcpy(img.data() + items_off, items_a.data(), 4 * items_a.size());
+    std::memcpy(img.data() + items_off + 4 * items_a.size(), items_b.data(), 4 * items_b.size());
+    AXS_CUDA_CHECK(cudaMemcpyAsync(p->table, img.data(), img.size(), cudaMemcpyHostToDevice, st));
+    AXS_CUDA_CHECK(cudaStreamSynchronize(st));
+    out.items_a = (int64_t)items_a.size();
+    out.items_b = (int64_t)items_b.size();
+    out.grid_a = (int)std::min<int64_t>(out.items_a, (int64_t)ba * sms);
+    out.grid_b = (int)std::min<int64_t>(out.items_b, (int64_t)bb * sms);
+    return AXS_OK;
+}
+
+template <typename T>
+static int patch_step(const axs_patches *p, const PatchGeom &g, const axs_patch_plan &plan, const axs_background &bg,
+                      double tau_i, double t, double dt, cudaStream_t st)
+{
+    using PT = PatchTilings<T>;
+    char *table = static_cast<char *>(p->table);
+    const int np = p->npatches;
+    SweepArgs<T> a{};
+    fill_step_constants(a, p->dx, dt);
+    a.ox = kPatchOX;
+    a.status = reinterpret_cast<unsigned *>(table);
+    a.maps = reinterpret_cast<const CUtensorMap *>(table + kPatchHeader);
+    a.boxes = reinterpret_cast<const EnsBoxDesc *>(table + kPatchHeader + 2 * sizeof(CUtensorMap) * np);
+    const uint32_t *items = reinterpret_cast<const uint32_t *>(a.boxes + 2 * np);
+    T *state = static_cast<T *>(p->state), *work = static_cast<T *>(p->work);
+    CUtensorMap unused;
+    std::memset(&unused, 0, sizeof(unused));
+    SweepArgs<T> aa = a;
+    aa.items = items;
+    aa.n_items = plan.items_a;
+    aa.map_sel = 0;
+    aa.c1 = stage_coef<T>(bg, tau_i + t);
+    aa.c2 = stage_coef<T>(bg, tau_i + t + 0.5 * dt);
+    for (int c = 0; c < 8; ++c) aa.out[c] = work + c * g.plane;
+    int rc = PT::LA::launch(unused, aa, plan.grid_a, st);
+    if (rc) return rc;
+    SweepArgs<T> ab = a;
+    ab.items = items + plan.items_a;
+    ab.n_items = plan.items_b;
+    ab.map_sel = 1;
+    ab.c2 = aa.c2;
+    ab.c4 = stage_coef<T>(bg, tau_i + t + dt);
+    for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.plane;
+    for (int c = 0; c < 4; ++c) ab.out[c] = state + c * g.plane;
+    return PT::LB::launch(unused, ab, plan.grid_b, st);
+}
+
+// ---------------------------------------------------------------- coarse <-> fine
+// Quartic Lagrange weights on coarse nodes -2..2 at offset -1/4 (s = 0) and
+// +1/4 (s = 1) from the parent's centre, in coarse-cell units.
+struct QuarticWeights {
+    double w[2][5];
+};
+
+static QuarticWeights quartic_weights()
+{
+    QuarticWeights q;
+    for (int s = 0; s < 2; ++s) {
+        const double xi = s == 0 ? -0.25 : 0.25;
+        for (int k = 0; k < 5; ++k) {
+            double num = 1.0, den = 1.0;
+            for (int m = 0; m < 5; ++m) {
+                if (m == k) continue;
+                num *= xi - (m - 2);
+                den *= (double)(k - m);
+            }
+            q.w[s][k] = num / den;
+        }
+    }
+    return q;
+}
+
+struct CoarseView {
+    const void *old_state, *new_state;  // level layout (new may equal old)
+    int nx, ny, nz;
+    int64_t js, ks, cs;
+    int ox, oy;
+};
+
+__device__ __forceinline__ int pwrap(int i, int n)
+{
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+// value of coarse component c interpolated to fine global cell (gx, gy, gz)
+template <typename T>
+__device__ __forceinline__ double coarse_interp(const T *__restrict__ cs, const CoarseView &v, int c, int gx, int gy,
+                                                int gz, const QuarticWeights &q)
+{
+    const int px = gx >> 1, py = gy >> 1, pz = gz >> 1;  // parent (floor for negative after wrap below)
+    const double *wx = q.w[gx & 1], *wy = q.w[gy & 1], *wz = q.w[gz & 1];
+    double acc = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < 5; ++k) {
+        const int zz = pwrap(pz + k - 2, v.nz);
+        double accy = 0.0;
+#pragma unroll 1
+        for (int j = 0; j < 5; ++j) {
+            const int yy = pwrap(py + j - 2, v.ny);
+            const T *row = cs + c * v.cs + (int64_t)(yy + v.oy) * v.js + (int64_t)zz * v.ks + v.ox;
+            double accx = 0.0;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) accx += wx[i] * (double)row[pwrap(px + i - 2, v.nx)];
+            accy += wy[j] * accx;
+        }
+        acc += wz[k] * accy;
+    }
+    return acc;
+}
+
+struct FillArgs {
+    int n, np;              // fine patch side, patch count
+    int nbx, nby, nbz;      // block grid of the coarse level
+    const int *patch_block; // 3 per patch
+    const int *block_patch; // nbx*nby*nbz -> patch or -1
+    int64_t js, ks, box, plane;
+    double theta, hdt;      // time fraction in the coarse step, coarse dt
+    int valid_too;          // 1: also the valid cells (initialisation)
+};
+
+template <typename T>
+__global__ void patch_fill_kernel(T *__restrict__ st, CoarseView cv, FillArgs f, QuarticWeights q)
+{
+    const int W = f.n + 2 * kRingX, H = f.n + 2 * kRingYZ;
+    const int64_t per = (int64_t)W * H * H;
+    const int64_t total = per * f.np;
+    const int nfx = cv.nx * 2, nfy = cv.ny * 2, nfz = cv.nz * 2;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int pq = (int)(idx / per);
+        const int64_t r = idx % per;
+        const int x = (int)(r % W) - kRingX, y = (int)((r / W) % H) - kRingYZ, z = (int)(r / ((int64_t)W * H)) - kRingYZ;
+        const bool inside = x >= 0 && x < f.n && y >= 0 && y < f.n && z >= 0 && z < f.n;
+        if (inside && !f.valid_too) continue;
+        const int bx = f.patch_block[3 * pq], by = f.patch_block[3 * pq + 1], bz = f.patch_block[3 * pq + 2];
+        const int gx = pwrap(bx * f.n + x, nfx), gy = pwrap(by * f.n + y, nfy), gz = pwrap(bz * f.n + z, nfz);
+        T *dst = st + (int64_t)pq * f.box + (x + kPatchOX) + (int64_t)(y + kPatchRY) * f.js + (int64_t)(z + kPatchRZ) * f.ks;
+        int src_patch = -1;
+        if (!inside) {
+            const int ob = (gx / f.n) + f.nbx * ((gy / f.n) + f.nby * (gz / f.n));
+            src_patch = f.block_patch[ob];
+        }
+        if (src_patch >= 0) {
+            const int lx = gx % f.n, ly = gy % f.n, lz = gz % f.n;
+            const T *src = st + (int64_t)src_patch * f.box + (lx + kPatchOX) + (int64_t)(ly + kPatchRY) * f.js +
+                           (int64_t)(lz + kPatchRZ) * f.ks;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) dst[c * f.plane] = src[c * f.plane];
+            continue;
+        }
+        const T *c0 = static_cast<const T *>(cv.old_state), *c1 = static_cast<const T *>(cv.new_state);
+        T *d0 = dst;
+#pragma unroll 1
+        for (int c = 0; c < 2; ++c) {  // (psi_c, Pi_c) pairs
+            if (f.theta == 0.0) {
+                d0[c * f.plane] = (T)coarse_interp<T>(c0, cv, c, gx, gy, gz, q);
+                d0[(2 + c) * f.plane] = (T)coarse_interp<T>(c0, cv, 2 + c, gx, gy, gz, q);
+            } else {
+                const double p0 = coarse_interp<T>(c0, cv, c, gx, gy, gz, q);
+                const double q0 = coarse_interp<T>(c0, cv, 2 + c, gx, gy, gz, q);
+                const double p1 = coarse_interp<T>(c1, cv, c, gx, gy, gz, q);
+                const double q1 = coarse_interp<T>(c1, cv, 2 + c, gx, gy, gz, q);
+                const double s = f.theta, s2 = s * s, s3 = s2 * s;
+                const double h00 = 2 * s3 - 3 * s2 + 1, h10 = s3 - 2 * s2 + s, h01 = -2 * s3 + 3 * s2, h11 = s3 - s2;
+                // psi: cubic Hermite with dpsi/dtau = Pi; Pi: linear
+                d0[c * f.plane] = (T)(h00 * p0 + h10 * f.hdt * q0 + h01 * p1 + h11 * f.hdt * q1);
+                d0[(2 + c) * f.plane] = (T)((1.0 - s) * q0 + s * q1);
+            }
+        }
+    }
+}
+
+// Mean of the 8 fine children of every coarse cell a patch covers (amrex::average_down).
+template <typename T>
+__global__ void patch_average_down_kernel(const T *__restrict__ st, T *__restrict__ coarse, CoarseView cv, FillArgs f)
+{
+    const int m = f.n / 2;
+    const int64_t per = (int64_t)m * m * m, total = per * f.np;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int pq = (int)(idx / per);
+        const int64_t r = idx % per;
+        const int cx = (int)(r % m), cy = (int)((r / m) % m), cz = (int)(r / ((int64_t)m * m));
+        const int bx = f.patch_block[3 * pq], by = f.patch_block[3 * pq + 1], bz = f.patch_block[3 * pq + 2];
+        const int gx = bx * m + cx, gy = by * m + cy, gz = bz * m + cz;
+        for (int c = 0; c < 4; ++c) {
+            double s = 0.0;
+            for (int d = 0; d < 8; ++d) {
+                const int fx = 2 * cx + (d & 1), fy = 2 * cy + ((d >> 1) & 1), fz = 2 * cz + (d >> 2);
+                s += (double)st[c * f.plane + (int64_t)pq * f.box + (fx + kPatchOX) + (int64_t)(fy + kPatchRY) * f.js +
+                                (int64_t)(fz + kPatchRZ) * f.ks];
+            }
+            coarse[c * cv.cs + (gx + cv.ox) + (int64_t)(gy + cv.oy) * cv.js + (int64_t)gz * cv.ks] = (T)(0.125 * s);
+        }
+    }
+}
+
+static int grid_cells(int64_t n)
+{
+    const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 16));
+}
+
+static int coarse_view(const axs_level *coarse_old, const axs_level *coarse_new, int32_t dtype, CoarseView &v)
+{
+    AXS_REQUIRE(coarse_old != nullptr && coarse_old->state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null coarse level");
+    AXS_REQUIRE(coarse_old->dtype == dtype, AXS_ERR_INVALID_ARGUMENT, "coarse level and patches differ in dtype");
+    LevelGeom g;
+    int rc = level_geom(coarse_old->dtype, coarse_old->nx, coarse_old->ny, coarse_old->nz, g);
+    if (rc) return rc;
+    if (coarse_new) {
+        AXS_REQUIRE(coarse_new->state && coarse_new->nx == coarse_old->nx && coarse_new->ny == coarse_old->ny &&
+                        coarse_new->nz == coarse_old->nz && coarse_new->dtype == dtype,
+                    AXS_ERR_INVALID_ARGUMENT, "coarse old/new levels differ");
+    }
+    v = CoarseView{coarse_old->state, coarse_new ? coarse_new->state : coarse_old->state, coarse_old->nx,
+                   coarse_old->ny, coarse_old->nz, g.js, g.ks, g.cs, g.ox, g.oy};
+    return AXS_OK;
+}
+
+static int fill_args(const axs_patches *p, const PatchGeom &g, const axs_patch_map *m, const CoarseView &cv,
+                     FillArgs &f)
+{
+    AXS_REQUIRE(m != nullptr && m->patch_block != nullptr && m->block_patch != nullptr, AXS_ERR_INVALID_ARGUMENT,
+                "null patch map");
+    AXS_REQUIRE(g.n % 2 == 0 && cv.nx * 2 % g.n == 0 && cv.ny * 2 % g.n == 0 && cv.nz * 2 % g.n == 0,
+                AXS_ERR_UNSUPPORTED, "the coarse level must tile into blocks of %d cells", g.n / 2);
+    f.n = g.n;
+    f.np = p->npatches;
+    f.nbx = cv.nx * 2 / g.n;
+    f.nby = cv.ny * 2 / g.n;
+    f.nbz = cv.nz * 2 / g.n;
+    f.patch_block = m->patch_block;
+    f.block_patch = m->block_patch;
+    f.js = g.js;
+    f.ks = g.ks;
+    f.box = g.box;
+    f.plane = g.plane;
+    f.theta = 0.0;
+    f.hdt = 0.0;
+    f.valid_too = 0;
+    return AXS_OK;
+}
+
+}  // namespace axs
+
+using namespace axs;
+
+extern "C" {
+
+int axs_patches_layout(int32_t dtype, int32_t n, int32_t npatches, axs_patch_layout *out)
+{
+    AXS_REQUIRE(out != nullptr, AXS_ERR_INVALID_ARGUMENT, "null output");
+    PatchGeom g;
+    int rc = patch_geom(dtype, n, npatches, g);
+    if (rc) return rc;
+    const int64_t es = (int64_t)dtype_size(dtype);
+    out->jstride = g.js;
+    out->kstride = g.ks;
+    out->patch_elems = g.box;
+    out->plane_elems = g.plane;
+    out->x_offset = kPatchOX;
+    out->y_offset = kPatchRY;
+    out->z_offset = kPatchRZ;
+    out->state_bytes = 4 * g.plane * es;
+    out->work_bytes = 8 * g.plane * es;
+    out->table_bytes = patch_table_bytes(g, npatches);
+    return AXS_OK;
+}
+
+int axs_patches_init(const axs_patches *p, axs_patch_plan *plan, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(p, g);
+    if (rc) return rc;
+    AXS_REQUIRE(plan != nullptr, AXS_ERR_INVALID_ARGUMENT, "null plan");
+    PatchTableOut o{};
+    rc = p->dtype == AXS_F32 ? build_patch_table<float>(p, g, (cudaStream_t)stream, o)
+                             : build_patch_table<double>(p, g, (cudaStream_t)stream, o);
+    if (rc) return rc;
+    plan->items_a = o.items_a;
+    plan->items_b = o.items_b;
+    plan->grid_a = o.grid_a;
+    plan->grid_b = o.grid_b;
+    return AXS_OK;
+}
+
+int axs_patches_rk4_step(const axs_patches *p, const axs_patch_plan *plan, const axs_background *bg, double tau_i,
+                         double t, double dt, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(p, g);
+    if (rc) return rc;
+    AXS_REQUIRE(plan != nullptr && bg != nullptr && plan->items_a > 0 && plan->items_b > 0, AXS_ERR_INVALID_ARGUMENT,
+                "null or empty plan (run axs_patches_init)");
+    AXS_REQUIRE(std::isfinite(dt) && dt > 0.0, AXS_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->dtype == AXS_F32 ? patch_step<float>(p, g, *plan, *bg, tau_i, t, dt, st)
+                               : patch_step<double>(p, g, *plan, *bg, tau_i, t, dt, st);
+}
+
+int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse_old,
+                     const axs_level *coarse_new, double theta, double coarse_dt, int32_t valid_too, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(p, g);
+    if (rc) return rc;
+    CoarseView cv;
+    if ((rc = coarse_view(coarse_old, coarse_new, p->dtype, cv))) return rc;
+    FillArgs f;
+    if ((rc = fill_args(p, g, m, cv, f))) return rc;
+    AXS_REQUIRE(theta >= 0.0 && theta <= 1.0, AXS_ERR_INVALID_ARGUMENT, "theta must be in [0, 1]");
+    AXS_REQUIRE(theta == 0.0 || coarse_new != nullptr, AXS_ERR_INVALID_ARGUMENT, "theta > 0 needs the new coarse state");
+    f.theta = theta;
+    f.hdt = coarse_dt;
+    f.valid_too = valid_too != 0;
+    const QuarticWeights q = quartic_weights();
+    const int64_t total = (int64_t)(g.n + 2 * kRingX) * (g.n + 2 * kRingYZ) * (g.n + 2 * kRingYZ) * p->npatches;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (p->dtype == AXS_F32)
+        patch_fill_kernel<float><<<grid_cells(total), 256, 0, st>>>(static_cast<float *>(p->state), cv, f, q);
+    else
+        patch_fill_kernel<double><<<grid_cells(total), 256, 0, st>>>(static_cast<double *>(p->state), cv, f, q);
+    return launch_status("patch fill");
+}
+
+int axs_patches_average_down(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(p, g);
+    if (rc) return rc;
+    CoarseView cv;
+    if ((rc = coarse_view(coarse, nullptr, p->dtype, cv))) return rc;
+    FillArgs f;
+    if ((rc = fill_args(p, g, m, cv, f))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t total = (int64_t)(g.n / 2) * (g.n / 2) * (g.n / 2) * p->npatches;
+    if (p->dtype == AXS_F32)
+        patch_average_down_kernel<float><<<grid_cells(total), 256, 0, st>>>(
+            static_cast<const float *>(p->state), static_cast<float *>(coarse->state), cv, f);
+    else
+        patch_average_down_kernel<double><<<grid_cells(total), 256, 0, st>>>(
+            static_cast<const double *>(p->state), static_cast<double *>(coarse->state), cv, f);
+    if ((rc = launch_status("average down"))) return rc;
+    LevelGeom lg;
+    level_geom(coarse->dtype, coarse->nx, coarse->ny, coarse->nz, lg);
+    return level_fill_ghosts(coarse->state, coarse->dtype, coarse->nx, coarse->ny, coarse->nz, lg, 4, st);
+}
+
+int axs_patches_device_status(const axs_patches *p, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(p, g);
+    if (rc) return rc;
+    unsigned host = 0;
+    unsigned *dev = static_cast<unsigned *>(p->table);
+    AXS_CUDA_CHECK(cudaMemcpyAsync(&host, dev, sizeof(unsigned), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    AXS_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    if (host) {
+        AXS_CUDA_CHECK(cudaMemsetAsync(dev, 0, sizeof(unsigned), (cudaStream_t)stream));
+        AXS_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+        set_error("a device-side wait timed out (status word 0x%x)", host);
+        return AXS_ERR_DEVICE_TIMEOUT;
+    }
+    return AXS_OK;
+}
+
+}  // extern "C"

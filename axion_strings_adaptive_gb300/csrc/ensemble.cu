@@ -366,6 +366,12 @@ int axs_ensemble_init(const axs_ensemble *e, axs_ensemble_plan *plan, void *stre
         d.js = geo.g[b].js;
         d.ks = geo.g[b].ks;
         d.base = geo.base[b];
+        d.xlo = d.ylo = d.zlo = 0;
+        d.oy = geo.g[b].oy;
+        d.oz = 0;
+        d.periodic = 1;
+        d.map_box = b;
+        d.pad = 0;
     }
     // work items: longest chunks first, then box-major, tile-fastest
     std::vector<int> order(nb);

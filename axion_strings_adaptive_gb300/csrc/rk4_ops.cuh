@@ -35,7 +35,8 @@ struct ForwardA {
             o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol);
+        for (int c = 0; c < 4; ++c)
+            store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol, b.periodic);
 #pragma unroll
         for (int c = 4; c < 8; ++c) st_out<T, V, HINT>(a.out[c] + off, o[c], pol);
     }
@@ -62,7 +63,8 @@ struct ForwardB {
             o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[3][v]));
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol);
+        for (int c = 0; c < 4; ++c)
+            store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol, b.periodic);
     }
 };
 

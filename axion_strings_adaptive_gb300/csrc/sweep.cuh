@@ -48,7 +48,7 @@ template <typename T> struct SweepArgs {
     double inv_lambda0;          // adjoint: dlambda_s/dlambda0 = lambda_s / lambda0
     double *lam_partial;         // adjoint: one lambda0-gradient partial per block
     unsigned *status;
-    // ensemble sweeps: box table, packed work items (box << 20 | item in box),
+    // box-table sweeps: box table, packed work items (box << 16 | item in box),
     // two tensor maps per box (state, stage buffers) and which one this sweep reads
     const struct EnsBoxDesc *boxes;
     const uint32_t *items;
@@ -56,15 +56,24 @@ template <typename T> struct SweepArgs {
     int map_sel;
 };
 
-// One box of an ensemble (device table entry). Element offsets are relative to
-// the arena base of each component plane.
+// One box of a box table (device table entry): an ensemble member, or the
+// sweep domain of one refined patch. Element offsets are relative to the arena
+// base of each component plane. The sweep covers the domain
+// [xlo, xlo+nx) x [ylo, ylo+ny) x [zlo, zlo+nz) (box coordinates, valid cell
+// (0,0,0) at padded position (ox, oy, oz)); periodic boxes wrap z by plane
+// index and write periodic copies, patches read and write explicit ghost rings.
 struct EnsBoxDesc {
     int nx, ny, nz;
     int tiles_x, ntiles, zchunk;
     int64_t js, ks;
     int64_t base;  // element offset of the box's (padded) origin in every component plane
+    int xlo, ylo, zlo;
+    int oy, oz;    // padded row / plane of valid y = 0 / z = 0
+    int periodic;  // 1: wrap z, write periodic copies; 0: explicit ghost rings
+    int map_box;   // tensor maps 2*map_box (state) and 2*map_box + 1 (stage buffers)
+    int pad;
 };
-constexpr int kEnsItemBits = 20;  // work items per box < 2^20; boxes < 2^12
+constexpr int kEnsItemBits = 16;  // work items per box < 2^16; boxes < 2^16
 
 // Geometry of the box a work item belongs to, and the item's number in it.
 struct BoxGeom {
@@ -73,25 +82,31 @@ struct BoxGeom {
     int64_t js, ks, base;
     const CUtensorMap *map;
     int64_t local;
+    int xlo, ylo, zlo, oy, oz;
+    bool periodic;
 };
 
 // Work-item sources.
-struct SingleLevel {  // the one level described by the launch parameters
+struct SingleLevel {  // the one periodic level described by the launch parameters
     template <typename T>
     __device__ __forceinline__ static BoxGeom item(const SweepArgs<T> &a, const CUtensorMap *map, int64_t it)
     {
-        return BoxGeom{a.nx, a.ny, a.nz, a.tiles_x, a.ntiles, a.zchunk, a.js, a.ks, 0, map, it};
+        return BoxGeom{a.nx, a.ny, a.nz, a.tiles_x, a.ntiles, a.zchunk, a.js, a.ks, 0, map, it, 0, 0, 0, 2, 0, true};
     }
 };
-struct BoxTable {  // the boxes of an ensemble
+struct BoxTable {  // the boxes of an ensemble, or the patches of a refined level
     template <typename T>
     __device__ __forceinline__ static BoxGeom item(const SweepArgs<T> &a, const CUtensorMap *, int64_t it)
     {
         const uint32_t e = __ldg(a.items + it);
         const int b = (int)(e >> kEnsItemBits);
         const EnsBoxDesc &d = a.boxes[b];
-        return BoxGeom{d.nx, d.ny, d.nz, d.tiles_x, d.ntiles, d.zchunk, d.js, d.ks, d.base,
-                       a.maps + 2 * b + a.map_sel, (int64_t)(e & ((1u << kEnsItemBits) - 1))};
+        return BoxGeom{d.nx,    d.ny,     d.nz,
+                       d.tiles_x, d.ntiles, d.zchunk,
+                       d.js,    d.ks,     d.base,
+                       a.maps + 2 * d.map_box + a.map_sel, (int64_t)(e & ((1u << kEnsItemBits) - 1)),
+                       d.xlo,   d.ylo,    d.zlo,
+                       d.oy,    d.oz,     d.periodic != 0};
     }
 };
 
@@ -125,9 +140,10 @@ __device__ __forceinline__ void st_out(T *p, const T *v, uint64_t pol)
 // in the x/y padding (4 columns, 2 rows).
 template <typename T, int V, bool HINT = false>
 __device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
-                                                  const T *v, uint64_t pol = 0)
+                                                  const T *v, uint64_t pol = 0, bool periodic = true)
 {
     st_out<T, V, HINT>(base + off, v, pol);
+    if (!periodic) return;
     if (x < 4) st_out<T, V, HINT>(base + off + nx, v, pol);
     if (x >= nx - 4) st_out<T, V, HINT>(base + off - nx, v, pol);
     if (y < 2) st_out<T, V, HINT>(base + off + (int64_t)ny * js, v, pol);
@@ -186,30 +202,43 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     int64_t p_item = blockIdx.x;
     int p_k = 0, p_len = 0, p_za = 0, p_nz = 1, p_x = 0, p_y = 0;
     const CUtensorMap *p_map = &tmap;
+    int p_oy = 2, p_oz = 0;
+    bool p_wrap = true;
     auto p_start = [&]() {
         if (p_item >= a.n_items) return;
         const BoxGeom b = Src::item(a, &tmap, p_item);
         const int tile = (int)(b.local % b.ntiles);
-        p_za = (int)(b.local / b.ntiles) * b.zchunk;
-        p_len = min(b.zchunk, b.nz - p_za);
+        const int c0 = (int)(b.local / b.ntiles) * b.zchunk;
+        p_za = b.zlo + c0;
+        p_len = min(b.zchunk, b.nz - c0);
         p_nz = b.nz;
-        p_x = (tile % b.tiles_x) * TX;
-        p_y = (tile / b.tiles_x) * TY;
+        p_x = b.xlo + (tile % b.tiles_x) * TX;
+        p_y = b.ylo + (tile / b.tiles_x) * TY;
+        p_oy = b.oy;
+        p_oz = b.oz;
+        p_wrap = b.periodic;
         p_map = b.map;
         if constexpr (!std::is_same<Src, SingleLevel>::value) fence_tensormap_acquire(p_map);
     };
     int64_t q_issued = 0;
     auto issue_one = [&]() -> bool {
         if (p_item >= a.n_items) return false;
-        int zp = (p_za - 2 + p_k) % p_nz;
-        if (zp < 0) zp += p_nz;
+        int zp = p_za - 2 + p_k;
+        if (p_wrap) {
+            zp %= p_nz;
+            if (zp < 0) zp += p_nz;
+        } else {
+            zp += p_oz;  // explicit ghost planes: padded plane index, no wrap
+        }
         const int slot = (int)(q_issued % NS);
         mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
-        // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned)
+        // box x starts 4 columns left of the tile: padded column ox + x0 - 4 (16-byte aligned);
+        // box y starts 2 rows above the tile: padded row y0 - 2 + oy
         if constexpr (HINT)
-            tma_load_4d_hint(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y, zp, 0, &full[slot], pol_last);
+            tma_load_4d_hint(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y - 2 + p_oy, zp, 0, &full[slot],
+                             pol_last);
         else
-            tma_load_4d(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y, zp, 0, &full[slot]);
+            tma_load_4d(ring + (size_t)slot * S::SLOT, p_map, a.ox - 4 + p_x, p_y - 2 + p_oy, zp, 0, &full[slot]);
         ++q_issued;
         if (++p_k == p_len + 4) {
             p_k = 0;
@@ -231,16 +260,18 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const BoxGeom b = Src::item(a, &tmap, item);
         const int tile = (int)(b.local % b.ntiles);
-        const int za = (int)(b.local / b.ntiles) * b.zchunk;
-        const int len = min(b.zchunk, b.nz - za);
-        const int x = (tile % b.tiles_x) * TX + V * tx;
-        const int y = (tile / b.tiles_x) * TY + ty;
-        const bool active = (x < b.nx) && (y < b.ny);
+        const int c0 = (int)(b.local / b.ntiles) * b.zchunk;
+        const int za = b.zlo + c0;
+        const int len = min(b.zchunk, b.nz - c0);
+        const int x = b.xlo + (tile % b.tiles_x) * TX + V * tx;
+        const int y = b.ylo + (tile / b.tiles_x) * TY + ty;
+        const bool active = (x < b.xlo + b.nx) && (y < b.ylo + b.ny);
         // pointwise components of the next plane, loaded one iteration ahead
         T pn[NPT > 0 ? NPT : 1][V];
         if constexpr (NPT > 0) {
             if (active) {
-                const int64_t off0 = b.base + (int64_t)(x + a.ox) + (int64_t)(y + 2) * b.js + (int64_t)za * b.ks;
+                const int64_t off0 =
+                    b.base + (int64_t)(x + a.ox) + (int64_t)(y + b.oy) * b.js + (int64_t)(za + b.oz) * b.ks;
 #pragma unroll
                 for (int c = 0; c < NPT; ++c) {
                     if constexpr (HINT)
@@ -252,7 +283,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
         }
         for (int m = 0; m < len; ++m) {
             const int z = za + m;
-            const int64_t off = b.base + (int64_t)(x + a.ox) + (int64_t)(y + 2) * b.js + (int64_t)z * b.ks;
+            const int64_t off = b.base + (int64_t)(x + a.ox) + (int64_t)(y + b.oy) * b.js + (int64_t)(z + b.oz) * b.ks;
 
             T pq[NPT > 0 ? NPT : 1][V];
             if constexpr (NPT > 0) {

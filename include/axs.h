@@ -325,6 +325,65 @@ int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *
 int axs_plaquette_winding_batch(const double *theta_dev, int64_t n, int32_t *w_dev, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Refined patches (the scale path's fine level; the reference's AMR is AMReX /
+ * GRTeclyn, absent from its tree): every patch refines one block^3 block of a
+ * periodic coarse level by 2 (n = 2 block fine cells per side, spacing dx/2,
+ * two fine steps per coarse step). Patches carry explicit ghost rings (6
+ * columns in x, 4 rows / planes in y, z); their state / work arenas are laid
+ * out like an ensemble's, padded position of valid (0,0,0) = (x_offset,
+ * y_offset, z_offset) inside each patch box of patch_elems elements.
+ * ------------------------------------------------------------------------- */
+typedef struct axs_patch_layout {
+    int64_t jstride, kstride, patch_elems, plane_elems;
+    int32_t x_offset, y_offset, z_offset;
+    int64_t state_bytes, work_bytes, table_bytes;
+} axs_patch_layout;
+
+typedef struct axs_patches {
+    int32_t dtype;
+    int32_t n;        /* fine cells per patch side */
+    int32_t npatches;
+    double dx;        /* fine spacing */
+    void *state;      /* 4 component planes */
+    void *work;       /* 8 component planes */
+    void *table;      /* written by axs_patches_init */
+    int64_t state_bytes, work_bytes, table_bytes;
+} axs_patches;
+
+typedef struct axs_patch_plan {
+    int64_t items_a, items_b;
+    int32_t grid_a, grid_b;
+} axs_patch_plan;
+
+/* Device arrays tying patches to coarse blocks: patch_block[3 q .. 3 q + 2] =
+ * block coordinates of patch q; block_patch[bx + nbx (by + nby bz)] = the patch
+ * refining that block or -1. */
+typedef struct axs_patch_map {
+    const int32_t *patch_block;
+    const int32_t *block_patch;
+} axs_patch_map;
+
+int axs_patches_layout(int32_t dtype, int32_t n, int32_t npatches, axs_patch_layout *out);
+/* Host-synchronous: writes the device table (sweep domains, work items, tensor maps). */
+int axs_patches_init(const axs_patches *p, axs_patch_plan *plan, void *stream);
+/* Ghost rings (valid_too = 1: the valid cells as well) at time fraction theta
+ * of the coarse step: ring cells owned by a patch are copied from it, the
+ * others interpolate the coarse level -- quartic Lagrange in space, in time
+ * cubic Hermite for psi (with Pi as its derivative) and linear for Pi between
+ * coarse_old (start of the coarse step) and coarse_new (its end; may be NULL
+ * when theta = 0). */
+int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse_old,
+                     const axs_level *coarse_new, double theta, double coarse_dt, int32_t valid_too, void *stream);
+/* One RK4 step of every patch (two persistent launches); the rings must hold
+ * psi, Pi at time t. */
+int axs_patches_rk4_step(const axs_patches *p, const axs_patch_plan *plan, const axs_background *bg, double tau_i,
+                         double t, double dt, void *stream);
+/* amrex::average_down: every coarse cell a patch covers becomes the mean of its
+ * 8 fine children (then the coarse periodic padding is refreshed). */
+int axs_patches_average_down(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse, void *stream);
+int axs_patches_device_status(const axs_patches *p, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Axion power spectrum (AxionStringsLevel.cpp:1583-1640): the masked a_dot
  * buffer, a caller-run unnormalised forward R2C (cuFFT), then shell binning.
  * ------------------------------------------------------------------------- */

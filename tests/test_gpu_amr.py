@@ -1,0 +1,172 @@
+"""Refined patches through the C ABI (the scale path's fine level):
+* a patch step with its ghost ring filled from a uniform fine level equals that
+  level's own step on the same cells, bit for bit;
+* the ring interpolation is exact for fields that are quartic polynomials
+  around the patch, and equals a numpy restatement on a random field;
+* with every block refined the patches evolve exactly as a uniform level of
+  twice the resolution (the coarse level never reaches their rings);
+* the homogeneous solution psi = R(tau), Pi = R'(tau) survives subcycling;
+* composite diagnostics count a straight string pair on the fine level."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _ring_from_level(patches, q, origin, fine):
+    """Fill patch q (valid + ring) from a periodic fine field (4, N, N, N)."""
+    n = patches.n
+    lay = patches.layout
+    N = fine.shape[-1]
+    box = patches.box(q)
+    ox, oy, oz = origin
+    xs = (ox + np.arange(-6, n + 6)) % N
+    ys = (oy + np.arange(-4, n + 4)) % N
+    zs = (oz + np.arange(-4, n + 4)) % N
+    sub = fine[:, zs][:, :, ys][:, :, :, xs]
+    box[:, lay.z_offset - 4:lay.z_offset + n + 4, lay.y_offset - 4:lay.y_offset + n + 4,
+        lay.x_offset - 6:lay.x_offset + n + 6] = sub
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_patch_step_matches_uniform_level(axs, dtype):
+    from axion_strings_adaptive_gb300 import ic
+    from axion_strings_adaptive_gb300.amr import Patches
+    Nf, n, dx = 64, 32, 0.25
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    s0 = ic.fourier_state(Nf, 6.0, seed=3)
+    s0[2:] = 0.1 * torch.randn_like(s0[2:])
+    s0 = s0.to(dtype)
+    fine = axs.PeriodicLevel(Nf, dx, dtype=dtype)
+    fine.set_state(s0)
+    origins = [(0, 0, 0), (32, 0, 32), (32, 32, 0)]
+    p = Patches(n, len(origins), dx, dtype=dtype)
+    for q, o in enumerate(origins):
+        _ring_from_level(p, q, o, s0.cuda())
+    p.step(bg, 1.0, 0.3, 0.05)
+    p.device_status()
+    fine.advance(bg, 1.0, 0.3, 0.05, 1)
+    ref = fine.get_state()
+    for q, (ox, oy, oz) in enumerate(origins):
+        assert torch.equal(p.valid(q), ref[:, oz:oz + n, oy:oy + n, ox:ox + n]), q
+
+
+def _quartic_weights():
+    w = np.zeros((2, 5))
+    for s, xi in enumerate((-0.25, 0.25)):
+        for k in range(5):
+            num = den = 1.0
+            for m in range(5):
+                if m != k:
+                    num *= xi - (m - 2)
+                    den *= k - m
+            w[s, k] = num / den
+    return w
+
+
+def test_interpolation_quartic_exact_and_restated(axs):
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block = 64, 16
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=torch.float64)
+    c = (np.arange(N) + 0.5)
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    xc = 24.0
+    poly = lambda x, y, z: (1.0 + 0.3 * (x - xc) - 0.02 * (x - xc) ** 4) * (0.5 + 0.1 * (y - xc) ** 3) + \
+        0.01 * (z - xc) ** 4 - 0.2 * (z - xc) * (y - xc)
+    st = np.stack([poly(X, Y, Z), poly(Y, Z, X), poly(Z, X, Y), 0.5 * poly(X, Z, Y)])
+    coarse.set_state(torch.from_numpy(st).cuda())
+    two = TwoLevel(coarse, block)
+    two.set_blocks(np.array([[1, 1, 1]]))  # coarse cells 16..31: its 5-point stencils stay inside 11..36
+    p = two.patches
+    box = p.box(0).cpu().numpy()
+    n, lay = p.n, p.layout
+    f = (np.arange(-4, n + 4) + 0.5) * 0.5 + 16.0  # fine centres in coarse units (coarse x = c + 0.5)
+    fx = (np.arange(-6, n + 6) + 0.5) * 0.5 + 16.0
+    FZ, FY, FX = np.meshgrid(f, f, fx, indexing="ij")
+    exact = np.stack([poly(FX, FY, FZ), poly(FY, FZ, FX), poly(FZ, FX, FY), 0.5 * poly(FX, FZ, FY)])
+    got = box[:, lay.z_offset - 4:lay.z_offset + n + 4, lay.y_offset - 4:lay.y_offset + n + 4,
+              lay.x_offset - 6:lay.x_offset + n + 6]
+    np.testing.assert_allclose(got, exact, rtol=1e-12, atol=1e-10 * np.abs(exact).max())
+
+    # a random field: the device interpolation equals a numpy restatement
+    rng = np.random.default_rng(5)
+    st = rng.standard_normal((4, N, N, N))
+    coarse.set_state(torch.from_numpy(st).cuda())
+    two.set_blocks(np.zeros((0, 3)))
+    two.set_blocks(np.array([[3, 0, 2]]))  # wraps in x and y around the periodic seam
+    w = _quartic_weights()
+    box = two.patches.box(0).cpu().numpy()
+    for (x, y, z) in [(0, 0, 0), (-6, 5, -4), (n + 5, n + 3, 7), (13, -1, n + 2)]:
+        gx, gy, gz = 3 * 32 + x, 0 * 32 + y, 2 * 32 + z
+        val = 0.0
+        for k in range(5):
+            for j in range(5):
+                for i in range(5):
+                    cx, cy, cz = (gx // 2 + i - 2) % N, (gy // 2 + j - 2) % N, (gz // 2 + k - 2) % N
+                    val += w[gx % 2, i] * w[gy % 2, j] * w[gz % 2, k] * st[0, cz, cy, cx]
+        got = box[0, z + lay.z_offset, y + lay.y_offset, x + lay.x_offset]
+        assert got == pytest.approx(val, rel=1e-12, abs=1e-12)
+
+
+def test_fully_refined_patches_evolve_as_uniform_fine_level(axs):
+    from axion_strings_adaptive_gb300 import ic
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block = 32, 16
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=torch.float32)
+    coarse.set_state(ic.fourier_state(N, 5.0, seed=9).float())
+    two = TwoLevel(coarse, block)
+    nb = N // block
+    two.set_blocks(np.array([[x, y, z] for z in range(nb) for y in range(nb) for x in range(nb)]))
+    n = two.patches.n
+    fine = axs.PeriodicLevel(2 * N, 0.25, dtype=torch.float32)
+    full = torch.empty((4, 2 * N, 2 * N, 2 * N), dtype=torch.float32, device="cuda")
+    for q, (bx, by, bz) in enumerate(two.blocks):
+        full[:, bz * n:(bz + 1) * n, by * n:(by + 1) * n, bx * n:(bx + 1) * n] = two.patches.valid(q)
+    fine.set_state(full)
+    two.advance(bg, 1.0, 0.0, 0.1, 3)
+    two.device_status()
+    fine.advance(bg, 1.0, 0.0, 0.05, 6)
+    ref = fine.get_state()
+    for q, (bx, by, bz) in enumerate(two.blocks):
+        assert torch.equal(two.patches.valid(q), ref[:, bz * n:(bz + 1) * n, by * n:(by + 1) * n,
+                                                    bx * n:(bx + 1) * n]), q
+
+
+def test_homogeneous_solution_survives_subcycling(axs):
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block = 64, 16
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)  # RD: R = tau, R' = 1, kappa = 0
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=torch.float64)
+    st = torch.zeros((4, N, N, N), dtype=torch.float64)
+    st[0], st[2] = 1.0, 1.0
+    coarse.set_state(st.cuda())
+    two = TwoLevel(coarse, block)
+    two.set_blocks(np.array([[0, 0, 0], [1, 0, 0], [3, 2, 1]]))
+    two.advance(bg, 1.0, 0.0, 0.1, 5)
+    two.device_status()
+    for q in range(two.patches.npatches):
+        v = two.patches.valid(q)
+        assert torch.allclose(v[0], torch.full_like(v[0], 1.5), rtol=1e-13, atol=0)
+        assert torch.allclose(v[2], torch.full_like(v[2], 1.0), rtol=1e-13, atol=0)
+        assert float(v[1].abs().max()) < 1e-14 and float(v[3].abs().max()) < 1e-14
+
+
+def test_composite_diagnostics_straight_strings(axs):
+    from test_gpu_physics import straight_string_pair
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, nz, dx, block = 64, 64, 0.5, 16
+    bg = axs.Background.expanding(2.0, 1.0)
+    v = bg.values(1.0)
+    coarse = axs.PeriodicLevel((N, N, nz), dx, dtype=torch.float64)
+    coarse.set_state(torch.from_numpy(straight_string_pair(N, nz, dx, v.R, v.m_r, v.R_prime_over_R)).cuda())
+    two = TwoLevel(coarse, block)
+    nref = two.regrid(n_error_buf=4)
+    assert 0 < nref < (N // block) ** 2 * (nz // block)
+    d = two.diagnostics(bg, 1.0)
+    # both strings run through refined blocks only: 2 pierced fine xy plaquettes per fine layer
+    assert d.n_p_plain == 2 * (2 * nz) and d.n_patches == nref
+    d0 = coarse.diagnostics(bg, 1.0)
+    # the same string length: twice the plaquettes at half the spacing (ell = (2/3) N_p dx)
+    assert d.xi_plain == pytest.approx(d0.xi_plain, rel=1e-12)
