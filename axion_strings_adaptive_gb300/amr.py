@@ -93,8 +93,11 @@ class TwoLevel:
             raise ValueError("the coarse level must tile into blocks")
         self.coarse, self.block = coarse, int(block)
         self.nb = (coarse.nx // block, coarse.ny // block, coarse.nz // block)
-        self.old = PeriodicLevel((coarse.nx, coarse.ny, coarse.nz), coarse.dx, dtype=coarse.dtype,
-                                 device=coarse.state.device, pierced_capacity=1, tile_config=coarse.tile_config)
+        # the coarse state at the start of the running coarse step (state only: the
+        # ghost fill reads nothing else)
+        self.old_state = torch.empty_like(coarse.state)
+        self.old_c = L.LevelC(self.old_state.data_ptr(), coarse.work.data_ptr(), coarse.c.dtype, coarse.nx, coarse.ny,
+                              coarse.nz, coarse.dx, 0)
         self.patches: Patches | None = None
         self.blocks = np.zeros((0, 3), dtype=np.int32)
         dev = coarse.state.device
@@ -148,10 +151,10 @@ class TwoLevel:
             if self.patches is None:
                 self.coarse.advance(bg, tau_i, t, dt, 1)
                 continue
-            self.old.state.copy_(self.coarse.state)
+            self.old_state.copy_(self.coarse.state)
             self.coarse.advance(bg, tau_i, t, dt, 1)
             for f, theta in enumerate((0.0, 0.5)):
-                L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.old.c),
+                L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.old_c),
                        C.byref(self.coarse.c), theta, dt, 0, None)
                 self.patches.step(bg, tau_i, t + f * 0.5 * dt, 0.5 * dt)
 

@@ -255,30 +255,34 @@ __device__ __forceinline__ int pwrap(int i, int n)
     return i < 0 ? i + n : i;
 }
 
-// value of coarse component c interpolated to fine global cell (gx, gy, gz)
+// value of coarse component c interpolated to fine global cell (gx, gy, gz),
+// accumulated in the field precision (FP32 fields: FP32 arithmetic)
 template <typename T>
 __device__ __forceinline__ double coarse_interp(const T *__restrict__ cs, const CoarseView &v, int c, int gx, int gy,
                                                 int gz, const QuarticWeights &q)
 {
-    const int px = gx >> 1, py = gy >> 1, pz = gz >> 1;  // parent (floor for negative after wrap below)
-    const double *wx = q.w[gx & 1], *wy = q.w[gy & 1], *wz = q.w[gz & 1];
-    double acc = 0.0;
+    const int px = gx >> 1, py = gy >> 1, pz = gz >> 1;  // parent (gx >= 0)
+    const int sx = gx & 1, sy = gy & 1, sz = gz & 1;
+    int xi[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) xi[i] = pwrap(px + i - 2, v.nx);
+    T acc = 0;
 #pragma unroll 1
     for (int k = 0; k < 5; ++k) {
         const int zz = pwrap(pz + k - 2, v.nz);
-        double accy = 0.0;
+        T accy = 0;
 #pragma unroll 1
         for (int j = 0; j < 5; ++j) {
             const int yy = pwrap(py + j - 2, v.ny);
             const T *row = cs + c * v.cs + (int64_t)(yy + v.oy) * v.js + (int64_t)zz * v.ks + v.ox;
-            double accx = 0.0;
+            T accx = 0;
 #pragma unroll
-            for (int i = 0; i < 5; ++i) accx += wx[i] * (double)row[pwrap(px + i - 2, v.nx)];
-            accy += wy[j] * accx;
+            for (int i = 0; i < 5; ++i) accx += (T)q.w[sx][i] * row[xi[i]];
+            accy += (T)q.w[sy][j] * accx;
         }
-        acc += wz[k] * accy;
+        acc += (T)q.w[sz][k] * accy;
     }
-    return acc;
+    return (double)acc;
 }
 
 struct FillArgs {

@@ -259,9 +259,14 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                 if (idx >= kVtxPts) break;
                 const int vy = idx / DVX, vx = idx % DVX;
                 const T a = sm.ps[slot][0][vy + 2][vx + 2], b = sm.ps[slot][1][vy + 2][vx + 2];
-                const double m = fmax(fabs((double)a), fabs((double)b));
                 // float conversion keeps the angle to ~1e-7 only away from under/overflow
-                sm.ok[ts][vy][vx] = (m > 1e-30 && m < 1e30) ? 1 : 0;
+                if constexpr (sizeof(T) == 4) {
+                    const float m = fmaxf(fabsf(a), fabsf(b));
+                    sm.ok[ts][vy][vx] = (m > 1e-30f && m < 1e30f) ? 1 : 0;
+                } else {
+                    const double m = fmax(fabs(a), fabs(b));
+                    sm.ok[ts][vy][vx] = (m > 1e-30 && m < 1e30) ? 1 : 0;
+                }
                 sm.th[ts][vy][vx] = atan2f((float)b, (float)a);
                 if (q.want_vel && FAST) {
                     const float psi1 = a, psi2 = b, Pi1 = sm.pi[ts][0][vy][vx], Pi2 = sm.pi[ts][1][vy][vx];

@@ -83,8 +83,13 @@ __global__ void __launch_bounds__(256) tag_kernel(const T *__restrict__ st, TagG
 #pragma unroll
         for (int v = 0; v < 7; ++v) {
             const T a = __ldg(p1 + offs[v]), b = __ldg(p2 + offs[v]);
-            const double m = fmax(fabs((double)a), fabs((double)b));
-            ok = ok && m > 1e-30 && m < 1e30;
+            if constexpr (sizeof(T) == 4) {
+                const float m = fmaxf(fabsf(a), fabsf(b));
+                ok = ok && m > 1e-30f && m < 1e30f;
+            } else {
+                const double m = fmax(fabs(a), fabs(b));
+                ok = ok && m > 1e-30 && m < 1e30;
+            }
             th[v] = atan2f((float)b, (float)a);
         }
         int w[3] = {0, 0, 0};

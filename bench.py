@@ -328,6 +328,70 @@ def replica_seed(rank: int) -> int:
     return SEED + rank
 
 
+# ---------------------------------------------------------------- scale configuration (two-level refinement)
+def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_every=10, n_error_buf=4):
+    """Physical mode (c0 = 0, lambda = 2) FP32 base level of n^3 plus 2x-refined
+    patches on every block^3 block the tagger flags (pierced plaquettes grown
+    by n_error_buf cells), `steps` coarse steps with two subcycled fine steps
+    each, regridding every `regrid_every` coarse steps. Reports throughput in
+    coarse + fine site-updates/s and the composite string-finder time."""
+    import torch
+    from axion_strings_adaptive_gb300 import ic
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    bg = A.Background.expanding(A_INV, 0.0, lambda0=LAMBDA0)
+    coarse = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev, pierced_capacity=1)
+    coarse.set_state(ic.fourier_state(n, ic.strict_cutoff(n / kdiv), seed=SEED + 11, dtype=torch.float64,
+                                      device=dev).float())
+    two = TwoLevel(coarse, block)
+    tags, n_tagged, _ = coarse.tag_cells(n_error_buf=n_error_buf)
+    del tags
+    two.regrid(n_error_buf=n_error_buf)
+    torch.cuda.synchronize()
+    fine_per_patch = (2 * block) ** 3
+    regrid_ms, t_ms, site_updates = [], 0.0, 0
+    patches = []
+    for s0 in range(0, steps, regrid_every):
+        if s0 > 0:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            two.regrid(n_error_buf=n_error_buf)
+            e1.record()
+            torch.cuda.synchronize()
+            regrid_ms.append(e0.elapsed_time(e1))
+        k = min(regrid_every, steps - s0)
+        np_ = 0 if two.patches is None else two.patches.npatches
+        patches.append(np_)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        two.advance(bg, TAU_I, s0 * DT, DT, k)
+        e1.record()
+        torch.cuda.synchronize()
+        t_ms += e0.elapsed_time(e1)
+        site_updates += k * (n ** 3 + 2 * np_ * fine_per_patch)
+    two.device_status()
+    tau = TAU_I + steps * DT
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    d = two.diagnostics(bg, tau)
+    e1.record()
+    torch.cuda.synchronize()
+    diag_ms = e0.elapsed_time(e1)
+    fine_words = 24  # per fine site-update, as on the coarse level (ghost-ring work excluded)
+    out = {"config": f"{n}^3 FP32 base, physical mode c0=0, lambda=2, IC |n|<N/{kdiv}, 2x-refined "
+                     f"{2 * block}^3-cell patches on tagged {block}^3 blocks (n_error_buf={n_error_buf}), {steps} "
+                     f"coarse steps with 2 subcycled fine steps each, regrid every {regrid_every}",
+           "coarse_sites": n ** 3, "patches_per_regrid": patches, "refined_block_fraction":
+               patches[-1] / float((n // block) ** 3), "tagged_cell_fraction_at_start": n_tagged / n ** 3,
+           "ms_per_coarse_step": t_ms / steps, "site_updates_per_s": site_updates / (t_ms * 1e-3),
+           "algorithmic_hbm_gbs": fine_words * 4 * site_updates / (t_ms * 1e-3) / 1e9,
+           "hbm_frac_of_measured": fine_words * 4 * site_updates / (t_ms * 1e-3) / 1e9 / hbm_peak,
+           "regrid_ms": regrid_ms, "composite_diagnostics_ms": diag_ms,
+           "composite": {"n_p": d.n_p_plain, "xi": d.xi_plain, "rho_tot": d.energy["rho_tot_unscreened"]}}
+    del two, coarse
+    torch.cuda.empty_cache()
+    return out
+
+
 # ---------------------------------------------------------------- native arm
 def run_native(args):
     import torch
@@ -583,6 +647,11 @@ def run_native(args):
     if not args.no_batching:
         batching = batching_report(A, ic, dev, hbm_peak)
 
+    # ---------------- scale: base level plus refined patches on tagged blocks, subcycled
+    scale = None
+    if not args.no_scale:
+        scale = scale_report(A, dev, hbm_peak, n=args.scale_n, steps=args.scale_steps, kdiv=args.scale_kdiv)
+
     # ---------------- end to end through the C ABI with host buffers: every step copies its input
     # state in from pinned host memory and its result back out; the copies of neighbouring steps
     # overlap the compute (HostStepPipeline), and the serial form is reported beside it
@@ -643,7 +712,7 @@ def run_native(args):
                 "autotune_ms_per_step": tune32, "diagnostics": diag, "fp64": fp64,
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision,
                 "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None,
-                "differentiation": differentiation, "batching": batching}
+                "differentiation": differentiation, "batching": batching, "scale": scale}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -668,6 +737,10 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--no-scale", action="store_true")
+    ap.add_argument("--scale-n", type=int, default=512)
+    ap.add_argument("--scale-steps", type=int, default=20)
+    ap.add_argument("--scale-kdiv", type=int, default=64)
     ap.add_argument("--diff-n", type=int, default=128)
     ap.add_argument("--diff-steps", type=int, default=200)
     ap.add_argument("--diff-directions", type=int, default=16)

@@ -31,20 +31,24 @@ def test_adjoint_matches_central_differences_fp64(axs, shape):
     s0 = torch.zeros((4, nz, ny, nx), dtype=torch.float64, device="cuda")
     s0[0] = ic.fourier_component((nx, ny, nz), 3.0, 11, 0).cuda()
     s0[1] = ic.fourier_component((nx, ny, nz), 3.0, 11, 1).cuda()
-    s0[2:] = 0.05 * torch.randn_like(s0[2:])
+    gen = torch.Generator(device="cuda").manual_seed(17)
+    s0[2:] = 0.05 * torch.randn(s0[2:].shape, generator=gen, device="cuda", dtype=torch.float64)
     lam = torch.tensor(2.0, dtype=torch.float64)
     x = s0.clone().requires_grad_(True)
     lv = lam.clone().requires_grad_(True)
     L0 = _loss(axs, x, lv, spec)
     L0.backward()
     g = x.grad.clone()
+    # central differences along unit-norm random directions (the loss has sharp
+    # features near string cores, so the step stays far inside its linear range)
     rng = torch.Generator(device="cuda").manual_seed(3)
-    eps = 1e-6
+    eps = 1e-5
     for _ in range(4):
         d = torch.randn(s0.shape, generator=rng, device="cuda", dtype=torch.float64)
+        d /= d.norm()
         fd = (float(_loss(axs, s0 + eps * d, lam, spec)) - float(_loss(axs, s0 - eps * d, lam, spec))) / (2 * eps)
         ad = float((g * d).sum())
-        assert ad == pytest.approx(fd, rel=2e-6, abs=1e-9), (ad, fd)
+        assert ad == pytest.approx(fd, rel=1e-6, abs=1e-7 * float(g.norm())), (ad, fd)
     fd_l = (float(_loss(axs, s0, lam + 1e-6, spec)) - float(_loss(axs, s0, lam - 1e-6, spec))) / 2e-6
     assert float(lv.grad) == pytest.approx(fd_l, rel=2e-6, abs=1e-9)
 
