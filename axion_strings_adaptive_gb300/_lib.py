@@ -154,6 +154,9 @@ SIGNATURES = {
                                     _dbl, _ptr]),
     "axs_patches_average_down": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchMap), C.POINTER(LevelC), _ptr]),
     "axs_patches_device_status": (_i32, [C.POINTER(PatchesC), _ptr]),
+    "axs_patches_diagnostics_scratch_bytes": (_i32, [_i32, _i32, C.POINTER(_i64)]),
+    "axs_patches_diagnostics": (_i32, [C.POINTER(PatchesC), C.POINTER(DiagParams), _ptr, _ptr, _i64, _ptr, _i64,
+                                       _ptr]),
     "axs_level_masked_a_dot": (_i32, [C.POINTER(LevelC), _i32, _dbl, _dbl, _ptr, _ptr, _ptr, _i64, _ptr]),
     "axs_spectrum_scratch_bytes": (_i32, [_i32, _i32, _i32, C.POINTER(_i64)]),
     "axs_spectrum_bin": (_i32, [_ptr, _i32, _i32, _i32, _i32, _ptr, _ptr, _ptr, _ptr, _i64, _ptr]),

@@ -62,6 +62,25 @@ class Patches:
     def device_status(self) -> None:
         L.call("axs_patches_device_status", C.byref(self.c), None)
 
+    def diagnostics(self, prm: L.DiagParams, list_capacity: int = 0):
+        """One diagnostics pass over every patch (rings as ghost cells), summed
+        into one DiagResult; with list_capacity > 0 also the pierced list
+        (entries 4 (q n^3 + cell) + plane), returned as (result, list)."""
+        nbytes = C.c_int64()
+        L.call("axs_patches_diagnostics_scratch_bytes", self.n, self.npatches, C.byref(nbytes))
+        dev = self.state.device
+        scratch = torch.zeros(nbytes.value, dtype=torch.uint8, device=dev)
+        res = torch.zeros(C.sizeof(L.DiagResult), dtype=torch.uint8, device=dev)
+        lst = torch.zeros(max(1, list_capacity), dtype=torch.int64, device=dev)
+        L.call("axs_patches_diagnostics", C.byref(self.c), C.byref(prm), res.data_ptr(),
+               lst.data_ptr() if list_capacity > 0 else None, int(list_capacity), scratch.data_ptr(), scratch.numel(),
+               torch.cuda.current_stream().cuda_stream)
+        out = L.DiagResult.from_buffer_copy(res.cpu().numpy().tobytes())
+        L.check(out.status)
+        if list_capacity > 0:
+            return out, lst[:out.n_listed].clone()
+        return out
+
     def fab(self, q: int) -> L.Fab:
         """axs_fab view of patch q with 4 ghost layers (its ring), for the diagnostics pass."""
         lay, es = self.layout, torch.finfo(self.dtype).bits // 8
@@ -123,17 +142,20 @@ class TwoLevel:
         dt = self.coarse.dtype
         self.patches = Patches(2 * self.block, len(blocks), 0.5 * self.coarse.dx, dtype=dt, device=dev)
         self._patch_block = torch.from_numpy(blocks.copy()).to(dev)
-        bp = torch.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=torch.int32)
-        for q, (bx, by, bz) in enumerate(blocks):
-            bp[bz, by, bx] = q
-        self._block_patch = bp.to(dev)
+        bp = np.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=np.int32)
+        bp[blocks[:, 2], blocks[:, 1], blocks[:, 0]] = np.arange(len(blocks), dtype=np.int32)
+        self._block_patch = torch.from_numpy(bp).to(dev)
         L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c), None, 0.0,
                0.0, 1, None)
         if old_patches is not None:
-            for q, b in enumerate(blocks):
-                oq = old_index.get(tuple(b))
-                if oq is not None:
-                    self.patches.valid(q).copy_(old_patches.valid(oq))
+            pairs = [(q, old_index[tuple(b)]) for q, b in enumerate(blocks.tolist()) if tuple(b) in old_index]
+            if pairs:
+                # whole patch boxes (valid cells and rings; the rings are refilled before use)
+                new_q, old_q = (torch.tensor(v, dtype=torch.int64, device=dev) for v in zip(*pairs))
+                box = self.patches.layout.patch_elems
+                dst = self.patches.state.view(4, self.patches.npatches, box)
+                src = old_patches.state.view(4, old_patches.npatches, box)
+                dst.index_copy_(1, new_q, src.index_select(1, old_q))
 
     def regrid(self, n_error_buf: int = 4, gradient_threshold: float = 1.7976931348623157e308,
                radial_gradient_threshold: float = 1.7976931348623157e308) -> int:
@@ -177,34 +199,26 @@ class TwoLevel:
         covered = covered.repeat_interleave(b, 0).repeat_interleave(b, 1).repeat_interleave(b, 2)
         return (1 - covered).contiguous()
 
-    def diagnostics(self, bg: Background, tau: float, masking_scheme: int = L.MASK_A,
-                    threshold: float = 0.8) -> CompositeDiagnostics:
+    def diagnostics(self, bg: Background, tau: float, masking_scheme: int = L.MASK_A, threshold: float = 0.8,
+                    strings_only: bool = False, per_cell_fp32: bool = False) -> CompositeDiagnostics:
+        """strings_only: the composite count_plaquettes alone (energies and the
+        velocity are left at zero); per_cell_fp32: see axs_diag_params."""
         v = bg.values(tau)
         rpr = 0.0 if bg.kind == L.BG_FLAT else v.R_prime_over_R
+        want = (0, 1, 0) if strings_only else (1, 1, 1)
+        fp32 = int(per_cell_fp32 and self.coarse.dtype == torch.float32)
         levels = []
         mask = self.coverage_mask().reshape(-1) if self.patches is not None else None
         levels.append((self.coarse.diagnostics_raw(
             L.DiagParams(self.coarse.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold, L.BOUNDARY_PERIODIC,
-                         1, 1, 1, 0), mask, want_list=False), self.coarse.dx))
+                         *want, fp32), mask, want_list=False), self.coarse.dx))
         if self.patches is not None:
             p = self.patches
             # rings at the current time: neighbours, else the (current) coarse level
             L.call("axs_patches_fill", C.byref(p.c), C.byref(self._map()), C.byref(self.coarse.c), None, 0.0, 0.0, 0,
                    None)
-            nbytes = C.c_int64()
-            L.call("axs_diagnostics_scratch_bytes", p.n, p.n, p.n, C.byref(nbytes))
-            dev = self.coarse.state.device
-            scratch = torch.zeros(nbytes.value, dtype=torch.uint8, device=dev)
-            res = torch.zeros((p.npatches, C.sizeof(L.DiagResult)), dtype=torch.uint8, device=dev)
-            prm = L.DiagParams(p.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold, L.BOUNDARY_GHOSTS, 1, 1,
-                               1, 0)
-            s = torch.cuda.current_stream().cuda_stream
-            for q in range(p.npatches):
-                L.call("axs_diagnostics", C.byref(p.fab(q)), C.byref(prm), None, res[q].data_ptr(), None, 0,
-                       scratch.data_ptr(), scratch.numel(), s)
-            host = res.cpu().numpy()
-            for q in range(p.npatches):
-                levels.append((L.DiagResult.from_buffer_copy(host[q].tobytes()), p.dx))
+            levels.append((p.diagnostics(L.DiagParams(p.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold,
+                                                      L.BOUNDARY_GHOSTS, *want, fp32)), p.dx))
         # composite combination (AxionStringsLevel.cpp:1302-1350, EnergyKernel.hpp:287-339)
         n_p = sum(r.n_p_plain for r, _ in levels)
         n_w = sum(r.n_p_weighted for r, _ in levels)
@@ -218,7 +232,7 @@ class TwoLevel:
         n_total, n_unmasked = acc[13], acc[12]
         energy = {"n_total": n_total, "n_unmasked": n_unmasked}
         for q, name in enumerate(self.ENERGY_NAMES):
-            energy[name + "_unscreened"] = acc[2 * q] / n_total
+            energy[name + "_unscreened"] = acc[2 * q] / n_total if n_total > 0.0 else 0.0
             energy[name + "_screened"] = acc[2 * q + 1] / n_unmasked if n_unmasked > 0.0 else 0.0
         L_tilde = self.coarse.nx * self.coarse.dx
         nref = 0 if self.patches is None else self.patches.npatches

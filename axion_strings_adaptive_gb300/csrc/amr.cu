@@ -36,6 +36,11 @@ namespace axs {
 int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g);
 int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, int ncomp,
                       cudaStream_t st);
+int diag_ghost_boxes(const void *data, int32_t dtype, int nx, int ny, int nz, int ox, int oy, int oz, int64_t js,
+                     int64_t ks, int64_t cs, int nboxes, int64_t box_stride, const axs_diag_params *p,
+                     axs_diag_result *out, int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes,
+                     cudaStream_t st);
+int64_t diag_scratch_bytes_for(int64_t ncell);
 constexpr int kPatchOX = 8, kPatchRY = 4, kPatchRZ = 4;  // padded position of valid (0, 0, 0)
 constexpr int kRingX = 6, kRingYZ = 4;                    // ghost ring widths the step reads
 constexpr int64_t kPatchHeader = 128;
@@ -66,6 +71,7 @@ static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g)
 static int64_t patch_items_bound(const PatchGeom &g, int npatches)
 {
     // sweep A domain (n+8) x (n+4) x (n+4) and sweep B n^3, tiles >= 16 x 8, chunks >= 1 plane
+    // (sweep A tiles are 40 x 12: at most as many as 16 x 8 tiles)
     const int64_t a = (int64_t)((g.n + 8 + 15) / 16) * ((g.n + 4 + 7) / 8) * (g.n + 4);
     const int64_t b = (int64_t)((g.n + 15) / 16) * ((g.n + 7) / 8) * g.n;
     return (a + b) * npatches;
@@ -95,11 +101,12 @@ static int validate_patches(const axs_patches *p, PatchGeom &g)
 
 // ---------------------------------------------------------------- the two sweeps
 template <typename T> struct PatchTilings {
-    // sweep A: domain x in [-4, n+4) (tiles start on 16-byte boundaries), y, z in [-2, n+2)
-    using LA = SweepLauncher<T, 2, 24, 16, 8, 2, ForwardA, BoxTable, true>;
+    // sweep A: domain x in [-4, n+4) (tiles start on 16-byte boundaries), y, z in [-2, n+2):
+    // 40 x 12 tiles cover the 40 x 36 domain of a 32^3 patch exactly
+    using LA = SweepLauncher<T, 2, 40, 12, 8, 2, ForwardA, BoxTable, true>;
     // sweep B: the valid cells
     using LB = SweepLauncher<T, 2, 32, 16, 8, 2, ForwardB, BoxTable, true>;
-    static constexpr int TXA = 24, TYA = 16, TXB = 32, TYB = 16;
+    static constexpr int TXA = 40, TYA = 12, TXB = 32, TYB = 16;
 };
 
 struct PatchTableOut {
@@ -139,7 +146,10 @@ template <typename T> static int build_patch_table(const axs_patches *p, const P
         d.map_box = map_box;
         d.pad = 0;
     };
-    // chunk length: about 4 chunks per patch side, at least 8 planes
+    // chunk length: about 4 chunks per patch side, at least 8 planes (whole
+    // patch heights re-read fewer halo planes but ran 30 % slower on GB300:
+    // neighbouring tiles then march at different heights and miss each
+    // other's halo rows in L2)
     const int zc_a = std::max(8, (n + 4 + 3) / 4), zc_b = std::max(8, (n + 3) / 4);
     for (int q = 0; q < np; ++q) {
         fill(desc[q], q, -4, -2, n + 8, n + 4, PT::TXA, PT::TYA, zc_a);
@@ -255,36 +265,6 @@ __device__ __forceinline__ int pwrap(int i, int n)
     return i < 0 ? i + n : i;
 }
 
-// value of coarse component c interpolated to fine global cell (gx, gy, gz),
-// accumulated in the field precision (FP32 fields: FP32 arithmetic)
-template <typename T>
-__device__ __forceinline__ double coarse_interp(const T *__restrict__ cs, const CoarseView &v, int c, int gx, int gy,
-                                                int gz, const QuarticWeights &q)
-{
-    const int px = gx >> 1, py = gy >> 1, pz = gz >> 1;  // parent (gx >= 0)
-    const int sx = gx & 1, sy = gy & 1, sz = gz & 1;
-    int xi[5];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) xi[i] = pwrap(px + i - 2, v.nx);
-    T acc = 0;
-#pragma unroll 1
-    for (int k = 0; k < 5; ++k) {
-        const int zz = pwrap(pz + k - 2, v.nz);
-        T accy = 0;
-#pragma unroll 1
-        for (int j = 0; j < 5; ++j) {
-            const int yy = pwrap(py + j - 2, v.ny);
-            const T *row = cs + c * v.cs + (int64_t)(yy + v.oy) * v.js + (int64_t)zz * v.ks + v.ox;
-            T accx = 0;
-#pragma unroll
-            for (int i = 0; i < 5; ++i) accx += (T)q.w[sx][i] * row[xi[i]];
-            accy += (T)q.w[sy][j] * accx;
-        }
-        acc += (T)q.w[sz][k] * accy;
-    }
-    return (double)acc;
-}
-
 struct FillArgs {
     int n, np;              // fine patch side, patch count
     int nbx, nby, nbz;      // block grid of the coarse level
@@ -295,53 +275,216 @@ struct FillArgs {
     int valid_too;          // 1: also the valid cells (initialisation)
 };
 
+// The fill works on tiles of kFillT x kFillT fine columns of one patch (one CTA
+// per tile) and marches in z, one coarse parent plane -- two fine planes -- at
+// a time. Quartic interpolation is separable, so the two fine planes are made
+// from the tile's coarse footprint (kFillC x kFillC coarse cells: the parents
+// plus 2 on either side) in three passes through shared memory: z (5 coarse
+// planes -> the footprint at both fine heights), x (-> fine columns x coarse
+// rows), y (-> fine cells). Both children of a parent use the same five
+// inputs on every axis, so each pass computes them together. The coarse planes
+// pass through a 5-slot window, each loaded once per tile with the time
+// interpolation already applied (it is linear, so it commutes with the spatial
+// one): per coarse cell, psi(theta) is the cubic Hermite blend of psi and
+// hdt * Pi at the two ends of the coarse step, Pi(theta) the linear blend of Pi.
+constexpr int kFillT = 16;
+constexpr int kFillC = kFillT / 2 + 4;
+constexpr int kFillCells = kFillC * kFillC;
+constexpr int kFillThreads = 256;
+constexpr int kFillWin = 4 * kFillCells;            // one window slot: 4 components
+constexpr int kFillXs = 4 * kFillC * kFillT;        // one fine plane of x-interpolated rows
+static_assert(2 * kFillCells <= 2 * kFillThreads, "coarse load tasks: two per thread");
+static_assert(kFillWin <= 3 * kFillThreads && 2 * kFillXs / 2 <= 3 * kFillThreads, "z / x tasks: three per thread");
+static_assert(kFillThreads == 2 * kFillT * kFillT / 2, "one y pair of one fine plane per thread");
+
+template <typename T> struct FillSmem {
+    T win[5][kFillWin];      // coarse plane p sits in slot p mod 5
+    T zs[2][kFillWin];       // footprint interpolated to the two fine heights
+    T xs[2][kFillXs];        // then to the tile's fine columns
+};
+
+// tiles start at fine x, y = -8 and cover [-kRingX, n + kRingX) x [-kRingYZ, n + kRingYZ)
+__host__ __device__ __forceinline__ int fill_tiles_x(int n) { return (n + 8 + kRingX + kFillT - 1) / kFillT; }
+__host__ __device__ __forceinline__ int fill_tiles_y(int n) { return (n + 8 + kRingYZ + kFillT - 1) / kFillT; }
+
 template <typename T>
-__global__ void patch_fill_kernel(T *__restrict__ st, CoarseView cv, FillArgs f, QuarticWeights q)
+__global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fill_kernel(T *__restrict__ st, CoarseView cv, FillArgs f,
+                                                                     QuarticWeights q)
 {
-    const int W = f.n + 2 * kRingX, H = f.n + 2 * kRingYZ;
-    const int64_t per = (int64_t)W * H * H;
-    const int64_t total = per * f.np;
-    const int nfx = cv.nx * 2, nfy = cv.ny * 2, nfz = cv.nz * 2;
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int pq = (int)(idx / per);
-        const int64_t r = idx % per;
-        const int x = (int)(r % W) - kRingX, y = (int)((r / W) % H) - kRingYZ, z = (int)(r / ((int64_t)W * H)) - kRingYZ;
-        const bool inside = x >= 0 && x < f.n && y >= 0 && y < f.n && z >= 0 && z < f.n;
-        if (inside && !f.valid_too) continue;
-        const int bx = f.patch_block[3 * pq], by = f.patch_block[3 * pq + 1], bz = f.patch_block[3 * pq + 2];
-        const int gx = pwrap(bx * f.n + x, nfx), gy = pwrap(by * f.n + y, nfy), gz = pwrap(bz * f.n + z, nfz);
-        T *dst = st + (int64_t)pq * f.box + (x + kPatchOX) + (int64_t)(y + kPatchRY) * f.js + (int64_t)(z + kPatchRZ) * f.ks;
-        int src_patch = -1;
-        if (!inside) {
-            const int ob = (gx / f.n) + f.nbx * ((gy / f.n) + f.nby * (gz / f.n));
-            src_patch = f.block_patch[ob];
-        }
-        if (src_patch >= 0) {
-            const int lx = gx % f.n, ly = gy % f.n, lz = gz % f.n;
-            const T *src = st + (int64_t)src_patch * f.box + (lx + kPatchOX) + (int64_t)(ly + kPatchRY) * f.js +
-                           (int64_t)(lz + kPatchRZ) * f.ks;
+    __shared__ FillSmem<T> sm;
+    __shared__ T w[2][5];
+    const int n = f.n, half = n / 2, tid = threadIdx.x;
+    const int ntx = fill_tiles_x(n), ntiles = ntx * fill_tiles_y(n);
+    const int pq = blockIdx.x / ntiles, tile = blockIdx.x % ntiles;
+    // tile origins are even, so a fine cell's child index on each axis is its parity
+    const int x0 = -8 + kFillT * (tile % ntx), y0 = -8 + kFillT * (tile / ntx);
+    const int bx = f.patch_block[3 * pq], by = f.patch_block[3 * pq + 1], bz = f.patch_block[3 * pq + 2];
+    const int cx0 = bx * half + x0 / 2 - 2, cy0 = by * half + y0 / 2 - 2;  // footprint origin (unwrapped)
+    if (tid == 0) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) dst[c * f.plane] = src[c * f.plane];
-            continue;
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) w[a][k] = (T)q.w[a][k];
+    }
+
+    // ---- this thread's cells: fine column pair (x, ya), (x, ya + 1) in plane sz of each parent.
+    // ya is even, so both share the block, the region and the inside tests.
+    const int sz = tid >> 7, tx = tid & 15, m = (tid >> 4) & 7;
+    const int x = x0 + tx, ya = y0 + 2 * m;
+    const bool col_region = x >= -kRingX && x < n + kRingX && ya >= -kRingYZ && ya < n + kRingYZ;
+    const bool col_inside = x >= 0 && x < n && ya >= 0 && ya < n;
+    const bool tile_inside = x0 >= 0 && x0 + kFillT <= n && y0 >= 0 && y0 + kFillT <= n;
+    const int gx = pwrap(bx * n + x, cv.nx * 2), gya = pwrap(by * n + ya, cv.ny * 2);
+    // the patches owning the column pair's cells below, inside and above this patch in z
+    int own_lo = -1, own_mid = -1, own_hi = -1;
+    if (col_region && !f.valid_too) {
+        const int ob = (gx / n) + f.nbx * (gya / n), bplane = f.nbx * f.nby;
+        own_lo = f.block_patch[ob + bplane * pwrap(bz - 1, f.nbz)];
+        own_mid = f.block_patch[ob + bplane * bz];
+        own_hi = f.block_patch[ob + bplane * pwrap(bz + 1, f.nbz)];
+    }
+    T *const dst_col = st + (int64_t)pq * f.box + (x + kPatchOX) + (int64_t)(ya + kPatchRY) * f.js;
+    const int64_t src_col = (gx % n + kPatchOX) + (int64_t)(gya % n + kPatchRY) * f.js;
+
+    // ---- coarse load tasks (two per thread at most): (pair, cell) -> psi_pair, Pi_pair
+    int64_t ld_off[2];
+    int ld_sm[2];
+    bool ld_on[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int t = tid + r * kFillThreads;
+        ld_on[r] = t < 2 * kFillCells;
+        const int pair = t / kFillCells, cell = t % kFillCells;
+        const int xx = pwrap(cx0 + cell % kFillC, cv.nx), yy = pwrap(cy0 + cell / kFillC, cv.ny);
+        ld_off[r] = (int64_t)(yy + cv.oy) * cv.js + cv.ox + xx + (pair ? cv.cs : 0);
+        ld_sm[r] = pair * kFillCells + cell;
+    }
+    // ---- z pass tasks: component-cell of the footprint, both heights
+    int zt[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const int t = tid + r * kFillThreads;
+        zt[r] = t < kFillWin ? t : -1;
+    }
+    // ---- x pass tasks: (height, component, coarse row, fine column pair)
+    int xin[3], xout[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const int t = tid + r * kFillThreads;
+        const int h = t / (kFillXs / 2), rem = t % (kFillXs / 2);
+        const int c = rem / (kFillC * kFillT / 2), rem2 = rem % (kFillC * kFillT / 2);
+        const int cyl = rem2 / (kFillT / 2), mm = rem2 % (kFillT / 2);
+        const bool on = t < kFillXs;
+        xin[r] = on ? h * kFillWin + c * kFillCells + cyl * kFillC + mm : -1;
+        xout[r] = h * kFillXs + c * kFillC * kFillT + cyl * kFillT + 2 * mm;
+    }
+
+    const T *c0 = static_cast<const T *>(cv.old_state), *c1 = static_cast<const T *>(cv.new_state);
+    const bool blend = f.theta != 0.0;
+    const double s = f.theta, s2 = s * s, s3 = s2 * s;
+    const double h00 = 2 * s3 - 3 * s2 + 1, h10 = (s3 - 2 * s2 + s) * f.hdt, h01 = -2 * s3 + 3 * s2,
+                 h11 = (s3 - s2) * f.hdt;
+    T v[2][4];
+    auto issue = [&](int p) {
+        const int64_t zoff = (int64_t)pwrap(p, cv.nz) * cv.ks;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!ld_on[r]) continue;
+            const int64_t off = zoff + ld_off[r];
+            v[r][0] = c0[off];
+            v[r][1] = c0[off + 2 * cv.cs];
+            if (blend) {
+                v[r][2] = c1[off];
+                v[r][3] = c1[off + 2 * cv.cs];
+            }
         }
-        const T *c0 = static_cast<const T *>(cv.old_state), *c1 = static_cast<const T *>(cv.new_state);
-        T *d0 = dst;
-#pragma unroll 1
-        for (int c = 0; c < 2; ++c) {  // (psi_c, Pi_c) pairs
-            if (f.theta == 0.0) {
-                d0[c * f.plane] = (T)coarse_interp<T>(c0, cv, c, gx, gy, gz, q);
-                d0[(2 + c) * f.plane] = (T)coarse_interp<T>(c0, cv, 2 + c, gx, gy, gz, q);
+    };
+    auto commit = [&](int p) {
+        T *slot = sm.win[pwrap(p, 5)];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!ld_on[r]) continue;
+            if (!blend) {
+                slot[ld_sm[r]] = v[r][0];
+                slot[ld_sm[r] + 2 * kFillCells] = v[r][1];
             } else {
-                const double p0 = coarse_interp<T>(c0, cv, c, gx, gy, gz, q);
-                const double q0 = coarse_interp<T>(c0, cv, 2 + c, gx, gy, gz, q);
-                const double p1 = coarse_interp<T>(c1, cv, c, gx, gy, gz, q);
-                const double q1 = coarse_interp<T>(c1, cv, 2 + c, gx, gy, gz, q);
-                const double s = f.theta, s2 = s * s, s3 = s2 * s;
-                const double h00 = 2 * s3 - 3 * s2 + 1, h10 = s3 - 2 * s2 + s, h01 = -2 * s3 + 3 * s2, h11 = s3 - s2;
-                // psi: cubic Hermite with dpsi/dtau = Pi; Pi: linear
-                d0[c * f.plane] = (T)(h00 * p0 + h10 * f.hdt * q0 + h01 * p1 + h11 * f.hdt * q1);
-                d0[(2 + c) * f.plane] = (T)((1.0 - s) * q0 + s * q1);
+                const double p0 = (double)v[r][0], q0 = (double)v[r][1], p1 = (double)v[r][2], q1 = (double)v[r][3];
+                slot[ld_sm[r]] = (T)(h00 * p0 + h10 * q0 + h01 * p1 + h11 * q1);
+                slot[ld_sm[r] + 2 * kFillCells] = (T)((1.0 - s) * q0 + s * q1);
+            }
+        }
+    };
+
+    // z segments: the whole height, or only the two z rings above and below a
+    // tile that lies inside the valid cells
+    const int nseg = (tile_inside && !f.valid_too) ? 2 : 1;
+    for (int sg = 0; sg < nseg; ++sg) {
+        const int za = nseg == 2 ? (sg == 0 ? -kRingYZ : n) : -kRingYZ;
+        const int zb = nseg == 2 ? (sg == 0 ? 0 : n + kRingYZ) : n + kRingYZ;
+        const int pa = bz * half + za / 2, pb = bz * half + zb / 2;  // parents of the segment (unwrapped)
+        __syncthreads();  // the previous segment is done with the window
+        for (int p = pa - 2; p < pa + 2; ++p) {
+            issue(p);
+            commit(p);
+        }
+        issue(pa + 2);
+        for (int pz = pa; pz < pb; ++pz) {
+            commit(pz + 2);
+            const int z = 2 * (pz - bz * half) + sz;
+            const int zone = z < 0 ? 0 : (z < n ? 1 : 2);
+            const int src_patch = zone == 0 ? own_lo : (zone == 1 ? own_mid : own_hi);
+            // 0: nothing, 1: copy from the patch owning the cells, 2: interpolate.
+            // An initialising fill (valid_too) interpolates every cell: the value
+            // depends only on the cell's global position, so a ring cell gets what
+            // its owner's valid cell gets in the same launch.
+            int mode = 0;
+            if (col_region && (f.valid_too || !(col_inside && zone == 1))) mode = src_patch >= 0 ? 1 : 2;
+            const bool any = __syncthreads_or(mode == 2);  // also publishes the committed plane
+            if (pz + 1 < pb) issue(pz + 3);
+            T *dst = dst_col + (int64_t)(z + kPatchRZ) * f.ks;
+            if (any) {
+                const T *s0 = sm.win[pwrap(pz - 2, 5)], *s1 = sm.win[pwrap(pz - 1, 5)], *s2p = sm.win[pwrap(pz, 5)];
+                const T *s3p = sm.win[pwrap(pz + 1, 5)], *s4 = sm.win[pwrap(pz + 2, 5)];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const int t = zt[r];
+                    if (t < 0) continue;
+                    const T a0 = s0[t], a1 = s1[t], a2 = s2p[t], a3 = s3p[t], a4 = s4[t];
+                    sm.zs[0][t] = w[0][0] * a0 + w[0][1] * a1 + w[0][2] * a2 + w[0][3] * a3 + w[0][4] * a4;
+                    sm.zs[1][t] = w[1][0] * a0 + w[1][1] * a1 + w[1][2] * a2 + w[1][3] * a3 + w[1][4] * a4;
+                }
+                __syncthreads();
+                const T *zsf = &sm.zs[0][0];
+                T *xsf = &sm.xs[0][0];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    if (xin[r] < 0) continue;
+                    const T *in = zsf + xin[r];
+                    const T a0 = in[0], a1 = in[1], a2 = in[2], a3 = in[3], a4 = in[4];
+                    xsf[xout[r]] = w[0][0] * a0 + w[0][1] * a1 + w[0][2] * a2 + w[0][3] * a3 + w[0][4] * a4;
+                    xsf[xout[r] + 1] = w[1][0] * a0 + w[1][1] * a1 + w[1][2] * a2 + w[1][3] * a3 + w[1][4] * a4;
+                }
+                __syncthreads();
+                if (mode == 2) {
+                    const T *xr = xsf + sz * kFillXs + m * kFillT + tx;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const T *in = xr + c * kFillC * kFillT;
+                        const T a0 = in[0], a1 = in[kFillT], a2 = in[2 * kFillT], a3 = in[3 * kFillT],
+                                a4 = in[4 * kFillT];
+                        dst[c * f.plane] = w[0][0] * a0 + w[0][1] * a1 + w[0][2] * a2 + w[0][3] * a3 + w[0][4] * a4;
+                        dst[c * f.plane + f.js] =
+                            w[1][0] * a0 + w[1][1] * a1 + w[1][2] * a2 + w[1][3] * a3 + w[1][4] * a4;
+                    }
+                }
+            }
+            if (mode == 1) {
+                const T *src = st + (int64_t)src_patch * f.box + src_col + (int64_t)(z - (zone - 1) * n + kPatchRZ) * f.ks;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    dst[c * f.plane] = src[c * f.plane];
+                    dst[c * f.plane + f.js] = src[c * f.plane + f.js];
+                }
             }
         }
     }
@@ -492,12 +635,13 @@ int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_lev
     f.hdt = coarse_dt;
     f.valid_too = valid_too != 0;
     const QuarticWeights q = quartic_weights();
-    const int64_t total = (int64_t)(g.n + 2 * kRingX) * (g.n + 2 * kRingYZ) * (g.n + 2 * kRingYZ) * p->npatches;
+    const int64_t blocks = (int64_t)fill_tiles_x(g.n) * fill_tiles_y(g.n) * p->npatches;
+    AXS_REQUIRE(blocks < (int64_t)INT32_MAX, AXS_ERR_UNSUPPORTED, "too many patches for one fill launch");
     cudaStream_t st = (cudaStream_t)stream;
     if (p->dtype == AXS_F32)
-        patch_fill_kernel<float><<<grid_cells(total), 256, 0, st>>>(static_cast<float *>(p->state), cv, f, q);
+        patch_fill_kernel<float><<<(unsigned)blocks, kFillThreads, 0, st>>>(static_cast<float *>(p->state), cv, f, q);
     else
-        patch_fill_kernel<double><<<grid_cells(total), 256, 0, st>>>(static_cast<double *>(p->state), cv, f, q);
+        patch_fill_kernel<double><<<(unsigned)blocks, kFillThreads, 0, st>>>(static_cast<double *>(p->state), cv, f, q);
     return launch_status("patch fill");
 }
 
@@ -522,6 +666,29 @@ int axs_patches_average_down(const axs_patches *p, const axs_patch_map *m, const
     LevelGeom lg;
     level_geom(coarse->dtype, coarse->nx, coarse->ny, coarse->nz, lg);
     return level_fill_ghosts(coarse->state, coarse->dtype, coarse->nx, coarse->ny, coarse->nz, lg, 4, st);
+}
+
+int axs_patches_diagnostics_scratch_bytes(int32_t n, int32_t npatches, int64_t *bytes)
+{
+    AXS_REQUIRE(bytes != nullptr, AXS_ERR_INVALID_ARGUMENT, "null output");
+    PatchGeom g;
+    int rc = patch_geom(AXS_F32, n, npatches, g);
+    if (rc) return rc;
+    *bytes = diag_scratch_bytes_for((int64_t)n * n * n * npatches);
+    return AXS_OK;
+}
+
+int axs_patches_diagnostics(const axs_patches *p, const axs_diag_params *prm, axs_diag_result *out, int64_t *list,
+                            int64_t capacity, void *scratch, int64_t scratch_bytes, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(p, g);
+    if (rc) return rc;
+    AXS_REQUIRE(prm != nullptr && prm->boundary == AXS_BOUNDARY_GHOSTS, AXS_ERR_INVALID_ARGUMENT,
+                "patch diagnostics read the rings: boundary must be AXS_BOUNDARY_GHOSTS");
+    return diag_ghost_boxes(p->state, p->dtype, g.n, g.n, g.n, kPatchOX, kPatchRY, kPatchRZ, g.js, g.ks, g.plane,
+                            p->npatches, g.box, prm, out, list, capacity, scratch, scratch_bytes,
+                            (cudaStream_t)stream);
 }
 
 int axs_patches_device_status(const axs_patches *p, void *stream)

@@ -172,13 +172,14 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                                                                DiagPartial *__restrict__ partials,
                                                                unsigned long long *__restrict__ list_counter,
                                                                long long *__restrict__ list, long long capacity,
-                                                               int tiles_x, int ntiles, int zchunk, long long n_items)
+                                                               int tiles_x, int ntiles, int zchunk, long long n_items,
+                                                               long long items_per_box, int64_t box_stride)
 {
     extern __shared__ __align__(16) unsigned char diag_smem_raw[];
     DiagSmem<T, FAST> &sm = *reinterpret_cast<DiagSmem<T, FAST> *>(diag_smem_raw);
     __shared__ int warp_tot[kDiagThreads / 32];
     __shared__ unsigned long long block_base;
-    const T *__restrict__ base = static_cast<const T *>(v.data);
+    const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
 
     double e[14];
 #pragma unroll
@@ -196,8 +197,11 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
     const int lx = tid % DTX, ly = tid / DTX;
 
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
-        const int tile = (int)(item % ntiles);
-        const int chunk = (int)(item / ntiles);
+        // boxes of one batch share the view's geometry and sit box_stride apart
+        const long long qbox = item / items_per_box, box_item = item % items_per_box;
+        const T *__restrict__ base = static_cast<const T *>(v.data) + qbox * box_stride;
+        const int tile = (int)(box_item % ntiles);
+        const int chunk = (int)(box_item / ntiles);
         const int x0 = (tile % tiles_x) * DTX, y0 = (tile / tiles_x) * DTY;
         const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
 
@@ -301,7 +305,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             __syncthreads();
 
             const int x = x0 + lx, y = y0 + ly;
-            const int64_t cell = (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
+            const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
             const bool in = x < v.nx && y < v.ny && (mask == nullptr || mask[cell] != 0);
             int w[3] = {0, 0, 0};
             if (in) {
@@ -547,25 +551,28 @@ static int diag_grid(int64_t ncell)
 
 // Work items (tile, z-chunk), tile fastest; chunks long enough to amortise
 // the 4 warm-up planes while giving every resident block several items.
-static void diag_plan(const DiagView &v, int max_grid, int &tiles_x, int &ntiles, int &zchunk, long long &items,
-                      int &grid)
+static void diag_plan(const DiagView &v, int nboxes, int max_grid, int &tiles_x, int &ntiles, int &zchunk,
+                      long long &items_per_box, long long &items, int &grid)
 {
     tiles_x = (v.nx + DTX - 1) / DTX;
     ntiles = tiles_x * ((v.ny + DTY - 1) / DTY);
     const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
     const long long resident = 2LL * sms;
-    int nch = (int)std::max<long long>(1, (4 * resident + ntiles - 1) / ntiles);
+    const long long tiles_all = (long long)ntiles * nboxes;
+    int nch = (int)std::max<long long>(1, (4 * resident + tiles_all - 1) / tiles_all);
     zchunk = std::max(1, (v.nz + nch - 1) / nch);
     if (zchunk < 16 && v.nz >= 16) zchunk = 16;
     if (zchunk > v.nz) zchunk = v.nz;
-    items = (long long)ntiles * ((v.nz + zchunk - 1) / zchunk);
+    items_per_box = (long long)ntiles * ((v.nz + zchunk - 1) / zchunk);
+    items = items_per_box * nboxes;
     grid = (int)std::min<long long>(std::min<long long>(items, resident), max_grid);
 }
 
 static int64_t diag_scratch_bytes(int64_t ncell) { return 256 + (int64_t)diag_grid(ncell) * sizeof(DiagPartial); }
 
 static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *mask, axs_diag_result *out,
-                    int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, cudaStream_t st)
+                    int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, cudaStream_t st,
+                    int nboxes = 1, int64_t box_stride = 0)
 {
     AXS_REQUIRE(p != nullptr && out != nullptr, AXS_ERR_INVALID_ARGUMENT, "null params or result");
     AXS_REQUIRE(p->dx > 0.0 && p->R > 0.0 && p->m_r > 0.0, AXS_ERR_INVALID_ARGUMENT,
@@ -574,7 +581,8 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
                 "bad masking scheme %d", p->masking_scheme);
     AXS_REQUIRE(capacity >= 0, AXS_ERR_INVALID_ARGUMENT, "negative list capacity");
     AXS_REQUIRE(capacity == 0 || list != nullptr, AXS_ERR_INVALID_ARGUMENT, "null list with positive capacity");
-    const int64_t ncell = (int64_t)v.nx * v.ny * v.nz;
+    AXS_REQUIRE(nboxes >= 1, AXS_ERR_INVALID_ARGUMENT, "no boxes");
+    const int64_t ncell = (int64_t)v.nx * v.ny * v.nz * nboxes;
     const int64_t need = diag_scratch_bytes(ncell);
     AXS_REQUIRE(scratch != nullptr && scratch_bytes >= need, AXS_ERR_WORKSPACE,
                 "diagnostics scratch too small (%lld < %lld bytes)", (long long)scratch_bytes, (long long)need);
@@ -617,14 +625,14 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     auto *partials = reinterpret_cast<DiagPartial *>(static_cast<char *>(scratch) + 256);
     AXS_CUDA_CHECK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
     int tiles_x, ntiles, zchunk, grid;
-    long long items;
-    diag_plan(v, diag_grid(ncell), tiles_x, ntiles, zchunk, items, grid);
+    long long items, items_per_box;
+    diag_plan(v, nboxes, diag_grid(ncell), tiles_x, ntiles, zchunk, items_per_box, items, grid);
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
     int rc0 = AXS_OK;
     auto launch = [&](auto kern, size_t smem) -> int {
         AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<grid, kDiagThreads, smem, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x, ntiles, zchunk,
-                                               items);
+                                               items, items_per_box, box_stride);
         return AXS_OK;
     };
     if (v.dtype == AXS_F64)
@@ -650,6 +658,18 @@ int diag_level_box(const void *data, int32_t dtype, int nx, int ny, int nz, cons
 }
 
 int64_t diag_scratch_bytes_for(int64_t ncell) { return diag_scratch_bytes(ncell); }
+
+// nboxes boxes of one geometry, box_stride elements apart, with explicit ghost
+// layers (refined patches), summed into one result. A pierced-list entry is
+// 4 * (q * nx * ny * nz + cell) + plane for box q.
+int diag_ghost_boxes(const void *data, int32_t dtype, int nx, int ny, int nz, int ox, int oy, int oz, int64_t js,
+                     int64_t ks, int64_t cs, int nboxes, int64_t box_stride, const axs_diag_params *p,
+                     axs_diag_result *out, int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes,
+                     cudaStream_t st)
+{
+    DiagView v{data, dtype, nx, ny, nz, ox, oy, oz, 0, 0, 0, js, ks, cs};
+    return run_diag(v, p, nullptr, out, list, capacity, scratch, scratch_bytes, st, nboxes, box_stride);
+}
 
 }  // namespace axs
 

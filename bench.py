@@ -370,12 +370,33 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
         site_updates += k * (n ** 3 + 2 * np_ * fine_per_patch)
     two.device_status()
     tau = TAU_I + steps * DT
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    d = two.diagnostics(bg, tau)
-    e1.record()
-    torch.cuda.synchronize()
-    diag_ms = e0.elapsed_time(e1)
+
+    def ev_ms(fn, reps=3):
+        best = float("inf")
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record()
+            r = fn()
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        return best, r
+
+    diag_ms, d = ev_ms(lambda: two.diagnostics(bg, tau), reps=1)
+    finder_ms, dstr = ev_ms(lambda: two.diagnostics(bg, tau, strings_only=True))
+    # one coarse step's parts, timed apart on the final patch set (best of 3)
+    import ctypes as C
+    from axion_strings_adaptive_gb300 import _lib as L
+    p = two.patches
+    parts = {}
+    if p is not None:
+        parts["coarse_step"] = ev_ms(lambda: coarse.advance(bg, TAU_I, tau, DT, 1))[0]
+        for name, theta in (("ring_fill_theta0", 0.0), ("ring_fill_theta_half", 0.5)):
+            parts[name] = ev_ms(lambda: L.call("axs_patches_fill", C.byref(p.c), C.byref(two._map()),
+                                               C.byref(two.old_c), C.byref(coarse.c), theta, DT, 0, None))[0]
+        parts["fine_step"] = ev_ms(lambda: p.step(bg, TAU_I, tau, 0.5 * DT))[0]
+        parts["ring_cells_per_fill"] = p.npatches * ((2 * block + 12) * (2 * block + 8) ** 2 - (2 * block) ** 3)
     fine_words = 24  # per fine site-update, as on the coarse level (ghost-ring work excluded)
     out = {"config": f"{n}^3 FP32 base, physical mode c0=0, lambda=2, IC |n|<N/{kdiv}, 2x-refined "
                      f"{2 * block}^3-cell patches on tagged {block}^3 blocks (n_error_buf={n_error_buf}), {steps} "
@@ -386,7 +407,9 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
            "algorithmic_hbm_gbs": fine_words * 4 * site_updates / (t_ms * 1e-3) / 1e9,
            "hbm_frac_of_measured": fine_words * 4 * site_updates / (t_ms * 1e-3) / 1e9 / hbm_peak,
            "regrid_ms": regrid_ms, "composite_diagnostics_ms": diag_ms,
-           "composite": {"n_p": d.n_p_plain, "xi": d.xi_plain, "rho_tot": d.energy["rho_tot_unscreened"]}}
+           "string_finder_ms": finder_ms, "coarse_step_parts_ms": parts,
+           "composite": {"n_p": d.n_p_plain, "n_p_finder_only": dstr.n_p_plain, "xi": d.xi_plain,
+                         "rho_tot": d.energy["rho_tot_unscreened"]}}
     del two, coarse
     torch.cuda.empty_cache()
     return out

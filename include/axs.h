@@ -382,6 +382,17 @@ int axs_patches_rk4_step(const axs_patches *p, const axs_patch_plan *plan, const
  * 8 fine children (then the coarse periodic padding is refreshed). */
 int axs_patches_average_down(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse, void *stream);
 int axs_patches_device_status(const axs_patches *p, void *stream);
+/* The fine level's part of the composite diagnostics (specific_post_timestep
+ * on the finest level, AxionStringsLevel.cpp:1296-1350; count_plaquettes,
+ * compute_total_energy_sums and compute_velocity_at_pierced_corners over every
+ * patch, reading the rings as ghost cells): one pass over all patches, summed
+ * into one result, since the patches share dx. The rings must hold the
+ * snapshot's time (axs_patches_fill first). p->boundary must be
+ * AXS_BOUNDARY_GHOSTS; a pierced-list entry is 4 (q n^3 + cell) + plane for
+ * patch q. scratch: axs_patches_diagnostics_scratch_bytes. */
+int axs_patches_diagnostics_scratch_bytes(int32_t n, int32_t npatches, int64_t *bytes);
+int axs_patches_diagnostics(const axs_patches *p, const axs_diag_params *prm, axs_diag_result *out, int64_t *list,
+                            int64_t capacity, void *scratch, int64_t scratch_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Axion power spectrum (AxionStringsLevel.cpp:1583-1640): the masked a_dot

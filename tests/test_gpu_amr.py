@@ -6,7 +6,10 @@
 * with every block refined the patches evolve exactly as a uniform level of
   twice the resolution (the coarse level never reaches their rings);
 * the homogeneous solution psi = R(tau), Pi = R'(tau) survives subcycling;
-* composite diagnostics count a straight string pair on the fine level."""
+* composite diagnostics count a straight string pair on the fine level;
+* a mid-step ring fill copies neighbour-owned cells and blends the coarse
+  states in time as a numpy restatement does;
+* the batched pass over all patches equals per-patch diagnostics passes."""
 import numpy as np
 import pytest
 import torch
@@ -170,3 +173,111 @@ def test_composite_diagnostics_straight_strings(axs):
     d0 = coarse.diagnostics(bg, 1.0)
     # the same string length: twice the plaquettes at half the spacing (ell = (2/3) N_p dx)
     assert d.xi_plain == pytest.approx(d0.xi_plain, rel=1e-12)
+
+
+def test_time_interpolated_ring_and_neighbour_copies(axs):
+    """Mid-step ring fill (theta > 0): cells a neighbouring patch owns are copied
+    from it; the others equal a numpy restatement of the cubic-Hermite (psi,
+    with Pi as its derivative) / linear (Pi) blend of the quartic spatial
+    interpolation of the coarse states at both ends of the coarse step."""
+    import ctypes as C
+    from axion_strings_adaptive_gb300 import _lib as L
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block, theta, cdt = 64, 16, 0.37, 0.1
+    rng = np.random.default_rng(11)
+    old = rng.standard_normal((4, N, N, N))
+    new = old + 0.1 * rng.standard_normal((4, N, N, N))
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=torch.float64)
+    coarse.set_state(torch.from_numpy(new).cuda())
+    two = TwoLevel(coarse, block)
+    start = axs.PeriodicLevel(N, 0.5, dtype=torch.float64)
+    start.set_state(torch.from_numpy(old).cuda())
+    two.old_state.copy_(start.state)
+    blocks = np.array([[3, 0, 2], [0, 0, 2], [3, 3, 2]])  # x-neighbours across the seam, a y-neighbour across it
+    two.set_blocks(blocks)
+    p = two.patches
+    p.state[:, :] = 0
+    for q in range(p.npatches):
+        p.valid(q).copy_(torch.from_numpy(rng.standard_normal((4, p.n, p.n, p.n))).cuda())
+    L.call("axs_patches_fill", C.byref(p.c), C.byref(two._map()), C.byref(two.old_c), C.byref(coarse.c), theta, cdt,
+           0, None)
+    torch.cuda.synchronize()
+    w = _quartic_weights()
+    n, lay = p.n, p.layout
+    boxes = [p.box(q).cpu().numpy() for q in range(p.npatches)]
+    s, s2, s3 = theta, theta ** 2, theta ** 3
+    h00, h10, h01, h11 = 2 * s3 - 3 * s2 + 1, (s3 - 2 * s2 + s) * cdt, -2 * s3 + 3 * s2, (s3 - s2) * cdt
+    nf = 2 * N
+
+    def interp(field, gx, gy, gz):
+        val = 0.0
+        for k in range(5):
+            for j in range(5):
+                for i in range(5):
+                    cx, cy, cz = (gx // 2 + i - 2) % N, (gy // 2 + j - 2) % N, (gz // 2 + k - 2) % N
+                    val += w[gx % 2, i] * w[gy % 2, j] * w[gz % 2, k] * field[cz, cy, cx]
+        return val
+
+    q = 0  # block (3, 0, 2): its +x ring is patch 1's valid cells, its -y ring patch 2's
+    # two cells owned by neighbours ((n+2, 5, 7) and (4, -3, 9)), four interpolated
+    cells = [(n + 2, 5, 7), (n + 5, n + 3, -4), (-6, 0, 0), (4, -3, 9), (13, -1, n + 2), (n - 1, n + 3, -2)]
+    for (x, y, z) in cells:
+        gx, gy, gz = (3 * n + x) % nf, (0 * n + y) % nf, (2 * n + z) % nf
+        got = boxes[q][:, z + lay.z_offset, y + lay.y_offset, x + lay.x_offset]
+        owner = {(0, 0, 2): 1, (3, 3, 2): 2}.get((gx // n, gy // n, gz // n))
+        if owner is not None:
+            lx, ly, lz = gx % n, gy % n, gz % n
+            want = boxes[owner][:, lz + lay.z_offset, ly + lay.y_offset, lx + lay.x_offset]
+            assert np.array_equal(got, want), (x, y, z)
+            continue
+        for c in range(2):
+            p0, p1 = interp(old[c], gx, gy, gz), interp(new[c], gx, gy, gz)
+            q0, q1 = interp(old[2 + c], gx, gy, gz), interp(new[2 + c], gx, gy, gz)
+            assert got[c] == pytest.approx(h00 * p0 + h10 * q0 + h01 * p1 + h11 * q1, rel=1e-12, abs=1e-12)
+            assert got[2 + c] == pytest.approx((1 - s) * q0 + s * q1, rel=1e-12, abs=1e-12)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_batched_patch_diagnostics_match_per_patch_passes(axs, dtype):
+    """axs_patches_diagnostics (one pass over all patches) equals the sum of
+    per-patch axs_diagnostics passes: counts, velocity count and the pierced set
+    exactly, sums to rounding."""
+    import ctypes as C
+    from axion_strings_adaptive_gb300 import _lib as L, ic
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block = 64, 16
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=dtype)
+    coarse.set_state(ic.fourier_state(N, 8.0, seed=21).to(dtype))
+    two = TwoLevel(coarse, block)
+    two.set_blocks(np.array([[0, 0, 0], [1, 0, 0], [3, 2, 1], [2, 2, 3], [0, 3, 3]]))
+    two.advance(bg, 1.0, 0.0, 0.1, 2)
+    L.call("axs_patches_fill", C.byref(two.patches.c), C.byref(two._map()), C.byref(coarse.c), None, 0.0, 0.0, 0,
+           None)
+    p = two.patches
+    v = bg.values(1.2)
+    prm = L.DiagParams(p.dx, v.R, v.lambda_, v.R_prime_over_R, v.m_r, L.MASK_A, 0.8, L.BOUNDARY_GHOSTS, 1, 1, 1, 0)
+    cap = 1 << 16
+    got, lst = p.diagnostics(prm, list_capacity=cap)
+    nbytes = C.c_int64()
+    L.call("axs_diagnostics_scratch_bytes", p.n, p.n, p.n, C.byref(nbytes))
+    scratch = torch.zeros(nbytes.value, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    sums, cnts, vsum, pierced = np.zeros(14), np.zeros(4, dtype=np.int64), 0.0, set()
+    ncell = p.n ** 3
+    for q in range(p.npatches):
+        res = torch.zeros(C.sizeof(L.DiagResult), dtype=torch.uint8, device="cuda")
+        one = torch.zeros(cap, dtype=torch.int64, device="cuda")
+        L.call("axs_diagnostics", C.byref(p.fab(q)), C.byref(prm), None, res.data_ptr(), one.data_ptr(), cap,
+               scratch.data_ptr(), scratch.numel(), s)
+        r = L.DiagResult.from_buffer_copy(res.cpu().numpy().tobytes())
+        sums += np.array(list(r.energy_sums))
+        cnts += [r.n_p_plain, r.n_p_weighted, r.vel_count, r.n_near_tie]
+        vsum += r.vel_sum
+        e = one[:r.n_listed].cpu().numpy()
+        pierced |= set((4 * (q * ncell + e // 4) + e % 4).tolist())
+    assert cnts[0] > 0
+    assert [got.n_p_plain, got.n_p_weighted, got.vel_count, got.n_near_tie] == cnts.tolist()
+    assert set(lst.cpu().numpy().tolist()) == pierced and got.n_listed == len(pierced)
+    np.testing.assert_allclose(np.array(list(got.energy_sums)), sums, rtol=1e-12)
+    assert got.vel_sum == pytest.approx(vsum, rel=1e-12)
