@@ -146,11 +146,11 @@ template <typename T> static int build_patch_table(const axs_patches *p, const P
         d.map_box = map_box;
         d.pad = 0;
     };
-    // chunk length: about 4 chunks per patch side, at least 8 planes (whole
-    // patch heights re-read fewer halo planes but ran 30 % slower on GB300:
-    // neighbouring tiles then march at different heights and miss each
-    // other's halo rows in L2)
-    const int zc_a = std::max(8, (n + 4 + 3) / 4), zc_b = std::max(8, (n + 3) / 4);
+    // chunk length: two chunks per patch side, at least 8 planes (a chunk
+    // re-reads 4 halo planes; on GB300 two chunks ran 3 % faster than four,
+    // and whole patch heights 30 % slower -- neighbouring tiles then march at
+    // different heights and miss each other's halo rows in L2)
+    const int zc_a = std::max(8, (n + 4 + 1) / 2), zc_b = std::max(8, (n + 1) / 2);
     for (int q = 0; q < np; ++q) {
         fill(desc[q], q, -4, -2, n + 8, n + 4, PT::TXA, PT::TYA, zc_a);
         fill(desc[np + q], q, 0, 0, n, n, PT::TXB, PT::TYB, zc_b);
@@ -232,6 +232,7 @@ static int patch_step(const axs_patches *p, const PatchGeom &g, const axs_patch_
 // +1/4 (s = 1) from the parent's centre, in coarse-cell units.
 struct QuarticWeights {
     double w[2][5];
+    float wf[2][5];
 };
 
 static QuarticWeights quartic_weights()
@@ -247,6 +248,7 @@ static QuarticWeights quartic_weights()
                 den *= (double)(k - m);
             }
             q.w[s][k] = num / den;
+            q.wf[s][k] = (float)q.w[s][k];
         }
     }
     return q;
@@ -273,7 +275,23 @@ struct FillArgs {
     int64_t js, ks, box, plane;
     double theta, hdt;      // time fraction in the coarse step, coarse dt
     int valid_too;          // 1: also the valid cells (initialisation)
+    // time blend weights (host-computed): psi = h[0] psi0 + h[1] Pi0 + h[2] psi1 + h[3] Pi1,
+    // Pi = h[4] Pi0 + h[5] Pi1 (h[1], h[3] include the coarse dt)
+    double hd[6];
+    float hf[6];
 };
+
+static void fill_time_weights(FillArgs &f)
+{
+    const double s = f.theta, s2 = s * s, s3 = s2 * s;
+    f.hd[0] = 2 * s3 - 3 * s2 + 1;
+    f.hd[1] = (s3 - 2 * s2 + s) * f.hdt;
+    f.hd[2] = -2 * s3 + 3 * s2;
+    f.hd[3] = (s3 - s2) * f.hdt;
+    f.hd[4] = 1.0 - s;
+    f.hd[5] = s;
+    for (int i = 0; i < 6; ++i) f.hf[i] = (float)f.hd[i];
+}
 
 // The fill works on tiles of kFillT x kFillT fine columns of one patch (one CTA
 // per tile) and marches in z, one coarse parent plane -- two fine planes -- at
@@ -324,7 +342,12 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
 #pragma unroll
         for (int a = 0; a < 2; ++a)
 #pragma unroll
-            for (int k = 0; k < 5; ++k) w[a][k] = (T)q.w[a][k];
+            for (int k = 0; k < 5; ++k) {
+                if constexpr (sizeof(T) == 4)
+                    w[a][k] = q.wf[a][k];
+                else
+                    w[a][k] = q.w[a][k];
+            }
     }
 
     // ---- this thread's cells: fine column pair (x, ya), (x, ya + 1) in plane sz of each parent.
@@ -380,10 +403,16 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
     }
 
     const T *c0 = static_cast<const T *>(cv.old_state), *c1 = static_cast<const T *>(cv.new_state);
+    // time blend in the field precision with host-computed weights (FP64
+    // issues at 1/64 of the FP32 rate on GB300, conversions included; the
+    // blend is rounded to T when stored anyway)
     const bool blend = f.theta != 0.0;
-    const double s = f.theta, s2 = s * s, s3 = s2 * s;
-    const double h00 = 2 * s3 - 3 * s2 + 1, h10 = (s3 - 2 * s2 + s) * f.hdt, h01 = -2 * s3 + 3 * s2,
-                 h11 = (s3 - s2) * f.hdt;
+    const T *hw;
+    if constexpr (sizeof(T) == 4)
+        hw = f.hf;
+    else
+        hw = f.hd;
+    const T h00 = hw[0], h10 = hw[1], h01 = hw[2], h11 = hw[3], l0 = hw[4], l1 = hw[5];
     T v[2][4];
     auto issue = [&](int p) {
         const int64_t zoff = (int64_t)pwrap(p, cv.nz) * cv.ks;
@@ -408,9 +437,9 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
                 slot[ld_sm[r]] = v[r][0];
                 slot[ld_sm[r] + 2 * kFillCells] = v[r][1];
             } else {
-                const double p0 = (double)v[r][0], q0 = (double)v[r][1], p1 = (double)v[r][2], q1 = (double)v[r][3];
-                slot[ld_sm[r]] = (T)(h00 * p0 + h10 * q0 + h01 * p1 + h11 * q1);
-                slot[ld_sm[r] + 2 * kFillCells] = (T)((1.0 - s) * q0 + s * q1);
+                const T p0 = v[r][0], q0 = v[r][1], p1 = v[r][2], q1 = v[r][3];
+                slot[ld_sm[r]] = h00 * p0 + h10 * q0 + h01 * p1 + h11 * q1;
+                slot[ld_sm[r] + 2 * kFillCells] = l0 * q0 + l1 * q1;
             }
         }
     };
@@ -442,6 +471,16 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
             const bool any = __syncthreads_or(mode == 2);  // also publishes the committed plane
             if (pz + 1 < pb) issue(pz + 3);
             T *dst = dst_col + (int64_t)(z + kPatchRZ) * f.ks;
+            // neighbour copies: loads now, stores after the interpolation passes
+            T cp[4][2];
+            if (mode == 1) {
+                const T *src = st + (int64_t)src_patch * f.box + src_col + (int64_t)(z - (zone - 1) * n + kPatchRZ) * f.ks;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    cp[c][0] = src[c * f.plane];
+                    cp[c][1] = src[c * f.plane + f.js];
+                }
+            }
             if (any) {
                 const T *s0 = sm.win[pwrap(pz - 2, 5)], *s1 = sm.win[pwrap(pz - 1, 5)], *s2p = sm.win[pwrap(pz, 5)];
                 const T *s3p = sm.win[pwrap(pz + 1, 5)], *s4 = sm.win[pwrap(pz + 2, 5)];
@@ -479,11 +518,10 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
                 }
             }
             if (mode == 1) {
-                const T *src = st + (int64_t)src_patch * f.box + src_col + (int64_t)(z - (zone - 1) * n + kPatchRZ) * f.ks;
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    dst[c * f.plane] = src[c * f.plane];
-                    dst[c * f.plane + f.js] = src[c * f.plane + f.js];
+                    dst[c * f.plane] = cp[c][0];
+                    dst[c * f.plane + f.js] = cp[c][1];
                 }
             }
         }
@@ -634,6 +672,7 @@ int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_lev
     f.theta = theta;
     f.hdt = coarse_dt;
     f.valid_too = valid_too != 0;
+    fill_time_weights(f);
     const QuarticWeights q = quartic_weights();
     const int64_t blocks = (int64_t)fill_tiles_x(g.n) * fill_tiles_y(g.n) * p->npatches;
     AXS_REQUIRE(blocks < (int64_t)INT32_MAX, AXS_ERR_UNSUPPORTED, "too many patches for one fill launch");

@@ -383,7 +383,8 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
             best = min(best, a.elapsed_time(b))
         return best, r
 
-    diag_ms, d = ev_ms(lambda: two.diagnostics(bg, tau), reps=1)
+    diag_ms, d = ev_ms(lambda: two.diagnostics(bg, tau), reps=2)  # the first call sets up scratch and masks
+    diag32_ms, d32 = ev_ms(lambda: two.diagnostics(bg, tau, per_cell_fp32=True), reps=2)
     finder_ms, dstr = ev_ms(lambda: two.diagnostics(bg, tau, strings_only=True))
     # one coarse step's parts, timed apart on the final patch set (best of 3)
     import ctypes as C
@@ -407,6 +408,9 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
            "algorithmic_hbm_gbs": fine_words * 4 * site_updates / (t_ms * 1e-3) / 1e9,
            "hbm_frac_of_measured": fine_words * 4 * site_updates / (t_ms * 1e-3) / 1e9 / hbm_peak,
            "regrid_ms": regrid_ms, "composite_diagnostics_ms": diag_ms,
+           "composite_diagnostics_fp32_cells_ms": diag32_ms,
+           "composite_rho_tot_rel_diff_fp32_cells": abs(d32.energy["rho_tot_unscreened"] /
+                                                        d.energy["rho_tot_unscreened"] - 1.0),
            "string_finder_ms": finder_ms, "coarse_step_parts_ms": parts,
            "composite": {"n_p": d.n_p_plain, "n_p_finder_only": dstr.n_p_plain, "xi": d.xi_plain,
                          "rho_tot": d.energy["rho_tot_unscreened"]}}
