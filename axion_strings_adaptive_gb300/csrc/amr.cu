@@ -42,6 +42,10 @@ int diag_ghost_boxes(const void *data, int32_t dtype, int nx, int ny, int nz, in
                      cudaStream_t st);
 int64_t diag_scratch_bytes_for(int64_t ncell);
 constexpr int kPatchOX = 8, kPatchRY = 4, kPatchRZ = 4;  // padded position of valid (0, 0, 0)
+// In the work arena (S3, S4, G, P) valid x = 0 sits at padded column 12, so
+// sweep A's domain x in [-4, n + 4) covers whole 32-byte sectors of every row
+// (padded 8 .. n + 16) and no output row leaves a partly written sector.
+constexpr int kWorkOX = 12;
 constexpr int kRingX = 6, kRingYZ = 4;                    // ghost ring widths the step reads
 constexpr int64_t kPatchHeader = 128;
 
@@ -211,6 +215,7 @@ static int patch_step(const axs_patches *p, const PatchGeom &g, const axs_patch_
     aa.items = items;
     aa.n_items = plan.items_a;
     aa.map_sel = 0;
+    aa.dox_out = kWorkOX - kPatchOX;  // stencil on the state, outputs to the work arena
     aa.c1 = stage_coef<T>(bg, tau_i + t);
     aa.c2 = stage_coef<T>(bg, tau_i + t + 0.5 * dt);
     for (int c = 0; c < 8; ++c) aa.out[c] = work + c * g.plane;
@@ -220,6 +225,8 @@ static int patch_step(const axs_patches *p, const PatchGeom &g, const axs_patch_
     ab.items = items + plan.items_a;
     ab.n_items = plan.items_b;
     ab.map_sel = 1;
+    ab.ox = kWorkOX;                   // stencil and pointwise inputs in the work arena,
+    ab.dox_out = kPatchOX - kWorkOX;   // outputs to the state
     ab.c2 = aa.c2;
     ab.c4 = stage_coef<T>(bg, tau_i + t + dt);
     for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.plane;

@@ -47,9 +47,9 @@ int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g)
                 nx);
     AXS_REQUIRE(ny >= 2, AXS_ERR_UNSUPPORTED, "level ny must be >= 2 (got %d)", ny);
     const int line = 128 / (int)dtype_size(dtype);  // elements per 128-byte line
-    g.ox = line;                                     // x = 0 starts a line; 4 periodic columns sit left of it
+    g.ox = line;                                     // x = 0 starts a line; 8 periodic columns sit left of it
     g.oy = 2;
-    g.js = ((int64_t)nx + g.ox + 4 + line - 1) / line * line;
+    g.js = ((int64_t)nx + g.ox + 8 + line - 1) / line * line;  // and at least 8 right of x = nx - 1
     g.ks = g.js * (ny + 4);
     g.cs = g.ks * nz;
     return AXS_OK;

@@ -39,7 +39,9 @@ template <typename T> struct SweepArgs {
     int tiles_x, ntiles, zchunk;
     int64_t n_items;
     int64_t js, ks, cs;
-    int ox;                      // x offset of the valid region in a padded row
+    int ox;                      // x offset of the valid region in a padded row of the stencil arrays
+    int dox_pt, dox_out;         // element offset of the pointwise inputs / the outputs relative to the
+                                 // stencil arrays' layout (0 unless their rows are shifted, refined patches)
     T wA, wB, wC;                // lap = wA*S1 + wB*S2 + wC*f0 (S1/S2: sums of +-1 / +-2 neighbours)
     StageCoef<T> c1, c2, c4;     // stage coefficients at t, t + h/2, t + h
     T h, h_half, h2_quarter, h2_half, h_sixth, h_third, h2_sixth;
@@ -137,24 +139,55 @@ __device__ __forceinline__ void st_out(T *p, const T *v, uint64_t pol)
 }
 
 // Store V sites and, for sites next to the domain edge, their periodic copies
-// in the x/y padding (4 columns, 2 rows).
+// in the x/y padding (8 columns, 2 rows). The stencils read 4 padding columns;
+// 8 fill whole 32-byte sectors (FP32; two for FP64), since a partly written
+// sector costs a DRAM read on top of its write.
 template <typename T, int V, bool HINT = false>
 __device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
                                                   const T *v, uint64_t pol = 0, bool periodic = true)
 {
     st_out<T, V, HINT>(base + off, v, pol);
     if (!periodic) return;
-    if (x < 4) st_out<T, V, HINT>(base + off + nx, v, pol);
-    if (x >= nx - 4) st_out<T, V, HINT>(base + off - nx, v, pol);
+    if (x < 8) st_out<T, V, HINT>(base + off + nx, v, pol);
+    if (x >= nx - 8) st_out<T, V, HINT>(base + off - nx, v, pol);
     if (y < 2) st_out<T, V, HINT>(base + off + (int64_t)ny * js, v, pol);
     if (y >= ny - 2) st_out<T, V, HINT>(base + off - (int64_t)ny * js, v, pol);
 }
+
+// Two FP32 sites per instruction: Blackwell's packed FP32x2 add, multiply and
+// fused multiply-add (__fadd2_rn, __fmul2_rn, __ffma2_rn; each lane rounds as
+// the scalar instruction does). A thread's V sites are consecutive in x, so a
+// pair of them is one F2. Differences are sums with a negated operand, which is
+// exact, so every expression below rounds exactly as its scalar form.
+using ::fma;  // the scalar overloads stay visible next to the F2 one below
+struct F2 {
+    float2 v;
+    __device__ __forceinline__ F2() {}
+    __device__ __forceinline__ F2(float a, float b) : v(make_float2(a, b)) {}
+    __device__ __forceinline__ explicit F2(float a) : v(make_float2(a, a)) {}
+    __device__ __forceinline__ explicit F2(float2 a) : v(a) {}
+};
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2(__fadd2_rn(a.v, make_float2(-b.v.x, -b.v.y))); }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 fma(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
+
+// FP32 with an even number of sites per thread goes through F2 pairs.
+template <typename T, int V> constexpr bool kPackedPairs = std::is_same<T, float>::value && V % 2 == 0;
 
 // F(u) = lap + (kappa - lambda/2 (|u|^2 - R^2)) u, one component pair.
 template <typename T>
 __device__ __forceinline__ void rhs_pair(const StageCoef<T> &c, T u1, T u2, T l1, T l2, T &f1, T &f2)
 {
     const T k = fma(-c.hlam, fma(u1, u1, u2 * u2) - c.R2, c.kappa);
+    f1 = fma(k, u1, l1);
+    f2 = fma(k, u2, l2);
+}
+
+// the same for two sites at once
+__device__ __forceinline__ void rhs_pair(const StageCoef<float> &c, F2 u1, F2 u2, F2 l1, F2 l2, F2 &f1, F2 &f2)
+{
+    const F2 k = fma(F2(-c.hlam), fma(u1, u1, u2 * u2) - F2(c.R2), F2(c.kappa));
     f1 = fma(k, u1, l1);
     f2 = fma(k, u2, l2);
 }
@@ -275,9 +308,9 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
 #pragma unroll
                 for (int c = 0; c < NPT; ++c) {
                     if constexpr (HINT)
-                        ldv_nc_hint<T, V>(a.pt[c] + off0, pn[c], pol_first);
+                        ldv_nc_hint<T, V>(a.pt[c] + off0 + a.dox_pt, pn[c], pol_first);
                     else
-                        ldv_nc<T, V>(a.pt[c] + off0, pn[c]);
+                        ldv_nc<T, V>(a.pt[c] + off0 + a.dox_pt, pn[c]);
                 }
             }
         }
@@ -295,9 +328,9 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
 #pragma unroll
                     for (int c = 0; c < NPT; ++c) {
                         if constexpr (HINT)
-                            ldv_nc_hint<T, V>(a.pt[c] + off + b.ks, pn[c], pol_first);
+                            ldv_nc_hint<T, V>(a.pt[c] + off + b.ks + a.dox_pt, pn[c], pol_first);
                         else
-                            ldv_nc<T, V>(a.pt[c] + off + b.ks, pn[c]);
+                            ldv_nc<T, V>(a.pt[c] + off + b.ks + a.dox_pt, pn[c]);
                     }
                 }
             }
@@ -332,6 +365,25 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                     ldv<T, V>(sl[3] + c * S::TILE + yl * S::BX + xl, zp1);
                     ldv<T, V>(sl[0] + c * S::TILE + yl * S::BX + xl, zm2);
                     ldv<T, V>(sl[4] + c * S::TILE + yl * S::BX + xl, zp2);
+                    if constexpr (kPackedPairs<T, V>) {
+                        // the FP32 difference form below, two sites per instruction
+#pragma unroll
+                        for (int v = 0; v < V; v += 2) {
+                            const int ci = S::PRE * V + v;
+                            const F2 f0(row[ci], row[ci + 1]);
+                            const F2 d1 = ((F2(row[ci - 1], row[ci]) - f0) + (F2(row[ci + 1], row[ci + 2]) - f0)) +
+                                          ((F2(ym1[v], ym1[v + 1]) - f0) + (F2(yp1[v], yp1[v + 1]) - f0)) +
+                                          ((F2(zm1[v], zm1[v + 1]) - f0) + (F2(zp1[v], zp1[v + 1]) - f0));
+                            const F2 d2 = ((F2(row[ci - 2], row[ci - 1]) - f0) + (F2(row[ci + 2], row[ci + 3]) - f0)) +
+                                          ((F2(ym2[v], ym2[v + 1]) - f0) + (F2(yp2[v], yp2[v + 1]) - f0)) +
+                                          ((F2(zm2[v], zm2[v + 1]) - f0) + (F2(zp2[v], zp2[v + 1]) - f0));
+                            const F2 l = fma(F2(a.wA), d1, F2(a.wB) * d2);
+                            lap[c][v] = l.v.x;
+                            lap[c][v + 1] = l.v.y;
+                            ctr[c][v] = f0.v.x;
+                            ctr[c][v + 1] = f0.v.y;
+                        }
+                    } else {
 #pragma unroll
                     for (int v = 0; v < V; ++v) {
                         const int ci = S::PRE * V + v;
@@ -353,8 +405,9 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                         }
                         ctr[c][v] = f0;
                     }
+                    }
                 }
-                Op::template apply<T, V, HINT>(a, b, lap, ctr, pq, off, x, y, lam_acc, pol_first);
+                Op::template apply<T, V, HINT>(a, b, lap, ctr, pq, off + a.dox_out, x, y, lam_acc, pol_first);
             }
 
             __syncthreads();  // everyone is done with the oldest plane of this window
