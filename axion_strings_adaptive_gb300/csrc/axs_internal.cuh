@@ -64,6 +64,21 @@ void rhs_coeffs(const axs_background &bg, double tau, axs_rhs_coeffs &c);
 // Codes OR-ed into a device status word by kernels whose bounded waits expire.
 constexpr unsigned kDevTimeout = 1u;
 
+// ---------------------------------------------------------------- element-wise async copies
+// cp.async of one element into shared memory; an invalid source fills zero
+// (src-size 0 reads nothing; the dummy address is never dereferenced).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src, bool valid, const T *dummy)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    const int nbytes = valid ? (int)sizeof(T) : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(valid ? src : dummy),
+                 "n"((int)sizeof(T)), "r"(nbytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // ---------------------------------------------------------------- vector types
 template <typename T> struct Vec;
 template <> struct Vec<float> {

@@ -144,11 +144,14 @@ __device__ __forceinline__ void cell_energy(const CellConst<M> &k, int scheme, M
 }
 
 // Tiled diagnostics pass. A block owns a DTX x DTY tile of cells and marches
-// in z over a chunk. Shared memory holds psi1/psi2 of five planes (tile plus a
-// 2-cell halo) for the gradient stencil, and for the two vertex planes z and
-// z+1 ((DTX+1) x (DTY+1) vertices): Pi1/Pi2, single-precision phases, and
-// gamma^2 v^2, each computed once per vertex. Plane loads use element offsets
-// precomputed per work item, so the march needs no index division.
+// in z over a chunk. Shared memory holds psi1/psi2 of six planes (tile plus a
+// 2-cell halo: the five of the gradient stencil and one in flight), Pi1/Pi2 of
+// three vertex planes ((DTX+1) x (DTY+1) vertices: z, z+1 and one in flight),
+// and for the two vertex planes z and z+1 the single-precision phases and
+// gamma^2 v^2, each computed once per vertex. Planes arrive by element-wise
+// cp.async one plane ahead of their use, so their latency overlaps the
+// current plane's work. Plane loads use element offsets precomputed per work
+// item, so the march needs no index division.
 constexpr int DTX = 32, DTY = 8, DHX = DTX + 4, DHY = DTY + 4, DVX = DTX + 1, DVY = DTY + 1;
 static_assert(DTX * DTY == kDiagThreads, "one cell per thread");
 constexpr int kPsiPts = DHX * DHY, kVtxPts = DVX * DVY;
@@ -156,9 +159,10 @@ constexpr int kPsiPer = (2 * kPsiPts + kDiagThreads - 1) / kDiagThreads;  // psi
 constexpr int kPiPer = (2 * kVtxPts + kDiagThreads - 1) / kDiagThreads;   // Pi loads per thread per plane
 constexpr int kVtxPer = (kVtxPts + kDiagThreads - 1) / kDiagThreads;      // vertices per thread per plane
 
+constexpr int kPsiSlots = 6, kPiSlots = 3;
 template <typename T, bool FAST> struct DiagSmem {
-    T ps[5][2][DHY][DHX];
-    T pi[2][2][DVY][DVX];
+    T ps[kPsiSlots][2][DHY][DHX];
+    T pi[kPiSlots][2][DVY][DVX];
     typename std::conditional<FAST, float, double>::type gv[2][DVY][DVX];
     float th[2][DVY][DVX];
     unsigned char ok[2][DVY][DVX];
@@ -234,29 +238,35 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             zin = v.wz || (z >= -v.oz && z < v.nz + v.oz);
             return (int64_t)(wrap_or_self(z, v.nz, v.wz) + v.oz) * v.ks;
         };
+        // psi of plane z (za - 2 <= z <= za + len + 1) sits in slot (z - za + 2) mod 6,
+        // Pi of vertex plane z (za <= z <= za + len) in slot (z - za) mod 3
+        auto psi_slot = [&](int z) { return (z - za + 2) % kPsiSlots; };
         auto load_psi = [&](int z) {
             bool zin;
             const int64_t po = plane_off(z, zin);
-            T *dst = &sm.ps[((z - za + 2) % 5 + 5) % 5][0][0][0];
+            T *dst = &sm.ps[psi_slot(z)][0][0][0];
 #pragma unroll
             for (int u = 0; u < kPsiPer; ++u) {
                 const int idx = tid + u * kDiagThreads;
-                if (idx < 2 * kPsiPts) dst[idx] = (zin && psi_ok[u]) ? __ldg(base + psi_off[u] + po) : T(0);
+                if (idx < 2 * kPsiPts) cp_async_elem(dst + idx, base + psi_off[u] + po, zin && psi_ok[u], base);
             }
         };
-        // vertex plane z: Pi, phases and gamma^2 v^2 (psi already in the ring)
-        auto vertex_plane = [&](int z) {
+        auto load_pi = [&](int z) {
+            if (!q.want_energy && !q.want_vel) return;  // the string finder alone reads psi only
             bool zin;
             const int64_t po = plane_off(z, zin);
-            const int ts = (z - za) & 1;
-            T *pdst = &sm.pi[ts][0][0][0];
+            T *pdst = &sm.pi[(z - za) % kPiSlots][0][0][0];
 #pragma unroll
             for (int u = 0; u < kPiPer; ++u) {
                 const int idx = tid + u * kDiagThreads;
-                if (idx < 2 * kVtxPts) pdst[idx] = (zin && pi_ok[u]) ? __ldg(base + pi_off[u] + po) : T(0);
+                if (idx < 2 * kVtxPts) cp_async_elem(pdst + idx, base + pi_off[u] + po, zin && pi_ok[u], base);
             }
-            const int slot = ((z - za + 2) % 5 + 5) % 5;
-            __syncthreads();
+        };
+        // vertex plane z: phases and gamma^2 v^2 from psi and Pi already in shared memory
+        auto vertex_plane = [&](int z) {
+            const int ts = (z - za) & 1;
+            const int ps_ = (z - za) % kPiSlots;
+            const int slot = psi_slot(z);
 #pragma unroll
             for (int u = 0; u < kVtxPer; ++u) {
                 const int idx = tid + u * kDiagThreads;
@@ -273,7 +283,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                 }
                 sm.th[ts][vy][vx] = atan2f((float)b, (float)a);
                 if (q.want_vel && FAST) {
-                    const float psi1 = a, psi2 = b, Pi1 = sm.pi[ts][0][vy][vx], Pi2 = sm.pi[ts][1][vy][vx];
+                    const float psi1 = a, psi2 = b, Pi1 = sm.pi[ps_][0][vy][vx], Pi2 = sm.pi[ps_][1][vy][vx];
                     const float phi1 = psi1 * q.f_inv_R, phi2 = psi2 * q.f_inv_R;
                     const float pd1 = (Pi1 - q.f_RpR * psi1) * q.f_inv_R2, pd2 = (Pi2 - q.f_RpR * psi2) * q.f_inv_R2;
                     const float phi_sq = phi1 * phi1 + phi2 * phi2;
@@ -281,7 +291,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     const float re = phi1 * pd1 + phi2 * pd2;
                     sm.gv[ts][vy][vx] = pd_sq * q.f_vel_a * (1.f - q.f_vel_b * phi_sq) - q.f_vel_c * re * re;
                 } else if (q.want_vel) {
-                    const double psi1 = a, psi2 = b, Pi1 = sm.pi[ts][0][vy][vx], Pi2 = sm.pi[ts][1][vy][vx];
+                    const double psi1 = a, psi2 = b, Pi1 = sm.pi[ps_][0][vy][vx], Pi2 = sm.pi[ps_][1][vy][vx];
                     const double phi1 = psi1 * q.inv_R, phi2 = psi2 * q.inv_R;
                     const double pd1 = (Pi1 - q.RpR * psi1) * q.inv_R2, pd2 = (Pi2 - q.RpR * psi2) * q.inv_R2;
                     const double phi_sq = phi1 * phi1 + phi2 * phi2;
@@ -293,13 +303,25 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             }
         };
 
-        for (int p = -2; p <= 1; ++p) load_psi(za + p);
+        // prologue: psi of za-2 .. za+2, Pi of za and za+1 (one group), then the first vertex plane
+        for (int p = -2; p <= 2; ++p) load_psi(za + p);
+        load_pi(za);
+        load_pi(za + 1);
+        cp_async_commit();
+        cp_async_wait<0>();
         __syncthreads();
         vertex_plane(za);
 
         for (int m = 0; m < len; ++m) {
             const int z = za + m;
-            load_psi(z + 2);
+            // one plane ahead: psi(z + 3) for the next plane's stencil, Pi(z + 2) for its
+            // vertex plane (their slots were last read before the previous barrier)
+            if (m + 1 < len) {
+                load_psi(z + 3);
+                load_pi(z + 2);
+            }
+            cp_async_commit();
+            cp_async_wait<1>();  // everything but this plane's group: psi(z + 2), Pi(z + 1)
             __syncthreads();
             vertex_plane(z + 1);
             __syncthreads();
@@ -309,13 +331,14 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             const bool in = x < v.nx && y < v.ny && (mask == nullptr || mask[cell] != 0);
             int w[3] = {0, 0, 0};
             if (in) {
-                const int s0 = (m + 2) % 5;
-                const int sm1 = (m + 1) % 5, sp1 = (m + 3) % 5, sm2 = m % 5, sp2 = (m + 4) % 5;
-                const int t0 = m & 1, t1 = (m + 1) & 1;
+                const int s0 = (m + 2) % kPsiSlots;
+                const int sm1 = (m + 1) % kPsiSlots, sp1 = (m + 3) % kPsiSlots, sm2 = m % kPsiSlots,
+                          sp2 = (m + 4) % kPsiSlots;
+                const int t0 = m & 1, t1 = (m + 1) & 1, tp = m % kPiSlots;
                 const int hx = lx + 2, hy = ly + 2;
                 if (q.want_energy) {
                     const T p1 = sm.ps[s0][0][hy][hx], p2 = sm.ps[s0][1][hy][hx];
-                    const T q1 = sm.pi[t0][0][ly][lx], q2 = sm.pi[t0][1][ly][lx];
+                    const T q1 = sm.pi[tp][0][ly][lx], q2 = sm.pi[tp][1][ly][lx];
                     bool done = false;
                     if constexpr (FAST) {
                         const float psq = p1 * p1 + p2 * p2;

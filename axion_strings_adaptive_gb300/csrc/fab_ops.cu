@@ -2,6 +2,7 @@
 // body of AxionStringsLevel::specific_eval_rhs, the periodic ghost fill, the
 // RK stage combinations, and copies between FABs and the fused-RK4 level
 // layout.
+#include <algorithm>
 #include "axs_internal.cuh"
 
 namespace axs {
@@ -179,15 +180,15 @@ __global__ void level_from_fab_kernel(T *lv, LevelGeom g, const axs_fab f, int t
     }
 }
 
-// Periodic copies in the 4-column x and 2-row y padding of `ncomp` level
+// Periodic copies in the 8-column x and 2-row y padding of `ncomp` level
 // components (corners included).
 template <typename T>
 __global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, LevelGeom g, int ncomp)
 {
-    const int px = nx + 8, py = ny + 4;
+    const int px = nx + 16, py = ny + 4;  // 8 padding columns either side, as the sweeps keep them
     const int64_t n = (int64_t)px * py * nz * ncomp;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(q % px) - 4;
+        const int x = (int)(q % px) - 8;
         const int y = (int)((q / px) % py) - 2;
         const int z = (int)((q / ((int64_t)px * py)) % nz);
         const int c = (int)(q / ((int64_t)px * py * nz));
@@ -195,6 +196,46 @@ __global__ void level_fill_ghosts_kernel(T *lv, int nx, int ny, int nz, LevelGeo
         const int xx = ((x % nx) + nx) % nx, yy = ((y % ny) + ny) % ny;
         T *base = lv + c * g.cs + (int64_t)z * g.ks;
         base[(x + g.ox) + (int64_t)(y + g.oy) * g.js] = base[(xx + g.ox) + (int64_t)(yy + g.oy) * g.js];
+    }
+}
+
+// Contiguous (4, nz, ny, nx) array -> level layout: valid cells and the
+// periodic padding (8 columns either side in x, 2 rows in y, corners included)
+// in one pass. One block per padded row; consecutive threads take consecutive
+// x, so reads and writes are coalesced.
+template <typename T>
+__global__ void level_scatter_kernel(T *__restrict__ lv, const T *__restrict__ src, int nx, int ny, int nz,
+                                     LevelGeom g)
+{
+    const int64_t rows = (int64_t)(ny + 4) * nz * 4;
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int y = (int)(r % (ny + 4)) - 2;
+        const int64_t zc = r / (ny + 4);  // z + nz c
+        const int z = (int)(zc % nz), c = (int)(zc / nz);
+        const int ys = ((y % ny) + ny) % ny;
+        const T *s = src + ((int64_t)c * nz + z) * ny * nx + (int64_t)ys * nx;
+        T *d = lv + c * g.cs + (int64_t)z * g.ks + (int64_t)(y + g.oy) * g.js + g.ox;
+        if (nx >= 8) {
+            for (int x = (int)threadIdx.x - 8; x < nx + 8; x += blockDim.x) d[x] = s[x < 0 ? x + nx : (x >= nx ? x - nx : x)];
+        } else {
+            for (int x = (int)threadIdx.x - 8; x < nx + 8; x += blockDim.x) d[x] = s[((x % nx) + nx) % nx];
+        }
+    }
+}
+
+// Level layout -> contiguous (4, nz, ny, nx) array, valid cells only.
+template <typename T>
+__global__ void level_gather_kernel(const T *__restrict__ lv, T *__restrict__ dst, int nx, int ny, int nz,
+                                    LevelGeom g)
+{
+    const int64_t rows = (int64_t)ny * nz * 4;
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int y = (int)(r % ny);
+        const int64_t zc = r / ny;
+        const int z = (int)(zc % nz), c = (int)(zc / nz);
+        const T *s = lv + c * g.cs + (int64_t)z * g.ks + (int64_t)(y + g.oy) * g.js + g.ox;
+        T *d = dst + r * nx;
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) d[x] = s[x];
     }
 }
 
@@ -240,12 +281,39 @@ static int same_shape(const axs_fab *a, const axs_fab *b, const char *what)
 int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, int ncomp,
                       cudaStream_t st)
 {
-    const int64_t n = (int64_t)(nx + 8) * (ny + 4) * nz * ncomp;
+    const int64_t n = (int64_t)(nx + 16) * (ny + 4) * nz * ncomp;
     if (dtype == AXS_F64)
         level_fill_ghosts_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<double *>(data), nx, ny, nz, g, ncomp);
     else
         level_fill_ghosts_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<float *>(data), nx, ny, nz, g, ncomp);
     return launch_status("level_fill_ghosts");
+}
+
+// Between a level and a contiguous (4, nz, ny, nx) device array (to_level: the
+// array into the level, padding included; else the level's valid cells out).
+int level_copy_contiguous(void *lv, void *arr, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g,
+                          int to_level, cudaStream_t st)
+{
+    const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
+    const int64_t rows = to_level ? (int64_t)(ny + 4) * nz * 4 : (int64_t)ny * nz * 4;
+    const int grid = (int)std::min<int64_t>(rows, (int64_t)sms * 16);
+    const int threads = nx + 16 <= 128 ? 128 : 256;
+    if (dtype == AXS_F64) {
+        if (to_level)
+            level_scatter_kernel<double><<<grid, threads, 0, st>>>(static_cast<double *>(lv),
+                                                                   static_cast<const double *>(arr), nx, ny, nz, g);
+        else
+            level_gather_kernel<double><<<grid, threads, 0, st>>>(static_cast<const double *>(lv),
+                                                                  static_cast<double *>(arr), nx, ny, nz, g);
+    } else {
+        if (to_level)
+            level_scatter_kernel<float><<<grid, threads, 0, st>>>(static_cast<float *>(lv),
+                                                                  static_cast<const float *>(arr), nx, ny, nz, g);
+        else
+            level_gather_kernel<float><<<grid, threads, 0, st>>>(static_cast<const float *>(lv),
+                                                                 static_cast<float *>(arr), nx, ny, nz, g);
+    }
+    return launch_status(to_level ? "level scatter" : "level gather");
 }
 
 int level_copy_fab(void *lv, int32_t dtype, const LevelGeom &g, const axs_fab &f, int to_level, cudaStream_t st)

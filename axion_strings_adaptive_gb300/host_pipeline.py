@@ -4,11 +4,14 @@ A caller that keeps its fields in host memory (a CPU code handing boxes to the
 GPU, or a stream of independent realisations) pays a host->device copy of each
 input and a device->host copy of each result per call. :class:`HostStepPipeline`
 rotates over `depth` device levels: the upload of call s+1, the compute of call
-s and the download of call s-1 use different levels and run on three streams,
-so the two copy directions (the link is full duplex) and the compute overlap.
-Every call is: pinned host state -> ``axs_level_upload`` (one strided DMA copy
-into the level layout + periodic padding) -> ``axs_level_rk4_advance`` ->
-``axs_level_download`` -> pinned host result.
+s and the download of call s-1 use different levels, so the two copy
+directions (the link is full duplex) and the compute overlap. Uploads and
+downloads run on streams of their own per level, so a level's scatter or
+gather kernel never holds up the copy engine for the next level. Every call is:
+pinned host state -> ``axs_level_upload`` (one contiguous DMA copy into the
+level's work buffer, then a scatter into the level layout with its periodic
+padding) -> ``axs_level_rk4_advance`` -> ``axs_level_download`` (gather into
+the work buffer, one contiguous DMA copy) -> pinned host result.
 """
 from __future__ import annotations
 
@@ -30,7 +33,9 @@ class HostStepPipeline:
             self.levels.append(lv)
         dev = level.state.device
         self.depth = len(self.levels)
-        self.up, self.comp, self.down = (torch.cuda.Stream(device=dev) for _ in range(3))
+        self.comp = torch.cuda.Stream(device=dev)
+        self.ups = [torch.cuda.Stream(device=dev) for _ in range(self.depth)]
+        self.downs = [torch.cuda.Stream(device=dev) for _ in range(self.depth)]
         self._up_done = [torch.cuda.Event() for _ in range(self.depth)]
         self._comp_done = [torch.cuda.Event() for _ in range(self.depth)]
         self._down_done = [torch.cuda.Event() for _ in range(self.depth)]
@@ -43,22 +48,23 @@ class HostStepPipeline:
         slot = self._k % self.depth
         self._k += 1
         lv = self.levels[slot]
+        up, down = self.ups[slot], self.downs[slot]
         if self._used[slot]:
-            self.up.wait_event(self._down_done[slot])  # the slot's previous result has left
+            up.wait_event(self._down_done[slot])  # the slot's previous result has left
         self._used[slot] = True
-        L.call("axs_level_upload", C.byref(lv.c), C.c_void_p(host_in.data_ptr()), self.up.cuda_stream)
-        self._up_done[slot].record(self.up)
+        L.call("axs_level_upload", C.byref(lv.c), C.c_void_p(host_in.data_ptr()), up.cuda_stream)
+        self._up_done[slot].record(up)
         self.comp.wait_event(self._up_done[slot])
         lv.advance(bg, tau_i, t0, dt, nsteps, self.comp)
         self._comp_done[slot].record(self.comp)
-        self.down.wait_event(self._comp_done[slot])
-        L.call("axs_level_download", C.byref(lv.c), C.c_void_p(host_out.data_ptr()), self.down.cuda_stream)
-        self._down_done[slot].record(self.down)
+        down.wait_event(self._comp_done[slot])
+        L.call("axs_level_download", C.byref(lv.c), C.c_void_p(host_out.data_ptr()), down.cuda_stream)
+        self._down_done[slot].record(down)
 
     def join(self, stream: torch.cuda.Stream | None = None) -> None:
         """Make `stream` (default: the current stream) wait for everything queued."""
         s = stream or torch.cuda.current_stream()
-        for st in (self.up, self.comp, self.down):
+        for st in [self.comp] + self.ups + self.downs:
             s.wait_stream(st)
 
     def device_status(self) -> None:

@@ -689,7 +689,7 @@ def run_native(args):
         lv.tile_config = [cid for cid, name in lv.tile_configs() if name == cfg32][0] if cfg32 != "default" else 0
         hin = [ic64.float().cpu().pin_memory(), (ic64.float() * 0.999).cpu().pin_memory()]
         hout = [torch.empty_like(hin[0]).pin_memory() for _ in range(2)]
-        steps_e = max(4, args.steps // 2)
+        steps_e = max(4, args.steps)
         pipe = HostStepPipeline(lv, depth=3)
 
         def run(k, serial):
@@ -721,9 +721,11 @@ def run_native(args):
                "steps": steps_e, "ms_per_step": ems / steps_e,
                "serial_value": ws * n ** 3 * steps_e / (ems_serial * 1e-3), "serial_ms_per_step": ems_serial / steps_e,
                "link_gbs_per_direction": nbytes / (ems / steps_e * 1e-3) / 1e9,
-               "path": "pinned host state -> axs_level_upload (strided DMA into the level layout) -> "
-                       "axs_level_rk4_advance(1 step) -> axs_level_download -> pinned host result; upload, compute "
-                       "and download of neighbouring steps overlap (HostStepPipeline, 3 levels, 3 streams)"}
+               "path": "pinned host state -> axs_level_upload (contiguous DMA into the level's work buffer, "
+                       "scatter into the level layout) -> axs_level_rk4_advance(1 step) -> axs_level_download "
+                       "(gather, contiguous DMA) -> pinned host result; upload, compute and download of "
+                       "neighbouring steps overlap (HostStepPipeline: 3 levels, a compute stream and an upload and "
+                       "a download stream per level)"}
         del lv, pipe, hin, hout
 
     cpu = None

@@ -145,9 +145,9 @@ int axs_rk4_combine(const axs_fab *dst, const axs_fab *uold, const axs_fab *k1, 
  *   (x + x_offset) + (y + y_offset)*jstride + z*kstride + c*cstride.
  * x_offset puts x = 0 on a 128-byte boundary (32 floats / 16 doubles) and
  * jstride is a multiple of 128 bytes, so every row of valid cells starts a
- * cache line; the 4 columns left of x = 0 and right of x = nx-1 and the 2 rows
- * outside y hold periodic copies that the kernels keep current (padding
- * corners excepted). `state` holds psi1, psi2, Pi1, Pi2; `work` holds 8
+ * cache line; the 8 columns left of x = 0 and right of x = nx-1 (the stencils
+ * read 4; 8 fill whole 32-byte sectors) and the 2 rows outside y hold periodic
+ * copies that the kernels keep current (padding corners excepted). `state` holds psi1, psi2, Pi1, Pi2; `work` holds 8
  * components of the same layout used between the two sweeps of a step, plus
  * a 256-byte status block. Both must be 128-byte aligned. */
 typedef struct axs_level_layout {
@@ -184,8 +184,12 @@ int axs_level_import_fab(const axs_level *lv, const axs_fab *src, void *stream);
 int axs_level_export_fab(const axs_level *lv, const axs_fab *dst, void *stream);
 
 /* The level's valid cells from / to a HOST array (4, nz, ny, nx) of its dtype
- * (pinned memory for asynchronous copies): one strided DMA copy each way, then
- * (upload) the periodic padding. For callers whose fields live in host memory. */
+ * (pinned memory for asynchronous copies): one contiguous DMA copy each way,
+ * staged in the level's work buffer, and one device pass between that staging
+ * array and the level layout (upload also fills the periodic padding). The
+ * work buffer holds stage values only inside a step, so do not call these
+ * between axs_level_rk4_sweep(A) and (B) of one step, nor concurrently with a
+ * step of the same level. For callers whose fields live in host memory. */
 int axs_level_upload(const axs_level *lv, const void *host_state, void *stream);
 int axs_level_download(const axs_level *lv, void *host_state, void *stream);
 
