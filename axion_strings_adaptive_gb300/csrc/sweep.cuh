@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     T *ring = reinterpret_cast<T *>(smem_raw);
     __shared__ uint64_t full[NS];
     __shared__ int abort_flag;
-    __shared__ double lam_red[S::NT / 32];
+    __shared__ double lam_red[(S::NT + 31) / 32];
 
     const int tid = threadIdx.x;
     const int tx = tid % S::NTX, ty = tid / S::NTX;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
         __syncthreads();
         if (tid == 0) {
             double s = 0.0;
-            for (int w = 0; w < S::NT / 32; ++w) s += lam_red[w];
+            for (int w = 0; w < (S::NT + 31) / 32; ++w) s += lam_red[w];
             a.lam_partial[blockIdx.x] = s * a.inv_lambda0;
         }
     }
