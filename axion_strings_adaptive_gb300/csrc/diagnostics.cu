@@ -177,7 +177,8 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                                                                unsigned long long *__restrict__ list_counter,
                                                                long long *__restrict__ list, long long capacity,
                                                                int tiles_x, int ntiles, int zchunk, long long n_items,
-                                                               long long items_per_box, int64_t box_stride)
+                                                               long long items_per_box, int64_t box_stride,
+                                                               uint8_t *__restrict__ tags)
 {
     extern __shared__ __align__(16) unsigned char diag_smem_raw[];
     DiagSmem<T, FAST> &sm = *reinterpret_cast<DiagSmem<T, FAST> *>(diag_smem_raw);
@@ -417,6 +418,9 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                         w[2] = winding4(d000, d001, d101, d100, ties);
                         cnt[3] += ties;
                     }
+                    // StringTagger (StringTagger.hpp:117-151): a cell is tagged when a
+                    // plaquette at its low corner is pierced
+                    if (tags != nullptr) tags[cell] = (w[0] | w[1] | w[2]) != 0;
                     cnt[0] += (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
                     cnt[1] += abs(w[0]) + abs(w[1]) + abs(w[2]);
                     if (q.want_vel && (w[0] | w[1] | w[2])) {
@@ -595,7 +599,7 @@ static int64_t diag_scratch_bytes(int64_t ncell) { return 256 + (int64_t)diag_gr
 
 static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *mask, axs_diag_result *out,
                     int64_t *list, int64_t capacity, void *scratch, int64_t scratch_bytes, cudaStream_t st,
-                    int nboxes = 1, int64_t box_stride = 0)
+                    int nboxes = 1, int64_t box_stride = 0, uint8_t *tags = nullptr)
 {
     AXS_REQUIRE(p != nullptr && out != nullptr, AXS_ERR_INVALID_ARGUMENT, "null params or result");
     AXS_REQUIRE(p->dx > 0.0 && p->R > 0.0 && p->m_r > 0.0, AXS_ERR_INVALID_ARGUMENT,
@@ -655,7 +659,7 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     auto launch = [&](auto kern, size_t smem) -> int {
         AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<grid, kDiagThreads, smem, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x, ntiles, zchunk,
-                                               items, items_per_box, box_stride);
+                                               items, items_per_box, box_stride, tags);
         return AXS_OK;
     };
     if (v.dtype == AXS_F64)
@@ -681,6 +685,24 @@ int diag_level_box(const void *data, int32_t dtype, int nx, int ny, int nz, cons
 }
 
 int64_t diag_scratch_bytes_for(int64_t ncell) { return diag_scratch_bytes(ncell); }
+
+// The refinement tagger's plaquette criterion on a periodic level: the string
+// finder's pass (same windings, bit for bit) writing one tag byte per cell
+// (x fastest) instead of a pierced list. `out` is a device result record.
+int diag_level_plaquette_tags(const void *state, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, double dx,
+                              uint8_t *tags, axs_diag_result *out, void *scratch, int64_t scratch_bytes,
+                              cudaStream_t st)
+{
+    DiagView v{state, dtype, nx, ny, nz, g.ox, g.oy, 0, 1, 1, 1, g.js, g.ks, g.cs};
+    axs_diag_params p{};
+    p.dx = dx;
+    p.R = 1.0;
+    p.m_r = 1.0;
+    p.masking_scheme = AXS_MASK_NONE;
+    p.boundary = AXS_BOUNDARY_PERIODIC;
+    p.want_plaquettes = 1;
+    return run_diag(v, &p, nullptr, out, nullptr, 0, scratch, scratch_bytes, st, 1, 0, tags);
+}
 
 // nboxes boxes of one geometry, box_stride elements apart, with explicit ghost
 // layers (refined patches), summed into one result. A pierced-list entry is

@@ -22,6 +22,16 @@
 namespace axs {
 
 int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g);
+int diag_level_plaquette_tags(const void *state, int32_t dtype, int nx, int ny, int nz, const LevelGeom &g, double dx,
+                              uint8_t *tags, axs_diag_result *out, void *scratch, int64_t scratch_bytes,
+                              cudaStream_t st);
+int64_t diag_scratch_bytes_for(int64_t ncell);
+
+// scratch: [0, 256) tag count and the plaquette pass's result record,
+// [256, 256 + tag bytes) buffer pass temporaries, then the plaquette pass's scratch
+constexpr int64_t kTagResultOffset = 64;
+static int64_t tag_bytes_rounded(int64_t n) { return (n + 255) / 256 * 256; }
+static_assert(kTagResultOffset + sizeof(axs_diag_result) <= 256, "tag scratch header");
 
 struct TagGeom {
     int nx, ny, nz, ox, oy;
@@ -209,7 +219,8 @@ extern "C" {
 int axs_tag_scratch_bytes(int32_t nx, int32_t ny, int32_t nz, int64_t *bytes)
 {
     AXS_REQUIRE(bytes != nullptr && nx > 0 && ny > 0 && nz > 0, AXS_ERR_INVALID_ARGUMENT, "bad arguments");
-    *bytes = 256 + ((int64_t)nx * ny * nz + 255) / 256 * 256;
+    const int64_t n = (int64_t)nx * ny * nz;
+    *bytes = 256 + tag_bytes_rounded(n) + diag_scratch_bytes_for(n);
     return AXS_OK;
 }
 
@@ -249,11 +260,22 @@ int axs_level_tag_cells(const axs_level *lv, const axs_tag_params *p, uint8_t *t
     q.use_rad = p->radial_gradient_threshold < DBL_MAX;
     const int grid = tag_grid(n);
     uint8_t *first = p->n_error_buf > 0 ? tmp : tags_dev;
-    if (lv->dtype == AXS_F32)
-        tag_kernel<float><<<grid, 256, 0, st>>>(static_cast<const float *>(lv->state), g, q, first);
-    else
-        tag_kernel<double><<<grid, 256, 0, st>>>(static_cast<const double *>(lv->state), g, q, first);
-    if ((rc = launch_status("tag cells"))) return rc;
+    if (!q.use_grad && !q.use_rad) {
+        // the plaquette criterion alone (the reference's default): the string
+        // finder's tiled pass, one phase per vertex instead of seven per cell
+        char *base = static_cast<char *>(scratch);
+        const int64_t off = 256 + tag_bytes_rounded(n);
+        auto *res = reinterpret_cast<axs_diag_result *>(base + kTagResultOffset);
+        if ((rc = diag_level_plaquette_tags(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, lg, p->dx, first, res,
+                                            base + off, scratch_bytes - off, st)))
+            return rc;
+    } else {
+        if (lv->dtype == AXS_F32)
+            tag_kernel<float><<<grid, 256, 0, st>>>(static_cast<const float *>(lv->state), g, q, first);
+        else
+            tag_kernel<double><<<grid, 256, 0, st>>>(static_cast<const double *>(lv->state), g, q, first);
+        if ((rc = launch_status("tag cells"))) return rc;
+    }
     if (p->n_error_buf > 0) {
         dilate_axis_kernel<<<grid, 256, 0, st>>>(tmp, tags_dev, lv->nx, lv->ny, lv->nz, 0, p->n_error_buf);
         dilate_axis_kernel<<<grid, 256, 0, st>>>(tags_dev, tmp, lv->nx, lv->ny, lv->nz, 1, p->n_error_buf);
