@@ -119,9 +119,10 @@ class Ensemble:
         return self.results(bg, tau)
 
     def capture(self, bg: Background, tau_i: float, t0: float, dt: float, nsteps: int,
-                diagnostics: bool = True) -> torch.cuda.CUDAGraph:
+                diagnostics: bool = True, per_cell_fp32: bool = False) -> torch.cuda.CUDAGraph:
         """Record nsteps RK4 steps of every box (plus per-box diagnostics at the
-        end) as one CUDA graph; replay it with ``graph.replay()``."""
+        end, per-cell terms in FP64 or, with per_cell_fp32, in FP32) as one CUDA
+        graph; replay it with ``graph.replay()``."""
         # warm-up outside the capture (module loading, kernel attributes), state restored
         saved = self.state.clone()
         side = torch.cuda.Stream(device=self.state.device)
@@ -129,7 +130,7 @@ class Ensemble:
         with torch.cuda.stream(side):
             self.advance(bg, tau_i, t0, dt, 1, side)
             if diagnostics:
-                self.diagnostics_async(bg, tau_i + t0 + nsteps * dt, stream=side)
+                self.diagnostics_async(bg, tau_i + t0 + nsteps * dt, per_cell_fp32=per_cell_fp32, stream=side)
         torch.cuda.current_stream().wait_stream(side)
         self.state.copy_(saved)
         del saved
@@ -139,7 +140,7 @@ class Ensemble:
             s = torch.cuda.current_stream()
             self.advance(bg, tau_i, t0, dt, nsteps, s)
             if diagnostics:
-                self.diagnostics_async(bg, tau_i + t0 + nsteps * dt, stream=s)
+                self.diagnostics_async(bg, tau_i + t0 + nsteps * dt, per_cell_fp32=per_cell_fp32, stream=s)
         return g
 
     def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 3, repeats: int = 2,

@@ -264,6 +264,18 @@ def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 
     same = bool(torch.equal(ens.state, eager_final))
     tau_f = TAU_I + nsteps * DT
     res = ens.results(bg, tau_f)
+    # the same graph with the diagnostics' per-cell terms in FP32 (FP64 accumulation)
+    del graph
+    ens.state.copy_(init)
+    graph = ens.capture(bg, TAU_I, 0.0, DT, nsteps, diagnostics=True, per_cell_fp32=True)
+    graph.replay()
+    ens.state.copy_(init)
+    ms_graph32 = timed(graph.replay)
+    ens.device_status()
+    res32 = ens.results(bg, tau_f)
+    rho_rel32 = max(abs(a.energy["rho_tot_unscreened"] / b.energy["rho_tot_unscreened"] - 1.0)
+                    for a, b in zip(res32, res))
+    same_np32 = all(a.n_p_plain == b.n_p_plain for a, b in zip(res32, res))
     cfg_name = dict(ens.tile_configs()).get(ens.plan.tile_config, "default")
     plan = {"tile_config": cfg_name, "z_chunk": ens.plan.z_chunk or "auto", "work_items": ens.plan.n_items,
             "grid": [ens.plan.grid_a, ens.plan.grid_b]}
@@ -296,6 +308,9 @@ def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 
             "graph_ms": ms_graph, "graph_site_updates_per_s": sites * nsteps / (ms_graph * 1e-3),
             "eager_ms": ms_eager, "eager_site_updates_per_s": sites * nsteps / (ms_eager * 1e-3),
             "graph_equals_eager": same,
+            "graph_fp32_cells_ms": ms_graph32,
+            "graph_fp32_cells_site_updates_per_s": sites * nsteps / (ms_graph32 * 1e-3),
+            "fp32_cells_max_rho_rel_diff": rho_rel32, "fp32_cells_same_n_p": same_np32,
             "hbm_frac_of_measured": words * 4 * sites * nsteps / (ms_eager * 1e-3) / 1e9 / hbm_peak,
             "per_box_levels_ms": ms_levels, "speedup_vs_per_box_levels": ms_levels / ms_graph,
             "plan": plan, "autotune_ms_per_step": tune,
