@@ -169,12 +169,13 @@ def test_homogeneous_solution_is_exact(axs, dtype, tol):
 
 
 def _check_padding(lv, val):
-    """The 4 columns either side in x and 2 rows either side in y hold periodic copies."""
+    """The 8 columns either side in x (whole 32-byte sectors; the stencils read 4)
+    and 2 rows either side in y hold periodic copies (nx >= 8)."""
     st = lv.state.cpu().numpy()
     ox, oy, nx, ny = lv.layout.x_offset, lv.layout.y_offset, lv.nx, lv.ny
     rows = st[:, :, oy:oy + ny]
-    np.testing.assert_array_equal(rows[..., ox - 4:ox], val[..., nx - 4:nx])
-    np.testing.assert_array_equal(rows[..., ox + nx:ox + nx + 4], val[..., :4])
+    np.testing.assert_array_equal(rows[..., ox - 8:ox], val[..., nx - 8:nx])
+    np.testing.assert_array_equal(rows[..., ox + nx:ox + nx + 8], val[..., :8])
     np.testing.assert_array_equal(st[:, :, oy - 2:oy, ox:ox + nx], val[:, :, ny - 2:ny, :])
     np.testing.assert_array_equal(st[:, :, oy + ny:oy + ny + 2, ox:ox + nx], val[:, :, :2, :])
 
