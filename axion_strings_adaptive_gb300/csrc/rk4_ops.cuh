@@ -7,44 +7,42 @@
 
 namespace axs {
 
-// Sweep A: stencil on (psi_n, Pi_n); writes S3, S4 (with periodic copies) and G, P.
-struct ForwardA {
-    static constexpr int kPointwise = 0;
-    static constexpr bool kLambdaGrad = false;
-    template <typename T, int V, bool HINT, typename PQ>
-    __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &, int64_t off, int x, int y, double &,
-                                 uint64_t pol)
-    {
-        T o[8][V];
-        if constexpr (kPackedPairs<T, V>) {
-            // the expressions below, two sites per instruction
+// Stage arithmetic of sweep A on V sites: from the Laplacians and centre
+// values of (psi1, psi2, Pi1, Pi2) to o = (S3_1, S3_2, S4_1, S4_2, G_1, G_2,
+// P_1, P_2). The separate sweeps and the fused patch step both call it, so
+// their results agree bit for bit.
+template <typename T, int V>
+__device__ __forceinline__ void stage_a(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V],
+                                        T (&o)[8][V])
+{
+    if constexpr (kPackedPairs<T, V>) {
+        // the expressions below, two sites per instruction
 #pragma unroll
-            for (int v = 0; v < V; v += 2) {
-                const F2 p1(ctr[0][v], ctr[0][v + 1]), p2(ctr[1][v], ctr[1][v + 1]);
-                const F2 q1(ctr[2][v], ctr[2][v + 1]), q2(ctr[3][v], ctr[3][v + 1]);
-                const F2 l0(lap[0][v], lap[0][v + 1]), l1(lap[1][v], lap[1][v + 1]);
-                const F2 l2(lap[2][v], lap[2][v + 1]), l3(lap[3][v], lap[3][v + 1]);
-                const F2 hh(a.h_half);
-                F2 f11, f12, f21, f22;
-                rhs_pair(a.c1, p1, p2, l0, l1, f11, f12);
-                const F2 c1 = fma(hh, q1, p1), c2 = fma(hh, q2, p2);
-                rhs_pair(a.c2, c1, c2, fma(hh, l2, l0), fma(hh, l3, l1), f21, f22);
-                const F2 r[8] = {fma(F2(a.h2_quarter), f11, c1),
-                                 fma(F2(a.h2_quarter), f12, c2),
-                                 fma(F2(a.h2_half), f21, fma(F2(a.h), q1, p1)),
-                                 fma(F2(a.h2_half), f22, fma(F2(a.h), q2, p2)),
-                                 fma(F2(-2.f), f21, f11),
-                                 fma(F2(-2.f), f22, f12),
-                                 fma(F2(a.h_third), f21, fma(F2(a.h_sixth), f11, q1)),
-                                 fma(F2(a.h_third), f22, fma(F2(a.h_sixth), f12, q2))};
+        for (int v = 0; v < V; v += 2) {
+            const F2 p1(ctr[0][v], ctr[0][v + 1]), p2(ctr[1][v], ctr[1][v + 1]);
+            const F2 q1(ctr[2][v], ctr[2][v + 1]), q2(ctr[3][v], ctr[3][v + 1]);
+            const F2 l0(lap[0][v], lap[0][v + 1]), l1(lap[1][v], lap[1][v + 1]);
+            const F2 l2(lap[2][v], lap[2][v + 1]), l3(lap[3][v], lap[3][v + 1]);
+            const F2 hh(a.h_half);
+            F2 f11, f12, f21, f22;
+            rhs_pair(a.c1, p1, p2, l0, l1, f11, f12);
+            const F2 c1 = fma(hh, q1, p1), c2 = fma(hh, q2, p2);
+            rhs_pair(a.c2, c1, c2, fma(hh, l2, l0), fma(hh, l3, l1), f21, f22);
+            const F2 r[8] = {fma(F2(a.h2_quarter), f11, c1),
+                             fma(F2(a.h2_quarter), f12, c2),
+                             fma(F2(a.h2_half), f21, fma(F2(a.h), q1, p1)),
+                             fma(F2(a.h2_half), f22, fma(F2(a.h), q2, p2)),
+                             fma(F2(-2.f), f21, f11),
+                             fma(F2(-2.f), f22, f12),
+                             fma(F2(a.h_third), f21, fma(F2(a.h_sixth), f11, q1)),
+                             fma(F2(a.h_third), f22, fma(F2(a.h_sixth), f12, q2))};
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    o[c][v] = r[c].v.x;
-                    o[c][v + 1] = r[c].v.y;
-                }
+            for (int c = 0; c < 8; ++c) {
+                o[c][v] = r[c].v.x;
+                o[c][v + 1] = r[c].v.y;
             }
-        } else {
+        }
+    } else {
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             const T p1 = ctr[0][v], p2 = ctr[1][v], q1 = ctr[2][v], q2 = ctr[3][v];
@@ -62,7 +60,59 @@ struct ForwardA {
             o[6][v] = fma(a.h_third, f21, fma(a.h_sixth, f11, q1));  // P = Pi + h/6 F1 + h/3 F2
             o[7][v] = fma(a.h_third, f22, fma(a.h_sixth, f12, q2));
         }
+    }
+}
+
+// Stage arithmetic of sweep B on V sites: from the Laplacians and centre
+// values of (S3_1, S3_2, S4_1, S4_2) and the pointwise (G, P) to
+// o = (psi1, psi2, Pi1, Pi2) at the end of the step.
+template <typename T, int V, typename PQ>
+__device__ __forceinline__ void stage_b(const SweepArgs<T> &a, const T (&lap)[4][V], const T (&ctr)[4][V],
+                                        const PQ &pq, T (&o)[4][V])
+{
+    if constexpr (kPackedPairs<T, V>) {
+        // the expressions below, two sites per instruction
+#pragma unroll
+        for (int v = 0; v < V; v += 2) {
+            auto pr = [&](const T (&x)[V]) { return F2(x[v], x[v + 1]); };
+            F2 f31, f32, f41, f42;
+            rhs_pair(a.c2, pr(ctr[0]), pr(ctr[1]), pr(lap[0]), pr(lap[1]), f31, f32);
+            rhs_pair(a.c4, pr(ctr[2]), pr(ctr[3]), pr(lap[2]), pr(lap[3]), f41, f42);
+            const F2 r[4] = {fma(F2(a.h2_sixth), pr(pq[0]) + f31, pr(ctr[2])),
+                             fma(F2(a.h2_sixth), pr(pq[1]) + f32, pr(ctr[3])),
+                             fma(F2(a.h_sixth), f41, fma(F2(a.h_third), f31, pr(pq[2]))),
+                             fma(F2(a.h_sixth), f42, fma(F2(a.h_third), f32, pr(pq[3])))};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                o[c][v] = r[c].v.x;
+                o[c][v + 1] = r[c].v.y;
+            }
         }
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            T f31, f32, f41, f42;
+            rhs_pair(a.c2, ctr[0][v], ctr[1][v], lap[0][v], lap[1][v], f31, f32);  // F3 = F(t + h/2, S3)
+            rhs_pair(a.c4, ctr[2][v], ctr[3][v], lap[2][v], lap[3][v], f41, f42);  // F4 = F(t + h, S4)
+            o[0][v] = fma(a.h2_sixth, pq[0][v] + f31, ctr[2][v]);
+            o[1][v] = fma(a.h2_sixth, pq[1][v] + f32, ctr[3][v]);
+            o[2][v] = fma(a.h_sixth, f41, fma(a.h_third, f31, pq[2][v]));
+            o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[3][v]));
+        }
+    }
+}
+
+// Sweep A: stencil on (psi_n, Pi_n); writes S3, S4 (with periodic copies) and G, P.
+struct ForwardA {
+    static constexpr int kPointwise = 0;
+    static constexpr bool kLambdaGrad = false;
+    template <typename T, int V, bool HINT, typename PQ>
+    __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
+                                 const T (&ctr)[4][V], const PQ &, int64_t off, int x, int y, double &,
+                                 uint64_t pol)
+    {
+        T o[8][V];
+        stage_a<T, V>(a, lap, ctr, o);
 #pragma unroll
         for (int c = 0; c < 4; ++c)
             store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol, b.periodic);
@@ -81,36 +131,7 @@ struct ForwardB {
                                  uint64_t pol)
     {
         T o[4][V];
-        if constexpr (kPackedPairs<T, V>) {
-            // the expressions below, two sites per instruction
-#pragma unroll
-            for (int v = 0; v < V; v += 2) {
-                auto pr = [&](const T (&x)[V]) { return F2(x[v], x[v + 1]); };
-                F2 f31, f32, f41, f42;
-                rhs_pair(a.c2, pr(ctr[0]), pr(ctr[1]), pr(lap[0]), pr(lap[1]), f31, f32);
-                rhs_pair(a.c4, pr(ctr[2]), pr(ctr[3]), pr(lap[2]), pr(lap[3]), f41, f42);
-                const F2 r[4] = {fma(F2(a.h2_sixth), pr(pq[0]) + f31, pr(ctr[2])),
-                                 fma(F2(a.h2_sixth), pr(pq[1]) + f32, pr(ctr[3])),
-                                 fma(F2(a.h_sixth), f41, fma(F2(a.h_third), f31, pr(pq[2]))),
-                                 fma(F2(a.h_sixth), f42, fma(F2(a.h_third), f32, pr(pq[3])))};
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    o[c][v] = r[c].v.x;
-                    o[c][v + 1] = r[c].v.y;
-                }
-            }
-        } else {
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            T f31, f32, f41, f42;
-            rhs_pair(a.c2, ctr[0][v], ctr[1][v], lap[0][v], lap[1][v], f31, f32);  // F3 = F(t + h/2, S3)
-            rhs_pair(a.c4, ctr[2][v], ctr[3][v], lap[2][v], lap[3][v], f41, f42);  // F4 = F(t + h, S4)
-            o[0][v] = fma(a.h2_sixth, pq[0][v] + f31, ctr[2][v]);
-            o[1][v] = fma(a.h2_sixth, pq[1][v] + f32, ctr[3][v]);
-            o[2][v] = fma(a.h_sixth, f41, fma(a.h_third, f31, pq[2][v]));
-            o[3][v] = fma(a.h_sixth, f42, fma(a.h_third, f32, pq[3][v]));
-        }
-        }
+        stage_b<T, V>(a, lap, ctr, pq, o);
 #pragma unroll
         for (int c = 0; c < 4; ++c)
             store_with_copies<T, V, HINT>(a.out[c], off, x, y, b.nx, b.ny, b.js, o[c], pol, b.periodic);

@@ -204,6 +204,70 @@ __device__ __forceinline__ void rhs_adjoint_pair(const StageCoef<T> &c, T u1, T 
     o2 = fma(k, a2, la2) - ua * u2;
 }
 
+// The 13-point 4th-order Laplacian and the centre values of V consecutive
+// sites of one component, from five z planes held in shared memory (planes
+// z-2 .. z+2; `at` is the first site's element offset in a plane, `bx` the row
+// length). Every sweep evaluates its stencils through this function, so all of
+// them round alike. FP32: differences from the centre first (exact while a
+// neighbour lies within a factor 2 of f0), so the -30 f0 term of the stencil
+// does not cancel against the neighbour sums: lap = wA sum(f+-1 - f0) +
+// wB sum(f+-2 - f0), two sites per packed instruction where V is even. FP64:
+// the plain weighted sums.
+template <typename T, int V>
+__device__ __forceinline__ void star_laplacian(const SweepArgs<T> &a, const T *zm2p, const T *zm1p, const T *P0,
+                                               const T *zp1p, const T *zp2p, int at, int bx, T (&lap)[V],
+                                               T (&ctr)[V])
+{
+    constexpr int PRE = (2 + V - 1) / V, NROW = 2 * PRE + 1;
+    T row[NROW * V], ym1[V], yp1[V], ym2[V], yp2[V], zm1[V], zp1[V], zm2[V], zp2[V];
+#pragma unroll
+    for (int r = 0; r < NROW; ++r) ldv<T, V>(P0 + at + (r - PRE) * V, row + r * V);
+    ldv<T, V>(P0 + at - bx, ym1);
+    ldv<T, V>(P0 + at + bx, yp1);
+    ldv<T, V>(P0 + at - 2 * bx, ym2);
+    ldv<T, V>(P0 + at + 2 * bx, yp2);
+    ldv<T, V>(zm1p + at, zm1);
+    ldv<T, V>(zp1p + at, zp1);
+    ldv<T, V>(zm2p + at, zm2);
+    ldv<T, V>(zp2p + at, zp2);
+    if constexpr (kPackedPairs<T, V>) {
+#pragma unroll
+        for (int v = 0; v < V; v += 2) {
+            const int ci = PRE * V + v;
+            const F2 f0(row[ci], row[ci + 1]);
+            const F2 d1 = ((F2(row[ci - 1], row[ci]) - f0) + (F2(row[ci + 1], row[ci + 2]) - f0)) +
+                          ((F2(ym1[v], ym1[v + 1]) - f0) + (F2(yp1[v], yp1[v + 1]) - f0)) +
+                          ((F2(zm1[v], zm1[v + 1]) - f0) + (F2(zp1[v], zp1[v + 1]) - f0));
+            const F2 d2 = ((F2(row[ci - 2], row[ci - 1]) - f0) + (F2(row[ci + 2], row[ci + 3]) - f0)) +
+                          ((F2(ym2[v], ym2[v + 1]) - f0) + (F2(yp2[v], yp2[v + 1]) - f0)) +
+                          ((F2(zm2[v], zm2[v + 1]) - f0) + (F2(zp2[v], zp2[v + 1]) - f0));
+            const F2 l = fma(F2(a.wA), d1, F2(a.wB) * d2);
+            lap[v] = l.v.x;
+            lap[v + 1] = l.v.y;
+            ctr[v] = f0.v.x;
+            ctr[v + 1] = f0.v.y;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const int ci = PRE * V + v;
+            const T f0 = row[ci];
+            if constexpr (std::is_same<T, float>::value) {
+                const T d1 = ((row[ci - 1] - f0) + (row[ci + 1] - f0)) + ((ym1[v] - f0) + (yp1[v] - f0)) +
+                             ((zm1[v] - f0) + (zp1[v] - f0));
+                const T d2 = ((row[ci - 2] - f0) + (row[ci + 2] - f0)) + ((ym2[v] - f0) + (yp2[v] - f0)) +
+                             ((zm2[v] - f0) + (zp2[v] - f0));
+                lap[v] = fma(a.wA, d1, a.wB * d2);
+            } else {
+                const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
+                const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
+                lap[v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
+            }
+            ctr[v] = f0;
+        }
+    }
+}
+
 template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel, bool HINT = false>
 __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     stencil_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
@@ -352,61 +416,10 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
             if (active) {
                 T lap[4][V], ctr[4][V];
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const T *P0 = sl[2] + c * S::TILE;
-                    T row[S::NROW * V], ym1[V], yp1[V], ym2[V], yp2[V], zm1[V], zp1[V], zm2[V], zp2[V];
-#pragma unroll
-                    for (int r = 0; r < S::NROW; ++r) ldv<T, V>(P0 + yl * S::BX + xl + (r - S::PRE) * V, row + r * V);
-                    ldv<T, V>(P0 + (yl - 1) * S::BX + xl, ym1);
-                    ldv<T, V>(P0 + (yl + 1) * S::BX + xl, yp1);
-                    ldv<T, V>(P0 + (yl - 2) * S::BX + xl, ym2);
-                    ldv<T, V>(P0 + (yl + 2) * S::BX + xl, yp2);
-                    ldv<T, V>(sl[1] + c * S::TILE + yl * S::BX + xl, zm1);
-                    ldv<T, V>(sl[3] + c * S::TILE + yl * S::BX + xl, zp1);
-                    ldv<T, V>(sl[0] + c * S::TILE + yl * S::BX + xl, zm2);
-                    ldv<T, V>(sl[4] + c * S::TILE + yl * S::BX + xl, zp2);
-                    if constexpr (kPackedPairs<T, V>) {
-                        // the FP32 difference form below, two sites per instruction
-#pragma unroll
-                        for (int v = 0; v < V; v += 2) {
-                            const int ci = S::PRE * V + v;
-                            const F2 f0(row[ci], row[ci + 1]);
-                            const F2 d1 = ((F2(row[ci - 1], row[ci]) - f0) + (F2(row[ci + 1], row[ci + 2]) - f0)) +
-                                          ((F2(ym1[v], ym1[v + 1]) - f0) + (F2(yp1[v], yp1[v + 1]) - f0)) +
-                                          ((F2(zm1[v], zm1[v + 1]) - f0) + (F2(zp1[v], zp1[v + 1]) - f0));
-                            const F2 d2 = ((F2(row[ci - 2], row[ci - 1]) - f0) + (F2(row[ci + 2], row[ci + 3]) - f0)) +
-                                          ((F2(ym2[v], ym2[v + 1]) - f0) + (F2(yp2[v], yp2[v + 1]) - f0)) +
-                                          ((F2(zm2[v], zm2[v + 1]) - f0) + (F2(zp2[v], zp2[v + 1]) - f0));
-                            const F2 l = fma(F2(a.wA), d1, F2(a.wB) * d2);
-                            lap[c][v] = l.v.x;
-                            lap[c][v + 1] = l.v.y;
-                            ctr[c][v] = f0.v.x;
-                            ctr[c][v + 1] = f0.v.y;
-                        }
-                    } else {
-#pragma unroll
-                    for (int v = 0; v < V; ++v) {
-                        const int ci = S::PRE * V + v;
-                        const T f0 = row[ci];
-                        if constexpr (std::is_same<T, float>::value) {
-                            // FP32: differences from the centre first (exact while a
-                            // neighbour lies within a factor 2 of f0), so the -30 f0
-                            // term of the 4th-order stencil does not cancel against
-                            // the neighbour sums: lap = wA sum(f+-1 - f0) + wB sum(f+-2 - f0)
-                            const T d1 = ((row[ci - 1] - f0) + (row[ci + 1] - f0)) + ((ym1[v] - f0) + (yp1[v] - f0)) +
-                                         ((zm1[v] - f0) + (zp1[v] - f0));
-                            const T d2 = ((row[ci - 2] - f0) + (row[ci + 2] - f0)) + ((ym2[v] - f0) + (yp2[v] - f0)) +
-                                         ((zm2[v] - f0) + (zp2[v] - f0));
-                            lap[c][v] = fma(a.wA, d1, a.wB * d2);
-                        } else {
-                            const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
-                            const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
-                            lap[c][v] = fma(a.wA, s1, fma(a.wB, s2, a.wC * f0));
-                        }
-                        ctr[c][v] = f0;
-                    }
-                    }
-                }
+                for (int c = 0; c < 4; ++c)
+                    star_laplacian<T, V>(a, sl[0] + c * S::TILE, sl[1] + c * S::TILE, sl[2] + c * S::TILE,
+                                         sl[3] + c * S::TILE, sl[4] + c * S::TILE, yl * S::BX + xl, S::BX, lap[c],
+                                         ctr[c]);
                 Op::template apply<T, V, HINT>(a, b, lap, ctr, pq, off + a.dox_out, x, y, lam_acc, pol_first);
             }
 

@@ -33,17 +33,21 @@ def _ring_from_level(patches, q, origin, fine):
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
-def test_patch_step_matches_uniform_level(axs, dtype):
+@pytest.mark.parametrize("n", [32, 64])
+def test_patch_step_matches_uniform_level(axs, dtype, n):
+    """Patch side 32 takes the fused step (one thread-block cluster of tiles per
+    patch) in both precisions, side 64 the fused step in FP32 (8 tiles) and the
+    two separate sweeps in FP64; all equal the uniform level."""
     from axion_strings_adaptive_gb300 import ic
     from axion_strings_adaptive_gb300.amr import Patches
-    Nf, n, dx = 64, 32, 0.25
+    Nf, dx = 2 * n, 0.25
     bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
-    s0 = ic.fourier_state(Nf, 6.0, seed=3)
+    s0 = ic.fourier_state(Nf, 6.0 * Nf / 64, seed=3)
     s0[2:] = 0.1 * torch.randn_like(s0[2:])
     s0 = s0.to(dtype)
     fine = axs.PeriodicLevel(Nf, dx, dtype=dtype)
     fine.set_state(s0)
-    origins = [(0, 0, 0), (32, 0, 32), (32, 32, 0)]
+    origins = [(0, 0, 0), (n, 0, n), (n, n, 0)]
     p = Patches(n, len(origins), dx, dtype=dtype)
     for q, o in enumerate(origins):
         _ring_from_level(p, q, o, s0.cuda())
