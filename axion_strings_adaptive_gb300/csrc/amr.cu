@@ -129,14 +129,16 @@ template <typename T> struct Fused {
     // FP32: two sites per thread on 32 x 16 tiles (174 KB of shared memory, one
     // block per SM); 32 x 8 tiles with one site per thread fit two blocks per SM
     // but ran 20 % slower on GB300. FP64: one site per thread on 32 x 8 tiles.
+    // NSW / NGP: S3, S4 and G, P slots, one more than sweep B reads, so sweep A of
+    // the next plane never overwrites what a slower thread's sweep B still reads
     static constexpr int V = sizeof(T) == 4 ? 2 : 1;
-    static constexpr int TX = 32, TY = sizeof(T) == 4 ? 16 : 8, NS = 6, THREADS = 256;
-    static constexpr int MIN_BLOCKS = 1;
+    static constexpr int TX = 32, TY = sizeof(T) == 4 ? 16 : 8, NS = sizeof(T) == 4 ? 6 : 5, THREADS = 256;
+    static constexpr int NSW = 6, NGP = 4;
     static constexpr int BX = TX + 8, BY = TY + 8;  // TMA box: the A region plus its stencil halo
     static constexpr int AX = TX + 4, AY = TY + 4;  // A region
     static constexpr int RING = 4 * BX * BY, SWIN = 4 * AX * AY, GPW = 4 * TX * TY;
     static constexpr int NA = AX * AY / V;          // sweep A units (V sites each)
-    static constexpr size_t SMEM = sizeof(T) * ((size_t)NS * RING + 5 * (size_t)SWIN + 3 * (size_t)GPW);
+    static constexpr size_t SMEM = sizeof(T) * ((size_t)NS * RING + NSW * (size_t)SWIN + NGP * (size_t)GPW);
     static_assert(TX * TY / V == THREADS, "one sweep B unit per thread");
     static_assert((BX * sizeof(T)) % 16 == 0 && (RING * sizeof(T)) % 128 == 0, "TMA box rows and slots");
     static_assert(SMEM <= 227 * 1024, "shared memory");
@@ -153,10 +155,13 @@ template <typename T> static void fused_tiles(int n, int &cx, int &cy)
     cy = y;
 }
 
-__device__ __forceinline__ void cluster_barrier()
-{
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
+// Execution barrier of the patch's tiles, split so that sweep B's shared-memory
+// work runs between arrive and wait. No data passes between the tiles through
+// memory: every (psi, Pi) plane a tile reads has landed in its shared memory
+// (its TMA transaction completed) before the tile arrives, so the arrive needs
+// no release fence.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
 
 struct FusedArgs {
     int n;
@@ -165,7 +170,7 @@ struct FusedArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256, Fused<T>::MIN_BLOCKS) patch_fused_kernel(T *__restrict__ st, const SweepArgs<T> a,
+__global__ void __launch_bounds__(256, 1) patch_fused_kernel(T *__restrict__ st, const SweepArgs<T> a,
                                                               const FusedArgs f)
 {
     using F = Fused<T>;
@@ -173,7 +178,7 @@ __global__ void __launch_bounds__(256, Fused<T>::MIN_BLOCKS) patch_fused_kernel(
     extern __shared__ __align__(128) unsigned char fused_smem[];
     T *ring = reinterpret_cast<T *>(fused_smem);
     T *swin = ring + (size_t)F::NS * F::RING;
-    T *gpw = swin + (size_t)5 * F::SWIN;
+    T *gpw = swin + (size_t)F::NSW * F::SWIN;
     __shared__ uint64_t full[F::NS];
     const int tid = threadIdx.x;
     const int q = blockIdx.z, n = f.n;
@@ -212,8 +217,8 @@ __global__ void __launch_bounds__(256, Fused<T>::MIN_BLOCKS) patch_fused_kernel(
             const T *pl[5];
 #pragma unroll
             for (int d = 0; d < 5; ++d) pl[d] = ring + (size_t)((i + d) % F::NS) * F::RING;
-            T *sz = swin + (size_t)(i % 5) * F::SWIN;  // S3, S4 of plane za
-            T *gz = gpw + (size_t)(i % 3) * F::GPW;    // G, P of plane za
+            T *sz = swin + (size_t)(i % F::NSW) * F::SWIN;  // S3, S4 of plane za
+            T *gz = gpw + (size_t)(i % F::NGP) * F::GPW;    // G, P of plane za
             for (int u = tid; u < F::NA; u += F::THREADS) {
                 const int lx = 2 + V * (u % (F::AX / V)), ly = 2 + u / (F::AX / V);  // box-local first site
                 T lap[4][V], ctr[4][V];
@@ -235,14 +240,20 @@ __global__ void __launch_bounds__(256, Fused<T>::MIN_BLOCKS) patch_fused_kernel(
                 }
             }
         }
-        // every tile of the patch is done with sweep A at za: (psi, Pi) of plane za - 2 is read no more
-        cluster_barrier();
+        __syncthreads();  // S3, S4, G, P of plane za are in place; ring plane k = i is read no more
+        if (tid == 0 && i + F::NS < K) {
+            fence_proxy_async_smem();
+            issue(i + F::NS);
+        }
+        // this tile is done with sweep A at za: (psi, Pi) of plane za - 2 is read no more here
+        cluster_arrive();
         const int zb = i - 4;
+        T o[4][V];
         if (ok && zb >= 0) {
             const T *sp[5];
 #pragma unroll
-            for (int d = 0; d < 5; ++d) sp[d] = swin + (size_t)((zb + d) % 5) * F::SWIN;  // planes zb-2 .. zb+2
-            const T *g = gpw + (size_t)((zb + 2) % 3) * F::GPW;                           // plane zb
+            for (int d = 0; d < 5; ++d) sp[d] = swin + (size_t)((zb + d) % F::NSW) * F::SWIN;  // planes zb-2 .. zb+2
+            const T *g = gpw + (size_t)((zb + 2) % F::NGP) * F::GPW;                           // plane zb
             T lap[4][V], ctr[4][V], pq[4][V];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
@@ -251,16 +262,14 @@ __global__ void __launch_bounds__(256, Fused<T>::MIN_BLOCKS) patch_fused_kernel(
                                      (byl + 2) * F::AX + (bxl + 2), F::AX, lap[c], ctr[c]);
                 ldv<T, V>(g + c * F::TX * F::TY + byl * F::TX + bxl, pq[c]);
             }
-            T o[4][V];
             stage_b<T, V>(a, lap, ctr, pq, o);
+        }
+        // every tile of the patch is done with sweep A at za: plane zb = za - 2 may be overwritten
+        cluster_wait();
+        if (ok && zb >= 0) {
             T *dst = dst0 + (int64_t)(kPatchRZ + zb) * f.ks;
 #pragma unroll
             for (int c = 0; c < 4; ++c) stv<T, V>(dst + c * f.plane, o[c]);
-        }
-        __syncthreads();  // sweep B is done with the window slots the next sweep A plane overwrites
-        if (tid == 0 && i + F::NS < K) {
-            fence_proxy_async_smem();
-            issue(i + F::NS);  // plane k = i is read no more
         }
     }
     // a wait expired: no bulk copy may still be landing in shared memory when the block exits
