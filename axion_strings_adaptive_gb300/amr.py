@@ -133,8 +133,7 @@ class TwoLevel:
         refined before keep their fine data, new ones interpolate the coarse level."""
         blocks = np.asarray(blocks, dtype=np.int32).reshape(-1, 3)
         dev = self.coarse.state.device
-        old_patches, old_blocks = self.patches, self.blocks
-        old_index = {tuple(b): q for q, b in enumerate(old_blocks)}
+        old_patches, old_block_patch = self.patches, self._block_patch
         self.blocks = blocks
         if len(blocks) == 0:
             self.patches = None
@@ -149,14 +148,17 @@ class TwoLevel:
         L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c), None, 0.0,
                0.0, 1, None)
         if old_patches is not None:
-            pairs = [(q, old_index[tuple(b)]) for q, b in enumerate(blocks.tolist()) if tuple(b) in old_index]
-            if pairs:
+            # the old patch of every new block, through the old block -> patch map (-1: newly refined)
+            b = torch.from_numpy(blocks.astype(np.int64)).to(dev)
+            old_q = old_block_patch[b[:, 2], b[:, 1], b[:, 0]].to(torch.int64)
+            keep = old_q >= 0
+            if bool(keep.any()):
                 # whole patch boxes (valid cells and rings; the rings are refilled before use)
-                new_q, old_q = (torch.tensor(v, dtype=torch.int64, device=dev) for v in zip(*pairs))
+                new_q = torch.nonzero(keep).flatten()
                 box = self.patches.layout.patch_elems
                 dst = self.patches.state.view(4, self.patches.npatches, box)
                 src = old_patches.state.view(4, old_patches.npatches, box)
-                dst.index_copy_(1, new_q, src.index_select(1, old_q))
+                dst.index_copy_(1, new_q, src.index_select(1, old_q[keep]))
 
     def regrid(self, n_error_buf: int = 4, gradient_threshold: float = 1.7976931348623157e308,
                radial_gradient_threshold: float = 1.7976931348623157e308) -> int:

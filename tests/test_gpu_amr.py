@@ -285,3 +285,23 @@ def test_batched_patch_diagnostics_match_per_patch_passes(axs, dtype):
     assert set(lst.cpu().numpy().tolist()) == pierced and got.n_listed == len(pierced)
     np.testing.assert_allclose(np.array(list(got.energy_sums)), sums, rtol=1e-12)
     assert got.vel_sum == pytest.approx(vsum, rel=1e-12)
+
+
+def test_regrid_keeps_the_fine_data_of_blocks_that_stay_refined(axs):
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block = 64, 16
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=torch.float32)
+    coarse.set_state(torch.randn((4, N, N, N)).cuda())
+    two = TwoLevel(coarse, block)
+    two.set_blocks(np.array([[0, 0, 0], [1, 2, 3], [3, 3, 1]]))
+    marks = {}
+    for q, b in enumerate(two.blocks):
+        two.patches.valid(q).fill_(float(q + 7))
+        marks[tuple(b)] = float(q + 7)
+    two.set_blocks(np.array([[2, 0, 0], [3, 3, 1], [0, 0, 0], [1, 1, 1]]))  # two kept, two new, one dropped
+    for q, b in enumerate(two.blocks):
+        v = two.patches.valid(q)
+        if tuple(b) in marks:
+            assert bool((v == marks[tuple(b)]).all()), tuple(b)
+        else:  # interpolated from the coarse level
+            assert not bool((v == 7.0).any()) and float(v.abs().max()) > 0.0
