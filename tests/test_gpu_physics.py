@@ -6,7 +6,9 @@
   evolution (the static profile with Pi = (R'/R) psi stays put);
 * the 4th-order Laplacian converges at order 4 on a smooth periodic field;
 * FP32 evolution tracks FP64 on the precision configuration's physics at a
-  reduced size.
+  reduced size;
+* a 1024^3 level (element offsets past 32 bits) evolves a z-only field exactly
+  as an 8 x 8 x 1024 column does.
 """
 import math
 
@@ -106,3 +108,37 @@ def test_fp32_tracks_fp64(axs):
     rel = abs(b.energy["rho_tot_unscreened"] - a.energy["rho_tot_unscreened"]) / a.energy["rho_tot_unscreened"]
     assert rel < 1e-5
     assert b.n_p_plain == a.n_p_plain
+
+
+def test_1024_cubed_level_indexes_beyond_32_bits(axs):
+    """A 1024^3 FP32 level holds 4.6 G elements per component-major array, past
+    32-bit offsets. A field that varies only in z must evolve as the same
+    column on an 8 x 8 x 1024 level does, bit for bit in every (x, y), and its
+    diagnostics must be the column's times the number of columns."""
+    free, _ = torch.cuda.mem_get_info()
+    if free < 120 * 2 ** 30:
+        pytest.skip("needs ~80 GB of free device memory")
+    n = 1024
+    bg = axs.Background.expanding(2.0, 2.0, lambda0=2.0)
+    z = torch.arange(n, dtype=torch.float64, device="cuda")
+    col = torch.stack([1.0 + 0.1 * torch.sin(2 * math.pi * 3 * z / n), 0.1 * torch.cos(2 * math.pi * 5 * z / n),
+                       0.02 * torch.sin(2 * math.pi * 2 * z / n), torch.zeros_like(z)]).float()  # (4, nz)
+    small = axs.PeriodicLevel((8, 8, n), 0.5, dtype=torch.float32, pierced_capacity=1)
+    small.set_state(col[:, :, None, None].expand(4, n, 8, 8))
+    big = axs.PeriodicLevel(n, 0.5, dtype=torch.float32, pierced_capacity=1)
+    big.set_state(col[:, :, None, None].expand(4, n, n, n))
+    for lv in (small, big):
+        lv.advance(bg, 1.0, 0.0, 0.1, 2)
+        lv.device_status()
+    ref = small.valid_view()[:, :, 0, 0]
+    got = big.valid_view()
+    for c in range(4):
+        assert bool((got[c] == ref[c][:, None, None]).all()), c
+    # FP64 per-cell terms: every cell's terms are the column's, only the summation order differs
+    ds = small.diagnostics(bg, 1.2, want_list=False)
+    db = big.diagnostics(bg, 1.2, want_list=False)
+    assert ds.n_p_plain == 0 and db.n_p_plain == 0
+    scale = (n * n) / 64.0
+    np.testing.assert_allclose(np.array(db.energy_sums), scale * np.array(ds.energy_sums), rtol=1e-10)
+    del big
+    torch.cuda.empty_cache()
