@@ -179,3 +179,31 @@ def test_per_cell_fp32_variant(axs):
     assert torch.equal(torch.sort(fast.pierced)[0], torch.sort(ref.pierced)[0])
     np.testing.assert_allclose(fast.energy_sums, ref.energy_sums, rtol=2e-6)
     assert fast.mean_gamma_sq_v_sq == pytest.approx(ref.mean_gamma_sq_v_sq, rel=1e-5)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_exact_zeros_and_a_vacuum_corner_match_oracle(axs, orc, dtype):
+    """Cells where psi is exactly zero (a core on a grid point: atan2(0, 0) = 0,
+    the 1/|psi|^2 guards) and a block of the false vacuum psi = 0, Pi = 0."""
+    n, dx = 16, 0.5
+    v = orc.fourier_ic_state(n, 4.0, seed=5)
+    v[2:] = 0.2 * np.random.default_rng(2).standard_normal((2, n, n, n))
+    rng = np.random.default_rng(3)
+    zs = rng.integers(0, n, size=(40, 3))
+    v[0, zs[:, 0], zs[:, 1], zs[:, 2]] = 0.0
+    v[1, zs[:, 0], zs[:, 1], zs[:, 2]] = 0.0
+    v[:, :4, :4, :4] = 0.0
+    if dtype == torch.float32:
+        v = v.astype(np.float32).astype(np.float64)  # the same values on both sides
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    bgo = orc.background(a_inv=2.0, c0=1.0, lambda_scale=2.0)
+    tau = 1.3
+    lvl = axs.PeriodicLevel(n, dx, dtype=dtype)
+    lvl.set_state(_dev(v).to(dtype))
+    d = lvl.diagnostics(bg, tau)
+    ref = orc.level_diagnostics(v, dx, bgo, tau)
+    assert (d.n_p_plain, d.n_p_weighted) == (ref.n_p_plain, ref.n_p_weighted)
+    assert np.all(np.isfinite(d.energy_sums))
+    if dtype == torch.float64:
+        np.testing.assert_allclose(d.energy_sums, ref.energy_sums, rtol=1e-12)
+        assert d.vel_count == ref.vel_count

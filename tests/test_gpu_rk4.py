@@ -113,7 +113,7 @@ def test_stagewise_rk4_matches_oracle(axs, orc):
     np.testing.assert_array_equal(got, ref)
 
 
-@pytest.mark.parametrize("shape", [(16, 12, 10), (32, 20, 7), (48, 33, 16)])
+@pytest.mark.parametrize("shape", [(16, 12, 10), (32, 20, 7), (48, 33, 16), (8, 4, 5), (4, 2, 3)])
 def test_fused_rk4_f64_matches_oracle(axs, orc, shape):
     nx, ny, nz = shape
     rng = np.random.default_rng(nx + ny + nz)
