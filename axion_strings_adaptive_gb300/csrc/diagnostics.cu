@@ -159,13 +159,22 @@ constexpr int kPsiPer = (2 * kPsiPts + kDiagThreads - 1) / kDiagThreads;  // psi
 constexpr int kPiPer = (2 * kVtxPts + kDiagThreads - 1) / kDiagThreads;   // Pi loads per thread per plane
 constexpr int kVtxPer = (kVtxPts + kDiagThreads - 1) / kDiagThreads;      // vertices per thread per plane
 
-constexpr int kPsiSlots = 6, kPiSlots = 3;
+// Ring depths for one block barrier per plane: a plane's loads are issued
+// before that barrier, so a slot may be refilled only once every thread is
+// past the plane that last read it (psi: the 5-plane stencil plus two;
+// Pi: read at its vertex plane and again at its cell plane, plus two).
+// Vertex planes are computed one plane ahead into a third slot.
+constexpr int kPsiSlots = 7, kPiSlots = 5, kVtxSlots = 3;
+// pierced plaquettes buffered per block; flushed to the global list with one
+// atomic once a plane could overflow it (at most 3 entries per cell)
+constexpr int kListBuf = 1536, kListFlushAt = kListBuf - 3 * kDiagThreads;
 template <typename T, bool FAST> struct DiagSmem {
+    long long lbuf[kListBuf];
     T ps[kPsiSlots][2][DHY][DHX];
     T pi[kPiSlots][2][DVY][DVX];
-    typename std::conditional<FAST, float, double>::type gv[2][DVY][DVX];
-    float th[2][DVY][DVX];
-    unsigned char ok[2][DVY][DVX];
+    typename std::conditional<FAST, float, double>::type gv[kVtxSlots][DVY][DVX];
+    float th[kVtxSlots][DVY][DVX];
+    unsigned char ok[kVtxSlots][DVY][DVX];
 };
 
 __device__ __forceinline__ int wrap_or_self(int i, int n, int wrap) { return wrap ? (i % n + n) % n : i; }
@@ -182,8 +191,8 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
 {
     extern __shared__ __align__(16) unsigned char diag_smem_raw[];
     DiagSmem<T, FAST> &sm = *reinterpret_cast<DiagSmem<T, FAST> *>(diag_smem_raw);
-    __shared__ int warp_tot[kDiagThreads / 32];
-    __shared__ unsigned long long block_base;
+    __shared__ int lcount, flush_n;
+    __shared__ unsigned long long flush_base;
     const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
 
     double e[14];
@@ -200,6 +209,24 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
 
     const int tid = threadIdx.x;
     const int lx = tid % DTX, ly = tid / DTX;
+    if (tid == 0) lcount = 0;
+    int warp_end = 0;  // end of this warp's last append to lbuf (lane-uniform)
+    // move the buffered pierced plaquettes to the global list (called by the whole block)
+    auto flush = [&]() {
+        if (tid == 0) {
+            const int nb = lcount;
+            flush_n = nb;
+            flush_base = nb ? atomicAdd(list_counter, (unsigned long long)nb) : 0ull;
+            lcount = 0;
+        }
+        __syncthreads();
+        const int nb = flush_n;
+        const unsigned long long b0 = flush_base;
+        for (int i = tid; i < nb; i += kDiagThreads)
+            if (b0 + i < (unsigned long long)capacity) list[b0 + i] = sm.lbuf[i];
+        __syncthreads();
+        warp_end = 0;
+    };
 
     for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
         // boxes of one batch share the view's geometry and sit box_stride apart
@@ -265,7 +292,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
         };
         // vertex plane z: phases and gamma^2 v^2 from psi and Pi already in shared memory
         auto vertex_plane = [&](int z) {
-            const int ts = (z - za) & 1;
+            const int ts = (z - za) % kVtxSlots;
             const int ps_ = (z - za) % kPiSlots;
             const int slot = psi_slot(z);
 #pragma unroll
@@ -304,28 +331,34 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             }
         };
 
-        // prologue: psi of za-2 .. za+2, Pi of za and za+1 (one group), then the first vertex plane
+        // prologue: psi of za-2 .. za+2 and Pi of za .. za+2 (one group), then the
+        // first two vertex planes. Vertex planes run za .. za+len, psi planes
+        // za-2 .. za+len+1.
         for (int p = -2; p <= 2; ++p) load_psi(za + p);
         load_pi(za);
         load_pi(za + 1);
+        if (len >= 2) load_pi(za + 2);
         cp_async_commit();
         cp_async_wait<0>();
         __syncthreads();
         vertex_plane(za);
+        vertex_plane(za + 1);
 
         for (int m = 0; m < len; ++m) {
             const int z = za + m;
-            // one plane ahead: psi(z + 3) for the next plane's stencil, Pi(z + 2) for its
-            // vertex plane (their slots were last read before the previous barrier)
-            if (m + 1 < len) {
-                load_psi(z + 3);
-                load_pi(z + 2);
-            }
+            // one plane ahead: psi(z + 3) for the next plane's stencil and vertex
+            // plane, Pi(z + 3) for its vertex plane. Their slots were last read
+            // two planes back, before the previous plane's barrier.
+            if (m + 1 < len) load_psi(z + 3);
+            if (m + 3 <= len) load_pi(z + 3);
             cp_async_commit();
-            cp_async_wait<1>();  // everything but this plane's group: psi(z + 2), Pi(z + 1)
-            __syncthreads();
-            vertex_plane(z + 1);
-            __syncthreads();
+            cp_async_wait<1>();  // everything but this plane's group: psi(z + 2), Pi(z + 2)
+            // the plane's one barrier: its psi / Pi and vertex planes z, z + 1 are
+            // visible, every thread is done with plane z - 1, and the block learns
+            // whether the pierced buffer could overflow during this plane
+            if (__syncthreads_or(warp_end > kListFlushAt)) flush();
+            // vertex plane z + 2 for the next plane, into the slot plane z - 1 read
+            if (m + 2 <= len) vertex_plane(z + 2);
 
             const int x = x0 + lx, y = y0 + ly;
             const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
@@ -335,7 +368,7 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                 const int s0 = (m + 2) % kPsiSlots;
                 const int sm1 = (m + 1) % kPsiSlots, sp1 = (m + 3) % kPsiSlots, sm2 = m % kPsiSlots,
                           sp2 = (m + 4) % kPsiSlots;
-                const int t0 = m & 1, t1 = (m + 1) & 1, tp = m % kPiSlots;
+                const int t0 = m % kVtxSlots, t1 = (m + 1) % kVtxSlots, tp = m % kPiSlots;
                 const int hx = lx + 2, hy = ly + 2;
                 if (q.want_energy) {
                     const T p1 = sm.ps[s0][0][hy][hx], p2 = sm.ps[s0][1][hy][hx];
@@ -438,37 +471,30 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     }
                 }
             }
-            // ---- compaction of the pierced plaquettes of this plane ----
+            // ---- pierced plaquettes of this plane into the block's buffer: a warp
+            // scan and one shared-memory atomic per warp that has any ----
             if (q.want_plaq && list != nullptr) {
                 const int mine = (w[0] != 0) + (w[1] != 0) + (w[2] != 0);
-                const int lane = tid & 31, warp = tid >> 5;
-                int incl = mine;
+                if (__any_sync(0xffffffffu, mine != 0)) {
+                    const int lane = tid & 31;
+                    int incl = mine;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int yv = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += yv;
-                }
-                if (lane == 31) warp_tot[warp] = incl;
-                __syncthreads();
-                int warp_off = 0, block_tot = 0;
-                for (int ww = 0; ww < kDiagThreads / 32; ++ww) {
-                    if (ww < warp) warp_off += warp_tot[ww];
-                    block_tot += warp_tot[ww];
-                }
-                if (tid == 0) block_base = block_tot ? atomicAdd(list_counter, (unsigned long long)block_tot) : 0ull;
-                __syncthreads();
-                if (mine) {
-                    long long pos = (long long)block_base + warp_off + incl - mine;
-                    for (int pl = 0; pl < 3; ++pl) {
-                        if (w[pl]) {
-                            if (pos < capacity) list[pos] = 4LL * cell + pl;
-                            ++pos;
-                        }
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int yv = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += yv;
                     }
+                    const int wtot = __shfl_sync(0xffffffffu, incl, 31);
+                    int wbase = 0;
+                    if (lane == 31) wbase = atomicAdd(&lcount, wtot);
+                    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+                    warp_end = wbase + wtot;
+                    int pos = wbase + incl - mine;
+                    for (int pl = 0; pl < 3; ++pl)
+                        if (w[pl]) sm.lbuf[pos++] = 4LL * cell + pl;
                 }
             }
-            __syncthreads();  // ring slots and vertex planes are rewritten next plane
         }
+        __syncthreads();  // the next item's prologue refills the rings
         if constexpr (FAST) {
 #pragma unroll
             for (int k = 0; k < 14; ++k) {
@@ -477,6 +503,8 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
             }
         }
     }
+    // the rest of the buffer (warp_end > 0: the warp appended since the last flush)
+    if (q.want_plaq && list != nullptr && __syncthreads_or(warp_end > 0)) flush();
 
     // ---- block reduction (fixed order) ----
     __shared__ double red_d[kDiagThreads / 32][15];
@@ -511,6 +539,286 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
         long long xv = 0;
         for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red_l[ww][tid - 32];
         partials[blockIdx.x].cnt[tid - 32] = xv;
+    }
+}
+
+// ---------------------------------------------------------------- string finder
+// The string finder and the tagger's plaquette criterion alone (no energy, no
+// velocity). A block owns a FTX x FTY tile of cells, two cells per thread, and
+// marches in z. Each fold decision is made once per edge: the winding of a
+// plaquette is the signed sum of its four edges' folds, #(d < -pi) - #(d > pi)
+// of the edge's phase difference d, and a plaquette walks an edge backwards
+// with exactly -d, so it adds exactly minus the forward fold. That is the
+// single-precision fast path of the fused pass edge for edge, with the same
+// fall back to the reference's double arithmetic: a cell is redone in double
+// when one of its nine edges lies within 1e-5 of +-pi or ends at a vertex
+// outside float range. Per vertex plane, with one block barrier:
+//   B: the x and y edge codes of the plane before, from the neighbours' phases;
+//   A: the thread's vertices' phases, from psi loaded into registers two
+//      planes ahead, and their z edges to the plane below (phase kept in a
+//      register);
+//   C: the windings of the cells three planes back.
+// Four slots per vertex-plane array keep every write two barriers from the
+// last read of its slot.
+constexpr int FTX = 32, FTY = 16, FVX = FTX + 1, FVY = FTY + 1;
+constexpr int kFinderExtra = FTX + FTY + 1;  // vertices of the last row (x < FTX) and last column
+constexpr int kFinderListBuf = 3072, kFinderFlushAt = kFinderListBuf - 6 * kDiagThreads;
+static_assert(FTX * FTY == 2 * kDiagThreads && kFinderExtra <= kDiagThreads, "two cells, at most three vertices per thread");
+
+struct FinderSmem {
+    long long lbuf[kFinderListBuf];
+    float th[4][FVY][FVX];           // phases of vertex plane p in slot p mod 4
+    unsigned char ok[4][FVY][FVX];   // the vertex lies inside float range
+    unsigned char inp[4][FVY][FVX];  // x edge code (bits 0-2), y edge code (bits 3-5)
+    unsigned char zc[4][FVY][FVX];   // z edge code to the plane above (bits 0-2)
+};
+
+struct CellWindings {
+    int w[3], ties;
+};
+
+// edge code: fold + 1 in bits 0-1, bit 2 set when the cell must be redone in
+// double (winding4_fast's band test on the same float difference)
+__device__ __forceinline__ unsigned edge_code(float ta, float tb, bool ok)
+{
+    const float pi = 3.14159265f, band = 1e-5f;
+    const float d = tb - ta;
+    const bool bad = !ok || fabsf(fabsf(d) - pi) < band;
+    return (unsigned)(1 + (d < -pi) - (d > pi)) | (bad ? 4u : 0u);
+}
+__device__ __forceinline__ int edge_fold(unsigned c) { return (int)(c & 3u) - 1; }
+
+// A cell's three windings in the reference's double arithmetic, psi read from
+// global memory at its seven corners (zero outside the view's ghost region, as
+// the plane loads fill it). Out of line: it is rare and needs many registers.
+template <typename T>
+__device__ __noinline__ CellWindings finder_cell_double(const DiagView v, const T *base, int x, int y, int z)
+{
+    auto ph = [&](int xx, int yy, int zz) {
+        const bool on = (v.wx || xx < v.nx + v.ox) && (v.wy || yy < v.ny + v.oy) && (v.wz || zz < v.nz + v.oz);
+        const double a = on ? (double)base[view_off<T>(v, 0, xx, yy, zz)] : 0.0;
+        const double b = on ? (double)base[view_off<T>(v, 1, xx, yy, zz)] : 0.0;
+        return atan2(b, a);
+    };
+    const double d000 = ph(x, y, z), d100 = ph(x + 1, y, z), d110 = ph(x + 1, y + 1, z), d010 = ph(x, y + 1, z);
+    const double d001 = ph(x, y, z + 1), d101 = ph(x + 1, y, z + 1), d011 = ph(x, y + 1, z + 1);
+    CellWindings r;
+    r.ties = 0;
+    cell_windings_double(d000, d100, d110, d010, d001, d101, d011, r.w, r.ties);
+    return r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
+    finder_kernel(const DiagView v, const uint8_t *__restrict__ mask, DiagPartial *__restrict__ partials,
+                  unsigned long long *__restrict__ list_counter, long long *__restrict__ list, long long capacity,
+                  int tiles_x, int ntiles, int zchunk, long long n_items, long long items_per_box,
+                  int64_t box_stride, uint8_t *__restrict__ tags)
+{
+    extern __shared__ __align__(16) unsigned char finder_smem_raw[];
+    FinderSmem &sm = *reinterpret_cast<FinderSmem *>(finder_smem_raw);
+    __shared__ int lcount, flush_n;
+    __shared__ unsigned long long flush_base;
+    __shared__ long long red[kDiagThreads / 32][3];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int lx = tid % FTX, ly = tid / FTX;  // cells (lx, ly) and (lx, ly + FTY / 2)
+    const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
+    int cnt_p = 0, cnt_w = 0, cnt_tie = 0;  // per-thread counts fit 32 bits
+    if (tid == 0) lcount = 0;
+    int warp_end = 0;  // end of this warp's last append to lbuf (lane-uniform)
+    auto flush = [&]() {
+        if (tid == 0) {
+            const int nb = lcount;
+            flush_n = nb;
+            flush_base = nb ? atomicAdd(list_counter, (unsigned long long)nb) : 0ull;
+            lcount = 0;
+        }
+        __syncthreads();
+        const int nb = flush_n;
+        const unsigned long long b0 = flush_base;
+        for (int i = tid; i < nb; i += kDiagThreads)
+            if (b0 + i < (unsigned long long)capacity) list[b0 + i] = sm.lbuf[i];
+        __syncthreads();
+        warp_end = 0;
+    };
+
+    // the thread's vertices: (lx, ly), (lx, ly + 8) and, for the first 49
+    // threads, one of the last row (y = FTY) or the last column (x = FTX)
+    const bool extra = tid < kFinderExtra;
+    const int vi[3] = {lx, lx, tid < FTX ? tid : FTX};
+    const int vj[3] = {ly, ly + FTY / 2, tid < FTX ? FTY : (extra ? tid - FTX : 0)};
+
+    for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const long long qbox = item / items_per_box, box_item = item % items_per_box;
+        const T *__restrict__ base = static_cast<const T *>(v.data) + qbox * box_stride;
+        const int tile = (int)(box_item % ntiles), chunk = (int)(box_item / ntiles);
+        const int x0 = (tile % tiles_x) * FTX, y0 = (tile / tiles_x) * FTY;
+        const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
+
+        // in-plane element offsets of the thread's vertices; psi is zero outside
+        // the ghost region
+        int64_t voff[3];
+        bool von[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int xx = x0 + vi[k], yy = y0 + vj[k];
+            von[k] = (k < 2 || extra) && xx <= v.nx && yy <= v.ny && (v.wx || xx < v.nx + v.ox) &&
+                     (v.wy || yy < v.ny + v.oy);
+            voff[k] = (int64_t)(wrap_or_self(xx, v.nx, v.wx) + v.ox) +
+                      (int64_t)(wrap_or_self(yy, v.ny, v.wy) + v.oy) * v.js;
+        }
+        // psi of vertex planes za, za + 1, ... in order, into registers
+        int lz = za, lzw = wrap_or_self(za, v.nz, v.wz);
+        auto load_plane = [&](T(&buf)[3][2]) {
+            const bool zin = v.wz || lz < v.nz + v.oz;
+            const T *pb = base + (int64_t)(lzw + v.oz) * v.ks;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const bool on = zin && von[k];
+                buf[k][0] = on ? __ldg(pb + voff[k]) : T(0);
+                buf[k][1] = on ? __ldg(pb + voff[k] + v.cs) : T(0);
+            }
+            ++lz;
+            lzw = v.wz ? (lzw + 1 == v.nz ? 0 : lzw + 1) : lzw + 1;
+        };
+        float thp[3];  // phase and range flag of the vertex one plane down
+        bool okp[3];
+
+        // B: x and y edge codes of vertex plane za + j - 1
+        auto stage_b = [&](int j) {
+            const int s = (j - 1) & 3;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (k == 2 && !extra) break;
+                const int i = vi[k], jj = vj[k];
+                unsigned code = 0;
+                if (i < FTX) code = edge_code(thp[k], sm.th[s][jj][i + 1], okp[k] && sm.ok[s][jj][i + 1]);
+                if (jj < FTY) code |= edge_code(thp[k], sm.th[s][jj + 1][i], okp[k] && sm.ok[s][jj + 1][i]) << 3;
+                sm.inp[s][jj][i] = (unsigned char)code;
+            }
+        };
+        // A: phases of vertex plane za + j and the z edges from plane za + j - 1
+        auto stage_a = [&](int j, const T(&buf)[3][2]) {
+            const int s = j & 3, sp = (j - 1) & 3;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (k == 2 && !extra) break;
+                const T a = buf[k][0], b = buf[k][1];
+                bool ok;
+                if constexpr (sizeof(T) == 4) {
+                    const float m = fmaxf(fabsf(a), fabsf(b));
+                    ok = m > 1e-30f && m < 1e30f;
+                } else {
+                    const double m = fmax(fabs(a), fabs(b));
+                    ok = m > 1e-30 && m < 1e30;
+                }
+                const float th = atan2f((float)b, (float)a);
+                sm.th[s][vj[k]][vi[k]] = th;
+                sm.ok[s][vj[k]][vi[k]] = ok;
+                if (j > 0) sm.zc[sp][vj[k]][vi[k]] = (unsigned char)edge_code(thp[k], th, okp[k] && ok);
+                thp[k] = th;
+                okp[k] = ok;
+            }
+        };
+        // C: windings of the cells of plane za + j - 3
+        auto stage_c = [&](int j) {
+            const int s0 = (j - 3) & 3, s1 = (j - 2) & 3, z = za + j - 3;
+            int w[2][3], mine = 0;
+            int64_t cells[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int cy = ly + h * (FTY / 2), x = x0 + lx, y = y0 + cy;
+                const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
+                cells[h] = cell;
+                w[h][0] = w[h][1] = w[h][2] = 0;
+                if (!(x < v.nx && y < v.ny && (mask == nullptr || mask[cell] != 0))) continue;
+                const unsigned c000 = sm.inp[s0][cy][lx], c100 = sm.inp[s0][cy][lx + 1];
+                const unsigned c010 = sm.inp[s0][cy + 1][lx], c001 = sm.inp[s1][cy][lx];
+                const unsigned z000 = sm.zc[s0][cy][lx], z100 = sm.zc[s0][cy][lx + 1], z010 = sm.zc[s0][cy + 1][lx];
+                const unsigned bad =
+                    ((c000 | c001) & 0x24u) | (c100 & 0x20u) | (c010 & 0x04u) | ((z000 | z100 | z010) & 0x04u);
+                if (!bad) {
+                    // StringFinder.hpp:45-68 order: xy (000 100 110 010), yz (000 010 011 001), zx (000 001 101 100)
+                    w[h][0] = edge_fold(c000) + edge_fold(c100 >> 3) - edge_fold(c010) - edge_fold(c000 >> 3);
+                    w[h][1] = edge_fold(c000 >> 3) + edge_fold(z010) - edge_fold(c001 >> 3) - edge_fold(z000);
+                    w[h][2] = edge_fold(z000) + edge_fold(c001) - edge_fold(z100) - edge_fold(c000);
+                } else {
+                    const CellWindings cw = finder_cell_double<T>(v, base, x, y, z);
+                    w[h][0] = cw.w[0];
+                    w[h][1] = cw.w[1];
+                    w[h][2] = cw.w[2];
+                    cnt_tie += cw.ties;
+                }
+                // StringTagger.hpp:117-151: a cell is tagged when a plaquette at its low corner is pierced
+                if (tags != nullptr) tags[cell] = (w[h][0] | w[h][1] | w[h][2]) != 0;
+                cnt_p += (w[h][0] != 0) + (w[h][1] != 0) + (w[h][2] != 0);
+                cnt_w += abs(w[h][0]) + abs(w[h][1]) + abs(w[h][2]);
+                mine += (w[h][0] != 0) + (w[h][1] != 0) + (w[h][2] != 0);
+            }
+            // pierced plaquettes into the block's buffer: a warp scan and one
+            // shared-memory atomic per warp that has any
+            if (list != nullptr && __any_sync(0xffffffffu, mine != 0)) {
+                int incl = mine;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int yv = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += yv;
+                }
+                const int wtot = __shfl_sync(0xffffffffu, incl, 31);
+                int wbase = 0;
+                if (lane == 31) wbase = atomicAdd(&lcount, wtot);
+                wbase = __shfl_sync(0xffffffffu, wbase, 31);
+                warp_end = wbase + wtot;
+                int pos = wbase + incl - mine;
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    for (int pl = 0; pl < 3; ++pl)
+                        if (w[h][pl]) sm.lbuf[pos++] = 4LL * cells[h] + pl;
+            }
+        };
+        // iteration j: B (plane za + j - 1), A (plane za + j, then the load of
+        // plane za + j + 2 into the registers A just read), C (cells of plane
+        // za + j - 3); the loop is unrolled by two so each register buffer has
+        // a fixed name
+        auto step = [&](int j, T(&buf)[3][2]) {
+            // the plane's one barrier; the block also learns whether the pierced
+            // buffer could overflow during this plane
+            if (__syncthreads_or(warp_end > kFinderFlushAt)) flush();
+            if (j >= 1 && j <= len + 1) stage_b(j);
+            if (j <= len) {
+                stage_a(j, buf);
+                if (j + 2 <= len) load_plane(buf);
+            }
+            if (j >= 3) stage_c(j);
+        };
+        T bufa[3][2], bufb[3][2];
+        load_plane(bufa);  // vertex plane za
+        load_plane(bufb);  // za + 1 (len >= 1)
+        for (int j = 0; j < len + 3; j += 2) {
+            step(j, bufa);
+            if (j + 1 < len + 3) step(j + 1, bufb);
+        }
+    }
+    if (list != nullptr && __syncthreads_or(warp_end > 0)) flush();
+
+    // ---- block reduction (fixed order) into the fused pass's partial record ----
+    long long c3[3] = {cnt_p, cnt_w, cnt_tie};
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        for (int o = 16; o > 0; o >>= 1) c3[s] += __shfl_down_sync(0xffffffffu, c3[s], o);
+        if (lane == 0) red[tid >> 5][s] = c3[s];
+    }
+    __syncthreads();
+    if (tid < 14)
+        partials[blockIdx.x].e[tid] = 0.0;
+    else if (tid == 14)
+        partials[blockIdx.x].vsum = 0.0;
+    else if (tid >= 32 && tid < 36) {
+        const int f = tid - 32;  // n_p_plain, n_p_weighted, vel_count, near_tie
+        long long xv = 0;
+        if (f != 2)
+            for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red[ww][f == 3 ? 2 : f];
+        partials[blockIdx.x].cnt[f] = xv;
     }
 }
 
@@ -578,13 +886,13 @@ static int diag_grid(int64_t ncell)
 
 // Work items (tile, z-chunk), tile fastest; chunks long enough to amortise
 // the 4 warm-up planes while giving every resident block several items.
-static void diag_plan(const DiagView &v, int nboxes, int max_grid, int &tiles_x, int &ntiles, int &zchunk,
-                      long long &items_per_box, long long &items, int &grid)
+static void diag_plan(const DiagView &v, int nboxes, int max_grid, int tx, int ty, int blocks_per_sm, int &tiles_x,
+                      int &ntiles, int &zchunk, long long &items_per_box, long long &items, int &grid)
 {
-    tiles_x = (v.nx + DTX - 1) / DTX;
-    ntiles = tiles_x * ((v.ny + DTY - 1) / DTY);
+    tiles_x = (v.nx + tx - 1) / tx;
+    ntiles = tiles_x * ((v.ny + ty - 1) / ty);
     const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
-    const long long resident = 2LL * sms;
+    const long long resident = (long long)blocks_per_sm * sms;
     const long long tiles_all = (long long)ntiles * nboxes;
     int nch = (int)std::max<long long>(1, (4 * resident + tiles_all - 1) / tiles_all);
     zchunk = std::max(1, (v.nz + nch - 1) / nch);
@@ -653,9 +961,29 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     AXS_CUDA_CHECK(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
     int tiles_x, ntiles, zchunk, grid;
     long long items, items_per_box;
-    diag_plan(v, nboxes, diag_grid(ncell), tiles_x, ntiles, zchunk, items_per_box, items, grid);
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
     int rc0 = AXS_OK;
+    if (q.want_plaq && !q.want_energy && !q.want_vel) {
+        // windings only: the edge-code finder
+        const bool f32 = v.dtype != AXS_F64;
+        diag_plan(v, nboxes, diag_grid(ncell), FTX, FTY, f32 ? 4 : 3, tiles_x, ntiles, zchunk, items_per_box, items,
+                  grid);
+        auto launch_f = [&](auto kern) -> int {
+            AXS_CUDA_CHECK(
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FinderSmem)));
+            kern<<<grid, kDiagThreads, sizeof(FinderSmem), st>>>(v, mask, partials, counter, lst, capacity, tiles_x,
+                                                                  ntiles, zchunk, items, items_per_box, box_stride,
+                                                                  tags);
+            return AXS_OK;
+        };
+        rc0 = f32 ? launch_f(finder_kernel<float>) : launch_f(finder_kernel<double>);
+        if (rc0) return rc0;
+        int rc = launch_status("string finder");
+        if (rc) return rc;
+        diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
+        return launch_status("diagnostics finalize");
+    }
+    diag_plan(v, nboxes, diag_grid(ncell), DTX, DTY, 2, tiles_x, ntiles, zchunk, items_per_box, items, grid);
     auto launch = [&](auto kern, size_t smem) -> int {
         AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<grid, kDiagThreads, smem, st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x, ntiles, zchunk,

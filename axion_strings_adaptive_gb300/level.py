@@ -295,14 +295,17 @@ class PeriodicLevel:
 
     def diagnostics(self, bg: Background, tau: float, masking_scheme: int = L.MASK_A, threshold: float = 0.8,
                     mask: torch.Tensor | None = None, want_list: bool = True, per_cell_fp32: bool = False,
-                    stream=None) -> Diagnostics:
+                    strings_only: bool = False, stream=None) -> Diagnostics:
         """specific_post_timestep's pass. per_cell_fp32 (FP32 levels): per-cell
         terms in FP32 with FP64 accumulation instead of the reference's double
-        per-cell arithmetic (energies to ~1e-7 relative, counts exact)."""
+        per-cell arithmetic (energies to ~1e-7 relative, counts exact).
+        strings_only: the string finder alone (count_plaquettes and the pierced
+        list; energies and the velocity are left at zero)."""
         v = bg.values(tau)
         rpr = 0.0 if bg.kind == L.BG_FLAT else v.R_prime_over_R
-        p = L.DiagParams(self.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold, L.BOUNDARY_PERIODIC, 1, 1,
-                         1, int(per_cell_fp32))
+        want = (0, 1, 0) if strings_only else (1, 1, 1)
+        p = L.DiagParams(self.dx, v.R, v.lambda_, rpr, v.m_r, masking_scheme, threshold, L.BOUNDARY_PERIODIC, *want,
+                         int(per_cell_fp32))
         r = self.diagnostics_raw(p, mask, want_list, stream)
         if r.status == L.AXS_ERR_CAPACITY:
             raise L.AxsError(L.AXS_ERR_CAPACITY, "pierced-plaquette list capacity exceeded")

@@ -553,15 +553,16 @@ def run_native(args):
                           "n_near_tie": res.n_near_tie, "rho_tot_sum": res.energy_sums[0]}
         diag["rho_tot_rel_diff"] = abs(diag["per_cell_fp32"]["rho_tot_sum"] - diag["per_cell_fp64"]["rho_tot_sum"]) / \
             abs(diag["per_cell_fp64"]["rho_tot_sum"])
-        # the string finder alone (windings, counts and the pierced list)
+        # the string finder alone (windings, counts and the whole pierced list)
         params = A._lib.DiagParams(DX, bv.R, bv.lambda_, bv.R_prime_over_R, bv.m_r, A._lib.MASK_A, 0.8,
                                    A._lib.BOUNDARY_PERIODIC, 0, 1, 0, 0)
+        full_list = torch.empty(n ** 3 // 4, dtype=torch.int64, device=dev)
         t_ev = []
         for r in range(3):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             A._lib.call("axs_level_diagnostics", _C.byref(lv32.c), _C.byref(params), None,
-                        lv32._result.data_ptr(), lv32._pierced.data_ptr(), lv32._pierced.numel(),
+                        lv32._result.data_ptr(), full_list.data_ptr(), full_list.numel(),
                         lv32._scratch.data_ptr(), lv32._scratch.numel(), torch.cuda.current_stream().cuda_stream)
             e1.record()
             e1.synchronize()
@@ -569,6 +570,7 @@ def run_native(args):
         res = A.level._result_from_bytes(lv32._result)
         diag["string_finder_only"] = {"ms": min(t_ev), "n_p_plain": res.n_p_plain, "n_listed": res.n_listed,
                                       "read_gbps": 8 * n ** 3 / (min(t_ev) * 1e-3) / 1e9}
+        del full_list
         tags, n_tagged, _ = lv32.tag_cells(n_error_buf=4, block=32)
         torch.cuda.synchronize()
         t_ev = []

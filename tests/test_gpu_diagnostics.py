@@ -207,3 +207,73 @@ def test_exact_zeros_and_a_vacuum_corner_match_oracle(axs, orc, dtype):
     if dtype == torch.float64:
         np.testing.assert_allclose(d.energy_sums, ref.energy_sums, rtol=1e-12)
         assert d.vel_count == ref.vel_count
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("box", ["rand", "ic"])
+@pytest.mark.parametrize("boundary", ["ghosts", "periodic"])
+def test_string_finder_alone_vs_reference(axs, golden, prec, box, boundary):
+    """The windings-only pass (the edge-code finder): the reference's counts and
+    pierced set, with and without a coverage mask."""
+    g = golden(f"fields_{prec}.npz")
+    dt = torch.float64 if prec == "f64" else torch.float32
+    st = g[f"{box}_state"]
+    c, nz, ny, nx = st.shape
+    ng = 2 if boundary == "ghosts" else 0
+    t = axs.new_fab((nx, ny, nz), ng, dtype=dt)
+    axs.valid(t, ng).copy_(_dev(st, dt))
+    if ng:
+        axs.fill_periodic_ghosts(t, ng)
+    bmode = axs._lib.BOUNDARY_GHOSTS if ng else axs._lib.BOUNDARY_PERIODIC
+    r, lst = _run_diag(axs, t, ng, _params(axs, g, 1, bmode, want=(0, 1, 0), prec=prec))
+    assert r.status == 0 and r.n_near_tie == 0
+    assert (r.n_p_plain, r.n_p_weighted) == tuple(g[f"{box}_counts"])
+    assert list(r.energy_sums) == [0.0] * 14 and r.vel_count == 0
+    np.testing.assert_array_equal(np.sort(lst), _pierced_from_windings(g[f"{box}_windings"]))
+    r, _ = _run_diag(axs, t, ng, _params(axs, g, 1, bmode, want=(0, 1, 0), prec=prec), mask=g[f"{box}_mask"])
+    assert (r.n_p_plain, r.n_p_weighted) == tuple(g[f"{box}_counts_masked"])
+
+
+def _finder_cases(orc, n):
+    rng = np.random.default_rng(11)
+    v = orc.fourier_ic_state(n, 4.0, seed=8)
+    v[2:] = 0.0
+    yield "ic", v
+    # exact zeros (atan2(0, 0)), a false-vacuum block and huge values: vertices outside float range
+    w = v.copy()
+    zs = rng.integers(0, n, size=(60, 3))
+    w[:2, zs[:, 0], zs[:, 1], zs[:, 2]] = 0.0
+    w[:2, :5, :3, :4] = 0.0
+    w[:2, 7, 7, 7] = 1e31
+    yield "zeros", w
+    # phases pi apart on every x edge: every cell goes to the double path, with
+    # near-ties counted
+    u = np.zeros_like(v)
+    x = np.arange(n)
+    u[0] = np.where(x % 2 == 0, 1.0, -1.0)[None, None, :] * (1.0 + 0.1 * rng.random((n, n, n)))
+    u[1] = np.where((x // 2) % 3 == 0, 0.0, 1e-9) * rng.standard_normal((n, n, n))
+    yield "pi", u
+    # random phases: many pierced plaquettes, many list flushes per block
+    r = rng.standard_normal((4, n, n, n))
+    r[2:] = 0.0
+    yield "rand", r
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("n", [24, 40])
+def test_string_finder_alone_equals_fused_pass(axs, orc, dtype, n):
+    """The edge-code finder against the fused pass (itself pinned to the
+    reference above): counts, near-ties and the pierced set, on fields that
+    take the double fall-back (zeros, huge values, edges pi apart) and on a
+    dense random field, at a size that leaves partial tiles."""
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    for name, v in _finder_cases(orc, n):
+        lvl = axs.PeriodicLevel(n, 0.5, dtype=dtype, pierced_capacity=3 * n ** 3)
+        lvl.set_state(_dev(v).to(dtype))
+        full = lvl.diagnostics(bg, 1.3)
+        alone = lvl.diagnostics(bg, 1.3, strings_only=True)
+        assert (alone.n_p_plain, alone.n_p_weighted, alone.n_near_tie) == \
+            (full.n_p_plain, full.n_p_weighted, full.n_near_tie), name
+        assert torch.equal(torch.sort(alone.pierced)[0], torch.sort(full.pierced)[0]), name
+        if name == "pi":
+            assert full.n_near_tie > 0
