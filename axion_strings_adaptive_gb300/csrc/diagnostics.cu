@@ -552,7 +552,10 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
 // single-precision fast path of the fused pass edge for edge, with the same
 // fall back to the reference's double arithmetic: a cell is redone in double
 // when one of its nine edges lies within 1e-5 of +-pi or ends at a vertex
-// outside float range. Per vertex plane, with one block barrier:
+// outside float range. Those cells are queued in shared memory and redone
+// after the z-chunk, outside the plane loop, so the rare double path costs
+// the loop no registers; a chunk with more than the queue holds is searched
+// again for them. Per vertex plane, with one block barrier:
 //   B: the x and y edge codes of the plane before, from the neighbours' phases;
 //   A: the thread's vertices' phases, from psi loaded into registers two
 //      planes ahead, and their z edges to the plane below (phase kept in a
@@ -563,10 +566,12 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
 constexpr int FTX = 32, FTY = 16, FVX = FTX + 1, FVY = FTY + 1;
 constexpr int kFinderExtra = FTX + FTY + 1;  // vertices of the last row (x < FTX) and last column
 constexpr int kFinderListBuf = 3072, kFinderFlushAt = kFinderListBuf - 6 * kDiagThreads;
+constexpr int kFinderBadQ = 1024;  // cells queued for the double path per z-chunk
 static_assert(FTX * FTY == 2 * kDiagThreads && kFinderExtra <= kDiagThreads, "two cells, at most three vertices per thread");
 
 struct FinderSmem {
     long long lbuf[kFinderListBuf];
+    int badq[kFinderBadQ];           // tile-local x | y << 5 | (z - za) << 9
     float th[4][FVY][FVX];           // phases of vertex plane p in slot p mod 4
     unsigned char ok[4][FVY][FVX];   // the vertex lies inside float range
     unsigned char inp[4][FVY][FVX];  // x edge code (bits 0-2), y edge code (bits 3-5)
@@ -608,8 +613,42 @@ __device__ __noinline__ CellWindings finder_cell_double(const DiagView v, const 
     return r;
 }
 
+// Whether the finder sends a cell to the double path: one of its seven
+// vertices outside float range, or one of its nine edges inside the band
+// (edge_code's test on the same float phases).
 template <typename T>
-__global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
+__device__ __noinline__ bool finder_cell_bad(const DiagView v, const T *base, int x, int y, int z)
+{
+    float th[8];
+    bool ok[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int xx = x + (c & 1), yy = y + ((c >> 1) & 1), zz = z + (c >> 2);
+        const bool on = (v.wx || xx < v.nx + v.ox) && (v.wy || yy < v.ny + v.oy) && (v.wz || zz < v.nz + v.oz);
+        const T a = on ? base[view_off<T>(v, 0, xx, yy, zz)] : T(0);
+        const T b = on ? base[view_off<T>(v, 1, xx, yy, zz)] : T(0);
+        if constexpr (sizeof(T) == 4) {
+            const float m = fmaxf(fabsf(a), fabsf(b));
+            ok[c] = m > 1e-30f && m < 1e30f;
+        } else {
+            const double m = fmax(fabs(a), fabs(b));
+            ok[c] = m > 1e-30 && m < 1e30;
+        }
+        th[c] = atan2f((float)b, (float)a);
+    }
+    // corners c = x + 2 y + 4 z; edges x: 0-1, 2-3, 4-5; y: 0-2, 1-3, 4-6; z: 0-4, 1-5, 2-6
+    const int ea[9] = {0, 2, 4, 0, 1, 4, 0, 1, 2}, eb[9] = {1, 3, 5, 2, 3, 6, 4, 5, 6};
+    unsigned bad = 0;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) bad |= edge_code(th[ea[e]], th[eb[e]], ok[ea[e]] && ok[eb[e]]);
+    return (bad & 4u) != 0;
+}
+
+template <typename T>
+#ifndef AXS_FINDER_MIN_BLOCKS
+#define AXS_FINDER_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_BLOCKS : 3)
     finder_kernel(const DiagView v, const uint8_t *__restrict__ mask, DiagPartial *__restrict__ partials,
                   unsigned long long *__restrict__ list_counter, long long *__restrict__ list, long long capacity,
                   int tiles_x, int ntiles, int zchunk, long long n_items, long long items_per_box,
@@ -617,14 +656,14 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
 {
     extern __shared__ __align__(16) unsigned char finder_smem_raw[];
     FinderSmem &sm = *reinterpret_cast<FinderSmem *>(finder_smem_raw);
-    __shared__ int lcount, flush_n;
+    __shared__ int lcount, flush_n, badn, bad_over;
     __shared__ unsigned long long flush_base;
     __shared__ long long red[kDiagThreads / 32][3];
     const int tid = threadIdx.x, lane = tid & 31;
     const int lx = tid % FTX, ly = tid / FTX;  // cells (lx, ly) and (lx, ly + FTY / 2)
     const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
     int cnt_p = 0, cnt_w = 0, cnt_tie = 0;  // per-thread counts fit 32 bits
-    if (tid == 0) lcount = 0;
+    if (tid == 0) lcount = badn = bad_over = 0;
     int warp_end = 0;  // end of this warp's last append to lbuf (lane-uniform)
     auto flush = [&]() {
         if (tid == 0) {
@@ -641,6 +680,24 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
         __syncthreads();
         warp_end = 0;
     };
+    // a cell of the double path: windings, counts, tag and list entries (one
+    // global atomic each: these cells are rare)
+    auto redo_cell = [&](const T *base, long long qbox, int x, int y, int z) {
+        const CellWindings cw = finder_cell_double<T>(v, base, x, y, z);
+        const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
+        cnt_tie += cw.ties;
+        if (tags != nullptr) tags[cell] = (cw.w[0] | cw.w[1] | cw.w[2]) != 0;
+#pragma unroll
+        for (int pl = 0; pl < 3; ++pl) {
+            if (!cw.w[pl]) continue;
+            ++cnt_p;
+            cnt_w += abs(cw.w[pl]);
+            if (list != nullptr) {
+                const unsigned long long pos = atomicAdd(list_counter, 1ull);
+                if (pos < (unsigned long long)capacity) list[pos] = 4LL * cell + pl;
+            }
+        }
+    };
 
     // the thread's vertices: (lx, ly), (lx, ly + 8) and, for the first 49
     // threads, one of the last row (y = FTY) or the last column (x = FTX)
@@ -655,17 +712,16 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
         const int x0 = (tile % tiles_x) * FTX, y0 = (tile / tiles_x) * FTY;
         const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
 
-        // in-plane element offsets of the thread's vertices; psi is zero outside
-        // the ghost region
-        int64_t voff[3];
-        bool von[3];
+        // in-plane element offsets of the thread's vertices (the host checks that
+        // a plane's offsets fit 31 bits), -1 outside the ghost region: psi is zero there
+        int voff[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const int xx = x0 + vi[k], yy = y0 + vj[k];
-            von[k] = (k < 2 || extra) && xx <= v.nx && yy <= v.ny && (v.wx || xx < v.nx + v.ox) &&
-                     (v.wy || yy < v.ny + v.oy);
-            voff[k] = (int64_t)(wrap_or_self(xx, v.nx, v.wx) + v.ox) +
-                      (int64_t)(wrap_or_self(yy, v.ny, v.wy) + v.oy) * v.js;
+            const bool on = (k < 2 || extra) && xx <= v.nx && yy <= v.ny && (v.wx || xx < v.nx + v.ox) &&
+                            (v.wy || yy < v.ny + v.oy);
+            voff[k] = on ? (wrap_or_self(xx, v.nx, v.wx) + v.ox) + (wrap_or_self(yy, v.ny, v.wy) + v.oy) * (int)v.js
+                         : -1;
         }
         // psi of vertex planes za, za + 1, ... in order, into registers
         int lz = za, lzw = wrap_or_self(za, v.nz, v.wz);
@@ -674,7 +730,7 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
             const T *pb = base + (int64_t)(lzw + v.oz) * v.ks;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const bool on = zin && von[k];
+                const bool on = zin && voff[k] >= 0;
                 buf[k][0] = on ? __ldg(pb + voff[k]) : T(0);
                 buf[k][1] = on ? __ldg(pb + voff[k] + v.cs) : T(0);
             }
@@ -723,38 +779,43 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
         // C: windings of the cells of plane za + j - 3
         auto stage_c = [&](int j) {
             const int s0 = (j - 3) & 3, s1 = (j - 2) & 3, z = za + j - 3;
-            int w[2][3], mine = 0;
-            int64_t cells[2];
+            // cell index of (lx, ly) and the step to (lx, ly + FTY / 2)
+            const int64_t cell0 = qbox * box_cells + (int64_t)(x0 + lx) +
+                                  (int64_t)v.nx * ((int64_t)(y0 + ly) + (int64_t)v.ny * z);
+            const int64_t hstep = (int64_t)v.nx * (FTY / 2);
+            unsigned pm = 0;  // pierced plaquettes: bit 3 h + plane
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int cy = ly + h * (FTY / 2), x = x0 + lx, y = y0 + cy;
-                const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
-                cells[h] = cell;
-                w[h][0] = w[h][1] = w[h][2] = 0;
-                if (!(x < v.nx && y < v.ny && (mask == nullptr || mask[cell] != 0))) continue;
+                if (!(x < v.nx && y < v.ny)) continue;
+                const int64_t cell = cell0 + h * hstep;
+                if (mask != nullptr && mask[cell] == 0) continue;
                 const unsigned c000 = sm.inp[s0][cy][lx], c100 = sm.inp[s0][cy][lx + 1];
                 const unsigned c010 = sm.inp[s0][cy + 1][lx], c001 = sm.inp[s1][cy][lx];
                 const unsigned z000 = sm.zc[s0][cy][lx], z100 = sm.zc[s0][cy][lx + 1], z010 = sm.zc[s0][cy + 1][lx];
                 const unsigned bad =
                     ((c000 | c001) & 0x24u) | (c100 & 0x20u) | (c010 & 0x04u) | ((z000 | z100 | z010) & 0x04u);
-                if (!bad) {
-                    // StringFinder.hpp:45-68 order: xy (000 100 110 010), yz (000 010 011 001), zx (000 001 101 100)
-                    w[h][0] = edge_fold(c000) + edge_fold(c100 >> 3) - edge_fold(c010) - edge_fold(c000 >> 3);
-                    w[h][1] = edge_fold(c000 >> 3) + edge_fold(z010) - edge_fold(c001 >> 3) - edge_fold(z000);
-                    w[h][2] = edge_fold(z000) + edge_fold(c001) - edge_fold(z100) - edge_fold(c000);
-                } else {
-                    const CellWindings cw = finder_cell_double<T>(v, base, x, y, z);
-                    w[h][0] = cw.w[0];
-                    w[h][1] = cw.w[1];
-                    w[h][2] = cw.w[2];
-                    cnt_tie += cw.ties;
+                if (bad) {
+                    // the double path after the chunk
+                    const int slot = atomicAdd(&badn, 1);
+                    if (slot < kFinderBadQ)
+                        sm.badq[slot] = lx | (cy << 5) | ((z - za) << 9);
+                    else
+                        bad_over = 1;
+                    continue;
                 }
+                // StringFinder.hpp:45-68 order: xy (000 100 110 010), yz (000 010 011 001), zx (000 001 101 100)
+                const int wxy = edge_fold(c000) + edge_fold(c100 >> 3) - edge_fold(c010) - edge_fold(c000 >> 3);
+                const int wyz = edge_fold(c000 >> 3) + edge_fold(z010) - edge_fold(c001 >> 3) - edge_fold(z000);
+                const int wzx = edge_fold(z000) + edge_fold(c001) - edge_fold(z100) - edge_fold(c000);
+                const unsigned cm = (wxy != 0) | (wyz != 0) << 1 | (wzx != 0) << 2;
                 // StringTagger.hpp:117-151: a cell is tagged when a plaquette at its low corner is pierced
-                if (tags != nullptr) tags[cell] = (w[h][0] | w[h][1] | w[h][2]) != 0;
-                cnt_p += (w[h][0] != 0) + (w[h][1] != 0) + (w[h][2] != 0);
-                cnt_w += abs(w[h][0]) + abs(w[h][1]) + abs(w[h][2]);
-                mine += (w[h][0] != 0) + (w[h][1] != 0) + (w[h][2] != 0);
+                if (tags != nullptr) tags[cell] = cm != 0;
+                cnt_w += abs(wxy) + abs(wyz) + abs(wzx);
+                pm |= cm << (3 * h);
             }
+            const int mine = __popc(pm);
+            cnt_p += mine;
             // pierced plaquettes into the block's buffer: a warp scan and one
             // shared-memory atomic per warp that has any
             if (list != nullptr && __any_sync(0xffffffffu, mine != 0)) {
@@ -770,10 +831,12 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
                 wbase = __shfl_sync(0xffffffffu, wbase, 31);
                 warp_end = wbase + wtot;
                 int pos = wbase + incl - mine;
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    for (int pl = 0; pl < 3; ++pl)
-                        if (w[h][pl]) sm.lbuf[pos++] = 4LL * cells[h] + pl;
+                const long long e0 = 4LL * cell0, eh = 4LL * hstep - 3;
+                while (pm) {
+                    const int b = __ffs(pm) - 1;
+                    pm &= pm - 1;
+                    sm.lbuf[pos++] = e0 + b + (b >= 3 ? eh : 0);  // 4 cell + plane
+                }
             }
         };
         // iteration j: B (plane za + j - 1), A (plane za + j, then the load of
@@ -798,6 +861,27 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? 4 : 3)
             step(j, bufa);
             if (j + 1 < len + 3) step(j + 1, bufb);
         }
+        // the chunk's double-path cells: from the queue, or, when it overflowed,
+        // by testing every cell of the chunk again
+        __syncthreads();
+        const int nbad = badn;
+        if (!bad_over) {
+            for (int i = tid; i < nbad; i += kDiagThreads) {
+                const int e = sm.badq[i];
+                redo_cell(base, qbox, x0 + (e & 31), y0 + ((e >> 5) & 15), za + (e >> 9));
+            }
+        } else {
+            for (int c = tid; c < FTX * FTY * len; c += kDiagThreads) {
+                const int x = x0 + c % FTX, y = y0 + (c / FTX) % FTY, z = za + c / (FTX * FTY);
+                if (x >= v.nx || y >= v.ny) continue;
+                if (mask != nullptr &&
+                    mask[qbox * box_cells + x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z)] == 0)
+                    continue;
+                if (finder_cell_bad<T>(v, base, x, y, z)) redo_cell(base, qbox, x, y, z);
+            }
+        }
+        __syncthreads();
+        if (tid == 0) badn = bad_over = 0;  // published by the next chunk's first barrier
     }
     if (list != nullptr && __syncthreads_or(warp_end > 0)) flush();
 
@@ -963,8 +1047,8 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     long long items, items_per_box;
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
     int rc0 = AXS_OK;
-    if (q.want_plaq && !q.want_energy && !q.want_vel) {
-        // windings only: the edge-code finder
+    if (q.want_plaq && !q.want_energy && !q.want_vel && (int64_t)(v.ny + 2 * v.oy + 2) * v.js < INT_MAX) {
+        // windings only: the edge-code finder (in-plane offsets in 31 bits)
         const bool f32 = v.dtype != AXS_F64;
         diag_plan(v, nboxes, diag_grid(ncell), FTX, FTY, f32 ? 4 : 3, tiles_x, ntiles, zchunk, items_per_box, items,
                   grid);
