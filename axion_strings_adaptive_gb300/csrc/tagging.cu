@@ -204,6 +204,103 @@ __global__ void tag_count_kernel(const uint8_t *__restrict__ tags, int nx, int n
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(count, mine);
 }
 
+// ---- the buffer on bit-packed tags (nx a multiple of 32): bit b of word w of
+// row (y, z) is cell x = 32 w + b. A pass handles 32 cells per word and moves
+// an eighth of the byte array's bytes (16 MB for 512^3, held in L2).
+
+// byte tags -> bits
+__global__ void tag_pack_kernel(const uint8_t *__restrict__ in, uint32_t *__restrict__ out, int64_t nwords)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(in + 32 * w);
+        const uint4 a = p[0], b = p[1];
+        const uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t bits = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) bits |= (uint32_t)(((v[q] >> (8 * k)) & 0xffu) != 0) << (4 * q + k);
+        out[w] = bits;
+    }
+}
+
+__device__ __forceinline__ int wrap_small(int i, int n)
+{
+    while (i < 0) i += n;
+    while (i >= n) i -= n;
+    return i;
+}
+
+// x: OR over cells x - nb .. x + nb of the row (periodic over W words)
+__global__ void tag_dilate_x_bits_kernel(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, int W,
+                                         int64_t nwords, int nb)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = w / W;
+        const int i = (int)(w - row * W);
+        const uint32_t *r = in + row * W;
+        uint32_t acc = r[i];
+        for (int d = 1; d <= nb; ++d) {
+            const int q = d >> 5, sh = d & 31;
+            // cells x + d from words i + q, i + q + 1; cells x - d from words i - q - 1, i - q
+            acc |= __funnelshift_r(r[wrap_small(i + q, W)], r[wrap_small(i + q + 1, W)], sh) |
+                   __funnelshift_l(r[wrap_small(i - q - 1, W)], r[wrap_small(i - q, W)], sh);
+        }
+        out[w] = acc;
+    }
+}
+
+// y or z: OR over rows pos - nb .. pos + nb along an axis of len rows, stride words apart
+__global__ void tag_dilate_rows_bits_kernel(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                                            int64_t nwords, int64_t stride, int len, int nb)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
+        const int pos = (int)((w / stride) % len);
+        const int64_t base = w - (int64_t)pos * stride;
+        uint32_t acc = 0;
+        for (int d = -nb; d <= nb; ++d) acc |= in[base + (int64_t)wrap_small(pos + d, len) * stride];
+        out[w] = acc;
+    }
+}
+
+// bits -> byte tags (when out is given), the tag count and the block flags
+__global__ void tag_unpack_count_kernel(const uint32_t *__restrict__ bits, uint8_t *__restrict__ out, int W, int ny,
+                                        int nz, int block, uint8_t *__restrict__ flags,
+                                        unsigned long long *__restrict__ count, int64_t nwords)
+{
+    const int nbx = block > 0 ? (32 * W + block - 1) / block : 0, nby = block > 0 ? (ny + block - 1) / block : 0;
+    unsigned long long mine = 0;
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = bits[w];
+        if (out != nullptr) {
+            uint32_t v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const uint32_t nib = (b >> (4 * q)) & 15u;  // cells 4q .. 4q + 3 -> bytes 0 .. 3
+                v[q] = (nib & 1u) | ((nib & 2u) << 7) | ((nib & 4u) << 14) | ((nib & 8u) << 21);
+            }
+            uint4 *o = reinterpret_cast<uint4 *>(out + 32 * w);
+            o[0] = make_uint4(v[0], v[1], v[2], v[3]);
+            o[1] = make_uint4(v[4], v[5], v[6], v[7]);
+        }
+        mine += __popc(b);
+        if (flags != nullptr && b != 0) {
+            const int64_t row = w / W;
+            const int i = (int)(w - row * W), j = (int)(row % ny), k = (int)(row / ny);
+            const int64_t fb = (int64_t)nbx * ((j / block) + (int64_t)nby * (k / block));
+            uint32_t m = b;
+            while (m) {
+                const int bx = (32 * i + __ffs(m) - 1) / block;
+                flags[bx + fb] = 1;
+                const int next = (bx + 1) * block - 32 * i;  // first bit of the next block
+                m = next >= 32 ? 0u : (m & (~0u << next));
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(count, mine);
+}
+
 static int tag_grid(int64_t n)
 {
     const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
@@ -275,6 +372,40 @@ int axs_level_tag_cells(const axs_level *lv, const axs_tag_params *p, uint8_t *t
         else
             tag_kernel<double><<<grid, 256, 0, st>>>(static_cast<const double *>(lv->state), g, q, first);
         if ((rc = launch_status("tag cells"))) return rc;
+    }
+    // the buffer and the count on bit-packed tags: rows of whole words, and
+    // 16-byte aligned byte arrays for the vector loads and stores
+    const bool bits = lv->nx % 32 == 0 && ((uintptr_t)tags_dev % 16) == 0 && ((uintptr_t)tmp % 16) == 0;
+    const int64_t nwords = n / 32;
+    const int wgrid = tag_grid(nwords);
+    const int W = lv->nx / 32;
+    if (bits) {
+        AXS_CUDA_CHECK(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
+        if (p->block > 0) {
+            const int64_t nb = (int64_t)((lv->nx + p->block - 1) / p->block) * ((lv->ny + p->block - 1) / p->block) *
+                               ((lv->nz + p->block - 1) / p->block);
+            AXS_CUDA_CHECK(cudaMemsetAsync(block_flags_dev, 0, (size_t)nb, st));
+        }
+        auto *tmp_bits = reinterpret_cast<uint32_t *>(tmp);
+        if (p->n_error_buf > 0) {
+            // bytes in tmp -> bits A (in the output array, not yet written) -> x -> B (tmp) -> y -> A -> z -> B
+            auto *a = reinterpret_cast<uint32_t *>(tags_dev);
+            tag_pack_kernel<<<wgrid, 256, 0, st>>>(tmp, a, nwords);
+            tag_dilate_x_bits_kernel<<<wgrid, 256, 0, st>>>(a, tmp_bits, W, nwords, p->n_error_buf);
+            tag_dilate_rows_bits_kernel<<<wgrid, 256, 0, st>>>(tmp_bits, a, nwords, W, lv->ny, p->n_error_buf);
+            tag_dilate_rows_bits_kernel<<<wgrid, 256, 0, st>>>(a, tmp_bits, nwords, (int64_t)W * lv->ny, lv->nz,
+                                                              p->n_error_buf);
+            tag_unpack_count_kernel<<<wgrid, 256, 0, st>>>(tmp_bits, tags_dev, W, lv->ny, lv->nz, p->block,
+                                                          p->block > 0 ? block_flags_dev : nullptr, count, nwords);
+        } else {
+            tag_pack_kernel<<<wgrid, 256, 0, st>>>(tags_dev, tmp_bits, nwords);
+            tag_unpack_count_kernel<<<wgrid, 256, 0, st>>>(tmp_bits, nullptr, W, lv->ny, lv->nz, p->block,
+                                                          p->block > 0 ? block_flags_dev : nullptr, count, nwords);
+        }
+        if ((rc = launch_status("tag buffer and count"))) return rc;
+        if (n_tagged_dev)
+            AXS_CUDA_CHECK(cudaMemcpyAsync(n_tagged_dev, count, sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+        return AXS_OK;
     }
     if (p->n_error_buf > 0) {
         dilate_axis_kernel<<<grid, 256, 0, st>>>(tmp, tags_dev, lv->nx, lv->ny, lv->nz, 0, p->n_error_buf);

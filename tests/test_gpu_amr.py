@@ -177,6 +177,9 @@ def test_composite_diagnostics_straight_strings(axs):
     d0 = coarse.diagnostics(bg, 1.0)
     # the same string length: twice the plaquettes at half the spacing (ell = (2/3) N_p dx)
     assert d.xi_plain == pytest.approx(d0.xi_plain, rel=1e-12)
+    # the string finder alone (masked coarse level and the patches) counts the same
+    ds = two.diagnostics(bg, 1.0, strings_only=True)
+    assert (ds.n_p_plain, ds.n_p_weighted) == (d.n_p_plain, d.n_p_weighted)
 
 
 def test_time_interpolated_ring_and_neighbour_copies(axs):
@@ -285,6 +288,12 @@ def test_batched_patch_diagnostics_match_per_patch_passes(axs, dtype):
     assert set(lst.cpu().numpy().tolist()) == pierced and got.n_listed == len(pierced)
     np.testing.assert_allclose(np.array(list(got.energy_sums)), sums, rtol=1e-12)
     assert got.vel_sum == pytest.approx(vsum, rel=1e-12)
+    # the string finder alone over all patches: the same counts and pierced set
+    prm_s = L.DiagParams(p.dx, v.R, v.lambda_, v.R_prime_over_R, v.m_r, L.MASK_A, 0.8, L.BOUNDARY_GHOSTS, 0, 1, 0, 0)
+    alone, lst_s = p.diagnostics(prm_s, list_capacity=cap)
+    assert [alone.n_p_plain, alone.n_p_weighted, alone.n_near_tie] == [got.n_p_plain, got.n_p_weighted,
+                                                                        got.n_near_tie]
+    assert set(lst_s.cpu().numpy().tolist()) == pierced and alone.n_listed == len(pierced)
 
 
 def test_regrid_keeps_the_fine_data_of_blocks_that_stay_refined(axs):
