@@ -36,8 +36,9 @@ class Patches:
         L.call("axs_patches_layout", _DT[dtype], int(n), int(npatches), C.byref(lay))
         self.layout, self.n, self.npatches, self.dx, self.dtype = lay, int(n), int(npatches), float(dx), dtype
         self.state = torch.zeros((4, lay.plane_elems), dtype=dtype, device=device)
-        # sweep A writes every work cell sweep B reads, so the work planes need no clearing
-        self.work = torch.empty((8, lay.plane_elems), dtype=dtype, device=device)
+        # sweep A writes every work cell sweep B reads, so the work planes need no
+        # clearing; patch sizes the fused step covers need no work arena
+        self.work = torch.empty((8, lay.plane_elems) if lay.work_bytes > 0 else (0,), dtype=dtype, device=device)
         self.table = torch.zeros(lay.table_bytes, dtype=torch.uint8, device=device)
         self.c = L.PatchesC(_DT[dtype], self.n, self.npatches, self.dx, self.state.data_ptr(), self.work.data_ptr(),
                             self.table.data_ptr(), lay.state_bytes, lay.work_bytes, lay.table_bytes)

@@ -87,17 +87,29 @@ static int64_t patch_table_bytes(const PatchGeom &g, int npatches)
            4 * patch_items_bound(g, npatches);
 }
 
+// The fused step (one launch per fine step, stage values in shared memory)
+// covers this patch size and count; otherwise the two sweeps through the
+// 8-component work arena step the patches.
+static bool patches_fused(int32_t dtype, int n, int npatches);
+
+// bytes of the work arena: none when the fused step covers the patches
+static int64_t patch_work_bytes(const PatchGeom &g, int32_t dtype, int n, int npatches)
+{
+    return patches_fused(dtype, n, npatches) ? 0 : 8 * g.plane * (int64_t)dtype_size(dtype);
+}
+
 static int validate_patches(const axs_patches *p, PatchGeom &g)
 {
     AXS_REQUIRE(p != nullptr, AXS_ERR_INVALID_ARGUMENT, "null patches");
     int rc = patch_geom(p->dtype, p->n, p->npatches, g);
     if (rc) return rc;
     AXS_REQUIRE(p->dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
-    AXS_REQUIRE(p->state && p->work && p->table, AXS_ERR_INVALID_ARGUMENT, "null patch buffer");
+    const int64_t need_work = patch_work_bytes(g, p->dtype, p->n, p->npatches);
+    AXS_REQUIRE(p->state && p->table && (p->work || need_work == 0), AXS_ERR_INVALID_ARGUMENT, "null patch buffer");
     AXS_REQUIRE(((uintptr_t)p->state % 128) == 0 && ((uintptr_t)p->work % 128) == 0 && ((uintptr_t)p->table % 128) == 0,
                 AXS_ERR_ALIGNMENT, "patch buffers must be 128-byte aligned");
     const int64_t es = (int64_t)dtype_size(p->dtype);
-    AXS_REQUIRE(p->state_bytes >= 4 * g.plane * es && p->work_bytes >= 8 * g.plane * es &&
+    AXS_REQUIRE(p->state_bytes >= 4 * g.plane * es && p->work_bytes >= need_work &&
                     p->table_bytes >= patch_table_bytes(g, p->npatches),
                 AXS_ERR_WORKSPACE, "patch buffer too small");
     return AXS_OK;
@@ -153,6 +165,16 @@ template <typename T> static void fused_tiles(int n, int &cx, int &cy)
     if (x * y > 8) return;  // portable cluster size
     cx = x;
     cy = y;
+}
+
+static bool patches_fused(int32_t dtype, int n, int npatches)
+{
+    int cx = 0, cy = 0;
+    if (dtype == AXS_F64)
+        fused_tiles<double>(n, cx, cy);
+    else
+        fused_tiles<float>(n, cx, cy);
+    return cx > 0 && npatches <= 65535;  // one grid z slice per patch
 }
 
 // Execution barrier of the patch's tiles, split so that sweep B's shared-memory
@@ -336,13 +358,11 @@ template <typename T> static int build_patch_table(const axs_patches *p, const P
                  items_off = desc_off + sizeof(EnsBoxDesc) * 2 * np;
     std::vector<unsigned char> img(items_off + 4 * (items_a.size() + items_b.size()), 0);
     const int64_t es = (int64_t)dtype_size(p->dtype);
-    int fcx = 0, fcy = 0;
-    fused_tiles<T>(n, fcx, fcy);
-    const bool fused = fcx > 0 && np <= 65535;
+    const bool fused = patches_fused(p->dtype, n, np);
     for (int q = 0; q < np; ++q) {
         auto *maps = reinterpret_cast<CUtensorMap *>(img.data() + maps_off) + 2 * q;
         const char *sb = static_cast<const char *>(p->state) + (int64_t)q * g.box * es;
-        const char *wb = static_cast<const char *>(p->work) + (int64_t)q * g.box * es;
+        const char *wb = fused ? nullptr : static_cast<const char *>(p->work) + (int64_t)q * g.box * es;
         // sweep A boxes are TXA+8 x TYA+4, sweep B boxes TXB+8 x TYB+4: one map each
         if ((rc = make_tensor_map_4d(&maps[0], sb, p->dtype, g.js, n + 2 * kPatchRY, n + 2 * kPatchRZ, 4, g.js * es,
                                      g.ks * es, g.plane * es, PT::TXA + 8, PT::TYA + 4, 1, 4)))
@@ -409,7 +429,7 @@ static int patch_step(const axs_patches *p, const PatchGeom &g, const axs_patch_
     a.maps = reinterpret_cast<const CUtensorMap *>(table + kPatchHeader);
     int fcx = 0, fcy = 0;
     fused_tiles<T>(g.n, fcx, fcy);
-    if (fcx > 0 && np <= 65535) {  // one grid z slice per patch
+    if (patches_fused(p->dtype, g.n, np)) {
         a.c1 = stage_coef<T>(bg, tau_i + t);
         a.c2 = stage_coef<T>(bg, tau_i + t + 0.5 * dt);
         a.c4 = stage_coef<T>(bg, tau_i + t + dt);
@@ -837,7 +857,7 @@ int axs_patches_layout(int32_t dtype, int32_t n, int32_t npatches, axs_patch_lay
     out->y_offset = kPatchRY;
     out->z_offset = kPatchRZ;
     out->state_bytes = 4 * g.plane * es;
-    out->work_bytes = 8 * g.plane * es;
+    out->work_bytes = patch_work_bytes(g, dtype, n, npatches);
     out->table_bytes = patch_table_bytes(g, npatches);
     return AXS_OK;
 }

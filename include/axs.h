@@ -349,7 +349,8 @@ typedef struct axs_patches {
     int32_t npatches;
     double dx;        /* fine spacing */
     void *state;      /* 4 component planes */
-    void *work;       /* 8 component planes */
+    void *work;       /* 8 component planes; may be NULL when axs_patches_layout reports
+                         work_bytes = 0 (the fused step covers the patch size and count) */
     void *table;      /* written by axs_patches_init */
     int64_t state_bytes, work_bytes, table_bytes;
 } axs_patches;
