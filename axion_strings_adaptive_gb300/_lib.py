@@ -150,6 +150,9 @@ SIGNATURES = {
     "axs_patches_init": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchPlan), _ptr]),
     "axs_patches_fill": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchMap), C.POINTER(LevelC), C.POINTER(LevelC), _dbl,
                                 _dbl, _i32, _ptr]),
+    "axs_patches_fill_list": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchMap), C.POINTER(LevelC), C.POINTER(LevelC),
+                                     _dbl, _dbl, _i32, _ptr, _i32, _ptr]),
+    "axs_patches_copy_boxes": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchesC), _ptr, _ptr]),
     "axs_patches_rk4_step": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchPlan), C.POINTER(BackgroundC), _dbl, _dbl,
                                     _dbl, _ptr]),
     "axs_patches_average_down": (_i32, [C.POINTER(PatchesC), C.POINTER(PatchMap), C.POINTER(LevelC), _ptr]),

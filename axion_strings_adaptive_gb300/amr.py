@@ -31,11 +31,21 @@ from .level import _DT, PeriodicLevel, _stream_ptr
 class Patches:
     """npatches refined patches of n^3 fine cells (spacing dx) with ghost rings."""
 
-    def __init__(self, n: int, npatches: int, dx: float, dtype=torch.float32, device="cuda"):
+    def __init__(self, n: int, npatches: int, dx: float, dtype=torch.float32, device="cuda",
+                 storage: torch.Tensor | None = None, clear: bool = True):
+        """storage: a 1-D tensor of dtype to lay the state arena in (its first
+        4 plane_elems elements), when it is large enough; else a new one.
+        clear: zero the arena (a caller that writes every box itself skips it)."""
         lay = L.PatchLayout()
         L.call("axs_patches_layout", _DT[dtype], int(n), int(npatches), C.byref(lay))
         self.layout, self.n, self.npatches, self.dx, self.dtype = lay, int(n), int(npatches), float(dx), dtype
-        self.state = torch.zeros((4, lay.plane_elems), dtype=dtype, device=device)
+        need = 4 * lay.plane_elems
+        if storage is None or storage.dtype != dtype or storage.numel() < need:
+            storage = torch.empty(need, dtype=dtype, device=device)
+        self.storage = storage
+        self.state = storage[:need].view(4, lay.plane_elems)
+        if clear:
+            self.state.zero_()
         # sweep A writes every work cell sweep B reads, so the work planes need no
         # clearing; patch sizes the fused step covers need no work arena
         self.work = torch.empty((8, lay.plane_elems) if lay.work_bytes > 0 else (0,), dtype=dtype, device=device)
@@ -109,10 +119,16 @@ class TwoLevel:
     ENERGY_NAMES = ["rho_tot", "rho_axion_kinetic", "rho_axion_gradient", "rho_radial_kinetic",
                     "rho_radial_gradient", "rho_radial_mass"]
 
-    def __init__(self, coarse: PeriodicLevel, block: int = 32):
+    def __init__(self, coarse: PeriodicLevel, block: int = 32, spare_arena: bool = True, headroom: float = 1.25):
+        """spare_arena: keep a second patch arena, sized with `headroom` over the
+        patch count, so that a regrid lays the new patches out in the arena the
+        old ones do not use (it copies the kept patches across) instead of
+        allocating one; a regrid allocates only when the patch count outgrows it."""
         if coarse.nx % block or coarse.ny % block or coarse.nz % block:
             raise ValueError("the coarse level must tile into blocks")
         self.coarse, self.block = coarse, int(block)
+        self.spare_arena, self.headroom = bool(spare_arena), float(headroom)
+        self._spare: torch.Tensor | None = None
         self.nb = (coarse.nx // block, coarse.ny // block, coarse.nz // block)
         # the coarse state at the start of the running coarse step (state only: the
         # ghost fill reads nothing else)
@@ -141,25 +157,40 @@ class TwoLevel:
             self._block_patch.fill_(-1)
             return
         dt = self.coarse.dtype
-        self.patches = Patches(2 * self.block, len(blocks), 0.5 * self.coarse.dx, dtype=dt, device=dev)
+        storage = None
+        if self.spare_arena:
+            lay = L.PatchLayout()
+            L.call("axs_patches_layout", _DT[dt], 2 * self.block, len(blocks), C.byref(lay))
+            need = 4 * lay.plane_elems
+            if self._spare is None or self._spare.numel() < need:
+                self._spare = None  # too small: free it before the new allocation
+                self._spare = torch.empty(int(need * self.headroom) + 1, dtype=dt, device=dev)
+            storage = self._spare
+        # every box is written below: copied from the old patch of its block, or
+        # cleared and interpolated from the coarse level
+        self.patches = Patches(2 * self.block, len(blocks), 0.5 * self.coarse.dx, dtype=dt, device=dev,
+                               storage=storage, clear=False)
         self._patch_block = torch.from_numpy(blocks.copy()).to(dev)
         bp = np.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=np.int32)
         bp[blocks[:, 2], blocks[:, 1], blocks[:, 0]] = np.arange(len(blocks), dtype=np.int32)
         self._block_patch = torch.from_numpy(bp).to(dev)
-        L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c), None, 0.0,
-               0.0, 1, None)
         if old_patches is not None:
             # the old patch of every new block, through the old block -> patch map (-1: newly refined)
             b = torch.from_numpy(blocks.astype(np.int64)).to(dev)
-            old_q = old_block_patch[b[:, 2], b[:, 1], b[:, 0]].to(torch.int64)
-            keep = old_q >= 0
-            if bool(keep.any()):
-                # whole patch boxes (valid cells and rings; the rings are refilled before use)
-                new_q = torch.nonzero(keep).flatten()
-                box = self.patches.layout.patch_elems
-                dst = self.patches.state.view(4, self.patches.npatches, box)
-                src = old_patches.state.view(4, old_patches.npatches, box)
-                dst.index_copy_(1, new_q, src.index_select(1, old_q[keep]))
+            old_q = old_block_patch[b[:, 2], b[:, 1], b[:, 0]].to(torch.int32).contiguous()
+        else:
+            old_q = torch.full((len(blocks),), -1, dtype=torch.int32, device=dev)
+        # whole patch boxes (valid cells and rings; the rings are refilled before use)
+        L.call("axs_patches_copy_boxes", C.byref(self.patches.c),
+               C.byref(old_patches.c) if old_patches is not None else None, old_q.data_ptr(), None)
+        new_list = torch.nonzero(old_q < 0).flatten().to(torch.int32).contiguous()
+        if new_list.numel():
+            L.call("axs_patches_fill_list", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c),
+                   None, 0.0, 0.0, 1, new_list.data_ptr(), int(new_list.numel()), None)
+        if self.spare_arena:
+            # the old arena is the next regrid's; the first patch set gets a second one
+            self._spare = old_patches.storage if old_patches is not None else \
+                torch.empty_like(self.patches.storage)
 
     def regrid(self, n_error_buf: int = 4, gradient_threshold: float = 1.7976931348623157e308,
                radial_gradient_threshold: float = 1.7976931348623157e308) -> int:

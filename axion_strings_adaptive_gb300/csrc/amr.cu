@@ -511,6 +511,7 @@ struct FillArgs {
     int64_t js, ks, box, plane;
     double theta, hdt;      // time fraction in the coarse step, coarse dt
     int valid_too;          // 1: also the valid cells (initialisation)
+    const int *patch_list;  // the patches to fill (NULL: all), one launch row of tiles each
     // time blend weights (host-computed): psi = h[0] psi0 + h[1] Pi0 + h[2] psi1 + h[3] Pi1,
     // Pi = h[4] Pi0 + h[5] Pi1 (h[1], h[3] include the coarse dt)
     double hd[6];
@@ -569,7 +570,9 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
     __shared__ T w[2][5];
     const int n = f.n, half = n / 2, tid = threadIdx.x;
     const int ntx = fill_tiles_x(n), ntiles = ntx * fill_tiles_y(n);
-    const int pq = blockIdx.x / ntiles, tile = blockIdx.x % ntiles;
+    const int li = blockIdx.x / ntiles, tile = blockIdx.x % ntiles;
+    const int pq = f.patch_list != nullptr ? f.patch_list[li] : li;
+    if (pq < 0 || pq >= f.np) return;  // a list entry outside the patches (whole block: no barrier skipped)
     // tile origins are even, so a fine cell's child index on each axis is its parity
     const int x0 = -8 + kFillT * (tile % ntx), y0 = -8 + kFillT * (tile / ntx);
     const int bx = f.patch_block[3 * pq], by = f.patch_block[3 * pq + 1], bz = f.patch_block[3 * pq + 2];
@@ -833,7 +836,26 @@ static int fill_args(const axs_patches *p, const PatchGeom &g, const axs_patch_m
     f.theta = 0.0;
     f.hdt = 0.0;
     f.valid_too = 0;
+    f.patch_list = nullptr;
     return AXS_OK;
+}
+
+// Whole patch boxes (4 components) of dst from src: box q from src box
+// src_of_dst[q], or zeros where that is negative (or not a src patch), in
+// 16-byte words. One launch row per dst patch (grid y strides over them).
+__global__ void patch_copy_boxes_kernel(uint4 *__restrict__ dst, const uint4 *__restrict__ src,
+                                        const int *__restrict__ src_of_dst, int np_dst, int np_src, int units,
+                                        int64_t dst_plane, int64_t src_plane)
+{
+    for (int q = blockIdx.y; q < np_dst; q += gridDim.y) {
+        const int s = src_of_dst[q];
+        const bool copy = src != nullptr && s >= 0 && s < np_src;
+        for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < 4 * units; u += gridDim.x * blockDim.x) {
+            const int c = u / units, r = u - c * units;
+            const uint4 v = copy ? src[c * src_plane + (int64_t)s * units + r] : make_uint4(0u, 0u, 0u, 0u);
+            dst[c * dst_plane + (int64_t)q * units + r] = v;
+        }
+    }
 }
 
 }  // namespace axs
@@ -896,6 +918,14 @@ int axs_patches_rk4_step(const axs_patches *p, const axs_patch_plan *plan, const
 int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse_old,
                      const axs_level *coarse_new, double theta, double coarse_dt, int32_t valid_too, void *stream)
 {
+    return axs_patches_fill_list(p, m, coarse_old, coarse_new, theta, coarse_dt, valid_too, nullptr,
+                                 p != nullptr ? p->npatches : 0, stream);
+}
+
+int axs_patches_fill_list(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse_old,
+                          const axs_level *coarse_new, double theta, double coarse_dt, int32_t valid_too,
+                          const int32_t *patch_list, int32_t count, void *stream)
+{
     PatchGeom g;
     int rc = validate_patches(p, g);
     if (rc) return rc;
@@ -908,9 +938,13 @@ int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_lev
     f.theta = theta;
     f.hdt = coarse_dt;
     f.valid_too = valid_too != 0;
+    AXS_REQUIRE(count >= 0 && (patch_list != nullptr || count == p->npatches), AXS_ERR_INVALID_ARGUMENT,
+                "a patch count without a list must be npatches");
+    f.patch_list = patch_list;
     fill_time_weights(f);
     const QuarticWeights q = quartic_weights();
-    const int64_t blocks = (int64_t)fill_tiles_x(g.n) * fill_tiles_y(g.n) * p->npatches;
+    if (count == 0) return AXS_OK;
+    const int64_t blocks = (int64_t)fill_tiles_x(g.n) * fill_tiles_y(g.n) * count;
     AXS_REQUIRE(blocks < (int64_t)INT32_MAX, AXS_ERR_UNSUPPORTED, "too many patches for one fill launch");
     cudaStream_t st = (cudaStream_t)stream;
     if (p->dtype == AXS_F32)
@@ -918,6 +952,31 @@ int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_lev
     else
         patch_fill_kernel<double><<<(unsigned)blocks, kFillThreads, 0, st>>>(static_cast<double *>(p->state), cv, f, q);
     return launch_status("patch fill");
+}
+
+int axs_patches_copy_boxes(const axs_patches *dst, const axs_patches *src, const int32_t *src_of_dst, void *stream)
+{
+    PatchGeom g;
+    int rc = validate_patches(dst, g);
+    if (rc) return rc;
+    AXS_REQUIRE(src_of_dst != nullptr, AXS_ERR_INVALID_ARGUMENT, "null patch index");
+    int64_t src_plane = 0;
+    if (src != nullptr) {
+        PatchGeom gs;
+        if ((rc = validate_patches(src, gs))) return rc;
+        AXS_REQUIRE(src->dtype == dst->dtype && src->n == dst->n, AXS_ERR_INVALID_ARGUMENT,
+                    "patches of another size or precision");
+        src_plane = gs.plane;
+    }
+    const int64_t es = (int64_t)dtype_size(dst->dtype);
+    AXS_REQUIRE(g.box * es % 16 == 0 && g.plane * es % 16 == 0, AXS_ERR_UNSUPPORTED, "patch boxes of 16-byte words");
+    const int units = (int)(g.box * es / 16);
+    const unsigned gx = (unsigned)std::min<int64_t>((4 * (int64_t)units + 1023) / 1024, 64);
+    const dim3 grid(gx, (unsigned)std::min(dst->npatches, 65535));
+    patch_copy_boxes_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
+        static_cast<uint4 *>(dst->state), src ? static_cast<const uint4 *>(src->state) : nullptr, src_of_dst,
+        dst->npatches, src ? src->npatches : 0, units, g.plane * es / 16, src_plane * es / 16);
+    return launch_status("patch box copy");
 }
 
 int axs_patches_average_down(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse, void *stream)

@@ -379,6 +379,15 @@ int axs_patches_init(const axs_patches *p, axs_patch_plan *plan, void *stream);
  * when theta = 0). */
 int axs_patches_fill(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse_old,
                      const axs_level *coarse_new, double theta, double coarse_dt, int32_t valid_too, void *stream);
+/* The same for the `count` patches listed in patch_list (device int32 indices;
+ * entries outside [0, npatches) are skipped); NULL with count = npatches: all. */
+int axs_patches_fill_list(const axs_patches *p, const axs_patch_map *m, const axs_level *coarse_old,
+                          const axs_level *coarse_new, double theta, double coarse_dt, int32_t valid_too,
+                          const int32_t *patch_list, int32_t count, void *stream);
+/* Regrid helper: every patch box of dst (4 components, rings and padding
+ * included) becomes box src_of_dst[q] of src (device int32 per dst patch), or
+ * zeros where that is -1 (src may then be NULL). Same patch side and dtype. */
+int axs_patches_copy_boxes(const axs_patches *dst, const axs_patches *src, const int32_t *src_of_dst, void *stream);
 /* One RK4 step of every patch (two persistent launches); the rings must hold
  * psi, Pi at time t. */
 int axs_patches_rk4_step(const axs_patches *p, const axs_patch_plan *plan, const axs_background *bg, double tau_i,
