@@ -164,7 +164,9 @@ class TwoLevel:
             need = 4 * lay.plane_elems
             if self._spare is None or self._spare.numel() < need:
                 self._spare = None  # too small: free it before the new allocation
-                self._spare = torch.empty(int(need * self.headroom) + 1, dtype=dt, device=dev)
+                # cleared once here: a regrid's first writes into freshly mapped memory
+                # would otherwise pay for the mapping
+                self._spare = torch.zeros(int(need * self.headroom) + 1, dtype=dt, device=dev)
             storage = self._spare
         # every box is written below: copied from the old patch of its block, or
         # cleared and interpolated from the coarse level
@@ -190,7 +192,7 @@ class TwoLevel:
         if self.spare_arena:
             # the old arena is the next regrid's; the first patch set gets a second one
             self._spare = old_patches.storage if old_patches is not None else \
-                torch.empty_like(self.patches.storage)
+                torch.zeros_like(self.patches.storage)
 
     def regrid(self, n_error_buf: int = 4, gradient_threshold: float = 1.7976931348623157e308,
                radial_gradient_threshold: float = 1.7976931348623157e308) -> int:

@@ -8,8 +8,10 @@
 // Patch layout: valid fine cell (0,0,0) sits at padded position (8, 4, 4);
 // every patch holds a ghost ring of 6 columns in x and 4 rows / planes in y
 // and z (plus 2 columns of slack on either side for the TMA boxes), rows are
-// padded to 128 bytes, and the patches are stacked along each component plane
-// as an ensemble's boxes are.
+// padded to whole 32-byte sectors (n + 16 columns: every TMA box and the work
+// arena's sweep A domain fit, and strides stay 16-byte multiples), boxes start
+// on 128-byte lines, and the patches are stacked along each component plane as
+// an ensemble's boxes are.
 //
 // One fine RK4 step of every patch is the two fused sweeps with explicit
 // ghost rings instead of periodic wrap: sweep A runs over the valid cells
@@ -61,11 +63,13 @@ static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g)
     AXS_REQUIRE(dtype == AXS_F32 || dtype == AXS_F64, AXS_ERR_INVALID_ARGUMENT, "bad dtype %d", dtype);
     AXS_REQUIRE(n >= 8 && n % 8 == 0 && n <= 256, AXS_ERR_UNSUPPORTED, "patch side %d must be a multiple of 8 in [8, 256]",
                 n);
-    AXS_REQUIRE(npatches > 0 && npatches < (1 << (32 - kEnsItemBits)) / 2, AXS_ERR_INVALID_ARGUMENT,
-                "patch count %d out of range", npatches);
-    const int64_t line = 128 / (int64_t)dtype_size(dtype);
+    // the fused step launches one grid z slice per patch; the two-sweep step's
+    // work items carry 2 * npatches box numbers in 16 bits (checked where it is used)
+    AXS_REQUIRE(npatches > 0 && npatches <= 65535, AXS_ERR_INVALID_ARGUMENT, "patch count %d out of range",
+                npatches);
+    const int64_t line = 128 / (int64_t)dtype_size(dtype), sector = 32 / (int64_t)dtype_size(dtype);
     g.n = n;
-    g.js = (kPatchOX + n + kRingX + 2 + line - 1) / line * line;
+    g.js = (kPatchOX + n + kRingX + 2 + sector - 1) / sector * sector;  // n + 16 (n is a multiple of 8)
     g.ks = g.js * (n + 2 * kPatchRY);
     g.box = (g.ks * (n + 2 * kPatchRZ) + line - 1) / line * line;
     g.plane = g.box * npatches;
@@ -347,7 +351,11 @@ template <typename T> static int build_patch_table(const axs_patches *p, const P
         fill(desc[q], q, -4, -2, n + 8, n + 4, PT::TXA, PT::TYA, zc_a);
         fill(desc[np + q], q, 0, 0, n, n, PT::TXB, PT::TYB, zc_b);
     }
-    for (int q = 0; q < np; ++q) {
+    // work items of the two-sweep step (the fused step needs none)
+    const bool fused = patches_fused(p->dtype, n, np);
+    AXS_REQUIRE(fused || 2 * np < (1 << (32 - kEnsItemBits)), AXS_ERR_UNSUPPORTED,
+                "%d patches of side %d: the two-sweep step takes fewer than %d", np, n, (1 << (32 - kEnsItemBits)) / 2);
+    for (int q = 0; q < np && !fused; ++q) {
         const EnsBoxDesc &da = desc[q], &db = desc[np + q];
         const int64_t na = (int64_t)da.ntiles * ((da.nz + da.zchunk - 1) / da.zchunk);
         const int64_t nb = (int64_t)db.ntiles * ((db.nz + db.zchunk - 1) / db.zchunk);
@@ -358,7 +366,6 @@ template <typename T> static int build_patch_table(const axs_patches *p, const P
                  items_off = desc_off + sizeof(EnsBoxDesc) * 2 * np;
     std::vector<unsigned char> img(items_off + 4 * (items_a.size() + items_b.size()), 0);
     const int64_t es = (int64_t)dtype_size(p->dtype);
-    const bool fused = patches_fused(p->dtype, n, np);
     for (int q = 0; q < np; ++q) {
         auto *maps = reinterpret_cast<CUtensorMap *>(img.data() + maps_off) + 2 * q;
         const char *sb = static_cast<const char *>(p->state) + (int64_t)q * g.box * es;
@@ -907,8 +914,9 @@ int axs_patches_rk4_step(const axs_patches *p, const axs_patch_plan *plan, const
     PatchGeom g;
     int rc = validate_patches(p, g);
     if (rc) return rc;
-    AXS_REQUIRE(plan != nullptr && bg != nullptr && plan->items_a > 0 && plan->items_b > 0, AXS_ERR_INVALID_ARGUMENT,
-                "null or empty plan (run axs_patches_init)");
+    AXS_REQUIRE(plan != nullptr && bg != nullptr, AXS_ERR_INVALID_ARGUMENT, "null plan or background");
+    AXS_REQUIRE(patches_fused(p->dtype, g.n, p->npatches) || (plan->items_a > 0 && plan->items_b > 0),
+                AXS_ERR_INVALID_ARGUMENT, "empty plan (run axs_patches_init)");
     AXS_REQUIRE(std::isfinite(dt) && dt > 0.0, AXS_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
     cudaStream_t st = (cudaStream_t)stream;
     return p->dtype == AXS_F32 ? patch_step<float>(p, g, *plan, *bg, tau_i, t, dt, st)

@@ -199,9 +199,17 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
 #pragma unroll
     for (int s = 0; s < 14; ++s) e[s] = 0.0;
     // per_cell_fp32: one work item's cells are summed in float, then added to e
-    float ef[FAST ? 14 : 1];
+    // with compensation (Neumaier) for the 13 real-valued sums; the cell count is exact
+    float ef[FAST ? 14 : 1], ec[FAST ? 13 : 1];
 #pragma unroll
     for (int s = 0; s < (FAST ? 14 : 1); ++s) ef[s] = 0.f;
+#pragma unroll
+    for (int s = 0; s < (FAST ? 13 : 1); ++s) ec[s] = 0.f;
+    auto csum = [](float &sum, float &comp, float x) {
+        const float t = sum + x;
+        comp += fabsf(sum) >= fabsf(x) ? (sum - t) + x : (x - t) + sum;
+        sum = t;
+    };
     const CellConst<double> kd{q.R2, q.inv_R, q.inv_R2, q.inv_R4, q.lambda, q.RpR, q.threshold};
     const CellConst<float> kf{q.f_R2, q.f_inv_R, q.f_inv_R2, q.f_inv_R4, q.f_lambda, q.f_RpR, q.f_threshold};
     double vsum = 0.0;
@@ -393,10 +401,10 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                             cell_energy<float, T>(kf, q.scheme, p1, p2, q1, q2, g, term, wgt);
 #pragma unroll
                             for (int k = 0; k < 6; ++k) {
-                                ef[2 * k] += term[k];
-                                ef[2 * k + 1] += term[k] * wgt;
+                                csum(ef[2 * k], ec[2 * k], term[k]);
+                                csum(ef[2 * k + 1], ec[2 * k + 1], term[k] * wgt);
                             }
-                            ef[12] += wgt;
+                            csum(ef[12], ec[12], wgt);
                             ef[13] += 1.f;
                             done = true;
                         }
@@ -498,8 +506,9 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
         if constexpr (FAST) {
 #pragma unroll
             for (int k = 0; k < 14; ++k) {
-                e[k] += (double)ef[k];
+                e[k] += (double)ef[k] + (k < 13 ? (double)ec[k < 13 ? k : 0] : 0.0);
                 ef[k] = 0.f;
+                if (k < 13) ec[k] = 0.f;
             }
         }
     }

@@ -695,6 +695,18 @@ def run_native(args):
     scale = None
     if not args.no_scale:
         scale = scale_report(A, dev, hbm_peak, n=args.scale_n, steps=args.scale_steps, kdiv=args.scale_kdiv)
+    # the same at the survey's scale configuration: a 1024^3 base and 100 coarse steps.
+    # IC |n| < N/112 tags ~2.5 % of the cells. At N/96 (3.2 %) the patch count grew to
+    # 65 177 during the run, at the fused step's limit of 65 535 patches (one grid z
+    # slice each), and its two arenas filled most of the memory next to the base level.
+    scale_1024 = None
+    if not args.no_scale_1024:
+        try:
+            scale_1024 = scale_report(A, dev, hbm_peak, n=1024, steps=args.scale1024_steps,
+                                      kdiv=args.scale1024_kdiv)
+        except (A._lib.AxsError, torch.OutOfMemoryError) as e:
+            scale_1024 = {"unavailable": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
 
     # ---------------- end to end through the C ABI with host buffers: every step copies its input
     # state in from pinned host memory and its result back out; the copies of neighbouring steps
@@ -758,7 +770,8 @@ def run_native(args):
                 "autotune_ms_per_step": tune32, "diagnostics": diag, "fp64": fp64,
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision,
                 "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None,
-                "differentiation": differentiation, "batching": batching, "scale": scale}
+                "differentiation": differentiation, "batching": batching, "scale": scale,
+                "scale_1024": scale_1024}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -787,6 +800,9 @@ def main():
     ap.add_argument("--scale-n", type=int, default=512)
     ap.add_argument("--scale-steps", type=int, default=20)
     ap.add_argument("--scale-kdiv", type=int, default=64)
+    ap.add_argument("--no-scale-1024", action="store_true")
+    ap.add_argument("--scale1024-steps", type=int, default=100)
+    ap.add_argument("--scale1024-kdiv", type=int, default=112)
     ap.add_argument("--diff-n", type=int, default=128)
     ap.add_argument("--diff-steps", type=int, default=200)
     ap.add_argument("--diff-directions", type=int, default=16)
