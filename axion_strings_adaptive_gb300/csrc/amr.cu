@@ -148,14 +148,22 @@ template <typename T> struct Fused {
     // NSW / NGP: S3, S4 and G, P slots, one more than sweep B reads, so sweep A of
     // the next plane never overwrites what a slower thread's sweep B still reads
     static constexpr int V = sizeof(T) == 4 ? 2 : 1;
-    static constexpr int TX = 32, TY = sizeof(T) == 4 ? 16 : 8, NS = sizeof(T) == 4 ? 6 : 5, THREADS = 256;
+    static constexpr int TX = 32, TY = sizeof(T) == 4 ? 16 : 8, NS = sizeof(T) == 4 ? 6 : 5;
     static constexpr int NSW = 6, NGP = 4;
     static constexpr int BX = TX + 8, BY = TY + 8;  // TMA box: the A region plus its stencil halo
     static constexpr int AX = TX + 4, AY = TY + 4;  // A region
     static constexpr int RING = 4 * BX * BY, SWIN = 4 * AX * AY, GPW = 4 * TX * TY;
     static constexpr int NA = AX * AY / V;          // sweep A units (V sites each)
+    static_assert(AX / V > 32 / V, "the A region is wider than one bank row");
     static constexpr size_t SMEM = sizeof(T) * ((size_t)NS * RING + NSW * (size_t)SWIN + NGP * (size_t)GPW);
-    static_assert(TX * TY / V == THREADS, "one sweep B unit per thread");
+    // 512 threads: sweep A's units run on threads 0 .., sweep B's (one per thread) on the
+    // last NB threads, so a plane's critical path is at most one A unit plus one B
+    // unit (256 threads: two A units plus one B). Running A and B side by side on
+    // separate threads, with B one plane further behind, saturated the shared-memory
+    // pipe and ran 10 % slower.
+    static constexpr int NB = TX * TY / V;  // sweep B units, one per thread of the last NB threads
+    static constexpr int THREADS = 512;
+    static_assert(NB <= THREADS, "one sweep B unit per thread");
     static_assert((BX * sizeof(T)) % 16 == 0 && (RING * sizeof(T)) % 128 == 0, "TMA box rows and slots");
     static_assert(SMEM <= 227 * 1024, "shared memory");
 };
@@ -196,7 +204,7 @@ struct FusedArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256, 1) patch_fused_kernel(T *__restrict__ st, const SweepArgs<T> a,
+__global__ void __launch_bounds__(Fused<T>::THREADS, 1) patch_fused_kernel(T *__restrict__ st, const SweepArgs<T> a,
                                                               const FusedArgs f)
 {
     using F = Fused<T>;
@@ -228,7 +236,9 @@ __global__ void __launch_bounds__(256, 1) patch_fused_kernel(T *__restrict__ st,
         for (int k = 0; k < F::NS && k < K; ++k) issue(k);
     int waited = 0;
     bool ok = true;
-    const int bxl = V * (tid % (F::TX / V)), byl = tid / (F::TX / V);  // this thread's sweep B sites (tile-local)
+    const int bt = tid - (F::THREADS - F::NB);  // sweep B unit of this thread (< 0: none)
+    const bool has_b = bt >= 0;
+    const int bxl = has_b ? V * (bt % (F::TX / V)) : 0, byl = has_b ? bt / (F::TX / V) : 0;  // tile-local sites
     T *const dst0 = st + (int64_t)q * f.box + (kPatchOX + x0 + bxl) + (int64_t)(kPatchRY + y0 + byl) * f.js;
     // iteration i: sweep A at plane za = i - 2 (reads planes k = i .. i + 4), sweep B at zb = za - 2
     for (int i = 0; i < n + 4; ++i) {
@@ -246,7 +256,13 @@ __global__ void __launch_bounds__(256, 1) patch_fused_kernel(T *__restrict__ st,
             T *sz = swin + (size_t)(i % F::NSW) * F::SWIN;  // S3, S4 of plane za
             T *gz = gpw + (size_t)(i % F::NGP) * F::GPW;    // G, P of plane za
             for (int u = tid; u < F::NA; u += F::THREADS) {
-                const int lx = 2 + V * (u % (F::AX / V)), ly = 2 + u / (F::AX / V);  // box-local first site
+                // units of the A region's first 32 / V columns row by row (a warp covers
+                // whole 128-byte bank rows, so its shared-memory accesses are conflict-free),
+                // then the remaining columns
+                constexpr int PR = F::AX / V, MAIN = 32 / V, EDGE = PR - MAIN;
+                const int row = u < MAIN * F::AY ? u / MAIN : (u - MAIN * F::AY) / EDGE;
+                const int col = u < MAIN * F::AY ? u % MAIN : MAIN + (u - MAIN * F::AY) % EDGE;
+                const int lx = 2 + V * col, ly = 2 + row;  // box-local first site
                 T lap[4][V], ctr[4][V];
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
@@ -275,7 +291,7 @@ __global__ void __launch_bounds__(256, 1) patch_fused_kernel(T *__restrict__ st,
         cluster_arrive();
         const int zb = i - 4;
         T o[4][V];
-        if (ok && zb >= 0) {
+        if (ok && zb >= 0 && has_b) {
             const T *sp[5];
 #pragma unroll
             for (int d = 0; d < 5; ++d) sp[d] = swin + (size_t)((zb + d) % F::NSW) * F::SWIN;  // planes zb-2 .. zb+2
@@ -292,7 +308,7 @@ __global__ void __launch_bounds__(256, 1) patch_fused_kernel(T *__restrict__ st,
         }
         // every tile of the patch is done with sweep A at za: plane zb = za - 2 may be overwritten
         cluster_wait();
-        if (ok && zb >= 0) {
+        if (ok && zb >= 0 && has_b) {
             T *dst = dst0 + (int64_t)(kPatchRZ + zb) * f.ks;
 #pragma unroll
             for (int c = 0; c < 4; ++c) stv<T, V>(dst + c * f.plane, o[c]);
