@@ -353,6 +353,7 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
     import torch
     from axion_strings_adaptive_gb300 import ic
     from axion_strings_adaptive_gb300.amr import TwoLevel
+    torch.cuda.empty_cache()  # earlier legs' cached blocks: the patch arenas want large free ranges
     bg = A.Background.expanding(A_INV, 0.0, lambda0=LAMBDA0)
     coarse = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev, pierced_capacity=1)
     coarse.set_state(ic.fourier_state(n, ic.strict_cutoff(n / kdiv), seed=SEED + 11, dtype=torch.float64,
