@@ -314,3 +314,33 @@ def test_regrid_keeps_the_fine_data_of_blocks_that_stay_refined(axs):
             assert bool((v == marks[tuple(b)]).all()), tuple(b)
         else:  # interpolated from the coarse level
             assert not bool((v == 7.0).any()) and float(v.abs().max()) > 0.0
+
+
+def test_patch_counts_past_the_two_sweep_limit(axs):
+    """33 000 patches: past the two-sweep step's 32 767 (its work items carry box
+    numbers in 16 bits), inside the fused step's 65 535. A homogeneous radiation-era
+    solution (psi = R = tau, Pi = R' = 1) survives a subcycled coarse step in every
+    patch, the last ones included."""
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    nx, ny, nz, block = 1024, 512, 512, 16
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)  # RD: R = tau, R' = 1, kappa = 0
+    coarse = axs.PeriodicLevel((nx, ny, nz), 0.5, dtype=torch.float32, pierced_capacity=1)
+    st = torch.zeros((4, nz, ny, nx), dtype=torch.float32, device="cuda")
+    st[0], st[2] = 1.0, 1.0
+    coarse.set_state(st)
+    del st
+    two = TwoLevel(coarse, block, spare_arena=False)
+    nbx, nby = nx // block, ny // block
+    q = np.arange(33000)
+    two.set_blocks(np.stack([q % nbx, (q // nbx) % nby, q // (nbx * nby)], axis=1))
+    assert two.patches.npatches == 33000 and two.patches.layout.work_bytes == 0
+    two.advance(bg, 1.0, 0.0, 0.1, 1)
+    two.device_status()
+    p, n = two.patches, two.patches.n
+    lay = p.layout
+    boxes = p.state.view(4, p.npatches, n + 8, n + 8, lay.jstride)
+    valid = boxes[:, :, lay.z_offset:lay.z_offset + n, lay.y_offset:lay.y_offset + n,
+                  lay.x_offset:lay.x_offset + n]
+    assert float((valid[0] - 1.1).abs().max()) < 2e-6
+    assert float((valid[2] - 1.0).abs().max()) < 2e-6
+    assert float(valid[1].abs().max()) < 1e-6 and float(valid[3].abs().max()) < 1e-6
