@@ -585,7 +585,23 @@ struct FinderSmem {
     unsigned char ok[4][FVY][FVX];   // the vertex lies inside float range
     unsigned char inp[4][FVY][FVX];  // x edge code (bits 0-2), y edge code (bits 3-5)
     unsigned char zc[4][FVY][FVX];   // z edge code to the plane above (bits 0-2)
+    float gv[4][FVY][FVX];           // gamma^2 v^2 of the vertex (velocity mode)
 };
+
+// gamma^2 v^2 at a vertex (Velocity.hpp:62-78 with the prefactors folded on the
+// host) in single precision, with every operation rounded as written so that the
+// plane pass and the after-chunk path agree to the bit
+__device__ __forceinline__ float vertex_gv(float psi1, float psi2, float Pi1, float Pi2, const DiagConst &q)
+{
+    const float phi1 = __fmul_rn(psi1, q.f_inv_R), phi2 = __fmul_rn(psi2, q.f_inv_R);
+    const float pd1 = __fmul_rn(__fsub_rn(Pi1, __fmul_rn(q.f_RpR, psi1)), q.f_inv_R2);
+    const float pd2 = __fmul_rn(__fsub_rn(Pi2, __fmul_rn(q.f_RpR, psi2)), q.f_inv_R2);
+    const float phi_sq = __fadd_rn(__fmul_rn(phi1, phi1), __fmul_rn(phi2, phi2));
+    const float pd_sq = __fadd_rn(__fmul_rn(pd1, pd1), __fmul_rn(pd2, pd2));
+    const float re = __fadd_rn(__fmul_rn(phi1, pd1), __fmul_rn(phi2, pd2));
+    return __fsub_rn(__fmul_rn(__fmul_rn(pd_sq, q.f_vel_a), __fsub_rn(1.f, __fmul_rn(q.f_vel_b, phi_sq))),
+                     __fmul_rn(__fmul_rn(q.f_vel_c, re), re));
+}
 
 struct CellWindings {
     int w[3], ties;
@@ -653,25 +669,37 @@ __device__ __noinline__ bool finder_cell_bad(const DiagView v, const T *base, in
     return (bad & 4u) != 0;
 }
 
-template <typename T>
-#ifndef AXS_FINDER_MIN_BLOCKS
-#define AXS_FINDER_MIN_BLOCKS 4
-#endif
-__global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_BLOCKS : 3)
-    finder_kernel(const DiagView v, const uint8_t *__restrict__ mask, DiagPartial *__restrict__ partials,
-                  unsigned long long *__restrict__ list_counter, long long *__restrict__ list, long long capacity,
-                  int tiles_x, int ntiles, int zchunk, long long n_items, long long items_per_box,
-                  int64_t box_stride, uint8_t *__restrict__ tags)
+// VEL (FP32 fields, beside energy32_kernel): also Pi at the vertices, gamma^2 v^2
+// per vertex and its sum over the corners of every pierced plaquette. Blocks from
+// e_from on clear their partial record's energy sums (energy32_kernel writes those
+// of the blocks below it).
+template <typename T, bool VEL>
+__global__ void __launch_bounds__(kDiagThreads, (sizeof(T) == 4 && !VEL) ? 4 : 3)
+    finder_kernel(const DiagView v, const DiagConst q, const uint8_t *__restrict__ mask,
+                  DiagPartial *__restrict__ partials, unsigned long long *__restrict__ list_counter,
+                  long long *__restrict__ list, long long capacity, int tiles_x, int ntiles, int zchunk,
+                  long long n_items, long long items_per_box, int64_t box_stride, uint8_t *__restrict__ tags,
+                  int e_from)
 {
     extern __shared__ __align__(16) unsigned char finder_smem_raw[];
     FinderSmem &sm = *reinterpret_cast<FinderSmem *>(finder_smem_raw);
     __shared__ int lcount, flush_n, badn, bad_over;
     __shared__ unsigned long long flush_base;
-    __shared__ long long red[kDiagThreads / 32][3];
+    __shared__ long long red[kDiagThreads / 32][4];
     const int tid = threadIdx.x, lane = tid & 31;
     const int lx = tid % FTX, ly = tid / FTX;  // cells (lx, ly) and (lx, ly + FTY / 2)
     const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
     int cnt_p = 0, cnt_w = 0, cnt_tie = 0;  // per-thread counts fit 32 bits
+    // velocity mode: corner sums in FP32, a chunk's running sum compensated (Neumaier),
+    // FP64 across chunks (GB300 issues FP64 at 1/64 of the FP32 rate)
+    int cnt_v = 0;
+    double vsum = 0.0;
+    float vacc = 0.f, vcomp = 0.f;
+    auto vadd = [&](float x) {
+        const float t = vacc + x;
+        vcomp += fabsf(vacc) >= fabsf(x) ? (vacc - t) + x : (x - t) + vacc;
+        vacc = t;
+    };
     if (tid == 0) lcount = badn = bad_over = 0;
     int warp_end = 0;  // end of this warp's last append to lbuf (lane-uniform)
     auto flush = [&]() {
@@ -696,6 +724,26 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
         const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
         cnt_tie += cw.ties;
         if (tags != nullptr) tags[cell] = (cw.w[0] | cw.w[1] | cw.w[2]) != 0;
+        if constexpr (VEL) {
+            if (cw.w[0] | cw.w[1] | cw.w[2]) {
+                // gamma^2 v^2 at the corners, from global memory (zero outside the ghost region)
+                auto gvat = [&](int dx_, int dy_, int dz_) -> float {
+                    const int xx = x + dx_, yy = y + dy_, zz = z + dz_;
+                    const bool on =
+                        (v.wx || xx < v.nx + v.ox) && (v.wy || yy < v.ny + v.oy) && (v.wz || zz < v.nz + v.oz);
+                    float c4[4];
+                    for (int c = 0; c < 4; ++c) c4[c] = on ? (float)base[view_off<T>(v, c, xx, yy, zz)] : 0.f;
+                    return vertex_gv(c4[0], c4[1], c4[2], c4[3], q);
+                };
+                const float g000 = gvat(0, 0, 0), g100 = gvat(1, 0, 0), g110 = gvat(1, 1, 0), g010 = gvat(0, 1, 0);
+                const float g001 = gvat(0, 0, 1), g101 = gvat(1, 0, 1), g011 = gvat(0, 1, 1);
+                float s_ = 0.f;
+                if (cw.w[0]) { s_ += g000 + g100 + g110 + g010; cnt_v += 4; }
+                if (cw.w[1]) { s_ += g000 + g010 + g011 + g001; cnt_v += 4; }
+                if (cw.w[2]) { s_ += g000 + g001 + g101 + g100; cnt_v += 4; }
+                vadd(s_);
+            }
+        }
 #pragma unroll
         for (int pl = 0; pl < 3; ++pl) {
             if (!cw.w[pl]) continue;
@@ -734,14 +782,15 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
         }
         // psi of vertex planes za, za + 1, ... in order, into registers
         int lz = za, lzw = wrap_or_self(za, v.nz, v.wz);
-        auto load_plane = [&](T(&buf)[3][2]) {
+        constexpr int NC = VEL ? 4 : 2;  // psi (and Pi) at the vertices
+        auto load_plane = [&](T(&buf)[3][NC]) {
             const bool zin = v.wz || lz < v.nz + v.oz;
             const T *pb = base + (int64_t)(lzw + v.oz) * v.ks;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const bool on = zin && voff[k] >= 0;
-                buf[k][0] = on ? __ldg(pb + voff[k]) : T(0);
-                buf[k][1] = on ? __ldg(pb + voff[k] + v.cs) : T(0);
+#pragma unroll
+                for (int c = 0; c < NC; ++c) buf[k][c] = on ? __ldg(pb + voff[k] + c * v.cs) : T(0);
             }
             ++lz;
             lzw = v.wz ? (lzw + 1 == v.nz ? 0 : lzw + 1) : lzw + 1;
@@ -763,7 +812,7 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
             }
         };
         // A: phases of vertex plane za + j and the z edges from plane za + j - 1
-        auto stage_a = [&](int j, const T(&buf)[3][2]) {
+        auto stage_a = [&](int j, const T(&buf)[3][NC]) {
             const int s = j & 3, sp = (j - 1) & 3;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -780,6 +829,7 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
                 const float th = atan2f((float)b, (float)a);
                 sm.th[s][vj[k]][vi[k]] = th;
                 sm.ok[s][vj[k]][vi[k]] = ok;
+                if constexpr (VEL) sm.gv[s][vj[k]][vi[k]] = vertex_gv((float)a, (float)b, (float)buf[k][2], (float)buf[k][3], q);
                 if (j > 0) sm.zc[sp][vj[k]][vi[k]] = (unsigned char)edge_code(thp[k], th, okp[k] && ok);
                 thp[k] = th;
                 okp[k] = ok;
@@ -820,6 +870,20 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
                 const unsigned cm = (wxy != 0) | (wyz != 0) << 1 | (wzx != 0) << 2;
                 // StringTagger.hpp:117-151: a cell is tagged when a plaquette at its low corner is pierced
                 if (tags != nullptr) tags[cell] = cm != 0;
+                if constexpr (VEL) {
+                    // VelocityKernel.hpp:37-141: gamma^2 v^2 of the 4 corners of every pierced plaquette
+                    if (cm) {
+                        const float g000 = sm.gv[s0][cy][lx], g100 = sm.gv[s0][cy][lx + 1];
+                        const float g110 = sm.gv[s0][cy + 1][lx + 1], g010 = sm.gv[s0][cy + 1][lx];
+                        const float g001 = sm.gv[s1][cy][lx], g101 = sm.gv[s1][cy][lx + 1];
+                        const float g011 = sm.gv[s1][cy + 1][lx];
+                        float s_ = 0.f;
+                        if (wxy) { s_ += g000 + g100 + g110 + g010; cnt_v += 4; }
+                        if (wyz) { s_ += g000 + g010 + g011 + g001; cnt_v += 4; }
+                        if (wzx) { s_ += g000 + g001 + g101 + g100; cnt_v += 4; }
+                        vadd(s_);
+                    }
+                }
                 cnt_w += abs(wxy) + abs(wyz) + abs(wzx);
                 pm |= cm << (3 * h);
             }
@@ -852,7 +916,7 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
         // plane za + j + 2 into the registers A just read), C (cells of plane
         // za + j - 3); the loop is unrolled by two so each register buffer has
         // a fixed name
-        auto step = [&](int j, T(&buf)[3][2]) {
+        auto step = [&](int j, T(&buf)[3][NC]) {
             // the plane's one barrier; the block also learns whether the pierced
             // buffer could overflow during this plane
             if (__syncthreads_or(warp_end > kFinderFlushAt)) flush();
@@ -863,7 +927,7 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
             }
             if (j >= 3) stage_c(j);
         };
-        T bufa[3][2], bufb[3][2];
+        T bufa[3][NC], bufb[3][NC];
         load_plane(bufa);  // vertex plane za
         load_plane(bufb);  // za + 1 (len >= 1)
         for (int j = 0; j < len + 3; j += 2) {
@@ -891,27 +955,302 @@ __global__ void __launch_bounds__(kDiagThreads, sizeof(T) == 4 ? AXS_FINDER_MIN_
         }
         __syncthreads();
         if (tid == 0) badn = bad_over = 0;  // published by the next chunk's first barrier
+        if constexpr (VEL) {
+            vsum += (double)vacc + (double)vcomp;
+            vacc = vcomp = 0.f;
+        }
     }
     if (list != nullptr && __syncthreads_or(warp_end > 0)) flush();
 
     // ---- block reduction (fixed order) into the fused pass's partial record ----
-    long long c3[3] = {cnt_p, cnt_w, cnt_tie};
+    __shared__ double redv[kDiagThreads / 32];
+    long long c4[4] = {cnt_p, cnt_w, VEL ? cnt_v : 0, cnt_tie};
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
-        for (int o = 16; o > 0; o >>= 1) c3[s] += __shfl_down_sync(0xffffffffu, c3[s], o);
-        if (lane == 0) red[tid >> 5][s] = c3[s];
+    for (int s = 0; s < 4; ++s) {
+        for (int o = 16; o > 0; o >>= 1) c4[s] += __shfl_down_sync(0xffffffffu, c4[s], o);
+        if (lane == 0) red[tid >> 5][s] = c4[s];
     }
+    if constexpr (VEL)
+        for (int o = 16; o > 0; o >>= 1) vsum += __shfl_down_sync(0xffffffffu, vsum, o);
+    if (lane == 0) redv[tid >> 5] = VEL ? vsum : 0.0;
     __syncthreads();
-    if (tid < 14)
-        partials[blockIdx.x].e[tid] = 0.0;
-    else if (tid == 14)
-        partials[blockIdx.x].vsum = 0.0;
-    else if (tid >= 32 && tid < 36) {
+    if (tid < 14) {
+        if ((int)blockIdx.x >= e_from) partials[blockIdx.x].e[tid] = 0.0;
+    } else if (tid == 14) {
+        double xv = 0.0;
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += redv[ww];
+        partials[blockIdx.x].vsum = xv;
+    } else if (tid >= 32 && tid < 36) {
         const int f = tid - 32;  // n_p_plain, n_p_weighted, vel_count, near_tie
         long long xv = 0;
-        if (f != 2)
-            for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red[ww][f == 3 ? 2 : f];
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red[ww][f];
         partials[blockIdx.x].cnt[f] = xv;
+    }
+}
+
+// ---------------------------------------------------------------- FP32 per-cell energy sums
+// The per_cell_fp32 energy sums on FP32 fields, run beside finder_kernel<float, VEL>
+// (windings, the pierced list and the velocity), each kernel with few registers.
+// A block owns a FTX x FTY tile, two cells per thread, and marches in z. psi of the
+// tile plus a 2-cell halo arrives by cp.async in a ring of seven planes (the
+// gradient stencil's five plus two, so one block barrier per plane suffices), Pi
+// of the tile in a ring of three. Per plane each warp adds up its cells' 13 terms
+// in FP32 with a butterfly over the lanes, and lane k adds sum k to a compensated
+// (Neumaier) FP32 accumulator, lane 13 the cell count. After each z-chunk the
+// accumulators go to per-warp FP64 slots. Cells where FP32 cannot hold 1/|psi|^4
+// (|psi|^2 outside (1e-15, 1e15): the cores' exact zeros) are queued and take the
+// reference's double arithmetic after the chunk, as the fused pass does.
+constexpr int EHX = FTX + 4, EHY = FTY + 4, kEnergySlots = 7, kEnergyPiSlots = 3, kEnergyBadQ = 1024;
+constexpr int kEnergyPts = 2 * EHX * EHY, kEnergyPer = (kEnergyPts + kDiagThreads - 1) / kDiagThreads;
+constexpr int kEnergyPiPts = 2 * FTX * FTY, kEnergyPiPer = kEnergyPiPts / kDiagThreads;
+static_assert(kEnergyPiPts % kDiagThreads == 0, "Pi loads per thread");
+struct EnergySmem {
+    double ew[kDiagThreads / 32][14];
+    float ps[kEnergySlots][2][EHY][EHX];
+    float pi[kEnergyPiSlots][2][FTY][FTX];
+    int badq[kEnergyBadQ];  // tile-local x | y << 5 | (z - za) << 9
+};
+
+struct CellTerms {
+    double t[14];
+};
+
+// One cell's 14 terms in the reference's double per-cell arithmetic, psi and Pi
+// read from global memory (zero outside the view's ghost region).
+__device__ __noinline__ CellTerms energy_cell_double(const DiagView v, const DiagConst q, const float *base, int x,
+                                                     int y, int z)
+{
+    auto at = [&](int c, int xx, int yy, int zz) -> double {
+        const bool on = (v.wx || (xx >= -v.ox && xx < v.nx + v.ox)) && (v.wy || (yy >= -v.oy && yy < v.ny + v.oy)) &&
+                        (v.wz || (zz >= -v.oz && zz < v.nz + v.oz));
+        return on ? (double)base[view_off<float>(v, c, xx, yy, zz)] : 0.0;
+    };
+    double g[2][3];
+    for (int c = 0; c < 2; ++c) {
+        g[c][0] = diff1_vals<float>(at(c, x - 2, y, z), at(c, x - 1, y, z), at(c, x + 1, y, z), at(c, x + 2, y, z),
+                                    q.one_over_dx);
+        g[c][1] = diff1_vals<float>(at(c, x, y - 2, z), at(c, x, y - 1, z), at(c, x, y + 1, z), at(c, x, y + 2, z),
+                                    q.one_over_dx);
+        g[c][2] = diff1_vals<float>(at(c, x, y, z - 2), at(c, x, y, z - 1), at(c, x, y, z + 1), at(c, x, y, z + 2),
+                                    q.one_over_dx);
+    }
+    const CellConst<double> kd{q.R2, q.inv_R, q.inv_R2, q.inv_R4, q.lambda, q.RpR, q.threshold};
+    double term[6], wgt;
+    cell_energy<double, float>(kd, q.scheme, at(0, x, y, z), at(1, x, y, z), at(2, x, y, z), at(3, x, y, z), g, term,
+                               wgt);
+    CellTerms r;
+    for (int k = 0; k < 6; ++k) {
+        r.t[2 * k] = term[k];
+        r.t[2 * k + 1] = term[k] * wgt;
+    }
+    r.t[12] = wgt;
+    r.t[13] = 1.0;
+    return r;
+}
+
+__global__ void __launch_bounds__(kDiagThreads, 3)
+    energy32_kernel(const DiagView v, const DiagConst q, const uint8_t *__restrict__ mask,
+                    DiagPartial *__restrict__ partials, int tiles_x, int ntiles, int zchunk, long long n_items,
+                    long long items_per_box, int64_t box_stride, int zero_counts)
+{
+    extern __shared__ __align__(16) unsigned char energy_smem_raw[];
+    EnergySmem &sm = *reinterpret_cast<EnergySmem *>(energy_smem_raw);
+    __shared__ int badn, bad_over;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lx = tid % FTX, ly = tid / FTX;  // cells (lx, ly) and (lx, ly + FTY / 2)
+    const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
+    const CellConst<float> kf{q.f_R2, q.f_inv_R, q.f_inv_R2, q.f_inv_R4, q.f_lambda, q.f_RpR, q.f_threshold};
+    for (int i = tid; i < (kDiagThreads / 32) * 14; i += kDiagThreads) sm.ew[i / 14][i % 14] = 0.0;
+    if (tid == 0) badn = bad_over = 0;
+    float acc = 0.f, comp = 0.f;  // lane k < 13: running sum k of the chunk; lane 13: its cell count
+
+    for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const long long qbox = item / items_per_box, box_item = item % items_per_box;
+        const float *__restrict__ base = static_cast<const float *>(v.data) + qbox * box_stride;
+        const int tile = (int)(box_item % ntiles), chunk = (int)(box_item / ntiles);
+        const int x0 = (tile % tiles_x) * FTX, y0 = (tile / tiles_x) * FTY;
+        const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
+
+        // load plans (in-plane offsets in 31 bits, checked on the host; -1: zero fill)
+        int poff[kEnergyPer];
+#pragma unroll
+        for (int u = 0; u < kEnergyPer; ++u) {
+            const int idx = tid + u * kDiagThreads, r = idx % (EHX * EHY);
+            const int xx = x0 - 2 + r % EHX, yy = y0 - 2 + r / EHX;
+            const bool on = idx < kEnergyPts && xx < v.nx + 2 && yy < v.ny + 2 &&
+                            (v.wx || (xx >= -v.ox && xx < v.nx + v.ox)) && (v.wy || (yy >= -v.oy && yy < v.ny + v.oy));
+            poff[u] = on ? (wrap_or_self(xx, v.nx, v.wx) + v.ox) + (wrap_or_self(yy, v.ny, v.wy) + v.oy) * (int)v.js
+                         : -1;
+        }
+        int qoff[kEnergyPiPer];
+#pragma unroll
+        for (int u = 0; u < kEnergyPiPer; ++u) {
+            const int idx = tid + u * kDiagThreads, r = idx % (FTX * FTY);
+            const int xx = x0 + r % FTX, yy = y0 + r / FTX;
+            qoff[u] = xx < v.nx && yy < v.ny ? (xx + v.ox) + (yy + v.oy) * (int)v.js : -1;
+        }
+        // psi planes za - 2 .. za + len + 1 (plane p in slot (p - za + 2) mod 7), Pi planes
+        // za .. za + len - 1 (slot (p - za) mod 3), each loaded in order
+        int lz = za - 2, lzw = wrap_or_self(za - 2, v.nz, v.wz);
+        auto load_psi_next = [&]() {
+            const bool zin = v.wz || (lz >= -v.oz && lz < v.nz + v.oz);
+            const float *pb = base + (int64_t)(lzw + v.oz) * v.ks;
+            float *dst = &sm.ps[(lz - za + 2) % kEnergySlots][0][0][0];
+#pragma unroll
+            for (int u = 0; u < kEnergyPer; ++u) {
+                const int idx = tid + u * kDiagThreads;
+                if (idx < kEnergyPts)
+                    cp_async_elem(dst + idx, pb + (idx >= EHX * EHY ? v.cs : 0) + poff[u], zin && poff[u] >= 0, base);
+            }
+            ++lz;
+            lzw = v.wz ? (lzw + 1 == v.nz ? 0 : lzw + 1) : lzw + 1;
+        };
+        int pz = za, pzw = wrap_or_self(za, v.nz, v.wz);
+        auto load_pi_next = [&]() {
+            const float *pb = base + (int64_t)(pzw + v.oz) * v.ks + 2 * v.cs;
+            float *dst = &sm.pi[(pz - za) % kEnergyPiSlots][0][0][0];
+#pragma unroll
+            for (int u = 0; u < kEnergyPiPer; ++u) {
+                const int idx = tid + u * kDiagThreads;
+                cp_async_elem(dst + idx, pb + (idx >= FTX * FTY ? v.cs : 0) + qoff[u], qoff[u] >= 0, base);
+            }
+            ++pz;
+            pzw = v.wz ? (pzw + 1 == v.nz ? 0 : pzw + 1) : pzw + 1;
+        };
+        for (int p = 0; p < 5; ++p) load_psi_next();  // za - 2 .. za + 2
+        load_pi_next();                               // za
+        cp_async_commit();
+
+        for (int m = 0; m < len; ++m) {
+            const int z = za + m;
+            // one plane ahead: psi(z + 3), Pi(z + 1); their slots were last read two planes back
+            if (m + 1 < len) {
+                load_psi_next();
+                load_pi_next();
+            }
+            cp_async_commit();
+            cp_async_wait<1>();  // psi(z + 2), Pi(z)
+            __syncthreads();
+            const int s0 = (m + 2) % kEnergySlots, sm1 = (m + 1) % kEnergySlots, sp1 = (m + 3) % kEnergySlots,
+                      sm2 = m % kEnergySlots, sp2 = (m + 4) % kEnergySlots, tp = m % kEnergyPiSlots;
+            float ts[13];
+#pragma unroll
+            for (int k = 0; k < 13; ++k) ts[k] = 0.f;
+            int ncell = 0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int cy = ly + h * (FTY / 2), x = x0 + lx, y = y0 + cy;
+                if (!(x < v.nx && y < v.ny)) continue;
+                if (mask != nullptr &&
+                    mask[qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z)] == 0)
+                    continue;
+                const int hx = lx + 2, hy = cy + 2;
+                const float p1 = sm.ps[s0][0][hy][hx], p2 = sm.ps[s0][1][hy][hx];
+                const float psq = p1 * p1 + p2 * p2;
+                if (!(psq > 1e-15f && psq < 1e15f)) {
+                    // the double path after the chunk
+                    const int slot = atomicAdd(&badn, 1);
+                    if (slot < kEnergyBadQ)
+                        sm.badq[slot] = lx | (cy << 5) | ((z - za) << 9);
+                    else
+                        bad_over = 1;
+                    continue;
+                }
+                float g[2][3];
+                const float wf = 0.0833333333f, wn = 0.666666667f;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    g[c][0] = (wf * (sm.ps[s0][c][hy][hx - 2] - sm.ps[s0][c][hy][hx + 2]) +
+                               wn * (sm.ps[s0][c][hy][hx + 1] - sm.ps[s0][c][hy][hx - 1])) * q.f_one_over_dx;
+                    g[c][1] = (wf * (sm.ps[s0][c][hy - 2][hx] - sm.ps[s0][c][hy + 2][hx]) +
+                               wn * (sm.ps[s0][c][hy + 1][hx] - sm.ps[s0][c][hy - 1][hx])) * q.f_one_over_dx;
+                    g[c][2] = (wf * (sm.ps[sm2][c][hy][hx] - sm.ps[sp2][c][hy][hx]) +
+                               wn * (sm.ps[sp1][c][hy][hx] - sm.ps[sm1][c][hy][hx])) * q.f_one_over_dx;
+                }
+                float term[6], wgt;
+                cell_energy<float, float>(kf, q.scheme, p1, p2, sm.pi[tp][0][cy][lx], sm.pi[tp][1][cy][lx], g,
+                                          term, wgt);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    ts[2 * k] += term[k];
+                    ts[2 * k + 1] += term[k] * wgt;
+                }
+                ts[12] += wgt;
+                ++ncell;
+            }
+            // the warp's sums of this plane (butterfly), then lane k's compensated accumulator
+#pragma unroll
+            for (int k = 0; k < 13; ++k)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) ts[k] += __shfl_xor_sync(0xffffffffu, ts[k], o);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ncell += __shfl_xor_sync(0xffffffffu, ncell, o);
+            float mine = (float)ncell;
+#pragma unroll
+            for (int k = 0; k < 13; ++k)
+                if (lane == k) mine = ts[k];
+            if (lane < 13) {
+                const float t = acc + mine;
+                comp += fabsf(acc) >= fabsf(mine) ? (acc - t) + mine : (mine - t) + acc;
+                acc = t;
+            } else if (lane == 13) {
+                acc += mine;  // cell counts stay exact in float: at most 512 per plane, 2^24 per chunk
+            }
+        }
+        __syncthreads();  // the queue is complete; the rings are free for the next chunk
+        if (lane < 14) sm.ew[warp][lane] += (double)acc + (double)comp;
+        acc = comp = 0.f;
+        // the chunk's double-path cells: from the queue or, when it overflowed, by testing
+        // every cell again; each warp sums its cells' terms and lane k adds sum k
+        const int nbad = badn;
+        if (nbad > 0) {
+            double d[14];
+#pragma unroll
+            for (int k = 0; k < 14; ++k) d[k] = 0.0;
+            auto add_cell = [&](int x, int y, int z) {
+                const CellTerms ct = energy_cell_double(v, q, base, x, y, z);
+#pragma unroll
+                for (int k = 0; k < 14; ++k) d[k] += ct.t[k];
+            };
+            if (!bad_over) {
+                for (int i = tid; i < nbad; i += kDiagThreads) {
+                    const int e = sm.badq[i];
+                    add_cell(x0 + (e & 31), y0 + ((e >> 5) & 15), za + (e >> 9));
+                }
+            } else {
+                for (int c = tid; c < FTX * FTY * len; c += kDiagThreads) {
+                    const int x = x0 + c % FTX, y = y0 + (c / FTX) % FTY, z = za + c / (FTX * FTY);
+                    if (x >= v.nx || y >= v.ny) continue;
+                    if (mask != nullptr &&
+                        mask[qbox * box_cells + x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z)] == 0)
+                        continue;
+                    const float *pc = base + view_off<float>(v, 0, x, y, z);
+                    const float p1 = pc[0], p2 = pc[v.cs], psq = p1 * p1 + p2 * p2;
+                    if (!(psq > 1e-15f && psq < 1e15f)) add_cell(x, y, z);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 14; ++k)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) d[k] += __shfl_xor_sync(0xffffffffu, d[k], o);
+            double dm = 0.0;
+#pragma unroll
+            for (int k = 0; k < 14; ++k)
+                if (lane == k) dm = d[k];
+            if (lane < 14) sm.ew[warp][lane] += dm;
+        }
+        __syncthreads();
+        if (tid == 0) badn = bad_over = 0;  // published by the next chunk's first barrier
+    }
+    __syncthreads();
+    if (tid < 14) {
+        double xv = 0.0;
+        for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += sm.ew[ww][tid];
+        partials[blockIdx.x].e[tid] = xv;
+    } else if (zero_counts && tid == 14) {
+        partials[blockIdx.x].vsum = 0.0;
+    } else if (zero_counts && tid >= 32 && tid < 36) {
+        partials[blockIdx.x].cnt[tid - 32] = 0;
     }
 }
 
@@ -1056,23 +1395,44 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
     long long items, items_per_box;
     long long *lst = (q.want_plaq && capacity > 0) ? reinterpret_cast<long long *>(list) : nullptr;
     int rc0 = AXS_OK;
-    if (q.want_plaq && !q.want_energy && !q.want_vel && (int64_t)(v.ny + 2 * v.oy + 2) * v.js < INT_MAX) {
-        // windings only: the edge-code finder (in-plane offsets in 31 bits)
+    const bool offs31 = (int64_t)(v.ny + 2 * v.oy + 2) * v.js < INT_MAX;  // in-plane offsets in 31 bits
+    auto launch_finder = [&](auto kern, int e_from) -> int {
+        AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FinderSmem)));
+        kern<<<grid, kDiagThreads, sizeof(FinderSmem), st>>>(v, q, mask, partials, counter, lst, capacity, tiles_x,
+                                                              ntiles, zchunk, items, items_per_box, box_stride, tags,
+                                                              e_from);
+        return launch_status("string finder");
+    };
+    if (q.want_plaq && !q.want_energy && !q.want_vel && offs31) {
+        // windings only: the edge-code finder
         const bool f32 = v.dtype != AXS_F64;
         diag_plan(v, nboxes, diag_grid(ncell), FTX, FTY, f32 ? 4 : 3, tiles_x, ntiles, zchunk, items_per_box, items,
                   grid);
-        auto launch_f = [&](auto kern) -> int {
-            AXS_CUDA_CHECK(
-                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FinderSmem)));
-            kern<<<grid, kDiagThreads, sizeof(FinderSmem), st>>>(v, mask, partials, counter, lst, capacity, tiles_x,
-                                                                  ntiles, zchunk, items, items_per_box, box_stride,
-                                                                  tags);
-            return AXS_OK;
-        };
-        rc0 = f32 ? launch_f(finder_kernel<float>) : launch_f(finder_kernel<double>);
+        rc0 = f32 ? launch_finder(finder_kernel<float, false>, 0) : launch_finder(finder_kernel<double, false>, 0);
         if (rc0) return rc0;
-        int rc = launch_status("string finder");
-        if (rc) return rc;
+        diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
+        return launch_status("diagnostics finalize");
+    }
+    if (q.want_energy && v.dtype == AXS_F32 && p->per_cell_fp32 && offs31) {
+        // per-cell FP32 terms: the energy sums (3 blocks per SM) and, over the same work
+        // items, the windings, the list and the velocity (4 per SM). Each kernel fills
+        // its own fields of the partial records; the finder clears the energy sums of
+        // the records the energy kernel has no block for.
+        const bool strings = q.want_plaq || q.want_vel;
+        diag_plan(v, nboxes, diag_grid(ncell), FTX, FTY, q.want_vel ? 3 : 4, tiles_x, ntiles, zchunk, items_per_box,
+                  items, grid);
+        const int sms = device_sm_count() > 0 ? device_sm_count() : 148;
+        const int egrid = strings ? std::min(grid, 3 * sms) : grid;
+        AXS_CUDA_CHECK(
+            cudaFuncSetAttribute(energy32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(EnergySmem)));
+        energy32_kernel<<<egrid, kDiagThreads, sizeof(EnergySmem), st>>>(v, q, mask, partials, tiles_x, ntiles, zchunk,
+                                                                          items, items_per_box, box_stride, !strings);
+        if ((rc0 = launch_status("energy sums"))) return rc0;
+        if (strings) {
+            rc0 = q.want_vel ? launch_finder(finder_kernel<float, true>, egrid)
+                             : launch_finder(finder_kernel<float, false>, egrid);
+            if (rc0) return rc0;
+        }
         diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
         return launch_status("diagnostics finalize");
     }
