@@ -719,30 +719,41 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
             commit(p);
         }
         issue(pa + 2);
+        // 0: nothing, 1: copy from the patch owning the cells, 2: interpolate. An
+        // initialising fill (valid_too) interpolates every cell: the value depends
+        // only on the cell's global position, so a ring cell gets what its owner's
+        // valid cell gets in the same launch.
+        auto mode_of = [&](int p_, int &z_, int &zone_) {
+            z_ = 2 * (p_ - bz * half) + sz;
+            zone_ = z_ < 0 ? 0 : (z_ < n ? 1 : 2);
+            const int src_patch = zone_ == 0 ? own_lo : (zone_ == 1 ? own_mid : own_hi);
+            int md = 0;
+            if (col_region && (f.valid_too || !(col_inside && zone_ == 1))) md = src_patch >= 0 ? 1 : 2;
+            return md;
+        };
+        // neighbour copies are loaded one parent ahead (other patches' valid cells,
+        // which this launch does not write), so their latency overlaps a parent's work
+        T cp[4][2];
+        auto load_copy = [&](int z_, int zone_) {
+            const int src_patch = zone_ == 0 ? own_lo : (zone_ == 1 ? own_mid : own_hi);
+            const T *src = st + (int64_t)src_patch * f.box + src_col + (int64_t)(z_ - (zone_ - 1) * n + kPatchRZ) * f.ks;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                cp[c][0] = src[c * f.plane];
+                cp[c][1] = src[c * f.plane + f.js];
+            }
+        };
+        {
+            int z_, zone_;
+            if (mode_of(pa, z_, zone_) == 1) load_copy(z_, zone_);
+        }
         for (int pz = pa; pz < pb; ++pz) {
             commit(pz + 2);
-            const int z = 2 * (pz - bz * half) + sz;
-            const int zone = z < 0 ? 0 : (z < n ? 1 : 2);
-            const int src_patch = zone == 0 ? own_lo : (zone == 1 ? own_mid : own_hi);
-            // 0: nothing, 1: copy from the patch owning the cells, 2: interpolate.
-            // An initialising fill (valid_too) interpolates every cell: the value
-            // depends only on the cell's global position, so a ring cell gets what
-            // its owner's valid cell gets in the same launch.
-            int mode = 0;
-            if (col_region && (f.valid_too || !(col_inside && zone == 1))) mode = src_patch >= 0 ? 1 : 2;
+            int z, zone;
+            const int mode = mode_of(pz, z, zone);
             const bool any = __syncthreads_or(mode == 2);  // also publishes the committed plane
             if (pz + 1 < pb) issue(pz + 3);
             T *dst = dst_col + (int64_t)(z + kPatchRZ) * f.ks;
-            // neighbour copies: loads now, stores after the interpolation passes
-            T cp[4][2];
-            if (mode == 1) {
-                const T *src = st + (int64_t)src_patch * f.box + src_col + (int64_t)(z - (zone - 1) * n + kPatchRZ) * f.ks;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    cp[c][0] = src[c * f.plane];
-                    cp[c][1] = src[c * f.plane + f.js];
-                }
-            }
             if (any) {
                 const T *s0 = sm.win[pwrap(pz - 2, 5)], *s1 = sm.win[pwrap(pz - 1, 5)], *s2p = sm.win[pwrap(pz, 5)];
                 const T *s3p = sm.win[pwrap(pz + 1, 5)], *s4 = sm.win[pwrap(pz + 2, 5)];
@@ -785,6 +796,10 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
                     dst[c * f.plane] = cp[c][0];
                     dst[c * f.plane + f.js] = cp[c][1];
                 }
+            }
+            if (pz + 1 < pb) {
+                int z_, zone_;
+                if (mode_of(pz + 1, z_, zone_) == 1) load_copy(z_, zone_);
             }
         }
     }
