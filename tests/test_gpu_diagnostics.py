@@ -277,3 +277,28 @@ def test_string_finder_alone_equals_fused_pass(axs, orc, dtype, n):
         assert torch.equal(torch.sort(alone.pierced)[0], torch.sort(full.pierced)[0]), name
         if name == "pi":
             assert full.n_near_tie > 0
+
+
+@pytest.mark.parametrize("vacuum", [4, 20])
+def test_per_cell_fp32_double_path_cells(axs, orc, vacuum):
+    """per_cell_fp32 on a field with exact zeros (|psi|^2 = 0: the double path)
+    and a false-vacuum block; at 20^3 the block overflows the energy kernel's
+    per-chunk queue, which then searches the chunk again. Counts, the velocity
+    count and the pierced set equal the FP64 per-cell pass; sums to 2e-6."""
+    n = 48
+    v = orc.fourier_ic_state(n, 6.0, seed=12)
+    v[2:] = 0.2 * np.random.default_rng(4).standard_normal((2, n, n, n))
+    zs = np.random.default_rng(5).integers(0, n, size=(80, 3))
+    v[:2, zs[:, 0], zs[:, 1], zs[:, 2]] = 0.0
+    v[:, 8:8 + vacuum, 8:8 + vacuum, 8:8 + vacuum] = 0.0
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    lvl = axs.PeriodicLevel(n, 0.5, dtype=torch.float32, pierced_capacity=3 * n ** 3)
+    lvl.set_state(_dev(v.astype(np.float32)))
+    ref = lvl.diagnostics(bg, 1.3)
+    fast = lvl.diagnostics(bg, 1.3, per_cell_fp32=True)
+    assert (fast.n_p_plain, fast.n_p_weighted, fast.vel_count, fast.n_near_tie) == \
+        (ref.n_p_plain, ref.n_p_weighted, ref.vel_count, ref.n_near_tie)
+    assert torch.equal(torch.sort(fast.pierced)[0], torch.sort(ref.pierced)[0])
+    np.testing.assert_allclose(fast.energy_sums, ref.energy_sums, rtol=2e-6)
+    assert fast.energy_sums[13] == ref.energy_sums[13] == n ** 3  # every cell counted once
+    assert fast.mean_gamma_sq_v_sq == pytest.approx(ref.mean_gamma_sq_v_sq, rel=1e-5)
