@@ -113,6 +113,37 @@ static uint64_t ens_key(const axs_ensemble *e, int32_t tile_config, int32_t z_ch
 
 // Key of the tiling each table currently holds (host side; set by init). A
 // plan is usable only while its key is the one last written to its table.
+// Per-box diagnostics run on up to kDiagLanes streams side by side (boxes of a
+// lane one after another, each lane with its own scratch slice), forked from and
+// joined back to the caller's stream with events; under graph capture the lanes
+// become parallel branches. Small boxes alone leave most of the GPU idle.
+constexpr int kDiagLanes = 8;
+struct DiagLanes {
+    cudaStream_t s[kDiagLanes];
+    cudaEvent_t fork, join[kDiagLanes];
+};
+static std::mutex g_lanes_mu;
+static std::unordered_map<int, DiagLanes> g_lanes;  // per device
+
+static int diag_lanes(DiagLanes *&out)
+{
+    int dev = 0;
+    AXS_CUDA_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_lanes_mu);
+    auto it = g_lanes.find(dev);
+    if (it == g_lanes.end()) {
+        DiagLanes l;
+        for (int i = 0; i < kDiagLanes; ++i) {
+            AXS_CUDA_CHECK(cudaStreamCreateWithFlags(&l.s[i], cudaStreamNonBlocking));
+            AXS_CUDA_CHECK(cudaEventCreateWithFlags(&l.join[i], cudaEventDisableTiming));
+        }
+        AXS_CUDA_CHECK(cudaEventCreateWithFlags(&l.fork, cudaEventDisableTiming));
+        it = g_lanes.emplace(dev, l).first;
+    }
+    out = &it->second;
+    return AXS_OK;
+}
+
 static std::mutex g_table_mu;
 static std::unordered_map<const void *, uint64_t> g_table_key;
 
@@ -463,7 +494,7 @@ int axs_ensemble_diagnostics_scratch_bytes(int32_t nboxes, const int32_t *dims, 
     int64_t m = 0;
     for (int b = 0; b < nboxes; ++b)
         m = std::max(m, diag_scratch_bytes_for((int64_t)dims[3 * b] * dims[3 * b + 1] * dims[3 * b + 2]));
-    *bytes = m;
+    *bytes = (m + 255) / 256 * 256 * std::min(nboxes, kDiagLanes);  // one slice per lane
     return AXS_OK;
 }
 
@@ -474,14 +505,31 @@ int axs_ensemble_diagnostics(const axs_ensemble *e, const axs_diag_params *p, ax
     int rc = validate_ensemble(e, geo);
     if (rc) return rc;
     AXS_REQUIRE(p != nullptr && result_dev != nullptr, AXS_ERR_INVALID_ARGUMENT, "null params or results");
+    int64_t need = 0;
+    if ((rc = axs_ensemble_diagnostics_scratch_bytes(e->nboxes, e->dims, &need))) return rc;
+    AXS_REQUIRE(scratch != nullptr && scratch_bytes >= need, AXS_ERR_WORKSPACE,
+                "ensemble diagnostics scratch too small (%lld < %lld bytes)", (long long)scratch_bytes, (long long)need);
+    const int lanes = std::min(e->nboxes, kDiagLanes);
+    const int64_t slice = need / lanes;
+    DiagLanes *L = nullptr;
+    if ((rc = diag_lanes(L))) return rc;
+    std::lock_guard<std::mutex> lock(g_lanes_mu);  // the lanes' streams and events are shared: one call at a time
+    cudaStream_t st = (cudaStream_t)stream;
+    AXS_CUDA_CHECK(cudaEventRecord(L->fork, st));
+    for (int i = 0; i < lanes; ++i) AXS_CUDA_CHECK(cudaStreamWaitEvent(L->s[i], L->fork, 0));
     const int64_t es = (int64_t)dtype_size(e->dtype);
-    for (int b = 0; b < e->nboxes; ++b) {
+    for (int b = 0; b < e->nboxes && rc == AXS_OK; ++b) {
+        const int i = b % lanes;
         const void *base = static_cast<const char *>(e->state) + geo.base[b] * es;
-        if ((rc = diag_level_box(base, e->dtype, e->dims[3 * b], e->dims[3 * b + 1], e->dims[3 * b + 2], geo.g[b], p,
-                                 result_dev + b, scratch, scratch_bytes, (cudaStream_t)stream)))
-            return rc;
+        rc = diag_level_box(base, e->dtype, e->dims[3 * b], e->dims[3 * b + 1], e->dims[3 * b + 2], geo.g[b], p,
+                            result_dev + b, static_cast<char *>(scratch) + i * slice, slice, L->s[i]);
     }
-    return AXS_OK;
+    // join every lane back, also after an error, so no lane is left forked from a capture
+    for (int i = 0; i < lanes; ++i) {
+        AXS_CUDA_CHECK(cudaEventRecord(L->join[i], L->s[i]));
+        AXS_CUDA_CHECK(cudaStreamWaitEvent(st, L->join[i], 0));
+    }
+    return rc;
 }
 
 int axs_ensemble_device_status(const axs_ensemble *e, void *stream)

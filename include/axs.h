@@ -519,8 +519,10 @@ int axs_ensemble_rk4_advance(const axs_ensemble *e, const axs_ensemble_plan *pla
                              double tau_i, double t0, double dt, int32_t nsteps, void *stream);
 
 /* Per-box diagnostics (as axs_level_diagnostics, without the pierced list)
- * into result_dev[0 .. nboxes-1]; scratch sized by
- * axs_ensemble_diagnostics_scratch_bytes and reused box after box. */
+ * into result_dev[0 .. nboxes-1]. The boxes run on up to 8 internal streams
+ * side by side, forked from and joined back to `stream` with events (parallel
+ * branches under graph capture); scratch, sized by
+ * axs_ensemble_diagnostics_scratch_bytes, holds one slice per stream. */
 int axs_ensemble_diagnostics_scratch_bytes(int32_t nboxes, const int32_t *dims, int64_t *bytes);
 int axs_ensemble_diagnostics(const axs_ensemble *e, const axs_diag_params *p, axs_diag_result *result_dev,
                              void *scratch, int64_t scratch_bytes, void *stream);
