@@ -262,14 +262,16 @@ typedef struct axs_diag_params {
     int32_t masking_scheme;                /* axs_masking_scheme (Masking.hpp:39-53) */
     double masking_threshold;
     int32_t boundary;                      /* axs_boundary */
-    int32_t want_energy, want_plaquettes, want_velocity;
+    int32_t want_energy, want_plaquettes, want_velocity; /* want_plaquettes alone: the string
+                                              finder (windings, counts, pierced list), its own
+                                              lean kernel */
     int32_t per_cell_fp32;                 /* FP32 fields only: 0 = per-cell energy, masking and
                                               gamma^2 v^2 in double as the reference computes them
                                               (sums equal the reference's FLOAT build); 1 = per-cell
-                                              terms in FP32, summed per work item in FP32 and
-                                              across items in FP64 (about 1e-7 relative; ~10x
-                                              faster on GB300, whose FP64 rate is 1/64 of FP32).
-                                              Windings and counts are exact either way. */
+                                              terms in FP32, summed per work item in compensated
+                                              FP32 and across items in FP64 (about 1e-8 relative;
+                                              ~14x faster on GB300, whose FP64 rate is 1/64 of
+                                              FP32). Windings and counts are exact either way. */
 } axs_diag_params;
 
 /* Written to device memory by the diagnostics pass. */
