@@ -288,6 +288,17 @@ def test_batched_patch_diagnostics_match_per_patch_passes(axs, dtype):
     assert set(lst.cpu().numpy().tolist()) == pierced and got.n_listed == len(pierced)
     np.testing.assert_allclose(np.array(list(got.energy_sums)), sums, rtol=1e-12)
     assert got.vel_sum == pytest.approx(vsum, rel=1e-12)
+    if dtype == torch.float32:
+        # FP32 per-cell terms over all patches (the energy kernel and the velocity finder
+        # on ghost-ring boxes): exact counts and pierced set, sums to FP32 accuracy
+        prm32 = L.DiagParams(p.dx, v.R, v.lambda_, v.R_prime_over_R, v.m_r, L.MASK_A, 0.8, L.BOUNDARY_GHOSTS,
+                             1, 1, 1, 1)
+        g32, l32 = p.diagnostics(prm32, list_capacity=cap)
+        assert [g32.n_p_plain, g32.n_p_weighted, g32.vel_count, g32.n_near_tie] == cnts.tolist()
+        assert set(l32.cpu().numpy().tolist()) == pierced
+        np.testing.assert_allclose(np.array(list(g32.energy_sums)), sums, rtol=2e-6)
+        assert g32.energy_sums[13] == sums[13]
+        assert g32.vel_sum == pytest.approx(vsum, rel=1e-5)
     # the string finder alone over all patches: the same counts and pierced set
     prm_s = L.DiagParams(p.dx, v.R, v.lambda_, v.R_prime_over_R, v.m_r, L.MASK_A, 0.8, L.BOUNDARY_GHOSTS, 0, 1, 0, 0)
     alone, lst_s = p.diagnostics(prm_s, list_capacity=cap)
