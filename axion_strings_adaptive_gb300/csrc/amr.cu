@@ -63,9 +63,9 @@ static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g)
     AXS_REQUIRE(dtype == AXS_F32 || dtype == AXS_F64, AXS_ERR_INVALID_ARGUMENT, "bad dtype %d", dtype);
     AXS_REQUIRE(n >= 8 && n % 8 == 0 && n <= 256, AXS_ERR_UNSUPPORTED, "patch side %d must be a multiple of 8 in [8, 256]",
                 n);
-    // the fused step launches one grid z slice per patch; the two-sweep step's
-    // work items carry 2 * npatches box numbers in 16 bits (checked where it is used)
-    AXS_REQUIRE(npatches > 0 && npatches <= 65535, AXS_ERR_INVALID_ARGUMENT, "patch count %d out of range",
+    // the two-sweep step's work items carry 2 * npatches box numbers in 16 bits
+    // (checked where it is used); the fused step takes any count
+    AXS_REQUIRE(npatches > 0 && npatches <= (1 << 22), AXS_ERR_INVALID_ARGUMENT, "patch count %d out of range",
                 npatches);
     const int64_t line = 128 / (int64_t)dtype_size(dtype), sector = 32 / (int64_t)dtype_size(dtype);
     g.n = n;
@@ -186,7 +186,7 @@ static bool patches_fused(int32_t dtype, int n, int npatches)
         fused_tiles<double>(n, cx, cy);
     else
         fused_tiles<float>(n, cx, cy);
-    return cx > 0 && npatches <= 65535;  // one grid z slice per patch
+    return cx > 0;
 }
 
 // Execution barrier of the patch's tiles, split so that sweep B's shared-memory
@@ -199,6 +199,7 @@ __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.w
 
 struct FusedArgs {
     int n;
+    int q0;  // patch of grid z slice 0 (launches of at most 65 535 patches each)
     int64_t js, ks, box, plane;
     const CUtensorMap *maps;  // per patch q: map 2 q + 1 boxes BX x BY of the state
 };
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(Fused<T>::THREADS, 1) patch_fused_kernel(T *__
     T *gpw = swin + (size_t)F::NSW * F::SWIN;
     __shared__ uint64_t full[F::NS];
     const int tid = threadIdx.x;
-    const int q = blockIdx.z, n = f.n;
+    const int q = f.q0 + (int)blockIdx.z, n = f.n;
     const int x0 = blockIdx.x * F::TX, y0 = blockIdx.y * F::TY;  // tile origin (valid cells)
     const CUtensorMap *map = f.maps + 2 * q + 1;
     if (tid == 0) {
@@ -421,9 +422,8 @@ static int patch_step_fused(const axs_patches *p, const PatchGeom &g, SweepArgs<
                                             (int)F::SMEM));
         attr_done = 1;
     }
-    FusedArgs f{g.n, g.js, g.ks, g.box, g.plane, a.maps};
+    FusedArgs f{g.n, 0, g.js, g.ks, g.box, g.plane, a.maps};
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)cx, (unsigned)cy, (unsigned)p->npatches);
     cfg.blockDim = dim3(F::THREADS, 1, 1);
     cfg.dynamicSmemBytes = F::SMEM;
     cfg.stream = st;
@@ -434,7 +434,13 @@ static int patch_step_fused(const axs_patches *p, const PatchGeom &g, SweepArgs<
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    AXS_CUDA_CHECK(cudaLaunchKernelEx(&cfg, patch_fused_kernel<T>, static_cast<T *>(p->state), a, f));
+    // patches step independently (each reads and writes only its own box), so a set
+    // larger than the grid's z limit goes in several launches
+    for (int q0 = 0; q0 < p->npatches; q0 += 65535) {
+        f.q0 = q0;
+        cfg.gridDim = dim3((unsigned)cx, (unsigned)cy, (unsigned)std::min(65535, p->npatches - q0));
+        AXS_CUDA_CHECK(cudaLaunchKernelEx(&cfg, patch_fused_kernel<T>, static_cast<T *>(p->state), a, f));
+    }
     return launch_status("patch fused step");
 }
 

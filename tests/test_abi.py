@@ -183,8 +183,9 @@ def test_cpp_host_demo_is_built(L):
 
 def test_patch_layout_rows_arenas_and_counts(L):
     """Patch rows are whole 32-byte sectors (n + 16 columns), boxes start on
-    128-byte lines, patch sizes the fused step takes need no work arena and
-    may number up to 65 535; the two-sweep sizes keep their work arena."""
+    128-byte lines, patch sizes the fused step takes need no work arena (and
+    their count is not tied to a grid dimension); the two-sweep sizes keep
+    their work arena."""
     lib = L.lib()
     lay = L.PatchLayout()
     assert lib.axs_patches_layout(L.AXS_F32, 32, 60000, C.byref(lay)) == L.AXS_OK
@@ -195,7 +196,8 @@ def test_patch_layout_rows_arenas_and_counts(L):
     assert lay.jstride == 48 and lay.work_bytes == 0
     assert lib.axs_patches_layout(L.AXS_F32, 16, 1000, C.byref(lay)) == L.AXS_OK  # two-sweep size
     assert lay.jstride == 32 and lay.work_bytes == 8 * lay.plane_elems * 4
-    assert lib.axs_patches_layout(L.AXS_F32, 32, 65536, C.byref(lay)) == L.AXS_ERR_INVALID_ARGUMENT
+    assert lib.axs_patches_layout(L.AXS_F32, 32, 70000, C.byref(lay)) == L.AXS_OK  # fused: launched in chunks
+    assert lib.axs_patches_layout(L.AXS_F32, 32, (1 << 22) + 1, C.byref(lay)) == L.AXS_ERR_INVALID_ARGUMENT
     # a two-sweep patch set needs its work arena
     p = L.PatchesC(L.AXS_F32, 16, 10, 0.25, C.c_void_p(1 << 20), None, C.c_void_p(1 << 21), 1 << 30, 0, 1 << 30)
     plan = L.PatchPlan()

@@ -327,13 +327,14 @@ def test_regrid_keeps_the_fine_data_of_blocks_that_stay_refined(axs):
             assert not bool((v == 7.0).any()) and float(v.abs().max()) > 0.0
 
 
-def test_patch_counts_past_the_two_sweep_limit(axs):
-    """33 000 patches: past the two-sweep step's 32 767 (its work items carry box
-    numbers in 16 bits), inside the fused step's 65 535. A homogeneous radiation-era
-    solution (psi = R = tau, Pi = R' = 1) survives a subcycled coarse step in every
-    patch, the last ones included."""
+def test_patch_counts_past_the_grid_and_two_sweep_limits(axs):
+    """70 000 patches: past the two-sweep step's 32 767 (its work items carry box
+    numbers in 16 bits) and past one grid's 65 535 z slices (the fused step then
+    launches in chunks). A homogeneous radiation-era solution (psi = R = tau,
+    Pi = R' = 1) survives a subcycled coarse step in every patch, the last ones
+    included."""
     from axion_strings_adaptive_gb300.amr import TwoLevel
-    nx, ny, nz, block = 1024, 512, 512, 16
+    nx, ny, nz, block = 1024, 1024, 512, 16
     bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)  # RD: R = tau, R' = 1, kappa = 0
     coarse = axs.PeriodicLevel((nx, ny, nz), 0.5, dtype=torch.float32, pierced_capacity=1)
     st = torch.zeros((4, nz, ny, nx), dtype=torch.float32, device="cuda")
@@ -342,9 +343,9 @@ def test_patch_counts_past_the_two_sweep_limit(axs):
     del st
     two = TwoLevel(coarse, block, spare_arena=False)
     nbx, nby = nx // block, ny // block
-    q = np.arange(33000)
+    q = np.arange(70000)
     two.set_blocks(np.stack([q % nbx, (q // nbx) % nby, q // (nbx * nby)], axis=1))
-    assert two.patches.npatches == 33000 and two.patches.layout.work_bytes == 0
+    assert two.patches.npatches == 70000 and two.patches.layout.work_bytes == 0
     two.advance(bg, 1.0, 0.0, 0.1, 1)
     two.device_status()
     p, n = two.patches, two.patches.n
