@@ -696,7 +696,7 @@ def run_native(args):
     scale = None
     if not args.no_scale:
         scale = scale_report(A, dev, hbm_peak, n=args.scale_n, steps=args.scale_steps, kdiv=args.scale_kdiv)
-    # the same at the survey's scale configuration: a 1024^3 base and 100 coarse steps.
+    # the same at the full scale configuration: a 1024^3 base and 100 coarse steps.
     # IC |n| < N/96 tags 3.2 % of the cells (59 k -> 65 k patches): with the spare
     # patch arena, about the densest set that fits in HBM beside the base level.
     scale_1024 = None
