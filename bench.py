@@ -640,15 +640,23 @@ def run_native(args):
     if not args.no_precision and args.precision_steps > 0:
         ps = args.precision_steps
         marks = sorted({min(40, ps), ps})
-        legs = (("fp64", torch.float64, ic64), ("fp32", torch.float32, ic64.float()),
-                ("fp64_rounded_ic", torch.float64, ic64.float().double()))
+        # fp64_fp32_storage: FP64 arithmetic with the state rounded to FP32 after every step
+        # (FP32 storage alone, without FP32 arithmetic)
+        legs = (("fp64", torch.float64, ic64, False), ("fp32", torch.float32, ic64.float(), False),
+                ("fp64_rounded_ic", torch.float64, ic64.float().double(), False),
+                ("fp64_fp32_storage", torch.float64, ic64.float().double(), True))
         out = {}
-        for name, dt_, s0 in legs:
+        for name, dt_, s0, round_state in legs:
             lv = A.PeriodicLevel(n, DX, dtype=dt_, device=dev, pierced_capacity=3 * n ** 3 // 8)
             lv.set_state(s0.to(dt_))
             done = 0
             for mk in marks:
-                lv.advance(bg, TAU_I, done * DT, DT, mk - done)
+                if round_state:
+                    for s_ in range(done, mk):
+                        lv.advance(bg, TAU_I, s_ * DT, DT, 1)
+                        lv.state.copy_(lv.state.float())
+                else:
+                    lv.advance(bg, TAU_I, done * DT, DT, mk - done)
                 done = mk
                 lv.device_status()
                 d = lv.diagnostics(bg, TAU_I + mk * DT, want_list=True)
@@ -674,7 +682,8 @@ def run_native(args):
             precision["by_step"][str(mk)] = {
                 "tau": TAU_I + mk * DT, "xi_fp64": ref[0].xi_plain, "n_p_fp64": ref[0].n_p_plain,
                 "fp32_vs_fp64": compare(ref, out[("fp32", mk)]),
-                "fp64_rounded_ic_vs_fp64": compare(ref, out[("fp64_rounded_ic", mk)])}
+                "fp64_rounded_ic_vs_fp64": compare(ref, out[("fp64_rounded_ic", mk)]),
+                "fp64_fp32_storage_vs_fp64": compare(ref, out[("fp64_fp32_storage", mk)])}
         fin = precision["by_step"][str(ps)]["fp32_vs_fp64"]
         precision["total_energy_rel_err"] = fin["total_energy_rel_err"]
         precision["max_energy_rel_err"] = fin["max_energy_rel_err"]

@@ -28,7 +28,9 @@ REF_PATHS = {
     "f64": os.path.join(HERE, "_ref", "libaxs_ref_f64.so"),
     "f32": os.path.join(HERE, "_ref", "libaxs_ref_f32.so"),
 }
-REF_SOURCE_DIR = "/root/reference/AxionStrings"
+# the reference project's root, where it exists (only the reference-built checker needs it)
+REF_ROOT = os.environ.get("AXS_REFERENCE_DIR", "")
+REF_SOURCE_DIR = os.path.join(REF_ROOT, "AxionStrings") if REF_ROOT else ""
 
 _dbl = C.c_double
 _i64 = C.c_int64
@@ -67,11 +69,11 @@ def background(kind=BG_EXPANDING, a_inv=2.0, c0=0.0, c1=0.0, tau_switch=0.0, has
 
 
 def build(force: bool = False) -> None:
-    """Compile the C restatement (and, where the reference tree exists, the
-    reference-built checker) with oracle/Makefile."""
+    """Compile the C restatement (and, where AXS_REFERENCE_DIR names the
+    reference tree, the reference-built checker) with oracle/Makefile."""
     if force or not os.path.exists(LIB_PATH):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if os.path.isdir(REF_SOURCE_DIR):
+    if REF_SOURCE_DIR and os.path.isdir(REF_SOURCE_DIR):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_SOURCE_DIR}"], check=True)
 
 

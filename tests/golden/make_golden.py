@@ -6,7 +6,7 @@ and records inputs + outputs as compressed .npz files. Needs the reference
 tree, so it only runs where that exists; the committed fixtures travel
 instead.
 
-    python tests/golden/make_golden.py
+    AXS_REFERENCE_DIR=<reference project root> python tests/golden/make_golden.py
 
 Fixtures:
   kats.npz        known-answer vectors of the reference's own unit tests
@@ -22,7 +22,7 @@ Fixtures:
   tagging.npz     StringTagger::operator() tags (plaquette, Laplacian and radial-
                   gradient criteria) on seeded boxes, both precision builds
 
-    python tests/golden/make_golden.py [fixture ...]   (default: all)
+    AXS_REFERENCE_DIR=<reference project root> python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
 from __future__ import annotations
 
@@ -276,7 +276,7 @@ def main(names=None) -> None:
     if not (O.ref_available("f64") and O.ref_available("f32")):
         O.build()
     if not (O.ref_available("f64") and O.ref_available("f32")):
-        raise SystemExit("reference-built checker unavailable (needs the reference tree)")
+        raise SystemExit("reference-built checker unavailable (set AXS_REFERENCE_DIR to the reference tree)")
     for name in names or FIXTURES:
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **FIXTURES[name]())
     print("golden fixtures written to", HERE)

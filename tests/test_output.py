@@ -40,9 +40,10 @@ def test_network_scalars_rows_and_restart(tmp_path):
 
 
 def test_reference_loader_reads_our_tables(tmp_path):
-    ref = "/root/reference/AxionStrings/analysis"
-    if not os.path.isdir(ref):
-        pytest.skip("reference analysis scripts not present")
+    root = os.environ.get("AXS_REFERENCE_DIR", "")
+    ref = os.path.join(root, "AxionStrings", "analysis")
+    if not root or not os.path.isdir(ref):
+        pytest.skip("AXS_REFERENCE_DIR does not name the reference tree (analysis scripts absent)")
     sys.path.insert(0, ref)
     try:
         import axion_analysis as A
