@@ -17,9 +17,10 @@
 // with J_s(u)^T a = lap a + kappa_s a - lambda_s/2 [(|u|^2 - R_s^2) a + 2 u (u . a)]
 // (the periodic centred Laplacian is symmetric), and the lambda0 gradient
 //   lambda0bar += sum_s sum_sites -(lambda_s/2)/lambda0 (|u_s|^2 - R_s^2) (u_s . F_sbar).
-// u3 and u4 are recomputed by re-running forward sweep A on psi_n, Pi_n.
+// u3 and u4 are recomputed by re-running forward sweep A on psi_n, Pi_n
+// (it stores d3 = u3 - psi_n, d4 = u4 - psi_n).
 // Each adjoint sweep is the same TMA-staged stencil pipeline as the forward
-// sweeps (sweep.cuh); sweep B reads 4+4 and writes 8 components per site,
+// sweeps (sweep.cuh); sweep B reads 4+6 and writes 8 components per site,
 // sweep A reads 4+12 and writes 4.
 #include <cmath>
 
@@ -32,10 +33,12 @@ int level_fill_ghosts(void *data, int32_t dtype, int nx, int ny, int nz, const L
 int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const LevelGeom &g, int ny, int nz,
                    uint32_t box_x, uint32_t box_y);
 
-// Adjoint sweep B: stencil on (psi'bar, Pi'bar); pointwise (u3, u4).
+// Adjoint sweep B: stencil on (psi'bar, Pi'bar); pointwise (d3, d4) of the
+// recomputed forward sweep A and psi_n, whose sums are the stage states
+// u3 = psi_n + d3, u4 = psi_n + d4 (the forward sweep B forms them alike).
 // Writes (F1bar, F2bar) with periodic copies and (u3bar, u4bar).
 struct AdjointB {
-    static constexpr int kPointwise = 4;
+    static constexpr int kPointwise = 6;
     static constexpr bool kLambdaGrad = true;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
@@ -50,7 +53,8 @@ struct AdjointB {
             const T lf3b1 = fma(a.h2_sixth, lap[0][v], a.h_third * lap[2][v]);
             const T lf3b2 = fma(a.h2_sixth, lap[1][v], a.h_third * lap[3][v]);
             const T f4b1 = a.h_sixth * pb1, f4b2 = a.h_sixth * pb2;
-            const T u31 = pq[0][v], u32 = pq[1][v], u41 = pq[2][v], u42 = pq[3][v];
+            const T u31 = pq[4][v] + pq[0][v], u32 = pq[5][v] + pq[1][v];
+            const T u41 = pq[4][v] + pq[2][v], u42 = pq[5][v] + pq[3][v];
             T u3b1, u3b2, u4b1, u4b2;
             rhs_adjoint_pair(a.c2, u31, u32, f3b1, f3b2, lf3b1, lf3b2, u3b1, u3b2);
             rhs_adjoint_pair(a.c4, u41, u42, f4b1, f4b2, a.h_sixth * lap[2][v], a.h_sixth * lap[3][v], u4b1, u4b2);
@@ -231,7 +235,8 @@ template <typename T> struct AdjointRunner {
         if ((rc = make_level_map(&map_fbar, fbar, lv->dtype, g, lv->ny, lv->nz, LA::box_x(), LA::box_y()))) return rc;
 
         SweepArgs<T> b = a;  // adjoint sweep B
-        for (int c = 0; c < 4; ++c) b.pt[c] = work + c * g.cs;  // u3, u4 from forward sweep A
+        for (int c = 0; c < 4; ++c) b.pt[c] = work + c * g.cs;  // d3, d4 from forward sweep A
+        for (int c = 0; c < 2; ++c) b.pt[4 + c] = state + c * g.cs;  // psi_n
         for (int c = 0; c < 4; ++c) b.out[c] = fbar + c * g.cs;
         for (int c = 0; c < 4; ++c) b.out[4 + c] = ubar + c * g.cs;
         b.lam_partial = lam_part;

@@ -17,7 +17,7 @@
 // ghost rings instead of periodic wrap: sweep A runs over the valid cells
 // plus a ring of 4 (x, keeping the TMA boxes 16-byte aligned) / 2 (y, z)
 // cells, reading psi, Pi on the 6 / 4-wide ring, so that sweep B over the
-// valid cells finds S3, S4 on its 2-wide stencil ring. The ring therefore has
+// valid cells finds d3, d4 on its 2-wide stencil ring. The ring therefore has
 // to hold psi, Pi at the step's start time; it is filled first from the
 // neighbouring patches (same fine level, same time) and, where no patch owns
 // a ring cell, by interpolating the coarse level: quartic Lagrange
@@ -44,7 +44,7 @@ int diag_ghost_boxes(const void *data, int32_t dtype, int nx, int ny, int nz, in
                      cudaStream_t st);
 int64_t diag_scratch_bytes_for(int64_t ncell);
 constexpr int kPatchOX = 8, kPatchRY = 4, kPatchRZ = 4;  // padded position of valid (0, 0, 0)
-// In the work arena (S3, S4, G, P) valid x = 0 sits at padded column 12, so
+// In the work arena (d3, d4, E, Q) valid x = 0 sits at padded column 12, so
 // sweep A's domain x in [-4, n + 4) covers whole 32-byte sectors of every row
 // (padded 8 .. n + 16) and no output row leaves a partly written sector.
 constexpr int kWorkOX = 12;
@@ -133,7 +133,7 @@ template <typename T> struct PatchTilings {
 // One RK4 step of a patch without the stage buffers: each CTA owns a TX x TY
 // tile of the valid cells and marches in z. Per plane it runs sweep A on the
 // tile plus a 2-cell halo (the A region) from a TMA ring of (psi, Pi) planes
-// and keeps S3, S4 (A region, 5 planes) and G, P (tile, 3 planes) in shared
+// and keeps d3, d4 (A region, 5 planes) and E, Q (tile, 3 planes) in shared
 // memory; sweep B follows two planes behind and writes psi, Pi of the step's
 // end over the old values. The tiles of one patch form a thread-block cluster
 // that advances in lockstep: after every plane of sweep A a cluster barrier
@@ -145,7 +145,7 @@ template <typename T> struct Fused {
     // FP32: two sites per thread on 32 x 16 tiles (174 KB of shared memory, one
     // block per SM); 32 x 8 tiles with one site per thread fit two blocks per SM
     // but ran 20 % slower on GB300. FP64: one site per thread on 32 x 8 tiles.
-    // NSW / NGP: S3, S4 and G, P slots, one more than sweep B reads, so sweep A of
+    // NSW / NGP: d3, d4 and E, Q slots, one more than sweep B reads, so sweep A of
     // the next plane never overwrites what a slower thread's sweep B still reads
     static constexpr int V = sizeof(T) == 4 ? 2 : 1;
     static constexpr int TX = 32, TY = sizeof(T) == 4 ? 16 : 8, NS = sizeof(T) == 4 ? 6 : 5;
@@ -254,8 +254,8 @@ __global__ void __launch_bounds__(Fused<T>::THREADS, 1) patch_fused_kernel(T *__
             const T *pl[5];
 #pragma unroll
             for (int d = 0; d < 5; ++d) pl[d] = ring + (size_t)((i + d) % F::NS) * F::RING;
-            T *sz = swin + (size_t)(i % F::NSW) * F::SWIN;  // S3, S4 of plane za
-            T *gz = gpw + (size_t)(i % F::NGP) * F::GPW;    // G, P of plane za
+            T *sz = swin + (size_t)(i % F::NSW) * F::SWIN;  // d3, d4 of plane za
+            T *gz = gpw + (size_t)(i % F::NGP) * F::GPW;    // E, Q of plane za
             for (int u = tid; u < F::NA; u += F::THREADS) {
                 // units of the A region's first 32 / V columns row by row (a warp covers
                 // whole 128-byte bank rows, so its shared-memory accesses are conflict-free),
@@ -283,21 +283,29 @@ __global__ void __launch_bounds__(Fused<T>::THREADS, 1) patch_fused_kernel(T *__
                 }
             }
         }
-        __syncthreads();  // S3, S4, G, P of plane za are in place; ring plane k = i is read no more
+        // sweep B's psi_n, Pi_n at plane zb = za - 2: ring plane k = i, whose slot is
+        // refilled after the barrier below
+        const int zb = i - 4;
+        T pq[8][V];
+        if (ok && zb >= 0 && has_b) {
+            const T *r0 = ring + (size_t)(i % F::NS) * F::RING + (byl + 4) * F::BX + (bxl + 4);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) ldv<T, V>(r0 + c * F::BX * F::BY, pq[4 + c]);
+        }
+        __syncthreads();  // d3, d4, E, Q of plane za are in place; ring plane k = i is read no more
         if (tid == 0 && i + F::NS < K) {
             fence_proxy_async_smem();
             issue(i + F::NS);
         }
         // this tile is done with sweep A at za: (psi, Pi) of plane za - 2 is read no more here
         cluster_arrive();
-        const int zb = i - 4;
         T o[4][V];
         if (ok && zb >= 0 && has_b) {
             const T *sp[5];
 #pragma unroll
             for (int d = 0; d < 5; ++d) sp[d] = swin + (size_t)((zb + d) % F::NSW) * F::SWIN;  // planes zb-2 .. zb+2
             const T *g = gpw + (size_t)((zb + 2) % F::NGP) * F::GPW;                           // plane zb
-            T lap[4][V], ctr[4][V], pq[4][V];
+            T lap[4][V], ctr[4][V];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const int co = c * F::AX * F::AY;
@@ -487,7 +495,11 @@ static int patch_step(const axs_patches *p, const PatchGeom &g, const axs_patch_
     ab.dox_out = kPatchOX - kWorkOX;   // outputs to the state
     ab.c2 = aa.c2;
     ab.c4 = stage_coef<T>(bg, tau_i + t + dt);
-    for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.plane;
+    for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.plane;  // E, Q
+    // psi_n, Pi_n: the state's rows start kWorkOX - kPatchOX columns later than the
+    // work arena's, so these pointers carry that shift (the loads add the work-arena
+    // offset of the site)
+    for (int c = 0; c < 4; ++c) ab.pt[4 + c] = state + c * g.plane - (kWorkOX - kPatchOX);
     for (int c = 0; c < 4; ++c) ab.out[c] = state + c * g.plane;
     return PT::LB::launch(unused, ab, plan.grid_b, st);
 }

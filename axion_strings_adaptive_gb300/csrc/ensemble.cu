@@ -18,7 +18,7 @@
 //
 // Device table (caller-owned, written once by axs_ensemble_init):
 //   [0, 128)                header: status word
-//   [128, 128 + 256 nboxes) two CUtensorMaps per box (state; stage buffers S3, S4)
+//   [128, 128 + 256 nboxes) two CUtensorMaps per box (state; stage increments d3, d4)
 //   then                    EnsBoxDesc[nboxes], then uint32 work items
 #include <algorithm>
 #include <cmath>
@@ -242,7 +242,8 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
             ab.map_sel = 1;
             ab.c2 = aa.c2;
             ab.c4 = stage_coef<T>(*r.bg, r.tau_i + t + r.dt);
-            for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * P;
+            for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * P;  // E, Q
+            for (int c = 0; c < 4; ++c) ab.pt[4 + c] = state + c * P;   // psi_n, Pi_n
             for (int c = 0; c < 4; ++c) ab.out[c] = state + c * P;
             if ((rc = LB::launch(unused, ab, r.plan->grid_b, r.st))) return rc;
         }

@@ -1,0 +1,338 @@
+// One-pass fused RK4 step of a periodic level (FP32).
+//
+// The two sweeps of a step (rk4_level.cu) move 28 words per site: sweep A
+// writes the stage increments (d3, d4, E, Q) to HBM and sweep B reads them
+// back. This kernel keeps them on chip. A CTA owns a TX x TY tile of the xy
+// plane over a chunk of z planes and marches in z. Per plane it
+//   - runs sweep A on the tile plus a 2-cell halo (the A region) from a TMA
+//     ring of (psi, Pi) planes with a 4-cell halo,
+//   - keeps d3, d4 (A region, 6 planes) and E, Q (tile, 4 planes) in shared
+//     memory,
+//   - runs sweep B two planes behind on the tile and writes psi, Pi of the
+//     step's end (with their periodic copies) to the other state buffer.
+// Reading one buffer and writing the other makes the tiles independent (no
+// tile reads what another writes), so the CTAs need no synchronisation with
+// each other; the level's work buffer serves as the second state buffer and
+// steps alternate between the two. A step moves 8 words per site (psi, Pi in
+// and out) plus the halo rows the L2 does not catch, against 28 for the two
+// sweeps; in return sweep A runs on (TX+4)(TY+4) sites per TX*TY.
+//
+// The per-site arithmetic is the two sweeps' own (lap_pair, stage_a,
+// stage_b), so both paths give the same bits.
+//
+// Halo: the box is (TX+16) x (TY+8) x 1 plane x 4 components, starting 8
+// columns and 4 rows before the tile. In x the level's 8 padding columns hold
+// the periodic copies; reading 8 columns (not the 4 the stencil needs) on
+// either side makes two box rows a whole number of 128-byte lines, so each
+// piece of a split box below lands 128-byte aligned. In y the padding holds 2
+// rows: tiles in the first or last row of tiles load their 4 components as
+// three pieces each (2 rows from the wrapped edge, the TY+4 rows through the
+// padding, 2 more wrapped rows). z wraps by plane index. The corners of the
+// padding are read here: the periodic stores write them.
+#pragma once
+
+#include "rk4_ops.cuh"
+
+namespace axs {
+
+template <int TX_, int TY_, int NS_, int THREADS_ = 512> struct LevelFusedShape {
+    using T = float;
+    static constexpr int V = 2, TX = TX_, TY = TY_, NS = NS_;
+    // sweep A units run on the first NA threads and sweep B units on the last NB:
+    // with 640 threads no thread runs both, so sweep B of one plane overlaps sweep
+    // A of the next; with 512 some threads run both every plane
+    static constexpr int THREADS = THREADS_;
+    static constexpr int BX = TX + 16, BY = TY + 8;  // TMA box: the A region, its stencil halo, alignment columns
+    static constexpr int AX = TX + 4, AY = TY + 4;   // A region
+    static constexpr int RING = 4 * BX * BY, SWIN = 4 * AX * AY, EQW = 4 * TX * TY;
+    // d3, d4 slots (sweep B reads 5 planes; one more so that sweep A of the next
+    // plane never overwrites a slot a slower thread still reads) and E, Q slots
+    // (written two planes before sweep B reads them, plus the same margin)
+    static constexpr int NSW = 6, NEQ = 4;
+    static_assert(NS >= 6 && NS <= 10 && NEQ == 4, "slot arithmetic below (wrap by one subtraction, E/Q by xor)");
+    static constexpr int NA = AX * AY / V;  // sweep A units (V sites each)
+    static constexpr int NB = TX * TY / V;  // sweep B units, one per thread of the last NB threads
+    static constexpr size_t SMEM = sizeof(T) * ((size_t)NS * RING + NSW * (size_t)SWIN + NEQ * (size_t)EQW);
+    static constexpr uint32_t SLOT_BYTES = RING * sizeof(T);
+    static_assert(NA <= THREADS && NB <= THREADS, "at most one unit of each sweep per thread");
+    static_assert(THREADS % 32 == 0 && THREADS <= 1024, "whole warps");
+    static_assert((2 * BX * sizeof(T)) % 128 == 0 && ((TY + 6) * BX * sizeof(T)) % 128 == 0,
+                  "the pieces of a split box land 128-byte aligned");
+    static_assert((BX * sizeof(T)) % 16 == 0, "TMA box rows of whole 16-byte units");
+    static_assert((RING * sizeof(T)) % 128 == 0 && (BX * BY * sizeof(T)) % 128 == 0, "ring slots and components");
+    static_assert(AX / V > 32 / V, "the A region is wider than one bank row");
+    static_assert(BX <= 256 && BY <= 256, "TMA box extent limit");
+    static_assert(SMEM + 1024 <= 227 * 1024, "shared memory");
+};
+
+// Shared-memory accesses by 32-bit shared address plus a compile-time byte
+// offset, one instruction each.
+template <int OFF> __device__ __forceinline__ float2 lds2(uint32_t addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(OFF));
+    return v;
+}
+template <int OFF> __device__ __forceinline__ void sts2(uint32_t addr, float x, float y)
+{
+    asm volatile("st.shared.v2.f32 [%0+%1], {%2, %3};" ::"r"(addr), "n"(OFF), "f"(x), "f"(y) : "memory");
+}
+
+// Laplacian and centre of two sites of one component: p[d] = shared address of
+// the first site in planes z-2 .. z+2, RB the row length in bytes, CO the
+// component's byte offset. The arithmetic is lap_pair's, as in every FP32 sweep.
+template <int RB, int CO>
+__device__ __forceinline__ void star_pair_sh(const SweepArgs<float> &a, const uint32_t (&p)[5], float (&lap)[2],
+                                             float (&ctr)[2])
+{
+    const float2 a0 = lds2<CO - 8>(p[2]), a1 = lds2<CO>(p[2]), a2 = lds2<CO + 8>(p[2]);
+    const float r[6] = {a0.x, a0.y, a1.x, a1.y, a2.x, a2.y};
+    lap_pair(a.wA, a.wB, r, lds2<CO - RB>(p[2]), lds2<CO + RB>(p[2]), lds2<CO - 2 * RB>(p[2]),
+             lds2<CO + 2 * RB>(p[2]), lds2<CO>(p[1]), lds2<CO>(p[3]), lds2<CO>(p[0]), lds2<CO>(p[4]), lap[0],
+             lap[1]);
+    ctr[0] = a1.x;
+    ctr[1] = a1.y;
+}
+
+// the same for the four components, CS bytes apart
+template <int RB, int CS>
+__device__ __forceinline__ void star4_sh(const SweepArgs<float> &a, const uint32_t (&p)[5], float (&lap)[4][2],
+                                         float (&ctr)[4][2])
+{
+    star_pair_sh<RB, 0 * CS>(a, p, lap[0], ctr[0]);
+    star_pair_sh<RB, 1 * CS>(a, p, lap[1], ctr[1]);
+    star_pair_sh<RB, 2 * CS>(a, p, lap[2], ctr[2]);
+    star_pair_sh<RB, 3 * CS>(a, p, lap[3], ctr[3]);
+}
+
+// The three tensor maps over one state buffer: the whole box (interior tile
+// rows), one component of TY + 4 rows, one component of 2 rows.
+struct LevelFusedMaps {
+    CUtensorMap full, mid, rows2;
+};
+
+template <class S>
+__global__ void __launch_bounds__(S::THREADS, 1)
+    level_fused_kernel(const __grid_constant__ LevelFusedMaps maps, const SweepArgs<float> a)
+{
+    using T = float;
+    constexpr int V = S::V, TX = S::TX, TY = S::TY, NS = S::NS, BX = S::BX, BY = S::BY, AX = S::AX, AY = S::AY;
+    extern __shared__ __align__(128) unsigned char lf_smem[];
+    T *ring = reinterpret_cast<T *>(lf_smem);
+    T *swin = ring + (size_t)NS * S::RING;
+    T *eqw = swin + (size_t)S::NSW * S::SWIN;
+    __shared__ uint64_t full[NS];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    constexpr int oy = 2;  // padded row of y = 0 in the level layout
+
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+        prefetch_tensormap(&maps.full);
+        prefetch_tensormap(&maps.mid);
+        prefetch_tensormap(&maps.rows2);
+    }
+    __syncthreads();
+
+    // ---- producer cursor (thread 0 only): planes z0 - 4 .. z0 + len + 3 of each item
+    int64_t p_item = blockIdx.x;
+    int p_k = 0, p_len = 0, p_z0 = 0, p_x0 = 0, p_y0 = 0;
+    bool p_edge = false;
+    auto p_start = [&]() {
+        if (p_item >= a.n_items) return;
+        const int tile = (int)(p_item % a.ntiles);
+        p_z0 = (int)(p_item / a.ntiles) * a.zchunk;
+        p_len = min(a.zchunk, nz - p_z0);
+        p_x0 = (tile % a.tiles_x) * TX;
+        p_y0 = (tile / a.tiles_x) * TY;
+        p_edge = p_y0 == 0 || p_y0 + TY == ny;  // rows y0 - 4, y0 - 3 or y0 + TY + 2, + 3 lie past the padding
+    };
+    int64_t q_issued = 0;
+    int p_slot = 0;  // ring slot of plane q_issued
+    auto issue_one = [&]() -> bool {
+        if (p_item >= a.n_items) return false;
+        int zp = (p_z0 - 4 + p_k) % nz;
+        if (zp < 0) zp += nz;
+        const int slot = p_slot;
+        if (++p_slot == NS) p_slot = 0;
+        T *dst = ring + (size_t)slot * S::RING;
+        mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
+        const int xc = a.ox - 8 + p_x0;  // padded column of the box's first column (16-byte aligned)
+        if (!p_edge) {
+            tma_load_4d(dst, &maps.full, xc, p_y0 - 4 + oy, zp, 0, &full[slot]);
+        } else {
+            const int rt = ((p_y0 - 4) % ny + ny) % ny + oy;  // rows y0 - 4, y0 - 3 (wrapped)
+            const int rb = (p_y0 + TY + 2) % ny + oy;        // rows y0 + TY + 2, + 3 (wrapped)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                T *dc = dst + (size_t)c * BX * BY;
+                tma_load_4d(dc, &maps.rows2, xc, rt, zp, c, &full[slot]);
+                tma_load_4d(dc + 2 * BX, &maps.mid, xc, p_y0 - 2 + oy, zp, c, &full[slot]);
+                tma_load_4d(dc + (TY + 6) * BX, &maps.rows2, xc, rb, zp, c, &full[slot]);
+            }
+        }
+        ++q_issued;
+        if (++p_k == p_len + 8) {
+            p_k = 0;
+            p_item += gridDim.x;
+            p_start();
+        }
+        return true;
+    };
+    if (tid == 0) {
+        p_start();
+        for (int s = 0; s < NS; ++s)
+            if (!issue_one()) break;
+    }
+
+    // sweep B unit of this thread (bt < 0: none), tile-local sites (bxl, byl) .. (bxl + V - 1, byl)
+    const int bt = tid - (S::THREADS - S::NB);
+    const bool has_b = bt >= 0;
+    const int bxl = has_b ? V * (bt % (TX / V)) : 0, byl = has_b ? bt / (TX / V) : 0;
+    // sweep A unit of this thread: units of the A region's first 32 / V columns row by
+    // row (a warp covers whole 128-byte bank rows: conflict-free), then the others
+    const bool has_a = tid < S::NA;
+    int alx = 0, aly = 0;  // A-region-local first site
+    {
+        constexpr int PR = AX / V, MAIN = 32 / V, EDGE = PR - MAIN;
+        const int u = tid;
+        const int row = u < MAIN * AY ? u / MAIN : (u - MAIN * AY) / EDGE;
+        const int col = u < MAIN * AY ? u % MAIN : MAIN + (u - MAIN * AY) % EDGE;
+        alx = V * col;
+        aly = row;
+    }
+    const int atx = alx - 2, aty = aly - 2;  // tile-local (V sites lie all inside or all outside the tile)
+    const bool a_in_tile = atx >= 0 && atx < TX && aty >= 0 && aty < TY;
+    // shared addresses of the three regions and this thread's byte offsets in them
+    const uint32_t ring_sh = smem_addr(ring), swin_sh = smem_addr(swin), eqw_sh = smem_addr(eqw);
+    const uint32_t a_at = 4u * (uint32_t)((aly + 2) * BX + (alx + 6));      // A site in the ring box
+    const uint32_t a_so = 4u * (uint32_t)(aly * AX + alx);                  // A site in the d3, d4 window
+    const uint32_t a_eo = 4u * (uint32_t)(a_in_tile ? aty * TX + atx : 0);  // A site in the E, Q window
+    const uint32_t b_ro = 4u * (uint32_t)((byl + 4) * BX + (bxl + 8));     // B site in the ring box
+    const uint32_t b_so = 4u * (uint32_t)((byl + 2) * AX + (bxl + 2));     // B site in the d3, d4 window
+    const uint32_t b_eo = 4u * (uint32_t)(byl * TX + bxl);                 // B site in the E, Q window
+
+    // Ring slots, their mbarrier phases and the window slots advance by one per
+    // plane: rotating small counters (a modulo by the slot count per plane and
+    // thread is a real cost in this issue-bound loop).
+    int r0 = 0;                   // ring slot of plane q_base + i (the oldest plane sweep A reads)
+    int w_slot = 0, w_phase = 0;  // the next plane to wait for: its slot and mbarrier parity
+    int s0 = 0, e0 = 0;           // d3, d4 slot and E, Q slot of sweep A's plane
+    int64_t q_waited = 0;
+    bool aborted = false;
+    for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+        const int tile = (int)(item % a.ntiles);
+        const int z0 = (int)(item / a.ntiles) * a.zchunk;
+        const int len = min(a.zchunk, nz - z0);
+        const int x0 = (tile % a.tiles_x) * TX, y0 = (tile / a.tiles_x) * TY;
+        // iteration i: sweep A at plane za = z0 - 2 + i (ring planes q_base + i .. + 4),
+        // sweep B at zb = za - 2 = z0 - 4 + i for i >= 4
+        for (int i = 0; i < len + 4; ++i) {
+            // planes up to q_base + i + 4 must have landed: the first iteration of an
+            // item waits for five, every later one for one more
+            for (int need = i == 0 ? 5 : 1; need > 0; --need) {
+                if (!mbar_wait_bounded(&full[w_slot], (uint32_t)w_phase)) {
+                    atomicOr(a.status, kDevTimeout);
+                    abort_flag = 1;
+                }
+                ++q_waited;
+                if (++w_slot == NS) {
+                    w_slot = 0;
+                    w_phase ^= 1;
+                }
+            }
+            uint32_t pl[5];  // shared addresses of ring planes q_base + i .. + 4
+#pragma unroll
+            for (int d = 0; d < 5; ++d) {
+                const int sd = r0 + d < NS ? r0 + d : r0 + d - NS;
+                pl[d] = ring_sh + (uint32_t)sd * (uint32_t)(S::RING * 4);
+            }
+            if (has_a && !abort_flag) {
+                uint32_t pa[5];
+#pragma unroll
+                for (int d = 0; d < 5; ++d) pa[d] = pl[d] + a_at;
+                T lap[4][V], ctr[4][V];
+                star4_sh<BX * 4, BX * BY * 4>(a, pa, lap, ctr);
+                T o[8][V];
+                stage_a<T, V>(a, lap, ctr, o);
+                const uint32_t sz = swin_sh + (uint32_t)s0 * (uint32_t)(S::SWIN * 4) + a_so;  // d3, d4 of plane za
+                sts2<0 * AX * AY * 4>(sz, o[0][0], o[0][1]);
+                sts2<1 * AX * AY * 4>(sz, o[1][0], o[1][1]);
+                sts2<2 * AX * AY * 4>(sz, o[2][0], o[2][1]);
+                sts2<3 * AX * AY * 4>(sz, o[3][0], o[3][1]);
+                if (a_in_tile) {
+                    const uint32_t ez = eqw_sh + (uint32_t)e0 * (uint32_t)(S::EQW * 4) + a_eo;  // E, Q of plane za
+                    sts2<0 * TX * TY * 4>(ez, o[4][0], o[4][1]);
+                    sts2<1 * TX * TY * 4>(ez, o[5][0], o[5][1]);
+                    sts2<2 * TX * TY * 4>(ez, o[6][0], o[6][1]);
+                    sts2<3 * TX * TY * 4>(ez, o[7][0], o[7][1]);
+                }
+            }
+            // sweep B's psi_n, Pi_n at plane zb: ring plane q_base + i, refilled after the barrier
+            float2 pn[4];
+            if (has_b && i >= 4 && !abort_flag) {
+                const uint32_t r0p = pl[0] + b_ro;
+                pn[0] = lds2<0 * BX * BY * 4>(r0p);
+                pn[1] = lds2<1 * BX * BY * 4>(r0p);
+                pn[2] = lds2<2 * BX * BY * 4>(r0p);
+                pn[3] = lds2<3 * BX * BY * 4>(r0p);
+            }
+            __syncthreads();  // d3, d4, E, Q of plane za are in place; ring plane q_base + i is read no more
+            if (abort_flag) {
+                aborted = true;
+                break;
+            }
+            if (tid == 0) {
+                // the oldest plane still needed: q_base + i + 1, or the next item's first
+                const int64_t next_needed = q_waited - 4 + (i + 1 < len + 4 ? 0 : 4);
+                fence_proxy_async_smem();
+                while (q_issued < next_needed + NS && issue_one()) {
+                }
+            }
+            if (has_b && i >= 4) {
+                const int zb = z0 - 4 + i;
+                const int b0 = s0 + 2 < S::NSW ? s0 + 2 : s0 + 2 - S::NSW;  // slot of plane za - 4 = zb - 2
+                uint32_t sp[5];
+#pragma unroll
+                for (int d = 0; d < 5; ++d) {
+                    const int sd = b0 + d < S::NSW ? b0 + d : b0 + d - S::NSW;
+                    sp[d] = swin_sh + (uint32_t)sd * (uint32_t)(S::SWIN * 4) + b_so;
+                }
+                const uint32_t ez = eqw_sh + (uint32_t)(e0 ^ 2) * (uint32_t)(S::EQW * 4) + b_eo;  // E, Q of plane zb
+                T lap[4][V], ctr[4][V], o[4][V], pq[8][V];
+                star4_sh<AX * 4, AX * AY * 4>(a, sp, lap, ctr);
+                const float2 e[4] = {lds2<0 * TX * TY * 4>(ez), lds2<1 * TX * TY * 4>(ez), lds2<2 * TX * TY * 4>(ez),
+                                     lds2<3 * TX * TY * 4>(ez)};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    pq[c][0] = e[c].x;
+                    pq[c][1] = e[c].y;
+                    pq[4 + c][0] = pn[c].x;
+                    pq[4 + c][1] = pn[c].y;
+                }
+                stage_b<T, V>(a, lap, ctr, pq, o);
+                const int x = x0 + bxl, y = y0 + byl;
+                const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + oy) * a.js + (int64_t)zb * a.ks;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, nx, ny, a.js, o[c]);
+            }
+            if (++r0 == NS) r0 = 0;
+            if (++s0 == S::NSW) s0 = 0;
+            e0 = (e0 + 1) & (S::NEQ - 1);
+        }
+        if (aborted) break;
+        // the next item's window starts 4 planes past this item's last window start + 1
+        r0 += 4;
+        if (r0 >= NS) r0 -= NS;
+    }
+    // A wait expired: make sure no bulk copy is still landing in shared memory
+    // before the block exits (bounded as well).
+    if (aborted && tid == 0) {
+        for (int64_t q = q_waited; q < q_issued; ++q) mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 1u << 20);
+    }
+}
+
+}  // namespace axs

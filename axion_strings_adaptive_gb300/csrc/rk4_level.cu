@@ -7,12 +7,15 @@
 // so the four stage RHS evaluations pair up:
 //   sweep A reads (psi_n, Pi_n) and evaluates F1 = F(t, psi_n),
 //                                             F2 = F(t+h/2, psi_n + h/2 Pi_n);
-//   sweep B reads (S3, S4)      and evaluates F3 = F(t+h/2, S3), F4 = F(t+h, S4),
-// with S3 = psi_n + h/2 Pi_n + h^2/4 F1, S4 = psi_n + h Pi_n + h^2/2 F2 and
-//   psi_{n+1} = S4 + h^2/6 (F1 - 2 F2 + F3),
-//   Pi_{n+1}  = [Pi_n + h/6 F1 + h/3 F2] + h/3 F3 + h/6 F4,
-// which is classic RK4 term for term (exact arithmetic). Per site and step
-// the sweeps move 4+8 and 8+4 words: 24 words instead of the 64 of a
+//   sweep B reads (d3, d4)      and evaluates F3 = F(t+h/2, S3), F4 = F(t+h, S4),
+// with S3 = psi_n + d3, d3 = h/2 Pi_n + h^2/4 F1, S4 = psi_n + d4,
+// d4 = h Pi_n + h^2/2 F2, and
+//   psi_{n+1} = psi_n + h Pi_n + h^2/6 (F1 + F2 + F3),
+//   Pi_{n+1}  = Pi_n + h/6 F1 + h/3 F2 + h/3 F3 + h/6 F4,
+// which is classic RK4 term for term (exact arithmetic). Sweep A stores only
+// increments (d3, d4 and the parts E, Q of the two updates known after F1,
+// F2; rk4_ops.cuh), so the state is rounded once per step. Per site and step
+// the sweeps move 4+8 and 12+4 words: 28 words instead of the 64 of a
 // stage-by-stage three-register RK4.
 //
 // Each sweep is a persistent kernel. A block owns a TX x TY tile of the xy
@@ -29,6 +32,7 @@
 #include <cmath>
 #include <vector>
 
+#include "level_fused.cuh"
 #include "rk4_ops.cuh"
 
 namespace axs {
@@ -141,11 +145,83 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
                 ab.zchunk = tmp.zchunk;
                 ab.c2 = stage_coef<T>(*r.bg, r.tau_i + t + 0.5 * r.dt);
                 ab.c4 = stage_coef<T>(*r.bg, r.tau_i + t + r.dt);
-                for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.cs;
+                for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.cs;  // E, Q
+                for (int c = 0; c < 4; ++c) ab.pt[4 + c] = state + c * g.cs;   // psi_n, Pi_n
                 for (int c = 0; c < 4; ++c) ab.out[c] = state + c * g.cs;
                 if ((rc = LB::launch(map_work, ab, grid_b, r.st))) return rc;
             }
         }
+        return AXS_OK;
+    }
+};
+
+// The one-pass fused step (level_fused.cuh) over FP32 levels whose extents are
+// multiples of its tile; single sweeps and other extents run the two sweeps of
+// the default tiling. Steps alternate between the level's state and the first
+// 4 component planes of its work buffer (same layout); after an odd number of
+// steps one copy brings the result back into the state.
+template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
+    using S = LevelFusedShape<TX, TY, NS, THREADS>;
+    using Fallback = SweepConfig<float, 2, 64, 8, 8, 2>;
+
+    static bool applies(const axs_level *lv)
+    {
+        return lv->dtype == AXS_F32 && lv->nx % TX == 0 && lv->ny % TY == 0;
+    }
+
+    static int maps_for(LevelFusedMaps &m, const float *base, const LevelGeom &g, int ny, int nz)
+    {
+        const uint64_t es = sizeof(float);
+        int rc = make_tensor_map_4d(&m.full, base, AXS_F32, g.js, ny + 4, nz, 4, g.js * es, g.ks * es, g.cs * es,
+                                    S::BX, S::BY, 1, 4);
+        if (rc) return rc;
+        if ((rc = make_tensor_map_4d(&m.mid, base, AXS_F32, g.js, ny + 4, nz, 4, g.js * es, g.ks * es, g.cs * es,
+                                     S::BX, TY + 4, 1, 1)))
+            return rc;
+        return make_tensor_map_4d(&m.rows2, base, AXS_F32, g.js, ny + 4, nz, 4, g.js * es, g.ks * es, g.cs * es,
+                                  S::BX, 2, 1, 1);
+    }
+
+    static int run(const SweepRunArgs &r)
+    {
+        const axs_level *lv = r.lv;
+        if (r.sweep_mask != 3 || !applies(lv)) return Fallback::run(r);
+        const LevelGeom &g = *r.g;
+        static int smem_set = 0;
+        auto kern = level_fused_kernel<S>;
+        if (!smem_set) {
+            AXS_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM));
+            smem_set = 1;
+        }
+        const int sms = device_sm_count();
+        AXS_REQUIRE(sms > 0, AXS_ERR_CUDA, "no CUDA device");
+        SweepArgs<float> a{};
+        a.nx = lv->nx;
+        a.ny = lv->ny;
+        a.nz = lv->nz;
+        a.tiles_x = lv->nx / TX;
+        a.ntiles = a.tiles_x * (lv->ny / TY);
+        int grid = 0;
+        plan_chunks(a.ntiles, lv->nz, sms, a.zchunk, a.n_items, grid);
+        fill_level_constants(a, lv, g, r.dt);
+        float *buf[2] = {static_cast<float *>(lv->state), static_cast<float *>(lv->work)};
+        LevelFusedMaps maps[2];
+        int rc;
+        for (int b = 0; b < 2; ++b)
+            if ((rc = maps_for(maps[b], buf[b], g, lv->ny, lv->nz))) return rc;
+        for (int s = 0; s < r.nsteps; ++s) {
+            const double t = r.t0 + s * r.dt;
+            SweepArgs<float> as = a;
+            as.c1 = stage_coef<float>(*r.bg, r.tau_i + t);
+            as.c2 = stage_coef<float>(*r.bg, r.tau_i + t + 0.5 * r.dt);
+            as.c4 = stage_coef<float>(*r.bg, r.tau_i + t + r.dt);
+            float *dst = buf[(s + 1) & 1];
+            for (int c = 0; c < 4; ++c) as.out[c] = dst + c * g.cs;
+            kern<<<grid, S::THREADS, S::SMEM, r.st>>>(maps[s & 1], as);
+            if ((rc = launch_status("fused level step"))) return rc;
+        }
+        if (r.nsteps & 1)
+            AXS_CUDA_CHECK(cudaMemcpyAsync(buf[0], buf[1], 4 * g.cs * sizeof(float), cudaMemcpyDeviceToDevice, r.st));
         return AXS_OK;
     }
 };
@@ -172,6 +248,11 @@ static const TileConfigEntry kF32Configs[] = {
     {"f32 v2 32x16 ring8 l2", &SweepConfig<float, 2, 32, 16, 8, 2, true>::run},
     {"f32 v2 32x8 ring8 l2", &SweepConfig<float, 2, 32, 8, 8, 3, true>::run},
     {"f32 v4 64x16 ring6 l2", &SweepConfig<float, 4, 64, 16, 6, 1, true>::run},
+    // one-pass fused step (level_fused.cuh)
+    {"f32 fused 32x16 ring6", &FusedConfig<32, 16, 6>::run},
+    {"f32 fused 32x16 ring7", &FusedConfig<32, 16, 7>::run},
+    {"f32 fused 32x16 ring6 t640", &FusedConfig<32, 16, 6, 640>::run},
+    {"f32 fused 32x16 ring7 t640", &FusedConfig<32, 16, 7, 640>::run},
 };
 static const TileConfigEntry kF64Configs[] = {
     {"f64 v1 32x8 ring6", &SweepConfig<double, 1, 32, 8, 6, 2>::run},

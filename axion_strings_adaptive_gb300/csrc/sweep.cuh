@@ -139,19 +139,30 @@ __device__ __forceinline__ void st_out(T *p, const T *v, uint64_t pol)
 }
 
 // Store V sites and, for sites next to the domain edge, their periodic copies
-// in the x/y padding (8 columns, 2 rows). The stencils read 4 padding columns;
-// 8 fill whole 32-byte sectors (FP32; two for FP64), since a partly written
-// sector costs a DRAM read on top of its write.
+// in the x/y padding (8 columns, 2 rows, and the corners where both meet).
+// The sweeps' stencils read 4 padding columns; 8 fill whole 32-byte sectors
+// (FP32; two for FP64), since a partly written sector costs a DRAM read on top
+// of its write. The one-pass level step reads all 8 columns and the corners.
 template <typename T, int V, bool HINT = false>
 __device__ __forceinline__ void store_with_copies(T *base, int64_t off, int x, int y, int nx, int ny, int64_t js,
                                                   const T *v, uint64_t pol = 0, bool periodic = true)
 {
     st_out<T, V, HINT>(base + off, v, pol);
     if (!periodic) return;
-    if (x < 8) st_out<T, V, HINT>(base + off + nx, v, pol);
-    if (x >= nx - 8) st_out<T, V, HINT>(base + off - nx, v, pol);
-    if (y < 2) st_out<T, V, HINT>(base + off + (int64_t)ny * js, v, pol);
-    if (y >= ny - 2) st_out<T, V, HINT>(base + off - (int64_t)ny * js, v, pol);
+    const bool xl = x < 8, xh = x >= nx - 8;
+    const int64_t sy = (int64_t)ny * js;
+    if (xl) st_out<T, V, HINT>(base + off + nx, v, pol);
+    if (xh) st_out<T, V, HINT>(base + off - nx, v, pol);
+    if (y < 2) {
+        st_out<T, V, HINT>(base + off + sy, v, pol);
+        if (xl) st_out<T, V, HINT>(base + off + sy + nx, v, pol);
+        if (xh) st_out<T, V, HINT>(base + off + sy - nx, v, pol);
+    }
+    if (y >= ny - 2) {
+        st_out<T, V, HINT>(base + off - sy, v, pol);
+        if (xl) st_out<T, V, HINT>(base + off - sy + nx, v, pol);
+        if (xh) st_out<T, V, HINT>(base + off - sy - nx, v, pol);
+    }
 }
 
 // Two FP32 sites per instruction: Blackwell's packed FP32x2 add, multiply and
@@ -187,7 +198,7 @@ __device__ __forceinline__ void rhs_pair(const StageCoef<T> &c, T u1, T u2, T l1
 // the same for two sites at once
 __device__ __forceinline__ void rhs_pair(const StageCoef<float> &c, F2 u1, F2 u2, F2 l1, F2 l2, F2 &f1, F2 &f2)
 {
-    const F2 k = fma(F2(-c.hlam), fma(u1, u1, u2 * u2) - F2(c.R2), F2(c.kappa));
+    const F2 k = fma(F2(-c.hlam), fma(u1, u1, u2 * u2) + F2(-c.R2), F2(c.kappa));
     f1 = fma(k, u1, l1);
     f2 = fma(k, u2, l2);
 }
@@ -202,6 +213,27 @@ __device__ __forceinline__ void rhs_adjoint_pair(const StageCoef<T> &c, T u1, T 
     const T ua = T(2) * c.hlam * fma(u1, a1, u2 * a2);
     o1 = fma(k, a1, la1) - ua * u1;
     o2 = fma(k, a2, la2) - ua * u2;
+}
+
+// The FP32 Laplacian of two neighbouring sites x, x+1 from their neighbours:
+// r[0..5] = f(x-2 .. x+3) along the row, and the y / z neighbour pairs. The
+// stencil as differences from the centre, lap = wA sum(f+-1 - f0) + wB
+// sum(f+-2 - f0): a neighbour within a factor 2 of f0 gives an exact
+// difference, so the -30 f0 term of the plain sum does not cancel against the
+// neighbours. f - f0 is formed as f + (-f0), the same IEEE result. Every FP32
+// sweep evaluates its stencils through this function.
+__device__ __forceinline__ void lap_pair(float wA, float wB, const float *r, float2 ym1, float2 yp1, float2 ym2,
+                                         float2 yp2, float2 zm1, float2 zp1, float2 zm2, float2 zp2, float &l0,
+                                         float &l1)
+{
+    const F2 m0(-r[2], -r[3]);
+    const F2 d1 = ((F2(r[1], r[2]) + m0) + (F2(r[3], r[4]) + m0)) + ((F2(ym1) + m0) + (F2(yp1) + m0)) +
+                  ((F2(zm1) + m0) + (F2(zp1) + m0));
+    const F2 d2 = ((F2(r[0], r[1]) + m0) + (F2(r[4], r[5]) + m0)) + ((F2(ym2) + m0) + (F2(yp2) + m0)) +
+                  ((F2(zm2) + m0) + (F2(zp2) + m0));
+    const F2 l = fma(F2(wA), d1, F2(wB) * d2);
+    l0 = l.v.x;
+    l1 = l.v.y;
 }
 
 // The 13-point 4th-order Laplacian and the centre values of V consecutive
@@ -234,18 +266,12 @@ __device__ __forceinline__ void star_laplacian(const SweepArgs<T> &a, const T *z
 #pragma unroll
         for (int v = 0; v < V; v += 2) {
             const int ci = PRE * V + v;
-            const F2 f0(row[ci], row[ci + 1]);
-            const F2 d1 = ((F2(row[ci - 1], row[ci]) - f0) + (F2(row[ci + 1], row[ci + 2]) - f0)) +
-                          ((F2(ym1[v], ym1[v + 1]) - f0) + (F2(yp1[v], yp1[v + 1]) - f0)) +
-                          ((F2(zm1[v], zm1[v + 1]) - f0) + (F2(zp1[v], zp1[v + 1]) - f0));
-            const F2 d2 = ((F2(row[ci - 2], row[ci - 1]) - f0) + (F2(row[ci + 2], row[ci + 3]) - f0)) +
-                          ((F2(ym2[v], ym2[v + 1]) - f0) + (F2(yp2[v], yp2[v + 1]) - f0)) +
-                          ((F2(zm2[v], zm2[v + 1]) - f0) + (F2(zp2[v], zp2[v + 1]) - f0));
-            const F2 l = fma(F2(a.wA), d1, F2(a.wB) * d2);
-            lap[v] = l.v.x;
-            lap[v + 1] = l.v.y;
-            ctr[v] = f0.v.x;
-            ctr[v + 1] = f0.v.y;
+            lap_pair(a.wA, a.wB, row + ci - 2, make_float2(ym1[v], ym1[v + 1]), make_float2(yp1[v], yp1[v + 1]),
+                     make_float2(ym2[v], ym2[v + 1]), make_float2(yp2[v], yp2[v + 1]), make_float2(zm1[v], zm1[v + 1]),
+                     make_float2(zp1[v], zp1[v + 1]), make_float2(zm2[v], zm2[v + 1]), make_float2(zp2[v], zp2[v + 1]),
+                     lap[v], lap[v + 1]);
+            ctr[v] = row[ci];
+            ctr[v + 1] = row[ci + 1];
         }
     } else {
 #pragma unroll

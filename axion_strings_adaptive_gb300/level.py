@@ -201,10 +201,12 @@ class PeriodicLevel:
         d = _DT[self.dtype]
         return [(i, lib.axs_level_tile_config_name(d, i).decode()) for i in range(1, lib.axs_level_tile_config_count(d) + 1)]
 
-    def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 3, repeats: int = 2,
+    def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 4, repeats: int = 2,
                  stream=None) -> dict:
-        """Time every compiled sweep tiling on this level (full RK4 steps, CUDA
-        events) and keep the fastest. The state is saved and restored, so the
+        """Time every compiled tiling on this level (the two-sweep tilings and
+        the one-pass fused step; full RK4 steps, CUDA events) and keep the
+        fastest. An even step count times the fused step without the copy an
+        odd count ends with. The state is saved and restored, so the
         level's contents are unchanged. Returns {name: ms_per_step}."""
         saved = self.state.clone()
         timings = {}

@@ -4,11 +4,12 @@ Workload (native arm, N=1): uniform periodic 512^3 box, Moore mode (c0 = 2),
 lambda0 = 2, radiation domination (a_inv = 2), dx = 0.5, dt = 0.1, seeded
 Gaussian Fourier initial data with |n| < N/8 (k < 2 pi/(8 dx)), Pi = 0;
 FP32 fields (the reference's default PRECISION=FLOAT), FP64 background.
-One "step" = one classic-RK4 step of the whole box (two fused sweeps).
+One "step" = one classic-RK4 step of the whole box: one launch of the one-pass
+fused step, or sweep A and sweep B, whichever tiling the autotuner picks.
 
 Reported on one JSON line: whole-job site-updates/s (value), the FP64 path on
 the same box, FP32-vs-FP64 energy / xi / string-count error after a short
-evolution, the roofline of the dominant sweep kernel, an end-to-end number
+evolution, the roofline of the dominant step kernel, an end-to-end number
 through the C ABI with host buffers, the CPU oracle baseline and the SM
 clocks sampled during the timed region.
 
@@ -35,7 +36,6 @@ N_DEFAULT = 512
 DX, DT, TAU_I = 0.5, 0.1, 1.0
 A_INV, C0, LAMBDA0 = 2.0, 2.0, 2.0
 SEED = 20261203
-WORDS_PER_SITE = {"sweep_A": 12, "sweep_B": 12}  # compulsory words per site per launch (read + write)
 
 
 def _dist():
@@ -461,36 +461,65 @@ def run_native(args):
         return replica_max(x, ws, dev)
 
     def timed_run(level, steps, warmup, t_start=0.0, sample_clocks=False):
+        """K RK4 steps of `level`, CUDA events on the launching stream around every
+        kernel launch. Two-sweep tilings: sweep A and sweep B each step. The fused
+        step: one launch per step, timed in pairs of steps (a pair returns the
+        state to the level's state buffer; an odd K ends with one step and the
+        copy back). Returns (total ms, {kernel: mean ms per launch}, clocks)."""
+        fused = "fused" in level_config_name(level)
         for w in range(warmup):
             level.advance(bg, TAU_I, t_start + w * DT, DT, 1)
         t0 = t_start + warmup * DT
-        evA = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        evB = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+        e0, e1 = ev(), ev()
         sampler = ClockSampler(local) if sample_clocks else None
         if sampler:
             sampler.start()
             time.sleep(0.3)
+        marks = []
         barrier()
         torch.cuda.synchronize()
         e0.record()
-        for s in range(steps):
-            t = t0 + s * DT
-            evA[s][0].record()
-            level.sweep(bg, TAU_I, t, DT, 0)
-            evA[s][1].record()
-            evB[s][0].record()
-            level.sweep(bg, TAU_I, t, DT, 1)
-            evB[s][1].record()
+        if fused:
+            s = 0
+            while s < steps:
+                k = 2 if s + 2 <= steps else 1
+                a_, b_ = ev(), ev()
+                a_.record()
+                level.advance(bg, TAU_I, t0 + s * DT, DT, k)
+                b_.record()
+                marks.append((k, a_, b_))
+                s += k
+        else:
+            for s in range(steps):
+                t = t0 + s * DT
+                ea, eb, ec = ev(), ev(), ev()
+                ea.record()
+                level.sweep(bg, TAU_I, t, DT, 0)
+                eb.record()
+                level.sweep(bg, TAU_I, t, DT, 1)
+                ec.record()
+                marks.append((ea, eb, ec))
         e1.record()
         torch.cuda.synchronize()
         barrier()
         clocks = sampler.stop() if sampler else None
         level.device_status()
         ms = e0.elapsed_time(e1)
-        a = sum(x.elapsed_time(y) for x, y in evA) / steps
-        b = sum(x.elapsed_time(y) for x, y in evB) / steps
-        return ms, a, b, clocks
+        if fused:
+            pairs = [x.elapsed_time(y) / 2 for k, x, y in marks if k == 2]
+            per = {"rk4_fused_level": sum(pairs) / len(pairs)} if pairs else \
+                {"rk4_fused_level": marks[0][1].elapsed_time(marks[0][2])}
+        else:
+            per = {"rk4_sweep_A": sum(a_.elapsed_time(b_) for a_, b_, c_ in marks) / steps,
+                   "rk4_sweep_B": sum(b_.elapsed_time(c_) for a_, b_, c_ in marks) / steps}
+        return ms, per, clocks
+
+    def level_config_name(level):
+        return dict(level.tile_configs())[level.tile_config] if level.tile_config else "default"
+
+    # algorithmic words per site and launch (read + write, each compulsory word once)
+    WORDS = {"rk4_sweep_A": 12, "rk4_sweep_B": 16, "rk4_fused_level": 8}
 
     # ---------------- FP32 (headline)
     lv32 = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev, pierced_capacity=1024)
@@ -498,8 +527,8 @@ def run_native(args):
     tune32 = None
     if not args.no_autotune:
         tune32 = lv32.autotune(bg, TAU_I, DT)
-    cfg32 = dict(lv32.tile_configs())[lv32.tile_config] if lv32.tile_config else "default"
-    ms, msA, msB, clocks = timed_run(lv32, args.steps, args.warmup, sample_clocks=True)
+    cfg32 = level_config_name(lv32)
+    ms, per32, clocks = timed_run(lv32, args.steps, args.warmup, sample_clocks=True)
     ms_max = allmax(ms)
     value = ws * n ** 3 * args.steps / (ms_max * 1e-3)
     es32 = 4
@@ -511,22 +540,25 @@ def run_native(args):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    dom, dom_ms = ("rk4_sweep_A", msA) if msA >= msB else ("rk4_sweep_B", msB)
-    bytes_per_launch = 12 * es32 * n ** 3
+    dom, dom_ms = max(per32.items(), key=lambda kv: kv[1])
+    bytes_per_launch = WORDS[dom] * es32 * n ** 3
     achieved = bytes_per_launch / (dom_ms * 1e-3) / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "rk4_sweep_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             t = json.load(f)
-        key = "sweep_A_bytes_per_site_f32" if dom.endswith("A") else "sweep_B_bytes_per_site_f32"
+        key = {"rk4_sweep_A": "sweep_A_bytes_per_site_f32", "rk4_sweep_B": "sweep_B_bytes_per_site_f32",
+               "rk4_fused_level": "fused_level_bytes_per_site_f32"}[dom]
         if key in t:
             traffic = t[key] * n ** 3
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": traffic, "kernel": dom, "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
-                "sweep_ms": {"A": msA, "B": msB},
+                "algorithmic_words_per_site": WORDS[dom],
+                "kernel_ms": per32,
                 "frac_of_nominal_8TBs": achieved / 8000.0}
+    launches32 = args.steps if "rk4_fused_level" in per32 else 2 * args.steps
 
     # ---------------- fused diagnostics pass (string finder + energies + velocities) on the FP32 box
     diag = None
@@ -625,10 +657,10 @@ def run_native(args):
         lv64.set_state(ic64)
         tune64 = None if args.no_autotune else lv64.autotune(bg, TAU_I, DT, steps=2, repeats=1)
         k64 = max(2, args.steps // 4)
-        ms64, a64, b64, _ = timed_run(lv64, k64, 1)
+        ms64, per64, _ = timed_run(lv64, k64, 1)
         v64 = ws * n ** 3 * k64 / (allmax(ms64) * 1e-3)
-        fp64 = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "sweep_ms": {"A": a64, "B": b64},
-                "tile_config": dict(lv64.tile_configs())[lv64.tile_config] if lv64.tile_config else "default",
+        fp64 = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "kernel_ms": per64,
+                "tile_config": level_config_name(lv64),
                 "autotune_ms_per_step": tune64}
         del lv64
         torch.cuda.empty_cache()
@@ -775,7 +807,7 @@ def run_native(args):
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": _config(n), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clocks, "gpu_launches": 2 * args.steps, "tile_config": cfg32,
+                "clocks": clocks, "gpu_launches": launches32, "tile_config": cfg32,
                 "autotune_ms_per_step": tune32, "diagnostics": diag, "fp64": fp64,
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision,
                 "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None,
