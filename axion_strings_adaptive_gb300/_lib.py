@@ -22,6 +22,8 @@ AXS_ERR_CUDA = 5
 AXS_ERR_DEVICE_TIMEOUT = 6
 AXS_ERR_CAPACITY = 7
 
+AXS_DEFAULT_WAIT_POLLS = 4194304
+
 AXS_F32, AXS_F64 = 1, 2
 BG_EXPANDING, BG_FLAT, BG_PRE_EVOLUTION = 0, 1, 2
 MASK_NONE, MASK_A, MASK_B = 0, 1, 2
@@ -121,6 +123,9 @@ SIGNATURES = {
     "axs_status_string": (C.c_char_p, [C.c_int]),
     "axs_last_error": (C.c_char_p, []),
     "axs_abi_version": (C.c_int, []),
+    "axs_set_device_wait_polls": (_i32, [C.c_uint32, C.POINTER(C.c_uint32)]),
+    "axs_count_nonfinite": (_i32, [C.POINTER(Fab), _ptr, _ptr]),
+    "axs_level_count_nonfinite": (_i32, [C.POINTER(LevelC), _ptr, _ptr]),
     "axs_eval_rhs": (_i32, [C.POINTER(Fab), C.POINTER(Fab), _dbl, C.POINTER(RhsCoeffs), _ptr]),
     "axs_fill_periodic_ghosts": (_i32, [C.POINTER(Fab), _ptr]),
     "axs_lincomb": (_i32, [C.POINTER(Fab), C.POINTER(Fab), _dbl, C.POINTER(Fab), _ptr]),
@@ -219,3 +224,11 @@ def check(status: int) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(lib(), name)(*args))
+
+
+def set_device_wait_polls(polls: int) -> int:
+    """Polls a bounded device-side wait makes before it gives up (0: at once,
+    for testing the timeout path); returns the previous value."""
+    prev = C.c_uint32()
+    call("axs_set_device_wait_polls", int(polls), C.byref(prev))
+    return prev.value

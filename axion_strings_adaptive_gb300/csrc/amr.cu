@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(Fused<T>::THREADS, 1) patch_fused_kernel(T *__
     // iteration i: sweep A at plane za = i - 2 (reads planes k = i .. i + 4), sweep B at zb = za - 2
     for (int i = 0; i < n + 4; ++i) {
         while (waited <= i + 4) {
-            if (!mbar_wait_bounded(&full[waited % F::NS], (uint32_t)((waited / F::NS) & 1))) {
+            if (!mbar_wait_bounded(&full[waited % F::NS], (uint32_t)((waited / F::NS) & 1), a.wait_polls)) {
                 if (ok) atomicOr(a.status, kDevTimeout);
                 ok = false;
             }

@@ -60,6 +60,10 @@ int level_geom(int32_t dtype, int nx, int ny, int nz, LevelGeom &g);
 void background_values(const axs_background &bg, double tau, axs_background_values &v);
 void rhs_coeffs(const axs_background &bg, double tau, axs_rhs_coeffs &c);
 
+// Polls a bounded device-side wait may make before it gives up (library-wide,
+// set by axs_set_device_wait_polls; read into each launch's arguments).
+uint32_t device_wait_polls();
+
 // ---------------------------------------------------------------- device status words
 // Codes OR-ed into a device status word by kernels whose bounded waits expire.
 constexpr unsigned kDevTimeout = 1u;

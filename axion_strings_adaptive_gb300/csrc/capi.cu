@@ -1,6 +1,7 @@
 // C-ABI plumbing: error reporting, host-side background/xi models, tensor-map
 // creation, and the two small device entry points that need no tiling
 // (winding known-answer batch, Fourier-IC spectral fill).
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -18,6 +19,10 @@ void set_error(const char *fmt, ...)
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
 }
+
+static std::atomic<uint32_t> g_wait_polls{AXS_DEFAULT_WAIT_POLLS};
+
+uint32_t device_wait_polls() { return g_wait_polls.load(std::memory_order_relaxed); }
 
 int device_sm_count()
 {
@@ -253,6 +258,13 @@ extern "C" {
 const char *axs_last_error(void) { return g_err; }
 
 int axs_abi_version(void) { return AXS_ABI_VERSION; }
+
+int axs_set_device_wait_polls(uint32_t polls, uint32_t *previous)
+{
+    const uint32_t prev = g_wait_polls.exchange(polls);
+    if (previous) *previous = prev;
+    return AXS_OK;
+}
 
 const char *axs_status_string(int s)
 {

@@ -517,18 +517,33 @@ int axs_ensemble_diagnostics(const axs_ensemble *e, const axs_diag_params *p, ax
     std::lock_guard<std::mutex> lock(g_lanes_mu);  // the lanes' streams and events are shared: one call at a time
     cudaStream_t st = (cudaStream_t)stream;
     AXS_CUDA_CHECK(cudaEventRecord(L->fork, st));
-    for (int i = 0; i < lanes; ++i) AXS_CUDA_CHECK(cudaStreamWaitEvent(L->s[i], L->fork, 0));
+    // Fork: a lane whose wait could not be recorded is left out of the work and
+    // the join (it was never forked). The first CUDA error is kept and returned.
+    bool forked[kDiagLanes] = {};
+    cudaError_t first = cudaSuccess;
+    for (int i = 0; i < lanes; ++i) {
+        const cudaError_t e_ = cudaStreamWaitEvent(L->s[i], L->fork, 0);
+        forked[i] = e_ == cudaSuccess;
+        if (e_ != cudaSuccess && first == cudaSuccess) first = e_;
+    }
     const int64_t es = (int64_t)dtype_size(e->dtype);
-    for (int b = 0; b < e->nboxes && rc == AXS_OK; ++b) {
+    for (int b = 0; b < e->nboxes && rc == AXS_OK && first == cudaSuccess; ++b) {
         const int i = b % lanes;
         const void *base = static_cast<const char *>(e->state) + geo.base[b] * es;
         rc = diag_level_box(base, e->dtype, e->dims[3 * b], e->dims[3 * b + 1], e->dims[3 * b + 2], geo.g[b], p,
                             result_dev + b, static_cast<char *>(scratch) + i * slice, slice, L->s[i]);
     }
-    // join every lane back, also after an error, so no lane is left forked from a capture
+    // Join every forked lane back, after an error too, so that no lane is left
+    // forked from a capturing stream; keep going past a failed join.
     for (int i = 0; i < lanes; ++i) {
-        AXS_CUDA_CHECK(cudaEventRecord(L->join[i], L->s[i]));
-        AXS_CUDA_CHECK(cudaStreamWaitEvent(st, L->join[i], 0));
+        if (!forked[i]) continue;
+        cudaError_t e_ = cudaEventRecord(L->join[i], L->s[i]);
+        if (e_ == cudaSuccess) e_ = cudaStreamWaitEvent(st, L->join[i], 0);
+        if (e_ != cudaSuccess && first == cudaSuccess) first = e_;
+    }
+    if (first != cudaSuccess) {
+        set_error("ensemble diagnostics: fork/join of the lane streams failed: %s", cudaGetErrorString(first));
+        return AXS_ERR_CUDA;
     }
     return rc;
 }

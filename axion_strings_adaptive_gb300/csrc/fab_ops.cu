@@ -262,6 +262,24 @@ __global__ void level_handoff_kernel(T *lv, int nx, int ny, int nz, LevelGeom g,
     }
 }
 
+// Cells (valid region from `base`, strides js, ks, cs) with a non-finite
+// component, summed per warp and added to *count with one atomic per warp.
+template <typename T>
+__global__ void count_nonfinite_kernel(const T *__restrict__ base, int nx, int ny, int nz, int64_t js, int64_t ks,
+                                       int64_t cs, unsigned long long *__restrict__ count)
+{
+    const int64_t n = (int64_t)nx * ny * nz;
+    unsigned long long c = 0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(q % nx), y = (int)((q / nx) % ny), z = (int)(q / ((int64_t)nx * ny));
+        const T *p = base + x + (int64_t)y * js + (int64_t)z * ks;
+        const bool bad = !isfinite(p[0]) || !isfinite(p[cs]) || !isfinite(p[2 * cs]) || !isfinite(p[3 * cs]);
+        c += bad ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
 static int grid_for(int64_t n)
 {
     const int sms = device_sm_count();
@@ -352,6 +370,44 @@ int axs_level_handoff_rescale(const axs_level *lv, double R_pre, double R_pre_pr
                                                                  (float)R_main, (float)R_main_prime);
     if ((rc = launch_status("handoff rescale"))) return rc;
     return level_fill_ghosts(lv->state, lv->dtype, lv->nx, lv->ny, lv->nz, g, 4, st);
+}
+
+static int count_nonfinite(const void *base, int32_t dtype, int nx, int ny, int nz, int64_t js, int64_t ks,
+                           int64_t cs, int64_t *count_dev, cudaStream_t st)
+{
+    AXS_REQUIRE(count_dev != nullptr, AXS_ERR_INVALID_ARGUMENT, "null count");
+    AXS_CUDA_CHECK(cudaMemsetAsync(count_dev, 0, sizeof(int64_t), st));
+    const int64_t n = (int64_t)nx * ny * nz;
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(count_dev);
+    if (dtype == AXS_F64)
+        count_nonfinite_kernel<double><<<grid_for(n), 256, 0, st>>>(static_cast<const double *>(base), nx, ny, nz, js,
+                                                                    ks, cs, cnt);
+    else
+        count_nonfinite_kernel<float><<<grid_for(n), 256, 0, st>>>(static_cast<const float *>(base), nx, ny, nz, js,
+                                                                   ks, cs, cnt);
+    return launch_status("non-finite count");
+}
+
+int axs_count_nonfinite(const axs_fab *state, int64_t *count_dev, void *stream)
+{
+    int rc = validate_fab(state, "state", 4, 0);
+    if (rc) return rc;
+    const size_t es = dtype_size(state->dtype);
+    const char *base = static_cast<const char *>(state->data) +
+                       (state->ng + state->ng * state->jstride + state->ng * state->kstride) * es;
+    return count_nonfinite(base, state->dtype, state->nx, state->ny, state->nz, state->jstride, state->kstride,
+                           state->cstride, count_dev, (cudaStream_t)stream);
+}
+
+int axs_level_count_nonfinite(const axs_level *lv, int64_t *count_dev, void *stream)
+{
+    AXS_REQUIRE(lv != nullptr && lv->state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null level");
+    LevelGeom g;
+    int rc = level_geom(lv->dtype, lv->nx, lv->ny, lv->nz, g);
+    if (rc) return rc;
+    const char *base = static_cast<const char *>(lv->state) + (g.ox + g.oy * g.js) * dtype_size(lv->dtype);
+    return count_nonfinite(base, lv->dtype, lv->nx, lv->ny, lv->nz, g.js, g.ks, g.cs, count_dev,
+                           (cudaStream_t)stream);
 }
 
 int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_rhs_coeffs *c, void *stream)

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
             // planes up to q_base + i + 4 must have landed: the first iteration of an
             // item waits for five, every later one for one more
             for (int need = i == 0 ? 5 : 1; need > 0; --need) {
-                if (!mbar_wait_bounded(&full[w_slot], (uint32_t)w_phase)) {
+                if (!mbar_wait_bounded(&full[w_slot], (uint32_t)w_phase, a.wait_polls)) {
                     atomicOr(a.status, kDevTimeout);
                     abort_flag = 1;
                 }

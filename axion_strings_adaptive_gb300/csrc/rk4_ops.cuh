@@ -155,7 +155,8 @@ struct ForwardB {
     }
 };
 
-// Host: step constants shared by every box (Laplacian weights for dx, RK4 step fractions).
+// Host: step constants shared by every box (Laplacian weights for dx, RK4 step
+// fractions) and the bounded-wait limit of this launch.
 template <typename T> inline void fill_step_constants(SweepArgs<T> &a, double dx, double dt)
 {
     const double inv_dx2 = 1.0 / (dx * dx);
@@ -169,6 +170,7 @@ template <typename T> inline void fill_step_constants(SweepArgs<T> &a, double dx
     a.h_sixth = T(dt / 6.0);
     a.h_third = T(dt / 3.0);
     a.h2_sixth = T(dt * dt / 6.0);
+    a.wait_polls = device_wait_polls();
 }
 
 // Host: kappa, lambda/2 and R^2 at one stage time (the reference's

@@ -50,6 +50,7 @@ template <typename T> struct SweepArgs {
     double inv_lambda0;          // adjoint: dlambda_s/dlambda0 = lambda_s / lambda0
     double *lam_partial;         // adjoint: one lambda0-gradient partial per block
     unsigned *status;
+    uint32_t wait_polls;         // polls before a bounded wait gives up (device_wait_polls at launch)
     // box-table sweeps: box table, packed work items (box << 16 | item in box),
     // two tensor maps per box (state, stage buffers) and which one this sweep reads
     const struct EnsBoxDesc *boxes;
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
             const int64_t need = q_base + m + 4;
             while (q_waited <= need) {
                 const int slot = (int)(q_waited % NS);
-                if (!mbar_wait_bounded(&full[slot], (uint32_t)((q_waited / NS) & 1))) {
+                if (!mbar_wait_bounded(&full[slot], (uint32_t)((q_waited / NS) & 1), a.wait_polls)) {
                     atomicOr(a.status, kDevTimeout);
                     abort_flag = 1;
                 }

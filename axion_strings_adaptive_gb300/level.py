@@ -257,6 +257,14 @@ class PeriodicLevel:
     def device_status(self, stream=None) -> None:
         L.call("axs_level_device_status", C.byref(self.c), _stream_ptr(stream))
 
+    def count_nonfinite(self, stream=None) -> int:
+        """Valid cells with a NaN or infinite component (axs_level_count_nonfinite);
+        synchronises the stream to read the count."""
+        if getattr(self, "_nonfinite", None) is None:
+            self._nonfinite = torch.zeros(1, dtype=torch.int64, device=self.state.device)
+        L.call("axs_level_count_nonfinite", C.byref(self.c), self._nonfinite.data_ptr(), _stream_ptr(stream))
+        return int(self._nonfinite.item())
+
     def tag_cells(self, gradient_threshold: float = 1.7976931348623157e308,
                   radial_gradient_threshold: float = 1.7976931348623157e308, n_error_buf: int = 0,
                   block: int = 0, stream=None):
@@ -373,6 +381,13 @@ class AxionStringsLevel:
                                      blend_curv_start=vp.kappa)
         self.bg = bg
         self.tau_i = tau_i_main - tau_pre_end
+
+    def check_finite(self, stream=None) -> None:
+        """Raise FloatingPointError if any valid cell holds a NaN or infinite
+        component (a run that has blown up). The reference has no such check."""
+        n = self.level.count_nonfinite(stream)
+        if n:
+            raise FloatingPointError(f"{n} cells of the level hold NaN or infinite values at tau = {self.tau}")
 
     # AxionStringsLevel::specific_post_timestep's diagnostics (AxionStringsLevel.cpp:1256-1434)
     def specific_post_timestep(self, mask: torch.Tensor | None = None, want_list: bool = True) -> Diagnostics:

@@ -112,6 +112,20 @@ const char *axs_status_string(int status);
 const char *axs_last_error(void);
 int axs_abi_version(void);
 
+/* Failure detection (no counterpart in the reference, whose CPU loops never
+ * wait). Every device-side wait of the stencil kernels (a thread block waiting
+ * for a TMA copy to land) gives up after a bounded number of polls; the kernel
+ * then sets AXS_ERR_DEVICE_TIMEOUT in the status word that the *_device_status
+ * calls report, waits (bounded again, with its own fixed limit) for its copies
+ * still in flight and ends, so the CUDA context stays usable. The limit is
+ * library-wide: AXS_DEFAULT_WAIT_POLLS until set here. 0 makes every such
+ * wait give up at once, which lets a test drive the timeout path without
+ * harming the device. Launches read the value when they are issued (a
+ * captured graph keeps the value of its capture). The previous value goes to
+ * *previous (nullable). */
+#define AXS_DEFAULT_WAIT_POLLS 4194304u
+int axs_set_device_wait_polls(uint32_t polls, uint32_t *previous);
+
 /* ---------------------------------------------------------------------------
  * (a) RHS on AMReX FABs -- the drop-in for the level hook
  * ------------------------------------------------------------------------- */
@@ -306,6 +320,15 @@ int axs_diagnostics(const axs_fab *state, const axs_diag_params *p, const uint8_
                     axs_diag_result *result_dev, int64_t *pierced_dev, int64_t pierced_capacity,
                     void *scratch_dev, int64_t scratch_bytes, void *stream);
 
+/* Non-finite cells: how many valid cells have a component (psi1, psi2, Pi1,
+ * Pi2) that is NaN or infinite, into *count_dev (a device int64, overwritten).
+ * A run that has blown up (a step too long for the stencil, a bad initial
+ * field) shows here before its diagnostics turn into NaN sums. The reference
+ * has no such check (it aborts on bad parameters, AxionStringsLevel.cpp:349-352,
+ * not on bad state). */
+int axs_count_nonfinite(const axs_fab *state, int64_t *count_dev, void *stream);
+int axs_level_count_nonfinite(const axs_level *lv, int64_t *count_dev, void *stream);
+
 /* Same pass on a fused-RK4 level (periodic wrap in z, ghost copies in x/y). */
 int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const uint8_t *mask,
                           axs_diag_result *result_dev, int64_t *pierced_dev,
@@ -315,12 +338,16 @@ int axs_level_diagnostics(const axs_level *lv, const axs_diag_params *p, const u
 /* axs_diagnostics for callers that cannot give this library device memory
  * (no counterpart in the reference, which has no GPU path): the per-block
  * partials live in a 256 KiB static device array inside the library instead of
- * caller scratch, and the call allocates nothing. Boxes whose pass would need
- * more than that array are rejected with AXS_ERR_WORKSPACE. The first call on
- * each device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture on the device. All calls
- * share the one array, so calls whose work overlaps on the GPU (different
- * streams or threads) race: serialise them. */
+ * caller scratch, and the call allocates nothing. A pass needs 256 bytes plus
+ * 160 bytes per block, with at most 8 blocks per SM, so every box fits on
+ * devices of up to 204 SMs (GB300 has 152); on larger devices boxes whose pass
+ * would need more than the array are rejected with AXS_ERR_WORKSPACE. The
+ * first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
+ * first call before any stream capture on the device, and do not call it
+ * again after a cudaDeviceReset of that device. All calls share the one array,
+ * so calls whose work overlaps on the GPU (different streams or threads) race:
+ * serialise them. */
 int axs_diagnostics_static_scratch(const axs_fab *state, const axs_diag_params *p, const uint8_t *mask,
                                    axs_diag_result *result_dev, int64_t *pierced_dev, int64_t pierced_capacity,
                                    void *stream);
@@ -524,7 +551,9 @@ int axs_ensemble_rk4_advance(const axs_ensemble *e, const axs_ensemble_plan *pla
  * into result_dev[0 .. nboxes-1]. The boxes run on up to 8 internal streams
  * side by side, forked from and joined back to `stream` with events (parallel
  * branches under graph capture); scratch, sized by
- * axs_ensemble_diagnostics_scratch_bytes, holds one slice per stream. */
+ * axs_ensemble_diagnostics_scratch_bytes, holds one slice per stream. The
+ * internal streams are created on a device's first call and kept for the life
+ * of the process: do not call it again after a cudaDeviceReset of that device. */
 int axs_ensemble_diagnostics_scratch_bytes(int32_t nboxes, const int32_t *dims, int64_t *bytes);
 int axs_ensemble_diagnostics(const axs_ensemble *e, const axs_diag_params *p, axs_diag_result *result_dev,
                              void *scratch, int64_t scratch_bytes, void *stream);

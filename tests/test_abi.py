@@ -202,3 +202,18 @@ def test_patch_layout_rows_arenas_and_counts(L):
     p = L.PatchesC(L.AXS_F32, 16, 10, 0.25, C.c_void_p(1 << 20), None, C.c_void_p(1 << 21), 1 << 30, 0, 1 << 30)
     plan = L.PatchPlan()
     assert lib.axs_patches_init(C.byref(p), C.byref(plan), None) == L.AXS_ERR_INVALID_ARGUMENT
+
+
+def test_device_wait_polls_setting_round_trips(L):
+    lib = L.lib()
+    prev = C.c_uint32()
+    assert lib.axs_set_device_wait_polls(123, C.byref(prev)) == L.AXS_OK
+    assert prev.value == L.AXS_DEFAULT_WAIT_POLLS
+    assert L.set_device_wait_polls(L.AXS_DEFAULT_WAIT_POLLS) == 123
+    assert lib.axs_set_device_wait_polls(L.AXS_DEFAULT_WAIT_POLLS, None) == L.AXS_OK
+
+
+def test_nonfinite_count_validates_arguments(L):
+    lib = L.lib()
+    assert lib.axs_count_nonfinite(None, None, None) == L.AXS_ERR_INVALID_ARGUMENT
+    assert lib.axs_level_count_nonfinite(None, None, None) == L.AXS_ERR_INVALID_ARGUMENT

@@ -2,9 +2,13 @@
 this library device memory (e.g. an application whose arena owns the GPU).
 
 axs_diagnostics_static_scratch must return what axs_diagnostics returns with
-caller-provided scratch, call after call: the second call checks that the
-shared static array is reset between passes. Kept in its own file, collected
-last, and independent of the other tests' state.
+caller-provided scratch, call after call. Consecutive calls switch between the
+pass's modes (the fused pass, the string finder alone, the split FP32
+per-cell pass), whose kernels fill different fields of the per-block records
+in the shared static array, so a record left over from the previous call in
+another mode would show. A 128^3 box uses the largest grid the pass launches
+(8 blocks per SM). Kept in its own file, collected last, and independent of
+the other tests' state.
 """
 import ctypes as C
 
@@ -13,6 +17,9 @@ import pytest
 import torch
 
 pytestmark = pytest.mark.gpu
+
+# (want_energy, want_plaquettes, want_velocity, per_cell_fp32)
+MODES = {"fused": (1, 1, 1, 0), "strings": (0, 1, 0, 0), "fp32cell": (1, 1, 1, 1)}
 
 
 def _read(L, res):
@@ -28,24 +35,19 @@ def _box(A, n, dtype, seed):
     return t
 
 
-@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_static_scratch_matches_caller_scratch(dtype):
-    if not torch.cuda.is_available():
-        pytest.skip("no CUDA device")
-    import axion_strings_adaptive_gb300 as A
-    A.build()
+def _compare(A, n, dtype, calls):
+    """calls: [(mode, seed), ...] run back to back through both entry points."""
     L = A._lib
     lib = L.lib()
     stream = torch.cuda.current_stream().cuda_stream
-    n = (24, 20, 18)
     ncell = n[0] * n[1] * n[2]
-    params = L.DiagParams(0.5, 1.1, 1.3, 0.4, 1.14, L.MASK_A, 0.8, L.BOUNDARY_GHOSTS, 1, 1, 1)
     ref_res = torch.zeros(C.sizeof(L.DiagResult), dtype=torch.uint8, device="cuda")
     ref_list = torch.full((3 * ncell,), -1, dtype=torch.int64, device="cuda")
     scratch = torch.zeros(A.level.scratch_bytes(*n), dtype=torch.uint8, device="cuda")
     res = torch.zeros_like(ref_res)
     lst = torch.full_like(ref_list, -1)
-    for call, seed in enumerate((7, 8)):  # two calls in a row, different inputs
+    for mode, seed in calls:
+        params = L.DiagParams(0.5, 1.1, 1.3, 0.4, 1.14, L.MASK_A, 0.8, L.BOUNDARY_GHOSTS, *MODES[mode])
         t = _box(A, n, dtype, seed)
         f = A.fab(t, 2)
         assert lib.axs_diagnostics(C.byref(f), C.byref(params), None, ref_res.data_ptr(), ref_list.data_ptr(),
@@ -57,9 +59,37 @@ def test_static_scratch_matches_caller_scratch(dtype):
         a, b = _read(L, ref_res), _read(L, res)
         assert b.status == L.AXS_OK and a.status == L.AXS_OK
         assert (b.n_p_plain, b.n_p_weighted, b.vel_count, b.n_listed) == \
-            (a.n_p_plain, a.n_p_weighted, a.vel_count, a.n_listed)
+            (a.n_p_plain, a.n_p_weighted, a.vel_count, a.n_listed), mode
         assert a.n_p_plain > 0, "the box should hold pierced plaquettes"
         np.testing.assert_allclose(list(b.energy_sums), list(a.energy_sums), rtol=1e-12, atol=0)
         assert b.vel_sum == pytest.approx(a.vel_sum, rel=1e-12)
         np.testing.assert_array_equal(np.sort(lst[: b.n_listed].cpu().numpy()),
                                       np.sort(ref_list[: a.n_listed].cpu().numpy()))
+
+
+def _lib_or_skip():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import axion_strings_adaptive_gb300 as A
+    A.build()
+    return A
+
+
+@pytest.mark.parametrize("dtype,calls", [
+    (torch.float64, [("fused", 7), ("fused", 8)]),
+    (torch.float64, [("fused", 9), ("strings", 10)]),
+    (torch.float64, [("strings", 11), ("fused", 12)]),
+    (torch.float32, [("fused", 7), ("fused", 8)]),
+    (torch.float32, [("strings", 13), ("fp32cell", 14)]),
+    (torch.float32, [("fp32cell", 15), ("fused", 16)]),
+])
+def test_static_scratch_matches_caller_scratch(dtype, calls):
+    _compare(_lib_or_skip(), (24, 20, 18), dtype, calls)
+
+
+@pytest.mark.parametrize("dtype,calls", [
+    (torch.float32, [("fp32cell", 21), ("fused", 22)]),
+    (torch.float64, [("fused", 23), ("strings", 24)]),
+])
+def test_static_scratch_full_grid(dtype, calls):
+    _compare(_lib_or_skip(), (128, 128, 128), dtype, calls)
