@@ -429,3 +429,53 @@ def level_diagnostics(state_valid: np.ndarray, dx: float, bg: OrcBackground, tau
     mean = (vs * dx) / (vc * dx) if vc > 0 else 0.0
     return LevelDiagnostics(plain, weighted, xi_p, xi_w, normalise_energy(sums, float(nx * ny * nz)),
                             sums, vs, vc, mean)
+
+
+def network_scalars_row(state_valid: np.ndarray, dx: float, bg: OrcBackground, tau: float,
+                        scheme: int = MASK_A, threshold: float = 0.8) -> np.ndarray:
+    """The 24 values of a network_scalars.dat row for one uncovered periodic
+    level, restating specific_post_timestep's host algebra:
+
+    * counts, comoving string lengths and the dx-weighted velocity sums of the
+      composite gathering (AxionStringsLevel.cpp:1296-1340);
+    * compute_composite_total_energy's volume-weighted normalisation
+      (EnergyKernel.hpp:287-339) with a single level;
+    * m_r/H from Background::H_over_mr_direct (AxionStringsLevel.cpp:1266-1269,
+      Background.hpp:112-116);
+    * <gamma^2 v^2>, <gamma>, the core energy, the axion tail and the two
+      tensions (AxionStringsLevel.cpp:1358-1434);
+    * the row order of AxionStringsLevel.cpp:1536-1579.
+    """
+    ng = 2
+    fab = to_fab(np.ascontiguousarray(state_valid), ng)
+    _, nz, ny, nx = state_valid.shape
+    co = background_eval(bg, tau)[0]
+    R, Rp, lam, H = co[0], co[1], co[3], co[4]
+    RpR = Rp / R if bg.kind != BG_FLAT else 0.0
+    m_r = float(np.sqrt(lam))
+    m_r_over_h = 1.0 / (H / m_r)
+    plain, weighted = count_plaquettes(fab, ng)
+    L_tilde = nx * dx
+    ell_p = (2.0 / 3.0) * float(plain) * dx
+    ell_w = (2.0 / 3.0) * float(weighted) * dx
+    xi_p = lib().oracle_xi_from_comoving_length(ell_p, L_tilde, bg.a_inv, tau)
+    xi_w = lib().oracle_xi_from_comoving_length(ell_w, L_tilde, bg.a_inv, tau)
+    vs, vc = velocity(fab, ng, R, RpR, m_r)
+    v_sum, v_cnt = vs * dx, float(vc) * dx
+    sums = energy_sums(fab, ng, dx, R, lam, RpR, scheme, threshold)
+    vol = dx * dx * dx
+    acc = [sums[q] * vol for q in range(12)]
+    n_total = float(nx * ny * nz) * vol
+    n_unmasked = sums[12] * vol
+    e = [0.0] * 12
+    for q in range(6):
+        e[2 * q] = acc[2 * q] / n_total
+        e[2 * q + 1] = acc[2 * q + 1] / n_unmasked if n_unmasked > 0.0 else 0.0
+    mean_g2v2 = v_sum / v_cnt if v_cnt > 0.0 else 0.0
+    mean_gamma = float(np.sqrt(1.0 + mean_g2v2))
+    core = n_total * e[0] - n_unmasked * e[1]
+    tail = n_unmasked * (e[5] - e[3])  # axion gradient minus axion kinetic, screened
+    t_core = (R * R) * core / ell_p if ell_p > 0.0 else 0.0
+    t_tail = (R * R) * (core + tail) / ell_p if ell_p > 0.0 else 0.0
+    return np.array([plain, weighted, xi_p, xi_w, m_r_over_h] + e + [n_total, n_unmasked, mean_g2v2, mean_gamma,
+                                                                     vc, t_core, t_tail], dtype=np.float64)

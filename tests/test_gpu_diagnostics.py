@@ -94,6 +94,32 @@ def test_velocity_matches_oracle_f32(axs, orc, golden):
     assert r.vel_sum == pytest.approx(vs_native, rel=1e-12)
 
 
+@pytest.mark.parametrize("box", ["rand", "ic"])
+def test_fp32_velocity_matches_float_build_fixture(axs, orc, golden, box):
+    """FP32 velocity against the reference's own FLOAT build. The FLOAT build
+    recomputes the windings it sums over with float atan2
+    (VelocityKernel.hpp:66-69); the GPU sums over the string finder's pierced
+    set, which uses double atan2 (StringFinder.hpp:49-53) in both precisions,
+    so that counts, list and velocities refer to the same plaquettes. The two
+    sets differ only where a float phase difference lands on the other side
+    of +-pi. The test counts that difference on the CPU (oracle, double atan2,
+    against the fixture's count); on these boxes it is zero, and the velocity
+    count and sum then equal the FLOAT build's."""
+    g = golden("fields_f32.npz")
+    st = g[f"{box}_state"]
+    plain_double, _ = orc.count_plaquettes(orc.to_fab(st, 2), 2)
+    vs_f, vc_f = g[f"{box}_velocity"]
+    set_difference = int(vc_f) // 4 - plain_double  # plaquettes pierced only under float atan2 (net)
+    t = axs.new_fab(st.shape[1:][::-1], 2, dtype=torch.float32)
+    axs.valid(t, 2).copy_(_dev(st))
+    axs.fill_periodic_ghosts(t, 2)
+    r, _ = _run_diag(axs, t, 2, _params(axs, g, 1, axs._lib.BOUNDARY_GHOSTS, prec="f32"))
+    assert r.vel_count == 4 * r.n_p_plain == 4 * plain_double
+    assert set_difference == 0
+    assert r.vel_count == int(vc_f)
+    assert r.vel_sum == pytest.approx(vs_f, rel=1e-12)
+
+
 def test_level_diagnostics_matches_oracle(axs, orc):
     n, dx = 24, 0.5
     v = orc.fourier_ic_state(n, 5.0, seed=99)
@@ -302,3 +328,32 @@ def test_per_cell_fp32_double_path_cells(axs, orc, vacuum):
     np.testing.assert_allclose(fast.energy_sums, ref.energy_sums, rtol=2e-6)
     assert fast.energy_sums[13] == ref.energy_sums[13] == n ** 3  # every cell counted once
     assert fast.mean_gamma_sq_v_sq == pytest.approx(ref.mean_gamma_sq_v_sq, rel=1e-5)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_network_scalars_row_matches_oracle(axs, orc, dtype):
+    """The 24-column network_scalars.dat row (counts, xi, m_r/H, the 12
+    normalised energies, volumes, <gamma^2 v^2>, <gamma>, the velocity corner
+    count and the two tensions) of an evolved Fourier-IC level against the
+    oracle's restatement of specific_post_timestep's host algebra on the same
+    field. FP64: to 1e-12; FP32 fields: the oracle's FP32 build on the GPU's
+    own FP32 state, with the per-cell terms in double on both sides."""
+    from axion_strings_adaptive_gb300 import output
+    n, dx, dt, steps = 48, 0.5, 0.1, 30
+    v = orc.fourier_ic_state(n, orc.strict_cutoff(n / 4), seed=77)
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    lv = axs.PeriodicLevel(n, dx, dtype=dtype)
+    lv.set_state(torch.from_numpy(v).cuda())
+    lv.advance(bg, 1.0, 0.0, dt, steps)
+    lv.device_status()
+    tau = 1.0 + steps * dt
+    d = lv.diagnostics(bg, tau)
+    assert d.n_p_plain > 0
+    row = np.array(output.network_scalars_row(d, 1.0 / bg.H_over_mr_direct(tau)), dtype=np.float64)
+    got_state = lv.get_state().cpu().numpy()
+    ref = orc.network_scalars_row(got_state, dx, orc.background(a_inv=2.0, c0=1.0, lambda_scale=2.0), tau)
+    assert row.shape == ref.shape == (24,)
+    # integer columns (counts) exactly; the rest to 1e-12 relative
+    for q in (0, 1, 21):
+        assert row[q] == ref[q], output.NETWORK_COLUMNS[q]
+    np.testing.assert_allclose(row, ref, rtol=1e-12, atol=0)
