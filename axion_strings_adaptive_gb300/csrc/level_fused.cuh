@@ -228,6 +228,8 @@ __global__ void __launch_bounds__(S::THREADS, 1)
         const int z0 = (int)(item / a.ntiles) * a.zchunk;
         const int len = min(a.zchunk, nz - z0);
         const int x0 = (tile % a.tiles_x) * TX, y0 = (tile / a.tiles_x) * TY;
+        // only tiles within 8 columns / 2 rows of the domain edge write periodic copies
+        const bool edge_tile = x0 < 8 || x0 + TX > nx - 8 || y0 < 2 || y0 + TY > ny - 2;
         // iteration i: sweep A at plane za = z0 - 2 + i (ring planes q_base + i .. + 4),
         // sweep B at zb = za - 2 = z0 - 4 + i for i >= 4
         for (int i = 0; i < len + 4; ++i) {
@@ -316,8 +318,13 @@ __global__ void __launch_bounds__(S::THREADS, 1)
                 stage_b<T, V>(a, lap, ctr, pq, o);
                 const int x = x0 + bxl, y = y0 + byl;
                 const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + oy) * a.js + (int64_t)zb * a.ks;
+                if (edge_tile) {
 #pragma unroll
-                for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, nx, ny, a.js, o[c]);
+                    for (int c = 0; c < 4; ++c) store_with_copies<T, V>(a.out[c], off, x, y, nx, ny, a.js, o[c]);
+                } else {  // no site of the tile has a periodic copy: plain stores, no per-site branches
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) stv<T, V>(a.out[c] + off, o[c]);
+                }
             }
             if (++r0 == NS) r0 = 0;
             if (++s0 == S::NSW) s0 = 0;
