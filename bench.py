@@ -108,7 +108,7 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle port)
-def cpu_baseline(seconds: float = 10.0, n: int = 256):
+def cpu_baseline(seconds: float = 10.0, n: int = N_DEFAULT):
     """The CPU restatement (oracle/, OpenMP over all host cores) on a bounded
     sample: FP32 RK4 steps of an n^3 box of the same workload until ~`seconds`."""
     import numpy as np
@@ -152,13 +152,62 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": _config(N_DEFAULT, {"reference_sample": f"each step = one FP32 RK4 step of a {n}^3 box "
-                                                              f"(bounded sample of the {N_DEFAULT}^3 workload)"}),
+            "config": _config(N_DEFAULT, {"reference_sample": f"each step = one FP32 RK4 step of a {n}^3 box"
+                                                              + (" (the workload itself)" if n == N_DEFAULT else
+                                                                 f" (bounded sample of the {N_DEFAULT}^3 workload)")}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{args.steps} FP32 RK4 steps of a {n}^3 box; CPU restatement of the "
                                        f"reference path (its AMReX build is not buildable here)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- drop-in per-stage path
+def dropin_report(A, ic, dev, n=512, steps=4, warmup=1):
+    """The one-for-one replacement of specific_eval_rhs under a host RK driver
+    (AxionStringsLevel.cpp:909-920, GRTeclyn's classic RK4): per step four
+    ghost fills + axs_eval_rhs on AMReX-layout FABs (ng = 2), three
+    axs_lincomb stage combinations and one axs_rk4_combine, in FP32 and FP64
+    on the headline box. Algorithmic words per site and step: eval_rhs 8
+    (4 read, 4 written) x 4, lincomb 12 x 3, rk4_combine 24: 92 (ghost fills
+    excluded)."""
+    import torch
+    bg = A.Background.expanding(A_INV, C0, lambda0=LAMBDA0)
+    out = {"words_per_site_step": 92, "kernels_per_step": ["fill_periodic x4", "eval_rhs x4", "lincomb x3",
+                                                           "rk4_combine"]}
+    s0 = ic.fourier_state(n, ic.strict_cutoff(n / 8), seed=SEED, dtype=torch.float64, device=dev)
+    for name, dt_ in (("f32", torch.float32), ("f64", torch.float64)):
+        ng = 2
+        u = A.new_fab((n, n, n), ng, dtype=dt_, device=dev)
+        A.valid(u, ng).copy_(s0)
+        uold, us = torch.empty_like(u), torch.empty_like(u)
+        ks = [torch.empty_like(u) for _ in range(4)]
+        def step(t):
+            uold.copy_(u)
+            for s_, (ts, cs) in enumerate(((t, 0.5 * DT), (t + 0.5 * DT, 0.5 * DT), (t + 0.5 * DT, DT), (t + DT, None))):
+                src = uold if s_ == 0 else us
+                A.fill_periodic_ghosts(src, ng)
+                # specific_eval_rhs: the stage's coefficients, then the RHS kernel
+                A.eval_rhs(src, ks[s_], ng, ng, DX, bg.rhs_coeffs(TAU_I + ts))
+                if cs is not None:
+                    A.lincomb(us, uold, cs, ks[s_], ng)
+            A.rk4_combine(u, uold, *ks, ng, DT)
+        for w in range(warmup):
+            step(w * DT)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for s_ in range(steps):
+            step((warmup + s_) * DT)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        es = 4 if dt_ == torch.float32 else 8
+        out[name] = {"ms_per_step": ms, "value": n ** 3 / (ms * 1e-3), "unit": UNIT,
+                     "achieved_gbs": 92 * es * n ** 3 / (ms * 1e-3) / 1e9}
+        del u, uold, us, ks
+        torch.cuda.empty_cache()
+    return out
 
 
 # ---------------------------------------------------------------- differentiation configuration
@@ -724,6 +773,10 @@ def run_native(args):
     # ---------------- differentiation: 128^3 FP32, c0 = 1, lambda0 = 2, 200 steps, checkpoint every 20;
     # gradients w.r.t. the initial psi and lambda0 against central differences (eps = 1e-3, FP64
     # evolution) on 16 unit-norm random directions in psi, and against the FP64 adjoint
+    dropin = None
+    if not args.no_dropin:
+        dropin = dropin_report(A, ic, dev, n=args.n)
+
     differentiation = None
     if not args.no_differentiation:
         differentiation = differentiation_report(A, ic, dev, args.diff_n, args.diff_steps, args.diff_directions)
@@ -812,7 +865,7 @@ def run_native(args):
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None, "precision": precision,
                 "adjoint": adj, "adjoint_over_forward": adj["adjoint_over_forward"] if adj else None,
                 "differentiation": differentiation, "batching": batching, "scale": scale,
-                "scale_1024": scale_1024}
+                "scale_1024": scale_1024, "dropin": dropin}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -825,7 +878,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--ref-n", type=int, default=256)
+    ap.add_argument("--ref-n", type=int, default=N_DEFAULT)
     ap.add_argument("--precision-steps", type=int, default=400)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-fp64", action="store_true")
@@ -837,6 +890,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--no-dropin", action="store_true")
     ap.add_argument("--no-scale", action="store_true")
     ap.add_argument("--scale-n", type=int, default=512)
     ap.add_argument("--scale-steps", type=int, default=20)

@@ -201,3 +201,30 @@ def test_fused_rk4_keeps_padding_current(axs):
     lv.set_state(_to_dev(v))
     lv.advance(axs.Background.flat(1.0), 0.0, 0.0, 0.05, 3)
     _check_padding(lv, lv.get_state().cpu().numpy())
+
+
+def test_fused_rk4_f64_512cubed_matches_oracle(axs, orc):
+    """The precision workload's grid in FP64 (512^3, dx 0.5, Moore c0 = 2,
+    lambda0 = 2, RD, Fourier IC |n| < N/8), 2 steps, against the oracle's
+    stage-by-stage RK4: element offsets past 32 bits on real 3-D data. The
+    oracle holds about 40 GB on the host."""
+    import os
+    if os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES") < 96 * 2 ** 30:
+        pytest.skip("the 512^3 FP64 oracle needs about 40 GB of host memory")
+    from axion_strings_adaptive_gb300 import ic
+    n, dx, dt, steps = 512, 0.5, 0.1, 2
+    s0 = ic.fourier_state(n, ic.strict_cutoff(n / 8), seed=31, dtype=torch.float64, device="cuda")
+    lv = axs.PeriodicLevel(n, dx, dtype=torch.float64, pierced_capacity=1024)
+    lv.set_state(s0)
+    lv.advance(axs.Background.expanding(2.0, 2.0, lambda0=2.0), 1.0, 0.0, dt, steps)
+    lv.device_status()
+    got = lv.get_state().cpu().numpy()
+    v = s0.cpu().numpy()
+    del lv, s0
+    torch.cuda.empty_cache()
+    fab = orc.to_fab(v, 2)
+    del v
+    orc.rk4_advance(fab, 2, dx, orc.background(a_inv=2.0, c0=2.0, lambda_scale=2.0), 1.0, 0.0, dt, steps)
+    ref = orc.from_fab(fab, 2)
+    del fab
+    assert _rel_max(got, ref) < 1e-12
