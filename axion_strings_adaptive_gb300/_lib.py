@@ -128,6 +128,9 @@ SIGNATURES = {
     "axs_level_count_nonfinite": (_i32, [C.POINTER(LevelC), _ptr, _ptr]),
     "axs_eval_rhs": (_i32, [C.POINTER(Fab), C.POINTER(Fab), _dbl, C.POINTER(RhsCoeffs), _ptr]),
     "axs_fill_periodic_ghosts": (_i32, [C.POINTER(Fab), _ptr]),
+    "axs_fill_periodic_ghosts_xy": (_i32, [C.POINTER(Fab), _ptr]),
+    "axs_fab_pack_z_planes": (_i32, [C.POINTER(Fab), _i32, _i32, _ptr, _ptr]),
+    "axs_fab_unpack_z_planes": (_i32, [C.POINTER(Fab), _i32, _i32, _ptr, _ptr]),
     "axs_lincomb": (_i32, [C.POINTER(Fab), C.POINTER(Fab), _dbl, C.POINTER(Fab), _ptr]),
     "axs_rk4_combine": (_i32, [C.POINTER(Fab)] * 6 + [_dbl, _ptr]),
     "axs_level_layout_for": (_i32, [_i32, _i32, _i32, _i32, C.POINTER(LevelLayout)]),

@@ -113,6 +113,46 @@ __global__ void fill_periodic_kernel(const axs_fab f)
     }
 }
 
+// x/y ghosts of the valid z planes only (a z slab of a larger periodic box:
+// its z ghosts come from the neighbouring slabs)
+template <typename T>
+__global__ void fill_periodic_xy_kernel(const axs_fab f)
+{
+    T *p = static_cast<T *>(f.data);
+    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng;
+    const int64_t n = (int64_t)gx * gy * f.nz * f.ncomp;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % gx) - f.ng;
+        const int j = (int)((q / gx) % gy) - f.ng;
+        const int k = (int)((q / ((int64_t)gx * gy)) % f.nz);
+        const int c = (int)(q / ((int64_t)gx * gy * f.nz));
+        if (i >= 0 && i < f.nx && j >= 0 && j < f.ny) continue;
+        const int ii = ((i % f.nx) + f.nx) % f.nx, jj = ((j % f.ny) + f.ny) % f.ny;
+        p[c * f.cstride + fab_off(f, i, j, k)] = p[c * f.cstride + fab_off(f, ii, jj, k)];
+    }
+}
+
+// Whole padded planes z0 .. z0 + np - 1 (ghost planes allowed: -ng <= z) of all
+// components, between the FAB and a contiguous (ncomp, np, ny+2ng, nx+2ng) buffer.
+template <typename T>
+__global__ void copy_z_planes_kernel(const axs_fab f, int z0, int np, T *buf, int to_buf)
+{
+    T *p = static_cast<T *>(f.data);
+    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng;
+    const int64_t n = (int64_t)gx * gy * np * f.ncomp;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % gx) - f.ng;
+        const int j = (int)((q / gx) % gy) - f.ng;
+        const int k = z0 + (int)((q / ((int64_t)gx * gy)) % np);
+        const int c = (int)(q / ((int64_t)gx * gy * np));
+        T *e = p + c * f.cstride + fab_off(f, i, j, k);
+        if (to_buf)
+            buf[q] = *e;
+        else
+            *e = buf[q];
+    }
+}
+
 // ---------------------------------------------------------------- stage combinations
 // Evaluated with explicit round-to-nearest operations in the host's
 // expression order (no contraction), so the per-stage drop-in path reproduces
@@ -427,6 +467,47 @@ int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_r
         eval_rhs_f32_kernel<<<grid_for(n), 256, 0, st>>>(*soln, *rhs, (float)one_over_dx2, (float)c->kappa,
                                                          (float)c->lambda, (float)c->R2);
     return launch_status("eval_rhs");
+}
+
+int axs_fill_periodic_ghosts_xy(const axs_fab *f, void *stream)
+{
+    int rc = validate_fab(f, "fab", 1, 0);
+    if (rc) return rc;
+    if (f->ng == 0) return AXS_OK;
+    AXS_REQUIRE(f->ng <= f->nx && f->ng <= f->ny, AXS_ERR_UNSUPPORTED, "periodic fill needs ng <= box extent");
+    const int64_t n = (int64_t)(f->nx + 2 * f->ng) * (f->ny + 2 * f->ng) * f->nz * f->ncomp;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (f->dtype == AXS_F64)
+        fill_periodic_xy_kernel<double><<<grid_for(n), 256, 0, st>>>(*f);
+    else
+        fill_periodic_xy_kernel<float><<<grid_for(n), 256, 0, st>>>(*f);
+    return launch_status("fill_periodic_ghosts_xy");
+}
+
+static int copy_z_planes(const axs_fab *f, int32_t z0, int32_t nplanes, void *buf, int to_buf, cudaStream_t st)
+{
+    int rc = validate_fab(f, "fab", 1, 0);
+    if (rc) return rc;
+    AXS_REQUIRE(buf != nullptr, AXS_ERR_INVALID_ARGUMENT, "null plane buffer");
+    AXS_REQUIRE(nplanes > 0 && z0 >= -f->ng && z0 + nplanes <= f->nz + f->ng, AXS_ERR_INVALID_ARGUMENT,
+                "planes %d .. %d outside the FAB's z range %d .. %d", z0, z0 + nplanes - 1, -f->ng,
+                f->nz + f->ng - 1);
+    const int64_t n = (int64_t)(f->nx + 2 * f->ng) * (f->ny + 2 * f->ng) * nplanes * f->ncomp;
+    if (f->dtype == AXS_F64)
+        copy_z_planes_kernel<double><<<grid_for(n), 256, 0, st>>>(*f, z0, nplanes, static_cast<double *>(buf), to_buf);
+    else
+        copy_z_planes_kernel<float><<<grid_for(n), 256, 0, st>>>(*f, z0, nplanes, static_cast<float *>(buf), to_buf);
+    return launch_status("z plane copy");
+}
+
+int axs_fab_pack_z_planes(const axs_fab *f, int32_t z0, int32_t nplanes, void *buf, void *stream)
+{
+    return copy_z_planes(f, z0, nplanes, buf, 1, (cudaStream_t)stream);
+}
+
+int axs_fab_unpack_z_planes(const axs_fab *f, int32_t z0, int32_t nplanes, const void *buf, void *stream)
+{
+    return copy_z_planes(f, z0, nplanes, const_cast<void *>(buf), 0, (cudaStream_t)stream);
 }
 
 int axs_fill_periodic_ghosts(const axs_fab *f, void *stream)

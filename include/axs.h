@@ -141,6 +141,28 @@ int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_r
  * domain (AxionStringsLevel.cpp:820, :1255): fills every ghost cell. */
 int axs_fill_periodic_ghosts(const axs_fab *f, void *stream);
 
+/* The halo seam of a z-slab decomposition (one slab of a periodic box per GPU;
+ * replaces the inter-rank part of FillBoundary, AxionStringsLevel.cpp:820,
+ * :1255). Per RK stage a slab
+ *   1. fills its x/y ghosts periodically (axs_fill_periodic_ghosts_xy, valid z
+ *      planes only),
+ *   2. packs its lowest and highest ng valid planes, x/y ghosts included
+ *      (axs_fab_pack_z_planes with z0 = 0 and z0 = nz - ng),
+ *   3. sends them to its lower / upper neighbour (NCCL or any transport of the
+ *      caller's choice) and
+ *   4. unpacks the planes it receives into its z ghosts (axs_fab_unpack_z_planes
+ *      with z0 = -ng and z0 = nz),
+ * after which axs_eval_rhs and axs_diagnostics (AXS_BOUNDARY_GHOSTS) run on the
+ * slab as on the whole box. A buffer holds planes z0 .. z0 + nplanes - 1 of all
+ * components, contiguous as (ncomp, nplanes, ny + 2 ng, nx + 2 ng). The
+ * diagnostics' result holds the slab's raw sums (14 energy sums, the two
+ * counts, the velocity sum and count): the all-reduce of those 18 scalars and an
+ * exclusive prefix sum of n_listed for the pierced-list offsets give the whole
+ * box (StringFinder.hpp:119-120, EnergyKernel.hpp:215, VelocityKernel.hpp:138-139). */
+int axs_fill_periodic_ghosts_xy(const axs_fab *f, void *stream);
+int axs_fab_pack_z_planes(const axs_fab *f, int32_t z0, int32_t nplanes, void *buf_dev, void *stream);
+int axs_fab_unpack_z_planes(const axs_fab *f, int32_t z0, int32_t nplanes, const void *buf_dev, void *stream);
+
 /* dst = x + b*y over the valid cells of all components: the stage combination
  * U_s = U_old + c_s dt k (AMReX MultiFab::LinComb in GRTeclyn's RK driver). */
 int axs_lincomb(const axs_fab *dst, const axs_fab *x, double b, const axs_fab *y, void *stream);
