@@ -158,8 +158,9 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
 // The one-pass fused step (level_fused.cuh) over FP32 levels whose extents are
 // multiples of its tile; single sweeps and other extents run the two sweeps of
 // the default tiling. Steps alternate between the level's state and the first
-// 4 component planes of its work buffer (same layout); after an odd number of
-// steps one copy brings the result back into the state.
+// 4 component planes of its work buffer (same layout); each step is the fused
+// launch and the padding launch; after an odd number of steps one copy brings
+// the result back into the state.
 template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
     using S = LevelFusedShape<TX, TY, NS, THREADS>;
     using Fallback = SweepConfig<float, 2, 64, 8, 8, 2>;
@@ -204,6 +205,8 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
         int grid = 0;
         plan_chunks(a.ntiles, lv->nz, sms, a.zchunk, a.n_items, grid);
         fill_level_constants(a, lv, g, r.dt);
+        const int64_t pad_n = (16LL * (lv->ny + 4) + 4LL * lv->nx) * lv->nz * 4;
+        const int pad_grid = (int)std::min<int64_t>((pad_n + 255) / 256, (int64_t)sms * 8);
         float *buf[2] = {static_cast<float *>(lv->state), static_cast<float *>(lv->work)};
         LevelFusedMaps maps[2];
         int rc;
@@ -219,6 +222,8 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
             for (int c = 0; c < 4; ++c) as.out[c] = dst + c * g.cs;
             kern<<<grid, S::THREADS, S::SMEM, r.st>>>(maps[s & 1], as);
             if ((rc = launch_status("fused level step"))) return rc;
+            level_pad_kernel<float><<<pad_grid, 256, 0, r.st>>>(dst, lv->nx, lv->ny, lv->nz, g.js, g.ks, g.cs, g.ox, g.oy);
+            if ((rc = launch_status("level padding"))) return rc;
         }
         if (r.nsteps & 1)
             AXS_CUDA_CHECK(cudaMemcpyAsync(buf[0], buf[1], 4 * g.cs * sizeof(float), cudaMemcpyDeviceToDevice, r.st));

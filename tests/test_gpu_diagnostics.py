@@ -336,8 +336,10 @@ def test_network_scalars_row_matches_oracle(axs, orc, dtype):
     normalised energies, volumes, <gamma^2 v^2>, <gamma>, the velocity corner
     count and the two tensions) of an evolved Fourier-IC level against the
     oracle's restatement of specific_post_timestep's host algebra on the same
-    field. FP64: to 1e-12; FP32 fields: the oracle's FP32 build on the GPU's
-    own FP32 state, with the per-cell terms in double on both sides."""
+    field. FP64: to 1e-12. FP32 fields: the oracle's FP32 build on the GPU's
+    own FP32 state; the FLOAT build holds R, lambda, R'/R and m_r as float
+    while the GPU's diagnostics take them in double, so the columns agree to
+    1e-6 there (counts still exactly)."""
     from axion_strings_adaptive_gb300 import output
     n, dx, dt, steps = 48, 0.5, 0.1, 30
     v = orc.fourier_ic_state(n, orc.strict_cutoff(n / 4), seed=77)
@@ -356,4 +358,4 @@ def test_network_scalars_row_matches_oracle(axs, orc, dtype):
     # integer columns (counts) exactly; the rest to 1e-12 relative
     for q in (0, 1, 21):
         assert row[q] == ref[q], output.NETWORK_COLUMNS[q]
-    np.testing.assert_allclose(row, ref, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(row, ref, rtol=1e-12 if dtype == torch.float64 else 1e-6, atol=0)
