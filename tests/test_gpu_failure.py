@@ -76,7 +76,7 @@ def test_nonfinite_cells_are_counted(axs, dtype):
         lvl.check_finite()
     # the FAB entry point on the same cells (ghosts hold finite garbage that must not count)
     t = axs.new_fab((n, n, n), 2, dtype=dtype)
-    t.fill(1e300 if dtype == torch.float64 else 1e30)
+    t.fill_(1e300 if dtype == torch.float64 else 1e30)
     axs.valid(t, 2).copy_(v.cuda())
     cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
     import ctypes as C
