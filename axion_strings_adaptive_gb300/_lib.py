@@ -81,7 +81,11 @@ class PatchLayout(C.Structure):
 
 class PatchesC(C.Structure):
     _fields_ = [("dtype", _i32), ("n", _i32), ("npatches", _i32), ("dx", _dbl), ("state", _ptr), ("work", _ptr),
-                ("table", _ptr), ("state_bytes", _i64), ("work_bytes", _i64), ("table_bytes", _i64)]
+                ("table", _ptr), ("state_bytes", _i64), ("work_bytes", _i64), ("table_bytes", _i64),
+                ("capacity", _i32)]
+
+
+PATCH_KEEP = -2
 
 
 class PatchPlan(C.Structure):

@@ -32,13 +32,20 @@ class Patches:
     """npatches refined patches of n^3 fine cells (spacing dx) with ghost rings."""
 
     def __init__(self, n: int, npatches: int, dx: float, dtype=torch.float32, device="cuda",
-                 storage: torch.Tensor | None = None, clear: bool = True):
-        """storage: a 1-D tensor of dtype to lay the state arena in (its first
+                 storage: torch.Tensor | None = None, clear: bool = True, capacity: int | None = None):
+        """capacity: patch slots the arena's component planes are laid out for
+        (>= npatches; default npatches): a later patch set of up to that many
+        patches can live in the same arena with every kept patch in place.
+        storage: a 1-D tensor of dtype to lay the state arena in (its first
         4 plane_elems elements), when it is large enough; else a new one.
         clear: zero the arena (a caller that writes every box itself skips it)."""
+        cap = int(npatches) if capacity is None else max(int(capacity), int(npatches))
         lay = L.PatchLayout()
-        L.call("axs_patches_layout", _DT[dtype], int(n), int(npatches), C.byref(lay))
-        self.layout, self.n, self.npatches, self.dx, self.dtype = lay, int(n), int(npatches), float(dx), dtype
+        L.call("axs_patches_layout", _DT[dtype], int(n), cap, C.byref(lay))
+        lay_n = L.PatchLayout()
+        L.call("axs_patches_layout", _DT[dtype], int(n), int(npatches), C.byref(lay_n))
+        self.layout, self.n, self.npatches, self.capacity = lay, int(n), int(npatches), cap
+        self.dx, self.dtype = float(dx), dtype
         need = 4 * lay.plane_elems
         if storage is None or storage.dtype != dtype or storage.numel() < need:
             storage = torch.empty(need, dtype=dtype, device=device)
@@ -49,9 +56,9 @@ class Patches:
         # sweep A writes every work cell sweep B reads, so the work planes need no
         # clearing; patch sizes the fused step covers need no work arena
         self.work = torch.empty((8, lay.plane_elems) if lay.work_bytes > 0 else (0,), dtype=dtype, device=device)
-        self.table = torch.zeros(lay.table_bytes, dtype=torch.uint8, device=device)
+        self.table = torch.zeros(lay_n.table_bytes, dtype=torch.uint8, device=device)
         self.c = L.PatchesC(_DT[dtype], self.n, self.npatches, self.dx, self.state.data_ptr(), self.work.data_ptr(),
-                            self.table.data_ptr(), lay.state_bytes, lay.work_bytes, lay.table_bytes)
+                            self.table.data_ptr(), lay.state_bytes, lay.work_bytes, lay_n.table_bytes, cap)
         self.plan = L.PatchPlan()
         L.call("axs_patches_init", C.byref(self.c), C.byref(self.plan), None)
 
@@ -119,16 +126,16 @@ class TwoLevel:
     ENERGY_NAMES = ["rho_tot", "rho_axion_kinetic", "rho_axion_gradient", "rho_radial_kinetic",
                     "rho_radial_gradient", "rho_radial_mass"]
 
-    def __init__(self, coarse: PeriodicLevel, block: int = 32, spare_arena: bool = True, headroom: float = 1.25):
-        """spare_arena: keep a second patch arena, sized with `headroom` over the
-        patch count, so that a regrid lays the new patches out in the arena the
-        old ones do not use (it copies the kept patches across) instead of
-        allocating one; a regrid allocates only when the patch count outgrows it."""
+    def __init__(self, coarse: PeriodicLevel, block: int = 32, headroom: float = 1.25):
+        """headroom: the patch arena is laid out for headroom x the patch count
+        (patch slots), so that regrids whose patch count stays within that keep
+        one arena: kept patches stay in their slots (or move down into free ones),
+        new patches take free slots. A regrid past the capacity lays the patches
+        out in a new arena once."""
         if coarse.nx % block or coarse.ny % block or coarse.nz % block:
             raise ValueError("the coarse level must tile into blocks")
         self.coarse, self.block = coarse, int(block)
-        self.spare_arena, self.headroom = bool(spare_arena), float(headroom)
-        self._spare: torch.Tensor | None = None
+        self.headroom = float(headroom)
         self.nb = (coarse.nx // block, coarse.ny // block, coarse.nz // block)
         # the coarse state at the start of the running coarse step (state only: the
         # ghost fill reads nothing else)
@@ -147,52 +154,69 @@ class TwoLevel:
 
     def set_blocks(self, blocks: np.ndarray) -> None:
         """Refine exactly these blocks ((k, 3) block coordinates x, y, z): blocks
-        refined before keep their fine data, new ones interpolate the coarse level."""
+        refined before keep their fine data, new ones interpolate the coarse level.
+
+        Within the arena's capacity the new set is laid out in the same arena: a
+        kept patch whose slot lies below the new patch count stays where it is,
+        kept patches above it move into the free slots below it, and new patches
+        take the slots left (one box-copy launch moves and clears, one fill
+        interpolates the new patches). Past the capacity, a new arena of headroom
+        x the count receives the kept patches."""
         blocks = np.asarray(blocks, dtype=np.int32).reshape(-1, 3)
         dev = self.coarse.state.device
         old_patches, old_block_patch = self.patches, self._block_patch
-        self.blocks = blocks
-        if len(blocks) == 0:
+        n_new = len(blocks)
+        if n_new == 0:
+            self.blocks = blocks
             self.patches = None
             self._block_patch.fill_(-1)
             return
         dt = self.coarse.dtype
-        storage = None
-        if self.spare_arena:
-            lay = L.PatchLayout()
-            L.call("axs_patches_layout", _DT[dt], 2 * self.block, len(blocks), C.byref(lay))
-            need = 4 * lay.plane_elems
-            if self._spare is None or self._spare.numel() < need:
-                self._spare = None  # too small: free it before the new allocation
-                # cleared once here: a regrid's first writes into freshly mapped memory
-                # would otherwise pay for the mapping
-                self._spare = torch.zeros(int(need * self.headroom) + 1, dtype=dt, device=dev)
-            storage = self._spare
-        # every box is written below: copied from the old patch of its block, or
-        # cleared and interpolated from the coarse level
-        self.patches = Patches(2 * self.block, len(blocks), 0.5 * self.coarse.dx, dtype=dt, device=dev,
-                               storage=storage, clear=False)
+        if old_patches is not None:
+            b = torch.from_numpy(blocks.astype(np.int64)).to(dev)
+            old_q = old_block_patch[b[:, 2], b[:, 1], b[:, 0]].cpu().numpy().astype(np.int64)
+        else:
+            old_q = np.full(n_new, -1, dtype=np.int64)
+        in_place = old_patches is not None and n_new <= old_patches.capacity
+        if in_place:
+            slot = np.full(n_new, -1, dtype=np.int64)
+            stay = (old_q >= 0) & (old_q < n_new)
+            slot[stay] = old_q[stay]
+            used = np.zeros(n_new, dtype=bool)
+            used[old_q[stay]] = True
+            holes = np.nonzero(~used)[0]
+            movers = np.nonzero(old_q >= n_new)[0]
+            fresh = np.nonzero(old_q < 0)[0]
+            slot[movers] = holes[:len(movers)]
+            slot[fresh] = holes[len(movers):]
+            src_of_dst = np.full(n_new, L.PATCH_KEEP, dtype=np.int32)
+            src_of_dst[slot[movers]] = old_q[movers]
+            src_of_dst[slot[fresh]] = -1
+            order = np.argsort(slot)  # patch q holds block order[q]
+            blocks = blocks[order]
+            new_slots = slot[fresh].astype(np.int32)
+            storage, cap = old_patches.storage, old_patches.capacity
+        else:
+            src_of_dst = old_q.astype(np.int32)  # -1: newly refined (cleared, then interpolated)
+            new_slots = np.nonzero(old_q < 0)[0].astype(np.int32)
+            # a new arena; the old one is read by the copy below and then released
+            # (stream-ordered: the allocator reuses it only after that copy)
+            storage, cap = None, max(n_new, int(np.ceil(n_new * self.headroom)))
+        self.blocks = blocks
+        self.patches = Patches(2 * self.block, n_new, 0.5 * self.coarse.dx, dtype=dt, device=dev, storage=storage,
+                               clear=False, capacity=cap)
         self._patch_block = torch.from_numpy(blocks.copy()).to(dev)
         bp = np.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=np.int32)
-        bp[blocks[:, 2], blocks[:, 1], blocks[:, 0]] = np.arange(len(blocks), dtype=np.int32)
+        bp[blocks[:, 2], blocks[:, 1], blocks[:, 0]] = np.arange(n_new, dtype=np.int32)
         self._block_patch = torch.from_numpy(bp).to(dev)
-        if old_patches is not None:
-            # the old patch of every new block, through the old block -> patch map (-1: newly refined)
-            b = torch.from_numpy(blocks.astype(np.int64)).to(dev)
-            old_q = old_block_patch[b[:, 2], b[:, 1], b[:, 0]].to(torch.int32).contiguous()
-        else:
-            old_q = torch.full((len(blocks),), -1, dtype=torch.int32, device=dev)
+        sod = torch.from_numpy(src_of_dst).to(dev)
         # whole patch boxes (valid cells and rings; the rings are refilled before use)
         L.call("axs_patches_copy_boxes", C.byref(self.patches.c),
-               C.byref(old_patches.c) if old_patches is not None else None, old_q.data_ptr(), None)
-        new_list = torch.nonzero(old_q < 0).flatten().to(torch.int32).contiguous()
-        if new_list.numel():
+               C.byref(old_patches.c) if old_patches is not None else None, sod.data_ptr(), None)
+        if len(new_slots):
+            lst = torch.from_numpy(new_slots).to(dev)
             L.call("axs_patches_fill_list", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.coarse.c),
-                   None, 0.0, 0.0, 1, new_list.data_ptr(), int(new_list.numel()), None)
-        if self.spare_arena:
-            # the old arena is the next regrid's; the first patch set gets a second one
-            self._spare = old_patches.storage if old_patches is not None else \
-                torch.zeros_like(self.patches.storage)
+                   None, 0.0, 0.0, 1, lst.data_ptr(), int(lst.numel()), None)
 
     def regrid(self, n_error_buf: int = 4, gradient_threshold: float = 1.7976931348623157e308,
                radial_gradient_threshold: float = 1.7976931348623157e308) -> int:

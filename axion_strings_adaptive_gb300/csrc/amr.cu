@@ -58,7 +58,8 @@ struct PatchGeom {
     int64_t plane;   // elements of one component plane (all patches)
 };
 
-static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g)
+// capacity: patch slots the component planes are laid out for (0: npatches)
+static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g, int capacity = 0)
 {
     AXS_REQUIRE(dtype == AXS_F32 || dtype == AXS_F64, AXS_ERR_INVALID_ARGUMENT, "bad dtype %d", dtype);
     AXS_REQUIRE(n >= 8 && n % 8 == 0 && n <= 256, AXS_ERR_UNSUPPORTED, "patch side %d must be a multiple of 8 in [8, 256]",
@@ -72,7 +73,9 @@ static int patch_geom(int32_t dtype, int n, int npatches, PatchGeom &g)
     g.js = (kPatchOX + n + kRingX + 2 + sector - 1) / sector * sector;  // n + 16 (n is a multiple of 8)
     g.ks = g.js * (n + 2 * kPatchRY);
     g.box = (g.ks * (n + 2 * kPatchRZ) + line - 1) / line * line;
-    g.plane = g.box * npatches;
+    AXS_REQUIRE(capacity == 0 || (capacity >= npatches && capacity <= (1 << 22)), AXS_ERR_INVALID_ARGUMENT,
+                "patch capacity %d below the patch count %d", capacity, npatches);
+    g.plane = g.box * (capacity > npatches ? capacity : npatches);
     return AXS_OK;
 }
 
@@ -105,7 +108,7 @@ static int64_t patch_work_bytes(const PatchGeom &g, int32_t dtype, int n, int np
 static int validate_patches(const axs_patches *p, PatchGeom &g)
 {
     AXS_REQUIRE(p != nullptr, AXS_ERR_INVALID_ARGUMENT, "null patches");
-    int rc = patch_geom(p->dtype, p->n, p->npatches, g);
+    int rc = patch_geom(p->dtype, p->n, p->npatches, g, p->capacity);
     if (rc) return rc;
     AXS_REQUIRE(p->dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
     const int64_t need_work = patch_work_bytes(g, p->dtype, p->n, p->npatches);
@@ -905,6 +908,7 @@ __global__ void patch_copy_boxes_kernel(uint4 *__restrict__ dst, const uint4 *__
 {
     for (int q = blockIdx.y; q < np_dst; q += gridDim.y) {
         const int s = src_of_dst[q];
+        if (s == AXS_PATCH_KEEP) continue;  // the box stays as it is
         const bool copy = src != nullptr && s >= 0 && s < np_src;
         for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < 4 * units; u += gridDim.x * blockDim.x) {
             const int c = u / units, r = u - c * units;

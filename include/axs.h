@@ -404,6 +404,9 @@ typedef struct axs_patches {
                          work_bytes = 0 (the fused step covers the patch size and count) */
     void *table;      /* written by axs_patches_init */
     int64_t state_bytes, work_bytes, table_bytes;
+    int32_t capacity; /* patch slots each component plane is laid out for (>= npatches; 0 = npatches):
+                         a regrid that changes npatches keeps every patch's data in place
+                         (size the arenas with axs_patches_layout(dtype, n, capacity)) */
 } axs_patches;
 
 typedef struct axs_patch_plan {
@@ -437,7 +440,12 @@ int axs_patches_fill_list(const axs_patches *p, const axs_patch_map *m, const ax
                           const int32_t *patch_list, int32_t count, void *stream);
 /* Regrid helper: every patch box of dst (4 components, rings and padding
  * included) becomes box src_of_dst[q] of src (device int32 per dst patch), or
- * zeros where that is -1 (src may then be NULL). Same patch side and dtype. */
+ * zeros where that is -1 (src may then be NULL), or is left as it is where
+ * that is AXS_PATCH_KEEP. Same patch side and dtype. src and dst may share
+ * their arena (same state pointer and capacity) when no box is both read and
+ * written: a regrid in place moves patches from slots >= dst->npatches into
+ * the free slots below it. */
+#define AXS_PATCH_KEEP (-2)
 int axs_patches_copy_boxes(const axs_patches *dst, const axs_patches *src, const int32_t *src_of_dst, void *stream);
 /* One RK4 step of every patch (two persistent launches); the rings must hold
  * psi, Pi at time t. */

@@ -327,6 +327,45 @@ def test_regrid_keeps_the_fine_data_of_blocks_that_stay_refined(axs):
             assert not bool((v == 7.0).any()) and float(v.abs().max()) > 0.0
 
 
+def test_regrid_in_place_moves_kept_patches_into_free_slots(axs):
+    """Six patches (arena laid out for 8 slots), then a set that drops the four
+    lowest slots, keeps the two highest and adds one: the regrid stays in the
+    arena, moves the kept patches down into slots 0 and 1 with their data, and
+    the new patch interpolates the coarse level; then a set past the capacity
+    moves everything to a new arena, data intact."""
+    from axion_strings_adaptive_gb300.amr import TwoLevel
+    N, block = 64, 16
+    coarse = axs.PeriodicLevel(N, 0.5, dtype=torch.float32)
+    coarse.set_state(torch.randn((4, N, N, N)).cuda())
+    two = TwoLevel(coarse, block, headroom=1.34)
+    first = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [3, 0, 0], [0, 1, 0], [1, 1, 0]])
+    two.set_blocks(first)
+    assert two.patches.capacity == 9
+    arena = two.patches.storage.data_ptr()
+    for q in range(6):
+        two.patches.valid(q).fill_(float(q + 7))
+    marks = {tuple(b): float(q + 7) for q, b in enumerate(two.blocks)}
+    two.set_blocks(np.array([[1, 1, 0], [3, 3, 3], [0, 1, 0]]))
+    assert two.patches.storage.data_ptr() == arena and two.patches.npatches == 3
+    for q, b in enumerate(two.blocks):
+        v = two.patches.valid(q)
+        if tuple(b) in marks:
+            assert bool((v == marks[tuple(b)]).all()), tuple(b)
+        else:
+            assert not bool((v >= 7.0).all()) and float(v.abs().max()) > 0.0
+    assert int((two._block_patch >= 0).sum()) == 3
+    for q, b in enumerate(two.blocks):
+        assert int(two._block_patch[b[2], b[1], b[0]]) == q
+    kept = {tuple(b): two.patches.valid(q).clone() for q, b in enumerate(two.blocks)}
+    bigger = np.array([[i % 4, (i // 4) % 4, i // 16] for i in range(12)] + [[3, 3, 3]])
+    bigger = np.unique(np.concatenate([bigger, np.array([[1, 1, 0], [0, 1, 0]])]), axis=0)
+    two.set_blocks(bigger)
+    assert two.patches.npatches == len(bigger) and two.patches.capacity >= len(bigger)
+    for q, b in enumerate(two.blocks):
+        if tuple(b) in kept:
+            assert torch.equal(two.patches.valid(q), kept[tuple(b)]), tuple(b)
+
+
 def test_patch_counts_past_the_grid_and_two_sweep_limits(axs):
     """70 000 patches: past the two-sweep step's 32 767 (its work items carry box
     numbers in 16 bits) and past one grid's 65 535 z slices (the fused step then
@@ -341,7 +380,7 @@ def test_patch_counts_past_the_grid_and_two_sweep_limits(axs):
     st[0], st[2] = 1.0, 1.0
     coarse.set_state(st)
     del st
-    two = TwoLevel(coarse, block, spare_arena=False)
+    two = TwoLevel(coarse, block, headroom=1.0)
     nbx, nby = nx // block, ny // block
     q = np.arange(70000)
     two.set_blocks(np.stack([q % nbx, (q // nbx) % nby, q // (nbx * nby)], axis=1))
