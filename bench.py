@@ -162,6 +162,42 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- CPU baseline table
+def cpu_table():
+    """The CPU oracle (OpenMP over all host cores) on the configurations of the
+    reference's CPU baseline table: RK4 site-updates/s and one diagnostics pass
+    (counts, 14 energy sums, velocity) per configuration, both precisions."""
+    import numpy as np
+    from oracle import oracle as O
+    O.lib()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    rows = []
+    for n, c0, kdiv, prec, steps in ((64, 1.0, 4, "f64", 100), (64, 1.0, 4, "f32", 100), (512, 2.0, 8, "f32", 4),
+                                     (512, 2.0, 8, "f64", 3)):
+        v = O.fourier_ic_state(n, O.strict_cutoff(n / kdiv), seed=SEED)
+        if prec == "f32":
+            v = v.astype(np.float32)
+        fab = O.to_fab(v, 2)
+        del v
+        bg = O.background(a_inv=A_INV, c0=c0, lambda_scale=LAMBDA0)
+        O.rk4_advance(fab, 2, DX, bg, TAU_I, 0.0, DT, 1)
+        t0 = time.perf_counter()
+        O.rk4_advance(fab, 2, DX, bg, TAU_I, DT, DT, steps)
+        el = time.perf_counter() - t0
+        tau = TAU_I + (steps + 1) * DT
+        co = O.background_eval(bg, tau)[0]
+        R, lam = co[0], co[3]
+        t1 = time.perf_counter()
+        O.count_plaquettes(fab, 2)
+        O.energy_sums(fab, 2, DX, R, lam, co[1] / R, O.MASK_A, 0.8)
+        O.velocity(fab, 2, R, co[1] / R, float(np.sqrt(lam)))
+        dg = time.perf_counter() - t1
+        rows.append({"grid": n, "c0": c0, "precision": prec, "steps": steps, "cores": cores,
+                     "site_updates_per_s": n ** 3 * steps / el, "diag_pass_ms": 1e3 * dg})
+        del fab
+    print(json.dumps({"cpu_table": rows, "host_cores": os.cpu_count()}), flush=True)
+
+
 # ---------------------------------------------------------------- drop-in per-stage path
 def dropin_report(A, ic, dev, n=512, steps=4, warmup=1):
     """The one-for-one replacement of specific_eval_rhs under a host RK driver
@@ -891,6 +927,7 @@ def main():
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-batching", action="store_true")
     ap.add_argument("--no-dropin", action="store_true")
+    ap.add_argument("--cpu-table", action="store_true", help="time the CPU oracle for the baseline table and exit")
     ap.add_argument("--no-scale", action="store_true")
     ap.add_argument("--scale-n", type=int, default=512)
     ap.add_argument("--scale-steps", type=int, default=20)
@@ -902,6 +939,9 @@ def main():
     ap.add_argument("--diff-steps", type=int, default=200)
     ap.add_argument("--diff-directions", type=int, default=16)
     args = ap.parse_args()
+    if args.cpu_table:
+        cpu_table()
+        return
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
     if args.impl == "reference":
