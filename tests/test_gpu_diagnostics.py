@@ -283,15 +283,28 @@ def _finder_cases(orc, n):
     r = rng.standard_normal((4, n, n, n))
     r[2:] = 0.0
     yield "rand", r
+    # phases on multiples of pi/4: vertices on the real axis (imaginary parts +0
+    # and -0), edges exactly pi apart, tiny and zero magnitudes
+    k = rng.integers(0, 8, size=(n, n, n))
+    mag = rng.choice([0.5, 1.0, 2.0, 1e-20, 0.0], size=(n, n, n), p=[0.3, 0.3, 0.3, 0.05, 0.05])
+    a = np.zeros_like(v)
+    a[0] = mag * np.cos(k * np.pi / 4)
+    a[1] = mag * np.sin(k * np.pi / 4)
+    on_axis = k % 4 == 0
+    a[1][on_axis] = np.where(rng.random(on_axis.sum()) < 0.5, 0.0, -0.0)
+    a[0][k % 4 == 2] = 0.0
+    yield "axes", a
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("n", [24, 40])
 def test_string_finder_alone_equals_fused_pass(axs, orc, dtype, n):
-    """The edge-code finder against the fused pass (itself pinned to the
-    reference above): counts, near-ties and the pierced set, on fields that
-    take the double fall-back (zeros, huge values, edges pi apart) and on a
-    dense random field, at a size that leaves partial tiles."""
+    """The windings-only finder (FP32: the phase-free finder; FP64: the
+    edge-code finder) against the fused pass (itself pinned to the reference
+    above): counts, near-ties and the pierced set, on fields that take the
+    double fall-back (zeros, huge values, edges pi apart, phases on the real
+    axis with signed zeros) and on a dense random field, at a size that leaves
+    partial tiles."""
     bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
     for name, v in _finder_cases(orc, n):
         lvl = axs.PeriodicLevel(n, 0.5, dtype=dtype, pierced_capacity=3 * n ** 3)
