@@ -989,329 +989,6 @@ __global__ void __launch_bounds__(kDiagThreads, (sizeof(T) == 4 && !VEL) ? 4 : 3
 }
 
 // ---------------------------------------------------------------- FP32 per-cell energy sums
-// ---------------------------------------------------------------------------
-// Phase-free string finder for FP32 fields (windings only: the string finder
-// alone, the tagger's plaquette criterion, the composite finder over patches).
-//
-// The fold of an edge a -> b, (d < -pi) - (d > pi) with d = atan2(b) - atan2(a)
-// and each phase in (-pi, pi], is nonzero only when a and b lie in opposite
-// half planes (Im a, Im b of opposite sign): for a in the upper half and b in
-// the lower, d < -pi exactly when the cross product a x b = |a||b| sin d is
-// positive (fold +1); for a lower and b upper, d > pi exactly when it is
-// negative (fold -1). Vertices on the positive real axis (Im = 0, Re > 0,
-// phase 0) never fold. So no phase is needed: a vertex carries two half-plane
-// bits, and a cell whose 7 vertices all share one half has windings 0 -- most
-// cells, decided from 7 flag bytes. The other cells evaluate the cross products
-// of their edges that join opposite halves.
-//
-// Exactness against the reference's double atan2: a vertex within 1e-5 rad of
-// the negative real axis (where a phase sits next to the +-pi cut), or with
-// max(|Re|, |Im|) outside (1e-15, 1e15) (products of two such values then stay
-// normal floats), or NaN, and an edge whose |cross| falls below
-// 1e-5 (|Re a| + |Im a|) (|Re b| + |Im b|) (nearly parallel or opposite
-// vectors), send the cell to the reference's double arithmetic after its
-// z-chunk, as in the other finders. Outside those margins the float cross
-// product (error below 2^-22 of the bound) and the double phases of the
-// reference decide every fold alike, and near ties (within 1e-12 of pi) lie
-// inside the margins, so their count comes from the double path too.
-//
-// Per vertex plane, with one block barrier: the thread's vertices' flags and
-// values into a 3-slot shared-memory ring, then the cells of the plane below.
-struct PfVertex {
-    float re, im;
-};
-struct FinderPfSmem {
-    long long lbuf[kFinderListBuf];
-    int badq[kFinderBadQ];
-    PfVertex val[3][FVY][FVX];
-    unsigned char fl[3][FVY][FVX];  // bit 0: Im > 0, bit 1: Im < 0, bit 2: the cell goes to the double path
-};
-
-__device__ __forceinline__ unsigned pf_flags(float re, float im)
-{
-    const float are = fabsf(re), aim = fabsf(im);
-    const float m = fmaxf(are, aim);
-    const bool in_range = m > 1e-15f && m < 1e15f;  // false for NaN
-    const bool near_cut = re < 0.f && aim <= __fmul_rn(1e-5f, are);
-    return (im > 0.f ? 1u : 0u) | (im < 0.f ? 2u : 0u) | ((!in_range || near_cut) ? 4u : 0u);
-}
-
-// Fold of the edge a -> b between two vertices without the double-path flag;
-// sets *bad when the cross product lies inside the margin.
-__device__ __forceinline__ int pf_fold(PfVertex a, unsigned fa, PfVertex b, unsigned fb, bool &bad)
-{
-    const bool up_down = (fa & 1u) && (fb & 2u), down_up = (fa & 2u) && (fb & 1u);
-    if (!(up_down || down_up)) return 0;
-    const float cr = __fsub_rn(__fmul_rn(a.re, b.im), __fmul_rn(a.im, b.re));
-    const float bound = __fmul_rn(__fmul_rn(1e-5f, __fadd_rn(fabsf(a.re), fabsf(a.im))),
-                                  __fadd_rn(fabsf(b.re), fabsf(b.im)));
-    if (!(fabsf(cr) > bound)) {
-        bad = true;
-        return 0;
-    }
-    return up_down ? (cr > 0.f ? 1 : 0) : (cr < 0.f ? -1 : 0);
-}
-
-// The three windings (xy, yz, zx: StringFinder.hpp:45-68 order) of a cell from
-// its 7 corners, or false for the double path.
-__device__ __forceinline__ bool pf_cell(const PfVertex (&v)[7], const unsigned (&f)[7], int (&w)[3])
-{
-    // corners 000, 100, 110, 010, 001, 101, 011
-    bool bad = false;
-    const int e_x000 = pf_fold(v[0], f[0], v[1], f[1], bad), e_y000 = pf_fold(v[0], f[0], v[3], f[3], bad);
-    const int e_z000 = pf_fold(v[0], f[0], v[4], f[4], bad), e_y100 = pf_fold(v[1], f[1], v[2], f[2], bad);
-    const int e_x010 = pf_fold(v[3], f[3], v[2], f[2], bad), e_z010 = pf_fold(v[3], f[3], v[6], f[6], bad);
-    const int e_y001 = pf_fold(v[4], f[4], v[6], f[6], bad), e_x001 = pf_fold(v[4], f[4], v[5], f[5], bad);
-    const int e_z100 = pf_fold(v[1], f[1], v[5], f[5], bad);
-    w[0] = e_x000 + e_y100 - e_x010 - e_y000;
-    w[1] = e_y000 + e_z010 - e_y001 - e_z000;
-    w[2] = e_z000 + e_x001 - e_z100 - e_x000;
-    return !bad;
-}
-
-// The same decision read from global memory (a chunk whose double-path queue
-// overflowed is searched again cell by cell): true when the cell goes to the
-// double path.
-__device__ __noinline__ bool pf_cell_bad(const DiagView v, const float *base, int x, int y, int z)
-{
-    const int dx_[7] = {0, 1, 1, 0, 0, 1, 0}, dy_[7] = {0, 0, 1, 1, 0, 0, 1}, dz_[7] = {0, 0, 0, 0, 1, 1, 1};
-    PfVertex c[7];
-    unsigned f[7], orf = 0;
-    for (int k = 0; k < 7; ++k) {
-        const int xx = x + dx_[k], yy = y + dy_[k], zz = z + dz_[k];
-        const bool on = (v.wx || xx < v.nx + v.ox) && (v.wy || yy < v.ny + v.oy) && (v.wz || zz < v.nz + v.oz);
-        c[k].re = on ? base[view_off<float>(v, 0, xx, yy, zz)] : 0.f;
-        c[k].im = on ? base[view_off<float>(v, 1, xx, yy, zz)] : 0.f;
-        f[k] = pf_flags(c[k].re, c[k].im);
-        orf |= f[k];
-    }
-    if (orf & 4u) return true;
-    int w[3];
-    return !pf_cell(c, f, w);
-}
-
-__global__ void __launch_bounds__(kDiagThreads, 4)
-    finder_pf_kernel(const DiagView v, const uint8_t *__restrict__ mask, DiagPartial *__restrict__ partials,
-                     unsigned long long *__restrict__ list_counter, long long *__restrict__ list, long long capacity,
-                     int tiles_x, int ntiles, int zchunk, long long n_items, long long items_per_box,
-                     int64_t box_stride, uint8_t *__restrict__ tags)
-{
-    extern __shared__ __align__(16) unsigned char finder_pf_smem_raw[];
-    FinderPfSmem &sm = *reinterpret_cast<FinderPfSmem *>(finder_pf_smem_raw);
-    __shared__ int lcount, flush_n, badn, bad_over;
-    __shared__ unsigned long long flush_base;
-    __shared__ long long red[kDiagThreads / 32][4];
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int lx = tid % FTX, ly = tid / FTX;  // cells (lx, ly) and (lx, ly + FTY / 2)
-    const int64_t box_cells = (int64_t)v.nx * v.ny * v.nz;
-    int cnt_p = 0, cnt_w = 0, cnt_tie = 0;
-    if (tid == 0) lcount = badn = bad_over = 0;
-    int warp_end = 0;
-    auto flush = [&]() {
-        if (tid == 0) {
-            const int nb = lcount;
-            flush_n = nb;
-            flush_base = nb ? atomicAdd(list_counter, (unsigned long long)nb) : 0ull;
-            lcount = 0;
-        }
-        __syncthreads();
-        const int nb = flush_n;
-        const unsigned long long b0 = flush_base;
-        for (int i = tid; i < nb; i += kDiagThreads)
-            if (b0 + i < (unsigned long long)capacity) list[b0 + i] = sm.lbuf[i];
-        __syncthreads();
-        warp_end = 0;
-    };
-    auto redo_cell = [&](const float *base, long long qbox, int x, int y, int z) {
-        const CellWindings cw = finder_cell_double<float>(v, base, x, y, z);
-        const int64_t cell = qbox * box_cells + (int64_t)x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z);
-        cnt_tie += cw.ties;
-        if (tags != nullptr) tags[cell] = (cw.w[0] | cw.w[1] | cw.w[2]) != 0;
-#pragma unroll
-        for (int pl = 0; pl < 3; ++pl) {
-            if (!cw.w[pl]) continue;
-            ++cnt_p;
-            cnt_w += abs(cw.w[pl]);
-            if (list != nullptr) {
-                const unsigned long long pos = atomicAdd(list_counter, 1ull);
-                if (pos < (unsigned long long)capacity) list[pos] = 4LL * cell + pl;
-            }
-        }
-    };
-
-    const bool extra = tid < kFinderExtra;
-    const int vi[3] = {lx, lx, tid < FTX ? tid : FTX};
-    const int vj[3] = {ly, ly + FTY / 2, tid < FTX ? FTY : (extra ? tid - FTX : 0)};
-
-    for (long long item = blockIdx.x; item < n_items; item += gridDim.x) {
-        const long long qbox = item / items_per_box, box_item = item % items_per_box;
-        const float *__restrict__ base = static_cast<const float *>(v.data) + qbox * box_stride;
-        const int tile = (int)(box_item % ntiles), chunk = (int)(box_item / ntiles);
-        const int x0 = (tile % tiles_x) * FTX, y0 = (tile / tiles_x) * FTY;
-        const int za = chunk * zchunk, len = min(zchunk, v.nz - za);
-        int voff[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int xx = x0 + vi[k], yy = y0 + vj[k];
-            const bool on = (k < 2 || extra) && xx <= v.nx && yy <= v.ny && (v.wx || xx < v.nx + v.ox) &&
-                            (v.wy || yy < v.ny + v.oy);
-            voff[k] = on ? (wrap_or_self(xx, v.nx, v.wx) + v.ox) + (wrap_or_self(yy, v.ny, v.wy) + v.oy) * (int)v.js
-                         : -1;
-        }
-        int lz = za, lzw = wrap_or_self(za, v.nz, v.wz);
-        auto load_plane = [&](float(&buf)[3][2]) {
-            const bool zin = v.wz || lz < v.nz + v.oz;
-            const float *pb = base + (int64_t)(lzw + v.oz) * v.ks;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const bool on = zin && voff[k] >= 0;
-                buf[k][0] = on ? __ldg(pb + voff[k]) : 0.f;
-                buf[k][1] = on ? __ldg(pb + voff[k] + v.cs) : 0.f;
-            }
-            ++lz;
-            lzw = v.wz ? (lzw + 1 == v.nz ? 0 : lzw + 1) : lzw + 1;
-        };
-        // vertex plane za + j into slot j mod 3
-        auto vertex_stage = [&](int j, const float(&buf)[3][2]) {
-            const int s = j % 3;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                if (k == 2 && !extra) break;
-                sm.val[s][vj[k]][vi[k]] = PfVertex{buf[k][0], buf[k][1]};
-                sm.fl[s][vj[k]][vi[k]] = (unsigned char)pf_flags(buf[k][0], buf[k][1]);
-            }
-        };
-        // cells of plane za + j - 1 (vertex planes in slots (j - 1) mod 3 and j mod 3)
-        auto cell_stage = [&](int j) {
-            const int s0 = (j + 2) % 3, s1 = j % 3, z = za + j - 1;
-            const int64_t cell0 = qbox * box_cells + (int64_t)(x0 + lx) +
-                                  (int64_t)v.nx * ((int64_t)(y0 + ly) + (int64_t)v.ny * z);
-            const int64_t hstep = (int64_t)v.nx * (FTY / 2);
-            unsigned pm = 0;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int cy = ly + h * (FTY / 2), x = x0 + lx, y = y0 + cy;
-                if (!(x < v.nx && y < v.ny)) continue;
-                const int64_t cell = cell0 + h * hstep;
-                if (mask != nullptr && mask[cell] == 0) continue;
-                unsigned f[7];
-                f[0] = sm.fl[s0][cy][lx];
-                f[1] = sm.fl[s0][cy][lx + 1];
-                f[2] = sm.fl[s0][cy + 1][lx + 1];
-                f[3] = sm.fl[s0][cy + 1][lx];
-                f[4] = sm.fl[s1][cy][lx];
-                f[5] = sm.fl[s1][cy][lx + 1];
-                f[6] = sm.fl[s1][cy + 1][lx];
-                const unsigned orf = f[0] | f[1] | f[2] | f[3] | f[4] | f[5] | f[6];
-                if (orf & 4u) {  // the double path after the chunk
-                    const int slot = atomicAdd(&badn, 1);
-                    if (slot < kFinderBadQ)
-                        sm.badq[slot] = lx | (cy << 5) | ((z - za) << 9);
-                    else
-                        bad_over = 1;
-                    continue;
-                }
-                int w[3] = {0, 0, 0};
-                // opposite halves among the corners: some edge may fold
-                if ((orf & 3u) == 3u) {
-                    const PfVertex c[7] = {sm.val[s0][cy][lx],     sm.val[s0][cy][lx + 1], sm.val[s0][cy + 1][lx + 1],
-                                           sm.val[s0][cy + 1][lx], sm.val[s1][cy][lx],     sm.val[s1][cy][lx + 1],
-                                           sm.val[s1][cy + 1][lx]};
-                    if (!pf_cell(c, f, w)) {
-                        const int slot = atomicAdd(&badn, 1);
-                        if (slot < kFinderBadQ)
-                            sm.badq[slot] = lx | (cy << 5) | ((z - za) << 9);
-                        else
-                            bad_over = 1;
-                        continue;
-                    }
-                }
-                const unsigned cm = (w[0] != 0) | (w[1] != 0) << 1 | (w[2] != 0) << 2;
-                if (tags != nullptr) tags[cell] = cm != 0;
-                cnt_w += abs(w[0]) + abs(w[1]) + abs(w[2]);
-                pm |= cm << (3 * h);
-            }
-            const int mine = __popc(pm);
-            cnt_p += mine;
-            if (list != nullptr && __any_sync(0xffffffffu, mine != 0)) {
-                int incl = mine;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int yv = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += yv;
-                }
-                const int wtot = __shfl_sync(0xffffffffu, incl, 31);
-                int wbase = 0;
-                if (lane == 31) wbase = atomicAdd(&lcount, wtot);
-                wbase = __shfl_sync(0xffffffffu, wbase, 31);
-                warp_end = wbase + wtot;
-                int pos = wbase + incl - mine;
-                const long long e0 = 4LL * cell0, eh = 4LL * hstep - 3;
-                while (pm) {
-                    const int b = __ffs(pm) - 1;
-                    pm &= pm - 1;
-                    sm.lbuf[pos++] = e0 + b + (b >= 3 ? eh : 0);  // 4 cell + plane
-                }
-            }
-        };
-        // iteration j: the vertices of plane za + j, the block barrier, the cells of
-        // plane za + j - 1; registers hold planes j + 1 and j + 2 (unrolled by two)
-        auto step = [&](int j, float(&buf)[3][2]) {
-            if (j <= len) {
-                vertex_stage(j, buf);
-                if (j + 2 <= len) load_plane(buf);
-            }
-            if (__syncthreads_or(warp_end > kFinderFlushAt)) flush();
-            if (j >= 1) cell_stage(j);
-        };
-        float bufa[3][2], bufb[3][2];
-        load_plane(bufa);
-        load_plane(bufb);
-        for (int j = 0; j < len + 1; j += 2) {
-            step(j, bufa);
-            if (j + 1 < len + 1) step(j + 1, bufb);
-        }
-        __syncthreads();
-        const int nbad = badn;
-        if (!bad_over) {
-            for (int i = tid; i < nbad; i += kDiagThreads) {
-                const int e = sm.badq[i];
-                redo_cell(base, qbox, x0 + (e & 31), y0 + ((e >> 5) & 15), za + (e >> 9));
-            }
-        } else {
-            for (int c = tid; c < FTX * FTY * len; c += kDiagThreads) {
-                const int x = x0 + c % FTX, y = y0 + (c / FTX) % FTY, z = za + c / (FTX * FTY);
-                if (x >= v.nx || y >= v.ny) continue;
-                if (mask != nullptr &&
-                    mask[qbox * box_cells + x + (int64_t)v.nx * ((int64_t)y + (int64_t)v.ny * z)] == 0)
-                    continue;
-                if (pf_cell_bad(v, base, x, y, z)) redo_cell(base, qbox, x, y, z);
-            }
-        }
-        __syncthreads();
-        if (tid == 0) badn = bad_over = 0;
-    }
-    if (list != nullptr && __syncthreads_or(warp_end > 0)) flush();
-
-    long long c4[4] = {cnt_p, cnt_w, 0, cnt_tie};
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-        for (int o = 16; o > 0; o >>= 1) c4[s] += __shfl_down_sync(0xffffffffu, c4[s], o);
-        if (lane == 0) red[tid >> 5][s] = c4[s];
-    }
-    __syncthreads();
-    if (tid < 14) {
-        partials[blockIdx.x].e[tid] = 0.0;
-    } else if (tid == 14) {
-        partials[blockIdx.x].vsum = 0.0;
-    } else if (tid >= 32 && tid < 36) {
-        const int f = tid - 32;
-        long long xv = 0;
-        for (int ww = 0; ww < kDiagThreads / 32; ++ww) xv += red[ww][f];
-        partials[blockIdx.x].cnt[f] = xv;
-    }
-}
-
 // The per_cell_fp32 energy sums on FP32 fields, run beside finder_kernel<float, VEL>
 // (windings, the pierced list and the velocity), each kernel with few registers.
 // A block owns a FTX x FTY tile, two cells per thread, and marches in z. psi of the
@@ -1727,20 +1404,11 @@ static int run_diag(const DiagView &v, const axs_diag_params *p, const uint8_t *
         return launch_status("string finder");
     };
     if (q.want_plaq && !q.want_energy && !q.want_vel && offs31) {
-        // windings only: the phase-free finder (FP32 fields) or the edge-code finder (FP64)
+        // windings only: the edge-code finder
         const bool f32 = v.dtype != AXS_F64;
         diag_plan(v, nboxes, diag_grid(ncell), FTX, FTY, f32 ? 4 : 3, tiles_x, ntiles, zchunk, items_per_box, items,
                   grid);
-        if (f32) {
-            AXS_CUDA_CHECK(cudaFuncSetAttribute(finder_pf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)sizeof(FinderPfSmem)));
-            finder_pf_kernel<<<grid, kDiagThreads, sizeof(FinderPfSmem), st>>>(
-                v, mask, partials, counter, lst, capacity, tiles_x, ntiles, zchunk, items, items_per_box, box_stride,
-                tags);
-            rc0 = launch_status("string finder");
-        } else {
-            rc0 = launch_finder(finder_kernel<double, false>, 0);
-        }
+        rc0 = f32 ? launch_finder(finder_kernel<float, false>, 0) : launch_finder(finder_kernel<double, false>, 0);
         if (rc0) return rc0;
         diag_finalize_kernel<<<1, 256, 0, st>>>(partials, grid, counter, capacity, lst != nullptr, out);
         return launch_status("diagnostics finalize");

@@ -340,31 +340,30 @@ __global__ void __launch_bounds__(S::THREADS, 1)
 
 // The periodic padding of one level-layout buffer (4 components): columns
 // x = -8 .. -1 and nx .. nx+7 of rows y = -2 .. ny+1, and rows y = -2, -1, ny,
-// ny+1 of columns 0 .. nx-1, each a copy of the valid cell it wraps to. One
-// thread per padding element; consecutive threads take consecutive elements
-// of a padding row.
+// ny+1 of columns 0 .. nx-1, each a copy of the valid cell it wraps to. Grid
+// rows are planes (z + nz c); within a plane, consecutive threads take
+// consecutive elements of a padding row.
 template <typename T>
 __global__ void level_pad_kernel(T *__restrict__ buf, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
                                  int ox, int oy)
 {
-    const int64_t per_plane = 16LL * (ny + 4) + 4LL * nx;
-    const int64_t n = per_plane * nz * 4;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = q % per_plane, zc = q / per_plane;
-        int x, y;
-        if (r < 16LL * (ny + 4)) {  // x padding: 16 columns of every padded row
-            const int k = (int)(r % 16);
-            x = k < 8 ? k - 8 : nx + (k - 8);
-            y = (int)(r / 16) - 2;
-        } else {  // y padding: 4 rows of the valid columns
-            const int64_t rr = r - 16LL * (ny + 4);
-            x = (int)(rr % nx);
-            const int k = (int)(rr / nx);
-            y = k < 2 ? k - 2 : ny + (k - 2);
+    const int xpad = 16 * (ny + 4), per_plane = xpad + 4 * nx;
+    for (int plane = blockIdx.y; plane < 4 * nz; plane += gridDim.y) {
+        T *p = buf + (int64_t)(plane / nz) * cs + (int64_t)(plane % nz) * ks + ox + (int64_t)oy * js;
+        for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < per_plane; r += gridDim.x * blockDim.x) {
+            int x, y;
+            if (r < xpad) {  // x padding: 16 columns of every padded row
+                const int k = r & 15;
+                x = k < 8 ? k - 8 : nx + (k - 8);
+                y = (r >> 4) - 2;
+            } else {  // y padding: 4 rows of the valid columns
+                const int rr = r - xpad, k = rr / nx;
+                x = rr - k * nx;
+                y = k < 2 ? k - 2 : ny + (k - 2);
+            }
+            const int xs = x < 0 ? x + nx : (x >= nx ? x - nx : x), ys = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+            p[x + (int64_t)y * js] = p[xs + (int64_t)ys * js];
         }
-        const int xs = x < 0 ? x + nx : (x >= nx ? x - nx : x), ys = y < 0 ? y + ny : (y >= ny ? y - ny : y);
-        T *p = buf + (zc / nz) * cs + (zc % nz) * ks;
-        p[(x + ox) + (int64_t)(y + oy) * js] = p[(xs + ox) + (int64_t)(ys + oy) * js];
     }
 }
 

@@ -205,8 +205,8 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
         int grid = 0;
         plan_chunks(a.ntiles, lv->nz, sms, a.zchunk, a.n_items, grid);
         fill_level_constants(a, lv, g, r.dt);
-        const int64_t pad_n = (16LL * (lv->ny + 4) + 4LL * lv->nx) * lv->nz * 4;
-        const int pad_grid = (int)std::min<int64_t>((pad_n + 255) / 256, (int64_t)sms * 8);
+        const int pad_per_plane = 16 * (lv->ny + 4) + 4 * lv->nx;
+        const dim3 pad_grid((unsigned)std::min(64, (pad_per_plane + 255) / 256), (unsigned)std::min(4 * lv->nz, 65535));
         float *buf[2] = {static_cast<float *>(lv->state), static_cast<float *>(lv->work)};
         LevelFusedMaps maps[2];
         int rc;
