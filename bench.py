@@ -386,7 +386,7 @@ def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 
     ms_levels = timed(per_box)
     del levels
     torch.cuda.empty_cache()
-    words = 24  # compulsory words per site per RK4 step (two sweeps of 4+8 and 8+4)
+    words = 28  # compulsory words per site per RK4 step (two sweeps of 4+8 and 12+4)
     return {"config": f"{nboxes} boxes, sizes uniform from {list(sizes)}^3 (seed {SEED}), FP32, c0=1, lambda0=2, "
                       f"IC |n|<N/4 seed+box, {nsteps} RK4 steps, per-box energy + winding diagnostics",
             "sizes": {str(k): ns.count(k) for k in sizes}, "sites": sites, "steps": nsteps,
@@ -499,7 +499,9 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
                                                C.byref(two.old_c), C.byref(coarse.c), theta, DT, 0, None))[0]
         parts["fine_step"] = ev_ms(lambda: p.step(bg, TAU_I, tau, 0.5 * DT))[0]
         parts["ring_cells_per_fill"] = p.npatches * ((2 * block + 12) * (2 * block + 8) ** 2 - (2 * block) ** 3)
-    fine_words = 24  # per fine site-update, as on the coarse level (ghost-ring work excluded)
+    # per site-update as the two sweeps move them on the coarse level (ghost-ring work excluded;
+    # the fused patch step moves fewer)
+    fine_words = 28
     out = {"config": f"{n}^3 FP32 base, physical mode c0=0, lambda=2, IC |n|<N/{kdiv}, 2x-refined "
                      f"{2 * block}^3-cell patches on tagged {block}^3 blocks (n_error_buf={n_error_buf}), {steps} "
                      f"coarse steps with 2 subcycled fine steps each, regrid every {regrid_every}",
