@@ -13,6 +13,27 @@ __host__ __device__ __forceinline__ int64_t fab_off(const axs_fab &f, int i, int
     return (int64_t)(i + f.ng) + (int64_t)(j + f.ng) * f.jstride + (int64_t)(k + f.ng) * f.kstride;
 }
 
+// The kernels below walk x rows one warp per row: a row's (j, k, component)
+// comes from two 32-bit divisions per row, and the lanes read and write
+// consecutive x. Warps take rows with a grid stride.
+__device__ __forceinline__ int row_warp() { return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
+__device__ __forceinline__ int row_warps() { return (int)((gridDim.x * blockDim.x) >> 5); }
+
+struct RowIdx {
+    int j, k, c;
+};
+
+// Row r of `ny` rows per plane and `nz` planes per component.
+__device__ __forceinline__ RowIdx row_index(int r, int ny, int nz)
+{
+    RowIdx q;
+    const int plane = r / ny;
+    q.j = r - plane * ny;
+    q.c = plane / nz;
+    q.k = plane - q.c * nz;
+    return q;
+}
+
 // ---------------------------------------------------------------- RHS
 // AxionStringsRHS<FourthOrderDerivatives>::operator() (AxionStringsRHS.impl.hpp:25-60).
 // FP64: evaluated with the reference's expression order and explicit
@@ -37,98 +58,168 @@ __global__ void eval_rhs_f64_kernel(const axs_fab s, const axs_fab r, double one
 {
     const double *__restrict__ sp = static_cast<const double *>(s.data);
     double *__restrict__ rp = static_cast<double *>(r.data);
-    const int64_t n = (int64_t)s.nx * s.ny * s.nz;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(q % s.nx), j = (int)((q / s.nx) % s.ny), k = (int)(q / ((int64_t)s.nx * s.ny));
-        const int64_t o = fab_off(s, i, j, k);
-        const int64_t st[3] = {1, s.jstride, s.kstride};
-        double lap1 = 0.0, lap2 = 0.0;
+    const int rows = s.ny * s.nz, lane = threadIdx.x & 31;
+    const int64_t st[3] = {1, s.jstride, s.kstride};
+    for (int row = row_warp(); row < rows; row += row_warps()) {
+        const RowIdx q = row_index(row, s.ny, s.nz);
+        const int64_t o0 = fab_off(s, 0, q.j, q.k), r0 = fab_off(r, 0, q.j, q.k);
+        for (int i = lane; i < s.nx; i += 32) {
+            const int64_t o = o0 + i;
+            double lap1 = 0.0, lap2 = 0.0;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) lap1 = __dadd_rn(lap1, diff2_exact(sp + o, st[d], one_over_dx2));
+            for (int d = 0; d < 3; ++d) lap1 = __dadd_rn(lap1, diff2_exact(sp + o, st[d], one_over_dx2));
 #pragma unroll
-        for (int d = 0; d < 3; ++d) lap2 = __dadd_rn(lap2, diff2_exact(sp + s.cstride + o, st[d], one_over_dx2));
-        const double psi1 = sp[o], psi2 = sp[s.cstride + o];
-        const double dsq = __dsub_rn(__dadd_rn(__dmul_rn(psi1, psi1), __dmul_rn(psi2, psi2)), R2);
-        const double pc = __dmul_rn(__dmul_rn(0.5, lambda), dsq);
-        const int64_t ro = fab_off(r, i, j, k);
-        rp[ro] = sp[2 * s.cstride + o];
-        rp[r.cstride + ro] = sp[3 * s.cstride + o];
-        rp[2 * r.cstride + ro] = __dsub_rn(__dadd_rn(lap1, __dmul_rn(kappa, psi1)), __dmul_rn(pc, psi1));
-        rp[3 * r.cstride + ro] = __dsub_rn(__dadd_rn(lap2, __dmul_rn(kappa, psi2)), __dmul_rn(pc, psi2));
+            for (int d = 0; d < 3; ++d) lap2 = __dadd_rn(lap2, diff2_exact(sp + s.cstride + o, st[d], one_over_dx2));
+            const double psi1 = sp[o], psi2 = sp[s.cstride + o];
+            const double dsq = __dsub_rn(__dadd_rn(__dmul_rn(psi1, psi1), __dmul_rn(psi2, psi2)), R2);
+            const double pc = __dmul_rn(__dmul_rn(0.5, lambda), dsq);
+            const int64_t ro = r0 + i;
+            rp[ro] = sp[2 * s.cstride + o];
+            rp[r.cstride + ro] = sp[3 * s.cstride + o];
+            rp[2 * r.cstride + ro] = __dsub_rn(__dadd_rn(lap1, __dmul_rn(kappa, psi1)), __dmul_rn(pc, psi1));
+            rp[3 * r.cstride + ro] = __dsub_rn(__dadd_rn(lap2, __dmul_rn(kappa, psi2)), __dmul_rn(pc, psi2));
+        }
     }
 }
 
 // FP32 (the reference's default PRECISION=FLOAT build): single-precision
-// arithmetic throughout, contraction allowed.
-__global__ void eval_rhs_f32_kernel(const axs_fab s, const axs_fab r, float one_over_dx2, float kappa, float lambda,
-                                    float R2)
+// arithmetic throughout, contraction allowed; the Laplacian sums the x, y and
+// z second differences in that order, each (-wf, wn, -wl, wn, -wf) . f / dx^2.
+// Marched along z: a block owns a 32 x TY column of cells and ZC planes of it.
+// Each plane's psi1, psi2 with a 2-cell x/y halo is staged in shared memory and
+// the z neighbours of a cell stay in its thread's registers, so a plane costs
+// about one global read per staged cell instead of 13 per component and cell.
+template <int TY, int ZC>
+__global__ void __launch_bounds__(32 * TY) eval_rhs_f32_zmarch_kernel(const axs_fab s, const axs_fab r,
+                                                                      float one_over_dx2, float kappa, float lambda,
+                                                                      float R2)
 {
+    constexpr int SX = 36, SY = TY + 4, CELLS = SX * SY, NT = 32 * TY, NST = (2 * CELLS + NT - 1) / NT;
+    __shared__ float sh[2][2][SY][SX];  // [plane buffer][component]
     const float *__restrict__ sp = static_cast<const float *>(s.data);
     float *__restrict__ rp = static_cast<float *>(r.data);
     const float wf = 8.33333333333333333333e-2f, wn = 1.33333333333333333333e+0f, wl = 2.5f;
-    const int64_t n = (int64_t)s.nx * s.ny * s.nz;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(q % s.nx), j = (int)((q / s.nx) % s.ny), k = (int)(q / ((int64_t)s.nx * s.ny));
-        const int64_t o = fab_off(s, i, j, k);
-        const int64_t st[3] = {1, s.jstride, s.kstride};
-        float lap[2];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * TY, z0 = blockIdx.z * ZC;
+    const int z1 = min(z0 + ZC, s.nz);
+    const int i = x0 + tx, j = y0 + ty;
+    const bool in = i < s.nx && j < s.ny;
+    const int64_t o0 = fab_off(s, in ? i : 0, in ? j : 0, 0), ro0 = fab_off(r, in ? i : 0, in ? j : 0, 0);
+    // The staged cells of this thread: shared index and plane-0 global offset
+    // (-1: outside the tile's halo or beyond the FAB's 2 ghost layers).
+    int sidx[NST];
+    int64_t goff[NST];
+#pragma unroll
+    for (int q = 0; q < NST; ++q) {
+        const int e = tid + q * NT;
+        const int c = e >= CELLS, rem = e - c * CELLS, yy = rem / SX, xx = rem - yy * SX;
+        const int gi = x0 - 2 + xx, gj = y0 - 2 + yy;
+        const bool ok = e < 2 * CELLS && gi < s.nx + 2 && gj < s.ny + 2;
+        sidx[q] = ok ? e : -1;
+        goff[q] = ok ? c * s.cstride + fab_off(s, gi, gj, 0) : 0;
+    }
+    float stg[NST];
+    auto load_stage = [&](int z) {
+#pragma unroll
+        for (int q = 0; q < NST; ++q) stg[q] = sidx[q] >= 0 ? __ldg(sp + goff[q] + (int64_t)z * s.kstride) : 0.f;
+    };
+    auto store_stage = [&](int buf) {
+        float *base = &sh[buf][0][0][0];
+#pragma unroll
+        for (int q = 0; q < NST; ++q)
+            if (sidx[q] >= 0) base[sidx[q]] = stg[q];
+    };
+    auto col = [&](int c, int z) { return in ? __ldg(sp + c * s.cstride + o0 + (int64_t)z * s.kstride) : 0.f; };
+    float v[2][5];  // psi_c at z-2 .. z+2
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) v[c][q] = col(c, z0 - 2 + q);
+    load_stage(z0);
+    store_stage(0);
+    __syncthreads();
+    for (int z = z0; z < z1; ++z) {
+        const int buf = (z - z0) & 1;
+        const bool more = z + 1 < z1;
+        float vn[2] = {0.f, 0.f};
+        if (more) {  // the next plane's loads are in flight while this one is computed
+            load_stage(z + 1);
+            vn[0] = col(0, z + 3);
+            vn[1] = col(1, z + 3);
+        }
+        if (in) {
+            const int64_t o = o0 + (int64_t)z * s.kstride, ro = ro0 + (int64_t)z * r.kstride;
+            const float pi1 = __ldg(sp + 2 * s.cstride + o), pi2 = __ldg(sp + 3 * s.cstride + o);
+            float lap[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const float(*t)[SX] = sh[buf][c];
+                float acc = 0.f;
+                acc += (-wf * t[ty + 2][tx] + wn * t[ty + 2][tx + 1] - wl * t[ty + 2][tx + 2] +
+                        wn * t[ty + 2][tx + 3] - wf * t[ty + 2][tx + 4]) *
+                       one_over_dx2;
+                acc += (-wf * t[ty][tx + 2] + wn * t[ty + 1][tx + 2] - wl * t[ty + 2][tx + 2] +
+                        wn * t[ty + 3][tx + 2] - wf * t[ty + 4][tx + 2]) *
+                       one_over_dx2;
+                acc += (-wf * v[c][0] + wn * v[c][1] - wl * v[c][2] + wn * v[c][3] - wf * v[c][4]) * one_over_dx2;
+                lap[c] = acc;
+            }
+            const float psi1 = v[0][2], psi2 = v[1][2];
+            const float pc = 0.5f * lambda * (psi1 * psi1 + psi2 * psi2 - R2);
+            rp[ro] = pi1;
+            rp[r.cstride + ro] = pi2;
+            rp[2 * r.cstride + ro] = lap[0] + kappa * psi1 - pc * psi1;
+            rp[3 * r.cstride + ro] = lap[1] + kappa * psi2 - pc * psi2;
+        }
+        if (more) store_stage(buf ^ 1);
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
-            const float *p = sp + c * s.cstride + o;
-            float acc = 0.f;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const int64_t t = st[d];
-                acc += (-wf * __ldg(p - 2 * t) + wn * __ldg(p - t) - wl * __ldg(p) + wn * __ldg(p + t) -
-                        wf * __ldg(p + 2 * t)) *
-                       one_over_dx2;
-            }
-            lap[c] = acc;
+            for (int q = 0; q < 4; ++q) v[c][q] = v[c][q + 1];
+            v[c][4] = vn[c];
         }
-        const float psi1 = sp[o], psi2 = sp[s.cstride + o];
-        const float pc = 0.5f * lambda * (psi1 * psi1 + psi2 * psi2 - R2);
-        const int64_t ro = fab_off(r, i, j, k);
-        rp[ro] = sp[2 * s.cstride + o];
-        rp[r.cstride + ro] = sp[3 * s.cstride + o];
-        rp[2 * r.cstride + ro] = lap[0] + kappa * psi1 - pc * psi1;
-        rp[3 * r.cstride + ro] = lap[1] + kappa * psi2 - pc * psi2;
+        __syncthreads();  // buffer buf^1 is complete and buf is free for plane z + 2
     }
 }
 
 // ---------------------------------------------------------------- ghost fill
-template <typename T>
-__global__ void fill_periodic_kernel(const axs_fab f)
-{
-    T *p = static_cast<T *>(f.data);
-    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng, gz = f.nz + 2 * f.ng;
-    const int64_t n = (int64_t)gx * gy * gz * f.ncomp;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(q % gx) - f.ng;
-        const int j = (int)((q / gx) % gy) - f.ng;
-        const int k = (int)((q / ((int64_t)gx * gy)) % gz) - f.ng;
-        const int c = (int)(q / ((int64_t)gx * gy * gz));
-        if (i >= 0 && i < f.nx && j >= 0 && j < f.ny && k >= 0 && k < f.nz) continue;
-        const int ii = ((i % f.nx) + f.nx) % f.nx, jj = ((j % f.ny) + f.ny) % f.ny, kk = ((k % f.nz) + f.nz) % f.nz;
-        p[c * f.cstride + fab_off(f, i, j, k)] = p[c * f.cstride + fab_off(f, ii, jj, kk)];
-    }
-}
+// Periodic images into the ghost cells only (ng <= each extent, so one wrap
+// reaches the valid box and no ghost reads another ghost). Per component
+// (blockIdx.y): the full ghost rows -- all rows of the 2 ng z ghost planes when
+// `with_z`, and the 2 ng y ghost rows of every valid plane -- one warp per row,
+// then the 2 ng x ghosts of each valid row one thread per cell. With with_z = 0
+// the z ghost planes are left alone (a z slab of a larger periodic box: they
+// come from the neighbouring slabs).
+__device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// x/y ghosts of the valid z planes only (a z slab of a larger periodic box:
-// its z ghosts come from the neighbouring slabs)
 template <typename T>
-__global__ void fill_periodic_xy_kernel(const axs_fab f)
+__global__ void fill_periodic_kernel(const axs_fab f, int with_z)
 {
-    T *p = static_cast<T *>(f.data);
-    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng;
-    const int64_t n = (int64_t)gx * gy * f.nz * f.ncomp;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(q % gx) - f.ng;
-        const int j = (int)((q / gx) % gy) - f.ng;
-        const int k = (int)((q / ((int64_t)gx * gy)) % f.nz);
-        const int c = (int)(q / ((int64_t)gx * gy * f.nz));
-        if (i >= 0 && i < f.nx && j >= 0 && j < f.ny) continue;
-        const int ii = ((i % f.nx) + f.nx) % f.nx, jj = ((j % f.ny) + f.ny) % f.ny;
-        p[c * f.cstride + fab_off(f, i, j, k)] = p[c * f.cstride + fab_off(f, ii, jj, k)];
+    T *p = static_cast<T *>(f.data) + blockIdx.y * f.cstride;
+    const int ng = f.ng, gx = f.nx + 2 * ng, gy = f.ny + 2 * ng, lane = threadIdx.x & 31;
+    const int zrows = with_z ? 2 * ng * gy : 0, rows = zrows + f.nz * 2 * ng;
+    for (int r = row_warp(); r < rows; r += row_warps()) {
+        int j, k;
+        if (r < zrows) {
+            const int kz = r / gy;
+            j = r - kz * gy - ng;
+            k = kz < ng ? kz - ng : f.nz + kz - ng;
+        } else {
+            const int b = r - zrows, g = b % (2 * ng);
+            k = b / (2 * ng);
+            j = g < ng ? g - ng : f.ny + g - ng;
+        }
+        T *dst = p + fab_off(f, 0, j, k);
+        const T *src = p + fab_off(f, 0, wrap_once(j, f.ny), wrap_once(k, f.nz));
+        for (int x = lane - ng; x < f.nx + ng; x += 32) dst[x] = src[wrap_once(x, f.nx)];
+    }
+    const int cells = f.ny * f.nz * 2 * ng;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cells; e += gridDim.x * blockDim.x) {
+        const int row = e / (2 * ng), g = e - row * 2 * ng;
+        const int k = row / f.ny, j = row - k * f.ny;
+        const int x = g < ng ? g - ng : f.nx + g - ng;
+        T *q = p + fab_off(f, 0, j, k);
+        q[x] = q[wrap_once(x, f.nx)];
     }
 }
 
@@ -137,19 +228,18 @@ __global__ void fill_periodic_xy_kernel(const axs_fab f)
 template <typename T>
 __global__ void copy_z_planes_kernel(const axs_fab f, int z0, int np, T *buf, int to_buf)
 {
-    T *p = static_cast<T *>(f.data);
-    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng;
-    const int64_t n = (int64_t)gx * gy * np * f.ncomp;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(q % gx) - f.ng;
-        const int j = (int)((q / gx) % gy) - f.ng;
-        const int k = z0 + (int)((q / ((int64_t)gx * gy)) % np);
-        const int c = (int)(q / ((int64_t)gx * gy * np));
-        T *e = p + c * f.cstride + fab_off(f, i, j, k);
-        if (to_buf)
-            buf[q] = *e;
-        else
-            *e = buf[q];
+    const int gx = f.nx + 2 * f.ng, gy = f.ny + 2 * f.ng, lane = threadIdx.x & 31;
+    const int rows = gy * np * f.ncomp;
+    for (int r = row_warp(); r < rows; r += row_warps()) {
+        const RowIdx q = row_index(r, gy, np);
+        T *e = static_cast<T *>(f.data) + q.c * f.cstride + fab_off(f, -f.ng, q.j - f.ng, z0 + q.k);
+        T *b = buf + (int64_t)r * gx;
+        for (int x = lane; x < gx; x += 32) {
+            if (to_buf)
+                b[x] = e[x];
+            else
+                e[x] = b[x];
+        }
     }
 }
 
@@ -169,18 +259,21 @@ __device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, 
 template <typename T>
 __global__ void lincomb_kernel(const axs_fab d, const axs_fab x, T b, const axs_fab y, int ncomp)
 {
-    T *dp = static_cast<T *>(d.data);
-    const T *xp = static_cast<const T *>(x.data);
-    const T *yp = static_cast<const T *>(y.data);
-    const int64_t nc = (int64_t)d.nx * d.ny * d.nz;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nc * ncomp;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t cell = q % nc;
-        const int c = (int)(q / nc);
-        const int i = (int)(cell % d.nx), j = (int)((cell / d.nx) % d.ny), k = (int)(cell / ((int64_t)d.nx * d.ny));
-        const T xv = xp[c * x.cstride + fab_off(x, i, j, k)];
-        const T yv = yp[c * y.cstride + fab_off(y, i, j, k)];
-        dp[c * d.cstride + fab_off(d, i, j, k)] = rn_add(xv, rn_mul(b, yv));
+    const int rows = d.ny * d.nz * ncomp, lane = threadIdx.x & 31;
+    for (int r = row_warp(); r < rows; r += row_warps()) {
+        const RowIdx q = row_index(r, d.ny, d.nz);
+        T *dr = static_cast<T *>(d.data) + q.c * d.cstride + fab_off(d, 0, q.j, q.k);
+        const T *xr = static_cast<const T *>(x.data) + q.c * x.cstride + fab_off(x, 0, q.j, q.k);
+        const T *yr = static_cast<const T *>(y.data) + q.c * y.cstride + fab_off(y, 0, q.j, q.k);
+        for (int i0 = lane; i0 < d.nx; i0 += 128) {
+            T xv[4], yv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + 32 * u < d.nx) xv[u] = xr[i0 + 32 * u], yv[u] = yr[i0 + 32 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + 32 * u < d.nx) dr[i0 + 32 * u] = rn_add(xv[u], rn_mul(b, yv[u]));
+        }
     }
 }
 
@@ -188,15 +281,30 @@ template <typename T>
 __global__ void rk4_combine_kernel(const axs_fab d, const axs_fab u, const axs_fab k1, const axs_fab k2,
                                    const axs_fab k3, const axs_fab k4, T h6, int ncomp)
 {
-    const int64_t nc = (int64_t)d.nx * d.ny * d.nz;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nc * ncomp;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t cell = q % nc;
-        const int c = (int)(q / nc);
-        const int i = (int)(cell % d.nx), j = (int)((cell / d.nx) % d.ny), k = (int)(cell / ((int64_t)d.nx * d.ny));
-        auto at = [&](const axs_fab &f) { return static_cast<const T *>(f.data)[c * f.cstride + fab_off(f, i, j, k)]; };
-        const T sum = rn_add(rn_add(rn_add(at(k1), rn_mul(T(2), at(k2))), rn_mul(T(2), at(k3))), at(k4));
-        static_cast<T *>(d.data)[c * d.cstride + fab_off(d, i, j, k)] = rn_add(at(u), rn_mul(h6, sum));
+    const int rows = d.ny * d.nz * ncomp, lane = threadIdx.x & 31;
+    for (int r = row_warp(); r < rows; r += row_warps()) {
+        const RowIdx q = row_index(r, d.ny, d.nz);
+        auto row = [&](const axs_fab &f) {
+            return static_cast<const T *>(f.data) + q.c * f.cstride + fab_off(f, 0, q.j, q.k);
+        };
+        const T *ur = row(u), *a = row(k1), *b = row(k2), *c = row(k3), *e = row(k4);
+        T *dr = static_cast<T *>(d.data) + q.c * d.cstride + fab_off(d, 0, q.j, q.k);
+        for (int i0 = lane; i0 < d.nx; i0 += 64) {
+            T v[2][5];
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const int i = i0 + 32 * w;
+                if (i < d.nx) v[w][0] = a[i], v[w][1] = b[i], v[w][2] = c[i], v[w][3] = e[i], v[w][4] = ur[i];
+            }
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const int i = i0 + 32 * w;
+                if (i < d.nx) {
+                    const T sum = rn_add(rn_add(rn_add(v[w][0], rn_mul(T(2), v[w][1])), rn_mul(T(2), v[w][2])), v[w][3]);
+                    dr[i] = rn_add(v[w][4], rn_mul(h6, sum));
+                }
+            }
+        }
     }
 }
 
@@ -329,6 +437,26 @@ static int grid_for(int64_t n)
     return (int)(g < 1 ? 1 : g);
 }
 
+// Blocks of 256 threads (8 row-walking warps) for `rows` rows: up to 8 blocks
+// per SM, grid-stride beyond that.
+static int grid_rows(int64_t rows)
+{
+    const int sms = device_sm_count();
+    int64_t g = (rows + 7) / 8;
+    const int64_t cap = (int64_t)(sms > 0 ? sms : 148) * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// The row-walking kernels index rows and ghost cells in 32 bits.
+static int rows_fit(const axs_fab *f, const char *what)
+{
+    const int64_t ry = f->ny + 2LL * f->ng, rz = f->nz + 2LL * f->ng;
+    AXS_REQUIRE(ry * rz * f->ncomp * (2LL * f->ng + 1) < (1LL << 31), AXS_ERR_UNSUPPORTED,
+                "%s: %lld rows x %d components exceed the 32-bit row index", what, (long long)(ry * rz), f->ncomp);
+    return AXS_OK;
+}
+
 static int same_shape(const axs_fab *a, const axs_fab *b, const char *what)
 {
     AXS_REQUIRE(a->dtype == b->dtype && a->nx == b->nx && a->ny == b->ny && a->nz == b->nz, AXS_ERR_INVALID_ARGUMENT,
@@ -458,15 +586,33 @@ int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_r
     if ((rc = same_shape(soln, rhs, "eval_rhs"))) return rc;
     AXS_REQUIRE(c != nullptr, AXS_ERR_INVALID_ARGUMENT, "null coefficients");
     AXS_REQUIRE(dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
-    const int64_t n = (int64_t)soln->nx * soln->ny * soln->nz;
+    if ((rc = rows_fit(soln, "eval_rhs"))) return rc;
+    const int g = grid_rows((int64_t)soln->ny * soln->nz);
     const double one_over_dx2 = 1.0 / (dx * dx);
     cudaStream_t st = (cudaStream_t)stream;
     if (soln->dtype == AXS_F64)
-        eval_rhs_f64_kernel<<<grid_for(n), 256, 0, st>>>(*soln, *rhs, one_over_dx2, c->kappa, c->lambda, c->R2);
+        eval_rhs_f64_kernel<<<g, 256, 0, st>>>(*soln, *rhs, one_over_dx2, c->kappa, c->lambda, c->R2);
     else
-        eval_rhs_f32_kernel<<<grid_for(n), 256, 0, st>>>(*soln, *rhs, (float)one_over_dx2, (float)c->kappa,
-                                                         (float)c->lambda, (float)c->R2);
+        eval_rhs_f32_zmarch_kernel<8, 32><<<dim3((soln->nx + 31) / 32, (soln->ny + 7) / 8, (soln->nz + 31) / 32),
+                                            dim3(32, 8), 0, st>>>(*soln, *rhs, (float)one_over_dx2, (float)c->kappa,
+                                                                  (float)c->lambda, (float)c->R2);
     return launch_status("eval_rhs");
+}
+
+static int fill_ghosts(const axs_fab *f, int with_z, cudaStream_t st)
+{
+    int rc = rows_fit(f, "periodic fill");
+    if (rc) return rc;
+    AXS_REQUIRE(f->ncomp <= 65535, AXS_ERR_UNSUPPORTED, "periodic fill: more than 65535 components");
+    const int64_t gy = f->ny + 2 * f->ng, rows = (with_z ? 2 * f->ng * gy : 0) + (int64_t)f->nz * 2 * f->ng;
+    const int64_t cells = (int64_t)f->ny * f->nz * 2 * f->ng;
+    const int64_t gr = grid_rows(rows), gc = grid_for(cells);
+    const dim3 grid((unsigned)(gr > gc ? gr : gc), (unsigned)f->ncomp);
+    if (f->dtype == AXS_F64)
+        fill_periodic_kernel<double><<<grid, 256, 0, st>>>(*f, with_z);
+    else
+        fill_periodic_kernel<float><<<grid, 256, 0, st>>>(*f, with_z);
+    return launch_status(with_z ? "fill_periodic_ghosts" : "fill_periodic_ghosts_xy");
 }
 
 int axs_fill_periodic_ghosts_xy(const axs_fab *f, void *stream)
@@ -475,12 +621,7 @@ int axs_fill_periodic_ghosts_xy(const axs_fab *f, void *stream)
     if (rc) return rc;
     if (f->ng == 0) return AXS_OK;
     AXS_REQUIRE(f->ng <= f->nx && f->ng <= f->ny, AXS_ERR_UNSUPPORTED, "periodic fill needs ng <= box extent");
-    const int64_t n = (int64_t)(f->nx + 2 * f->ng) * (f->ny + 2 * f->ng) * f->nz * f->ncomp;
-    cudaStream_t st = (cudaStream_t)stream;
-    if (f->dtype == AXS_F64)
-        fill_periodic_xy_kernel<double><<<grid_for(n), 256, 0, st>>>(*f);
-    else
-        fill_periodic_xy_kernel<float><<<grid_for(n), 256, 0, st>>>(*f);
+    return fill_ghosts(f, 0, (cudaStream_t)stream);
     return launch_status("fill_periodic_ghosts_xy");
 }
 
@@ -492,11 +633,12 @@ static int copy_z_planes(const axs_fab *f, int32_t z0, int32_t nplanes, void *bu
     AXS_REQUIRE(nplanes > 0 && z0 >= -f->ng && z0 + nplanes <= f->nz + f->ng, AXS_ERR_INVALID_ARGUMENT,
                 "planes %d .. %d outside the FAB's z range %d .. %d", z0, z0 + nplanes - 1, -f->ng,
                 f->nz + f->ng - 1);
-    const int64_t n = (int64_t)(f->nx + 2 * f->ng) * (f->ny + 2 * f->ng) * nplanes * f->ncomp;
+    if ((rc = rows_fit(f, "z plane copy"))) return rc;
+    const int g = grid_rows((int64_t)(f->ny + 2 * f->ng) * nplanes * f->ncomp);
     if (f->dtype == AXS_F64)
-        copy_z_planes_kernel<double><<<grid_for(n), 256, 0, st>>>(*f, z0, nplanes, static_cast<double *>(buf), to_buf);
+        copy_z_planes_kernel<double><<<g, 256, 0, st>>>(*f, z0, nplanes, static_cast<double *>(buf), to_buf);
     else
-        copy_z_planes_kernel<float><<<grid_for(n), 256, 0, st>>>(*f, z0, nplanes, static_cast<float *>(buf), to_buf);
+        copy_z_planes_kernel<float><<<g, 256, 0, st>>>(*f, z0, nplanes, static_cast<float *>(buf), to_buf);
     return launch_status("z plane copy");
 }
 
@@ -517,13 +659,7 @@ int axs_fill_periodic_ghosts(const axs_fab *f, void *stream)
     if (f->ng == 0) return AXS_OK;
     AXS_REQUIRE(f->ng <= f->nx && f->ng <= f->ny && f->ng <= f->nz, AXS_ERR_UNSUPPORTED,
                 "periodic fill needs ng <= box extent");
-    const int64_t n = (int64_t)(f->nx + 2 * f->ng) * (f->ny + 2 * f->ng) * (f->nz + 2 * f->ng) * f->ncomp;
-    cudaStream_t st = (cudaStream_t)stream;
-    if (f->dtype == AXS_F64)
-        fill_periodic_kernel<double><<<grid_for(n), 256, 0, st>>>(*f);
-    else
-        fill_periodic_kernel<float><<<grid_for(n), 256, 0, st>>>(*f);
-    return launch_status("fill_periodic_ghosts");
+    return fill_ghosts(f, 1, (cudaStream_t)stream);
 }
 
 int axs_lincomb(const axs_fab *dst, const axs_fab *x, double b, const axs_fab *y, void *stream)
@@ -534,12 +670,13 @@ int axs_lincomb(const axs_fab *dst, const axs_fab *x, double b, const axs_fab *y
     if ((rc = same_shape(dst, x, "lincomb")) || (rc = same_shape(dst, y, "lincomb"))) return rc;
     const int nc = dst->ncomp < x->ncomp ? (dst->ncomp < y->ncomp ? dst->ncomp : y->ncomp)
                                          : (x->ncomp < y->ncomp ? x->ncomp : y->ncomp);
-    const int64_t n = (int64_t)dst->nx * dst->ny * dst->nz * nc;
+    if ((rc = rows_fit(dst, "lincomb"))) return rc;
+    const int g = grid_rows((int64_t)dst->ny * dst->nz * nc);
     cudaStream_t st = (cudaStream_t)stream;
     if (dst->dtype == AXS_F64)
-        lincomb_kernel<double><<<grid_for(n), 256, 0, st>>>(*dst, *x, b, *y, nc);
+        lincomb_kernel<double><<<g, 256, 0, st>>>(*dst, *x, b, *y, nc);
     else
-        lincomb_kernel<float><<<grid_for(n), 256, 0, st>>>(*dst, *x, (float)b, *y, nc);
+        lincomb_kernel<float><<<g, 256, 0, st>>>(*dst, *x, (float)b, *y, nc);
     return launch_status("lincomb");
 }
 
@@ -553,12 +690,14 @@ int axs_rk4_combine(const axs_fab *dst, const axs_fab *uold, const axs_fab *k1, 
         if (rc) return rc;
         if (q && (rc = same_shape(dst, all[q], "rk4_combine"))) return rc;
     }
-    const int64_t n = (int64_t)dst->nx * dst->ny * dst->nz * 4;
+    int rc = rows_fit(dst, "rk4_combine");
+    if (rc) return rc;
+    const int g = grid_rows((int64_t)dst->ny * dst->nz * 4);
     cudaStream_t st = (cudaStream_t)stream;
     if (dst->dtype == AXS_F64)
-        rk4_combine_kernel<double><<<grid_for(n), 256, 0, st>>>(*dst, *uold, *k1, *k2, *k3, *k4, dt / 6.0, 4);
+        rk4_combine_kernel<double><<<g, 256, 0, st>>>(*dst, *uold, *k1, *k2, *k3, *k4, dt / 6.0, 4);
     else
-        rk4_combine_kernel<float><<<grid_for(n), 256, 0, st>>>(*dst, *uold, *k1, *k2, *k3, *k4, (float)(dt / 6.0), 4);
+        rk4_combine_kernel<float><<<g, 256, 0, st>>>(*dst, *uold, *k1, *k2, *k3, *k4, (float)(dt / 6.0), 4);
     return launch_status("rk4_combine");
 }
 
