@@ -86,16 +86,19 @@ __global__ void eval_rhs_f64_kernel(const axs_fab s, const axs_fab r, double one
 // arithmetic throughout, contraction allowed; the Laplacian sums the x, y and
 // z second differences in that order, each (-wf, wn, -wl, wn, -wf) . f / dx^2.
 // Marched along z: a block owns a 32 x TY column of cells and ZC planes of it.
-// Each plane's psi1, psi2 with a 2-cell x/y halo is staged in shared memory and
-// the z neighbours of a cell stay in its thread's registers, so a plane costs
-// about one global read per staged cell instead of 13 per component and cell.
-template <int TY, int ZC>
+// Plane p's psi1, psi2 over the tile plus a 2-cell x/y halo, and Pi1, Pi2 over
+// the tile, are copied by cp.async into a (D + 5)-slot shared-memory ring, D
+// planes ahead of the plane the block computes: every stencil operand then
+// comes from shared memory, each staged value is read from global memory once
+// per block, and a thread keeps about 5 D copies in flight.
+template <int TY, int ZC, int D>
 __global__ void __launch_bounds__(32 * TY) eval_rhs_f32_zmarch_kernel(const axs_fab s, const axs_fab r,
                                                                       float one_over_dx2, float kappa, float lambda,
                                                                       float R2)
 {
-    constexpr int SX = 36, SY = TY + 4, CELLS = SX * SY, NT = 32 * TY, NST = (2 * CELLS + NT - 1) / NT;
-    __shared__ float sh[2][2][SY][SX];  // [plane buffer][component]
+    constexpr int SX = 36, SY = TY + 4, PSI = SX * SY, NT = 32 * TY, PI = NT, SLOT = 2 * PSI + 2 * PI;
+    constexpr int NSLOT = D + 5, NPS = (2 * PSI + NT - 1) / NT;
+    __shared__ float sh[NSLOT * SLOT];
     const float *__restrict__ sp = static_cast<const float *>(s.data);
     float *__restrict__ rp = static_cast<float *>(r.data);
     const float wf = 8.33333333333333333333e-2f, wn = 1.33333333333333333333e+0f, wl = 2.5f;
@@ -105,80 +108,64 @@ __global__ void __launch_bounds__(32 * TY) eval_rhs_f32_zmarch_kernel(const axs_
     const int i = x0 + tx, j = y0 + ty;
     const bool in = i < s.nx && j < s.ny;
     const int64_t o0 = fab_off(s, in ? i : 0, in ? j : 0, 0), ro0 = fab_off(r, in ? i : 0, in ? j : 0, 0);
-    // The staged cells of this thread: shared index and plane-0 global offset
-    // (-1: outside the tile's halo or beyond the FAB's 2 ghost layers).
-    int sidx[NST];
-    int64_t goff[NST];
+    // This thread's staged psi cells: plane-0 global offset, and whether the cell
+    // lies within the FAB's 2 ghost layers (else it is zero-filled, and no
+    // computed cell reads it).
+    int64_t psi_off[NPS];
+    bool psi_ok[NPS];
 #pragma unroll
-    for (int q = 0; q < NST; ++q) {
+    for (int q = 0; q < NPS; ++q) {
         const int e = tid + q * NT;
-        const int c = e >= CELLS, rem = e - c * CELLS, yy = rem / SX, xx = rem - yy * SX;
+        const int c = e >= PSI, rem = e - c * PSI, yy = rem / SX, xx = rem - yy * SX;
         const int gi = x0 - 2 + xx, gj = y0 - 2 + yy;
-        const bool ok = e < 2 * CELLS && gi < s.nx + 2 && gj < s.ny + 2;
-        sidx[q] = ok ? e : -1;
-        goff[q] = ok ? c * s.cstride + fab_off(s, gi, gj, 0) : 0;
+        psi_ok[q] = e < 2 * PSI && gi < s.nx + 2 && gj < s.ny + 2;
+        psi_off[q] = psi_ok[q] ? c * s.cstride + fab_off(s, gi, gj, 0) : 0;
     }
-    float stg[NST];
-    auto load_stage = [&](int z) {
+    auto slot = [&](int p) { return sh + ((p - z0 + 2) % NSLOT) * SLOT; };
+    auto issue = [&](int p) {
+        if (p > z1 + 1) return;  // beyond the last plane a computed cell reads
+        float *dst = slot(p);
+        const int64_t po = (int64_t)p * s.kstride;
 #pragma unroll
-        for (int q = 0; q < NST; ++q) stg[q] = sidx[q] >= 0 ? __ldg(sp + goff[q] + (int64_t)z * s.kstride) : 0.f;
-    };
-    auto store_stage = [&](int buf) {
-        float *base = &sh[buf][0][0][0];
-#pragma unroll
-        for (int q = 0; q < NST; ++q)
-            if (sidx[q] >= 0) base[sidx[q]] = stg[q];
-    };
-    auto col = [&](int c, int z) { return in ? __ldg(sp + c * s.cstride + o0 + (int64_t)z * s.kstride) : 0.f; };
-    float v[2][5];  // psi_c at z-2 .. z+2
-#pragma unroll
-    for (int c = 0; c < 2; ++c)
-#pragma unroll
-        for (int q = 0; q < 5; ++q) v[c][q] = col(c, z0 - 2 + q);
-    load_stage(z0);
-    store_stage(0);
-    __syncthreads();
-    for (int z = z0; z < z1; ++z) {
-        const int buf = (z - z0) & 1;
-        const bool more = z + 1 < z1;
-        float vn[2] = {0.f, 0.f};
-        if (more) {  // the next plane's loads are in flight while this one is computed
-            load_stage(z + 1);
-            vn[0] = col(0, z + 3);
-            vn[1] = col(1, z + 3);
+        for (int q = 0; q < NPS; ++q)
+            if (tid + q * NT < 2 * PSI) cp_async_elem(dst + tid + q * NT, sp + psi_off[q] + po, psi_ok[q], sp);
+        if (p >= z0 && p < z1) {
+            cp_async_elem(dst + 2 * PSI + tid, sp + 2 * s.cstride + o0 + po, in, sp);
+            cp_async_elem(dst + 2 * PSI + PI + tid, sp + 3 * s.cstride + o0 + po, in, sp);
         }
+    };
+    for (int p = z0 - 2; p <= z0 + 1 + D; ++p) {
+        issue(p);
+        cp_async_commit();
+    }
+    const int c0 = (ty + 2) * SX + tx + 2;  // this thread's cell in a plane's psi tile
+    for (int z = z0; z < z1; ++z) {
+        cp_async_wait<D - 1>();  // planes up to z + 2 have landed (this thread's copies)
+        __syncthreads();         // ... and everyone's; the slot of plane z - 3 is free
+        issue(z + 2 + D);
+        cp_async_commit();
         if (in) {
-            const int64_t o = o0 + (int64_t)z * s.kstride, ro = ro0 + (int64_t)z * r.kstride;
-            const float pi1 = __ldg(sp + 2 * s.cstride + o), pi2 = __ldg(sp + 3 * s.cstride + o);
+            const float *t = slot(z);
+            const float *zm2 = slot(z - 2), *zm1 = slot(z - 1), *zp1 = slot(z + 1), *zp2 = slot(z + 2);
             float lap[2];
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
-                const float(*t)[SX] = sh[buf][c];
+                const int b = c * PSI + c0;
                 float acc = 0.f;
-                acc += (-wf * t[ty + 2][tx] + wn * t[ty + 2][tx + 1] - wl * t[ty + 2][tx + 2] +
-                        wn * t[ty + 2][tx + 3] - wf * t[ty + 2][tx + 4]) *
+                acc += (-wf * t[b - 2] + wn * t[b - 1] - wl * t[b] + wn * t[b + 1] - wf * t[b + 2]) * one_over_dx2;
+                acc += (-wf * t[b - 2 * SX] + wn * t[b - SX] - wl * t[b] + wn * t[b + SX] - wf * t[b + 2 * SX]) *
                        one_over_dx2;
-                acc += (-wf * t[ty][tx + 2] + wn * t[ty + 1][tx + 2] - wl * t[ty + 2][tx + 2] +
-                        wn * t[ty + 3][tx + 2] - wf * t[ty + 4][tx + 2]) *
-                       one_over_dx2;
-                acc += (-wf * v[c][0] + wn * v[c][1] - wl * v[c][2] + wn * v[c][3] - wf * v[c][4]) * one_over_dx2;
+                acc += (-wf * zm2[b] + wn * zm1[b] - wl * t[b] + wn * zp1[b] - wf * zp2[b]) * one_over_dx2;
                 lap[c] = acc;
             }
-            const float psi1 = v[0][2], psi2 = v[1][2];
+            const int64_t ro = ro0 + (int64_t)z * r.kstride;
+            const float psi1 = t[c0], psi2 = t[PSI + c0];
             const float pc = 0.5f * lambda * (psi1 * psi1 + psi2 * psi2 - R2);
-            rp[ro] = pi1;
-            rp[r.cstride + ro] = pi2;
+            rp[ro] = t[2 * PSI + tid];
+            rp[r.cstride + ro] = t[2 * PSI + PI + tid];
             rp[2 * r.cstride + ro] = lap[0] + kappa * psi1 - pc * psi1;
             rp[3 * r.cstride + ro] = lap[1] + kappa * psi2 - pc * psi2;
         }
-        if (more) store_stage(buf ^ 1);
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) v[c][q] = v[c][q + 1];
-            v[c][4] = vn[c];
-        }
-        __syncthreads();  // buffer buf^1 is complete and buf is free for plane z + 2
     }
 }
 
@@ -593,7 +580,7 @@ int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_r
     if (soln->dtype == AXS_F64)
         eval_rhs_f64_kernel<<<g, 256, 0, st>>>(*soln, *rhs, one_over_dx2, c->kappa, c->lambda, c->R2);
     else
-        eval_rhs_f32_zmarch_kernel<8, 32><<<dim3((soln->nx + 31) / 32, (soln->ny + 7) / 8, (soln->nz + 31) / 32),
+        eval_rhs_f32_zmarch_kernel<8, 64, 2><<<dim3((soln->nx + 31) / 32, (soln->ny + 7) / 8, (soln->nz + 63) / 64),
                                             dim3(32, 8), 0, st>>>(*soln, *rhs, (float)one_over_dx2, (float)c->kappa,
                                                                   (float)c->lambda, (float)c->R2);
     return launch_status("eval_rhs");

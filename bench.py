@@ -612,7 +612,12 @@ def run_native(args):
     lv32 = A.PeriodicLevel(n, DX, dtype=torch.float32, device=dev, pierced_capacity=1024)
     lv32.set_state(ic64.float())
     tune32 = None
-    if not args.no_autotune:
+    if args.tile_config:
+        ids = {name: cid for cid, name in lv32.tile_configs()}
+        if args.tile_config not in ids:
+            raise SystemExit(f"unknown FP32 tile configuration {args.tile_config!r}; one of {sorted(ids)}")
+        lv32.tile_config = ids[args.tile_config]
+    elif not args.no_autotune:
         tune32 = lv32.autotune(bg, TAU_I, DT)
     cfg32 = level_config_name(lv32)
     ms, per32, clocks = timed_run(lv32, args.steps, args.warmup, sample_clocks=True)
@@ -924,6 +929,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tile-config", default=None,
+                    help="run the FP32 headline with this tile configuration (by name) instead of autotuning")
     ap.add_argument("--no-diag", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-differentiation", action="store_true")
