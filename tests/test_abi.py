@@ -217,3 +217,16 @@ def test_nonfinite_count_validates_arguments(L):
     lib = L.lib()
     assert lib.axs_count_nonfinite(None, None, None) == L.AXS_ERR_INVALID_ARGUMENT
     assert lib.axs_level_count_nonfinite(None, None, None) == L.AXS_ERR_INVALID_ARGUMENT
+
+
+def test_diagnostics_rejects_small_scratch_without_gpu(L):
+    """The scratch check runs before any launch: AXS_ERR_WORKSPACE, nothing
+    dereferenced (the data pointer is never touched)."""
+    lib = L.lib()
+    f = L.Fab(C.c_void_p(4096), L.AXS_F32, 8, 8, 8, 2, 4, 12, 144, 1728)
+    p = L.DiagParams(0.5, 1.0, 2.0, 0.1, 1.0, L.MASK_NONE, 0.8, L.BOUNDARY_GHOSTS, 1, 1, 1, 0)
+    need = C.c_int64()
+    assert lib.axs_diagnostics_scratch_bytes(8, 8, 8, C.byref(need)) == L.AXS_OK and need.value > 16
+    rc = lib.axs_diagnostics(C.byref(f), C.byref(p), None, C.c_void_p(8192), None, 0, C.c_void_p(16384), 16, None)
+    assert rc == L.AXS_ERR_WORKSPACE
+    assert b"scratch too small" in lib.axs_last_error()
