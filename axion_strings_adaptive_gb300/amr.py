@@ -145,7 +145,10 @@ class TwoLevel:
         self.patches: Patches | None = None
         self.blocks = np.zeros((0, 3), dtype=np.int32)
         dev = coarse.state.device
-        self._block_patch = torch.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=torch.int32, device=dev)
+        # block -> patch slot (-1: not refined), on the device for the kernels and
+        # on the host for the regrid's bookkeeping
+        self._block_patch_host = np.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=np.int32)
+        self._block_patch = torch.from_numpy(self._block_patch_host.copy()).to(dev)
         self._patch_block = torch.zeros((1, 3), dtype=torch.int32, device=dev)
 
     # ------------------------------------------------------------------ patch management
@@ -164,17 +167,17 @@ class TwoLevel:
         x the count receives the kept patches."""
         blocks = np.asarray(blocks, dtype=np.int32).reshape(-1, 3)
         dev = self.coarse.state.device
-        old_patches, old_block_patch = self.patches, self._block_patch
+        old_patches = self.patches
         n_new = len(blocks)
         if n_new == 0:
             self.blocks = blocks
             self.patches = None
             self._block_patch.fill_(-1)
+            self._block_patch_host.fill(-1)
             return
         dt = self.coarse.dtype
         if old_patches is not None:
-            b = torch.from_numpy(blocks.astype(np.int64)).to(dev)
-            old_q = old_block_patch[b[:, 2], b[:, 1], b[:, 0]].cpu().numpy().astype(np.int64)
+            old_q = self._block_patch_host[blocks[:, 2], blocks[:, 1], blocks[:, 0]].astype(np.int64)
         else:
             old_q = np.full(n_new, -1, dtype=np.int64)
         in_place = old_patches is not None and n_new <= old_patches.capacity
@@ -208,7 +211,8 @@ class TwoLevel:
         self._patch_block = torch.from_numpy(blocks.copy()).to(dev)
         bp = np.full((self.nb[2], self.nb[1], self.nb[0]), -1, dtype=np.int32)
         bp[blocks[:, 2], blocks[:, 1], blocks[:, 0]] = np.arange(n_new, dtype=np.int32)
-        self._block_patch = torch.from_numpy(bp).to(dev)
+        self._block_patch_host = bp
+        self._block_patch = torch.from_numpy(bp.copy()).to(dev)
         sod = torch.from_numpy(src_of_dst).to(dev)
         # whole patch boxes (valid cells and rings; the rings are refilled before use)
         L.call("axs_patches_copy_boxes", C.byref(self.patches.c),

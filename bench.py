@@ -834,8 +834,8 @@ def run_native(args):
     if not args.no_scale:
         scale = scale_report(A, dev, hbm_peak, n=args.scale_n, steps=args.scale_steps, kdiv=args.scale_kdiv)
     # the same at the full scale configuration: a 1024^3 base and 100 coarse steps.
-    # IC |n| < N/96 tags 3.2 % of the cells (59 k -> 65 k patches): with the spare
-    # patch arena, about the densest set that fits in HBM beside the base level.
+    # IC |n| < N/76 tags 5.2 % of the cells (91 k -> 100 k patches of 32^3 in one
+    # arena laid out for 1.25 x the first count).
     scale_1024 = None
     if not args.no_scale_1024:
         try:
@@ -943,7 +943,7 @@ def main():
     ap.add_argument("--scale-kdiv", type=int, default=64)
     ap.add_argument("--no-scale-1024", action="store_true")
     ap.add_argument("--scale1024-steps", type=int, default=100)
-    ap.add_argument("--scale1024-kdiv", type=int, default=96)
+    ap.add_argument("--scale1024-kdiv", type=int, default=76)
     ap.add_argument("--diff-n", type=int, default=128)
     ap.add_argument("--diff-steps", type=int, default=200)
     ap.add_argument("--diff-directions", type=int, default=16)
