@@ -157,13 +157,13 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
 
 // The one-pass fused step (level_fused.cuh) over FP32 levels whose extents are
 // multiples of its tile; single sweeps and other extents run the two sweeps of
-// the default tiling. Steps alternate between the level's state and the first
-// 4 component planes of its work buffer (same layout); each step is the fused
-// launch and the padding launch; after an odd number of steps one copy brings
-// the result back into the state.
+// the fastest two-sweep tiling. Steps alternate between the level's state and
+// the first 4 component planes of its work buffer (same layout); each step is
+// the fused launch and the padding launch. An odd step count runs its first
+// step as the two sweeps, which step the state in place.
 template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
     using S = LevelFusedShape<TX, TY, NS, THREADS>;
-    using Fallback = SweepConfig<float, 2, 64, 8, 8, 2>;
+    using Fallback = SweepConfig<float, 2, 32, 8, 8, 3, true>;  // the fastest two-sweep tiling at 512^3
 
     static bool applies(const axs_level *lv)
     {
@@ -187,6 +187,19 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
     {
         const axs_level *lv = r.lv;
         if (r.sweep_mask != 3 || !applies(lv)) return Fallback::run(r);
+        // An odd step count takes its first step as the two sweeps (in place; the
+        // results are the same bits), so the fused steps after it come in pairs
+        // and end in the state buffer.
+        if (r.nsteps & 1) {
+            SweepRunArgs one = r;
+            one.nsteps = 1;
+            const int rc1 = Fallback::run(one);
+            if (rc1 || r.nsteps == 1) return rc1;
+            SweepRunArgs rest = r;
+            rest.t0 = r.t0 + r.dt;
+            rest.nsteps = r.nsteps - 1;
+            return run(rest);
+        }
         const LevelGeom &g = *r.g;
         static int smem_set = 0;
         auto kern = level_fused_kernel<S>;
@@ -225,8 +238,6 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
             level_pad_kernel<float><<<pad_grid, 256, 0, r.st>>>(dst, lv->nx, lv->ny, lv->nz, g.js, g.ks, g.cs, g.ox, g.oy);
             if ((rc = launch_status("level padding"))) return rc;
         }
-        if (r.nsteps & 1)
-            AXS_CUDA_CHECK(cudaMemcpyAsync(buf[0], buf[1], 4 * g.cs * sizeof(float), cudaMemcpyDeviceToDevice, r.st));
         return AXS_OK;
     }
 };

@@ -205,8 +205,8 @@ class PeriodicLevel:
                  stream=None) -> dict:
         """Time every compiled tiling on this level (the two-sweep tilings and
         the one-pass fused step; full RK4 steps, CUDA events) and keep the
-        fastest. An even step count times the fused step without the copy an
-        odd count ends with. The state is saved and restored, so the
+        fastest. An even step count times the fused step alone (an odd count
+        runs its first step as the two sweeps). The state is saved and restored, so the
         level's contents are unchanged. Returns {name: ms_per_step}."""
         saved = self.state.clone()
         timings = {}

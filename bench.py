@@ -550,9 +550,10 @@ def run_native(args):
     def timed_run(level, steps, warmup, t_start=0.0, sample_clocks=False):
         """K RK4 steps of `level`, CUDA events on the launching stream around every
         kernel launch. Two-sweep tilings: sweep A and sweep B each step. The fused
-        step: one launch per step, timed in pairs of steps (a pair returns the
-        state to the level's state buffer; an odd K ends with one step and the
-        copy back). Returns (total ms, {kernel: mean ms per launch}, clocks)."""
+        step (the fused launch and the padding launch), timed in pairs of steps:
+        a pair returns the state to the level's state buffer; a single step runs
+        as the two sweeps, so an odd K ends with one of those. Returns (total ms,
+        {kernel: mean ms per launch}, clocks)."""
         fused = "fused" in level_config_name(level)
         for w in range(warmup):
             level.advance(bg, TAU_I, t_start + w * DT, DT, 1)
@@ -650,7 +651,7 @@ def run_native(args):
                 "algorithmic_words_per_site": WORDS[dom],
                 "kernel_ms": per32,
                 "frac_of_nominal_8TBs": achieved / 8000.0}
-    launches32 = args.steps if "rk4_fused_level" in per32 else 2 * args.steps
+    launches32 = 2 * args.steps  # fused + padding, or sweep A + sweep B, per step
 
     # ---------------- fused diagnostics pass (string finder + energies + velocities) on the FP32 box
     diag = None

@@ -3,8 +3,8 @@ and the FP32 level step against the CPU oracle's FP32 and FP64 builds.
 
 The fused step and the two sweeps evaluate the same per-site arithmetic, so the
 state they leave (valid cells, periodic padding and its corners) must agree bit
-for bit, whatever the step count (odd counts end with a copy back into the
-state) and whatever the tile row (the first and last tile rows load their y
+for bit, whatever the step count (an odd count runs its first step as the two
+sweeps, then fused pairs) and whatever the tile row (the first and last tile rows load their y
 halo in wrapped pieces)."""
 import numpy as np
 import pytest
