@@ -596,10 +596,18 @@ static_assert(2 * kFillCells <= 2 * kFillThreads, "coarse load tasks: two per th
 static_assert(kFillWin <= 3 * kFillThreads && 2 * kFillXs / 2 <= 3 * kFillThreads, "z / x tasks: three per thread");
 static_assert(kFillThreads == 2 * kFillT * kFillT / 2, "one y pair of one fine plane per thread");
 
+// Coarse planes are staged raw by cp.async kFillAhead parents ahead of the
+// plane the window takes next, in kFillAhead + 1 staging slots: per load task
+// psi_pair and Pi_pair at the start of the coarse step and, when blending, at
+// its end.
+constexpr int kFillAhead = 2;
+constexpr int kFillStage = kFillAhead + 1;
+
 template <typename T> struct FillSmem {
-    T win[5][kFillWin];      // coarse plane p sits in slot p mod 5
-    T zs[2][kFillWin];       // footprint interpolated to the two fine heights
-    T xs[2][kFillXs];        // then to the tile's fine columns
+    T win[5][kFillWin];                         // coarse plane p sits in slot p mod 5
+    T zs[2][kFillWin];                          // footprint interpolated to the two fine heights
+    T xs[2][kFillXs];                           // then to the tile's fine columns
+    T stage[kFillStage][4][2 * kFillCells];     // raw plane p in slot p mod kFillStage
 };
 
 // tiles start at fine x, y = -8 and cover [-kRingX, n + kRingX) x [-kRingYZ, n + kRingYZ)
@@ -610,7 +618,8 @@ template <typename T>
 __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fill_kernel(T *__restrict__ st, CoarseView cv, FillArgs f,
                                                                      QuarticWeights q)
 {
-    __shared__ FillSmem<T> sm;
+    extern __shared__ __align__(16) unsigned char fill_smem_raw[];  // FillSmem<T>, sizeof bytes
+    FillSmem<T> &sm = *reinterpret_cast<FillSmem<T> *>(fill_smem_raw);
     __shared__ T w[2][5];
     const int n = f.n, half = n / 2, tid = threadIdx.x;
     const int ntx = fill_tiles_x(n), ntiles = ntx * fill_tiles_y(n);
@@ -696,33 +705,42 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
     else
         hw = f.hd;
     const T h00 = hw[0], h10 = hw[1], h01 = hw[2], h11 = hw[3], l0 = hw[4], l1 = hw[5];
-    T v[2][4];
-    auto issue = [&](int p) {
-        const int64_t zoff = (int64_t)pwrap(p, cv.nz) * cv.ks;
+    // plane p's raw values into its staging slot (this thread's load tasks; only
+    // this thread reads them back, after its own cp.async wait), one group per
+    // plane, an empty group past `plast`
+    auto issue = [&](int p, int plast) {
+        if (p <= plast) {
+            const int64_t zoff = (int64_t)pwrap(p, cv.nz) * cv.ks;
+            T(*sg)[2 * kFillCells] = sm.stage[pwrap(p, kFillStage)];
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            if (!ld_on[r]) continue;
-            const int64_t off = zoff + ld_off[r];
-            v[r][0] = c0[off];
-            v[r][1] = c0[off + 2 * cv.cs];
-            if (blend) {
-                v[r][2] = c1[off];
-                v[r][3] = c1[off + 2 * cv.cs];
+            for (int r = 0; r < 2; ++r) {
+                if (!ld_on[r]) continue;
+                const int64_t off = zoff + ld_off[r];
+                cp_async_elem(&sg[0][ld_sm[r]], c0 + off, true, c0);
+                cp_async_elem(&sg[1][ld_sm[r]], c0 + off + 2 * cv.cs, true, c0);
+                if (blend) {
+                    cp_async_elem(&sg[2][ld_sm[r]], c1 + off, true, c0);
+                    cp_async_elem(&sg[3][ld_sm[r]], c1 + off + 2 * cv.cs, true, c0);
+                }
             }
         }
+        cp_async_commit();
     };
+    // plane p from its staging slot into its window slot, time-blended
     auto commit = [&](int p) {
         T *slot = sm.win[pwrap(p, 5)];
+        const T(*sg)[2 * kFillCells] = sm.stage[pwrap(p, kFillStage)];
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
             if (!ld_on[r]) continue;
+            const int i = ld_sm[r];
             if (!blend) {
-                slot[ld_sm[r]] = v[r][0];
-                slot[ld_sm[r] + 2 * kFillCells] = v[r][1];
+                slot[i] = sg[0][i];
+                slot[i + 2 * kFillCells] = sg[1][i];
             } else {
-                const T p0 = v[r][0], q0 = v[r][1], p1 = v[r][2], q1 = v[r][3];
-                slot[ld_sm[r]] = h00 * p0 + h10 * q0 + h01 * p1 + h11 * q1;
-                slot[ld_sm[r] + 2 * kFillCells] = l0 * q0 + l1 * q1;
+                const T p0 = sg[0][i], q0 = sg[1][i], p1 = sg[2][i], q1 = sg[3][i];
+                slot[i] = h00 * p0 + h10 * q0 + h01 * p1 + h11 * q1;
+                slot[i + 2 * kFillCells] = l0 * q0 + l1 * q1;
             }
         }
     };
@@ -734,12 +752,14 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
         const int za = nseg == 2 ? (sg == 0 ? -kRingYZ : n) : -kRingYZ;
         const int zb = nseg == 2 ? (sg == 0 ? 0 : n + kRingYZ) : n + kRingYZ;
         const int pa = bz * half + za / 2, pb = bz * half + zb / 2;  // parents of the segment (unwrapped)
-        __syncthreads();  // the previous segment is done with the window
+        __syncthreads();  // the previous segment is done with the window and the staging slots
+        const int plast = pb + 1;  // the last plane the segment's window takes
         for (int p = pa - 2; p < pa + 2; ++p) {
-            issue(p);
+            issue(p, plast);
+            cp_async_wait<0>();
             commit(p);
         }
-        issue(pa + 2);
+        for (int p = pa + 2; p < pa + 2 + kFillAhead; ++p) issue(p, plast);
         // 0: nothing, 1: copy from the patch owning the cells, 2: interpolate. An
         // initialising fill (valid_too) interpolates every cell: the value depends
         // only on the cell's global position, so a ring cell gets what its owner's
@@ -769,11 +789,14 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
             if (mode_of(pa, z_, zone_) == 1) load_copy(z_, zone_);
         }
         for (int pz = pa; pz < pb; ++pz) {
+            cp_async_wait<kFillAhead - 1>();  // plane pz + 2 has landed (this thread's copies)
             commit(pz + 2);
             int z, zone;
             const int mode = mode_of(pz, z, zone);
             const bool any = __syncthreads_or(mode == 2);  // also publishes the committed plane
-            if (pz + 1 < pb) issue(pz + 3);
+            // the staging slot of plane pz + 2 + kFillAhead last held plane pz - 1,
+            // committed before the barrier above
+            issue(pz + 2 + kFillAhead, plast);
             T *dst = dst_col + (int64_t)(z + kPatchRZ) * f.ks;
             if (any) {
                 const T *s0 = sm.win[pwrap(pz - 2, 5)], *s1 = sm.win[pwrap(pz - 1, 5)], *s2p = sm.win[pwrap(pz, 5)];
@@ -824,6 +847,19 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
             }
         }
     }
+}
+
+// The fill's shared memory is dynamic (36 KB in FP32, 72 KB in FP64): the
+// opt-in above 48 KB, once per precision.
+template <typename T> static int fill_smem_attr()
+{
+    static int attr_done = 0;  // setting it twice is harmless
+    if (!attr_done) {
+        AXS_CUDA_CHECK(cudaFuncSetAttribute(patch_fill_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)sizeof(FillSmem<T>)));
+        attr_done = 1;
+    }
+    return AXS_OK;
 }
 
 // Mean of the 8 fine children of every coarse cell a patch covers (amrex::average_down).
@@ -1008,10 +1044,15 @@ int axs_patches_fill_list(const axs_patches *p, const axs_patch_map *m, const ax
     const int64_t blocks = (int64_t)fill_tiles_x(g.n) * fill_tiles_y(g.n) * count;
     AXS_REQUIRE(blocks < (int64_t)INT32_MAX, AXS_ERR_UNSUPPORTED, "too many patches for one fill launch");
     cudaStream_t st = (cudaStream_t)stream;
-    if (p->dtype == AXS_F32)
-        patch_fill_kernel<float><<<(unsigned)blocks, kFillThreads, 0, st>>>(static_cast<float *>(p->state), cv, f, q);
-    else
-        patch_fill_kernel<double><<<(unsigned)blocks, kFillThreads, 0, st>>>(static_cast<double *>(p->state), cv, f, q);
+    if (p->dtype == AXS_F32) {
+        if ((rc = fill_smem_attr<float>())) return rc;
+        patch_fill_kernel<float><<<(unsigned)blocks, kFillThreads, sizeof(FillSmem<float>), st>>>(
+            static_cast<float *>(p->state), cv, f, q);
+    } else {
+        if ((rc = fill_smem_attr<double>())) return rc;
+        patch_fill_kernel<double><<<(unsigned)blocks, kFillThreads, sizeof(FillSmem<double>), st>>>(
+            static_cast<double *>(p->state), cv, f, q);
+    }
     return launch_status("patch fill");
 }
 
