@@ -614,6 +614,13 @@ template <typename T> struct FillSmem {
 __host__ __device__ __forceinline__ int fill_tiles_x(int n) { return (n + 8 + kRingX + kFillT - 1) / kFillT; }
 __host__ __device__ __forceinline__ int fill_tiles_y(int n) { return (n + 8 + kRingYZ + kFillT - 1) / kFillT; }
 
+// One element, global -> shared by cp.async, to the 32-bit shared address dst + OFF.
+template <int BYTES, uint32_t OFF> __device__ __forceinline__ void cp_async_to(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0+%2], [%1], %3;\n" ::"r"(dst), "l"(src), "n"(OFF), "n"(BYTES)
+                 : "memory");
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fill_kernel(T *__restrict__ st, CoarseView cv, FillArgs f,
                                                                      QuarticWeights q)
@@ -705,31 +712,39 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
     else
         hw = f.hd;
     const T h00 = hw[0], h10 = hw[1], h01 = hw[2], h11 = hw[3], l0 = hw[4], l1 = hw[5];
-    // plane p's raw values into its staging slot (this thread's load tasks; only
-    // this thread reads them back, after its own cp.async wait), one group per
-    // plane, an empty group past `plast`
+    // plane p's raw values into the next staging slot (this thread's load tasks;
+    // only this thread reads them back, after its own cp.async wait), one group
+    // per plane, an empty group past `plast`. Planes are issued and committed in
+    // order, so the slots rotate: iss for the next issue, cmt for the next commit.
+    constexpr uint32_t kCompBytes = 2 * kFillCells * sizeof(T), kSlotBytes = 4 * kCompBytes;
+    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(&sm.stage[0][0][0]);
+    int iss = 0, cmt = 0;
     auto issue = [&](int p, int plast) {
         if (p <= plast) {
             const int64_t zoff = (int64_t)pwrap(p, cv.nz) * cv.ks;
-            T(*sg)[2 * kFillCells] = sm.stage[pwrap(p, kFillStage)];
+            const uint32_t sl = stage0 + (uint32_t)iss * kSlotBytes;
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 if (!ld_on[r]) continue;
-                const int64_t off = zoff + ld_off[r];
-                cp_async_elem(&sg[0][ld_sm[r]], c0 + off, true, c0);
-                cp_async_elem(&sg[1][ld_sm[r]], c0 + off + 2 * cv.cs, true, c0);
+                const uint32_t d = sl + (uint32_t)ld_sm[r] * (uint32_t)sizeof(T);
+                const T *g0 = c0 + (zoff + ld_off[r]);
+                cp_async_to<sizeof(T), 0>(d, g0);
+                cp_async_to<sizeof(T), kCompBytes>(d, g0 + 2 * cv.cs);
                 if (blend) {
-                    cp_async_elem(&sg[2][ld_sm[r]], c1 + off, true, c0);
-                    cp_async_elem(&sg[3][ld_sm[r]], c1 + off + 2 * cv.cs, true, c0);
+                    const T *g1 = c1 + (zoff + ld_off[r]);
+                    cp_async_to<sizeof(T), 2 * kCompBytes>(d, g1);
+                    cp_async_to<sizeof(T), 3 * kCompBytes>(d, g1 + 2 * cv.cs);
                 }
             }
         }
         cp_async_commit();
+        iss = iss + 1 == kFillStage ? 0 : iss + 1;
     };
     // plane p from its staging slot into its window slot, time-blended
     auto commit = [&](int p) {
         T *slot = sm.win[pwrap(p, 5)];
-        const T(*sg)[2 * kFillCells] = sm.stage[pwrap(p, kFillStage)];
+        const T(*sg)[2 * kFillCells] = sm.stage[cmt];
+        cmt = cmt + 1 == kFillStage ? 0 : cmt + 1;
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
             if (!ld_on[r]) continue;
@@ -754,6 +769,7 @@ __global__ void __launch_bounds__(kFillThreads, sizeof(T) == 4 ? 4 : 2) patch_fi
         const int pa = bz * half + za / 2, pb = bz * half + zb / 2;  // parents of the segment (unwrapped)
         __syncthreads();  // the previous segment is done with the window and the staging slots
         const int plast = pb + 1;  // the last plane the segment's window takes
+        iss = cmt = 0;
         for (int p = pa - 2; p < pa + 2; ++p) {
             issue(p, plast);
             cp_async_wait<0>();
