@@ -147,6 +147,7 @@ SIGNATURES = {
     "axs_level_download": (_i32, [C.POINTER(LevelC), _ptr, _ptr]),
     "axs_level_rk4_advance": (_i32, [C.POINTER(LevelC), C.POINTER(BackgroundC), _dbl, _dbl, _dbl, _i32, _ptr]),
     "axs_level_rk4_sweep": (_i32, [C.POINTER(LevelC), C.POINTER(BackgroundC), _dbl, _dbl, _dbl, _i32, _ptr]),
+    "axs_level_rk4_step_to": (_i32, [C.POINTER(LevelC), _ptr, C.POINTER(BackgroundC), _dbl, _dbl, _dbl, _ptr]),
     "axs_level_device_status": (_i32, [C.POINTER(LevelC), _ptr]),
     "axs_level_handoff_rescale": (_i32, [C.POINTER(LevelC), _dbl, _dbl, _dbl, _dbl, _ptr]),
     "axs_level_adjoint_work_bytes": (_i32, [_i32, _i32, _i32, _i32, C.POINTER(_i64)]),

@@ -139,7 +139,7 @@ class TwoLevel:
         self.nb = (coarse.nx // block, coarse.ny // block, coarse.nz // block)
         # the coarse state at the start of the running coarse step (state only: the
         # ghost fill reads nothing else)
-        self.old_state = torch.empty_like(coarse.state)
+        self.old_state = torch.zeros_like(coarse.state)
         self.old_c = L.LevelC(self.old_state.data_ptr(), coarse.work.data_ptr(), coarse.c.dtype, coarse.nx, coarse.ny,
                               coarse.nz, coarse.dx, 0)
         self.patches: Patches | None = None
@@ -238,8 +238,11 @@ class TwoLevel:
             if self.patches is None:
                 self.coarse.advance(bg, tau_i, t, dt, 1)
                 continue
-            self.old_state.copy_(self.coarse.state)
-            self.coarse.advance(bg, tau_i, t, dt, 1)
+            # the step goes into the spare buffer, which then becomes the state;
+            # the previous state stays in the other one as the step's start
+            self.coarse.step_to(self.old_state, bg, tau_i, t, dt)
+            self.old_state = self.coarse.swap_state(self.old_state)
+            self.old_c.state = self.old_state.data_ptr()
             for f, theta in enumerate((0.0, 0.5)):
                 L.call("axs_patches_fill", C.byref(self.patches.c), C.byref(self._map()), C.byref(self.old_c),
                        C.byref(self.coarse.c), theta, dt, 0, None)

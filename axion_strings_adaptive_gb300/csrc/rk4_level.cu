@@ -87,6 +87,7 @@ struct SweepRunArgs {
     int nsteps;
     int sweep_mask;
     cudaStream_t st;
+    void *out_state;  // one whole step into this buffer (level layout), the state unchanged; null: in place
 };
 
 // Step constants plus this level's strides and status word.
@@ -147,7 +148,8 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
                 ab.c4 = stage_coef<T>(*r.bg, r.tau_i + t + r.dt);
                 for (int c = 0; c < 4; ++c) ab.pt[c] = work + (4 + c) * g.cs;  // E, Q
                 for (int c = 0; c < 4; ++c) ab.pt[4 + c] = state + c * g.cs;   // psi_n, Pi_n
-                for (int c = 0; c < 4; ++c) ab.out[c] = state + c * g.cs;
+                T *dst = r.out_state != nullptr ? static_cast<T *>(r.out_state) : state;
+                for (int c = 0; c < 4; ++c) ab.out[c] = dst + c * g.cs;
                 if ((rc = LB::launch(map_work, ab, grid_b, r.st))) return rc;
             }
         }
@@ -189,8 +191,9 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
         if (r.sweep_mask != 3 || !applies(lv)) return Fallback::run(r);
         // An odd step count takes its first step as the two sweeps (in place; the
         // results are the same bits), so the fused steps after it come in pairs
-        // and end in the state buffer.
-        if (r.nsteps & 1) {
+        // and end in the state buffer. A step into another buffer is one fused
+        // launch from the state.
+        if ((r.nsteps & 1) && r.out_state == nullptr) {
             SweepRunArgs one = r;
             one.nsteps = 1;
             const int rc1 = Fallback::run(one);
@@ -220,7 +223,8 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
         fill_level_constants(a, lv, g, r.dt);
         const int pad_per_plane = 16 * (lv->ny + 4) + 4 * lv->nx;
         const dim3 pad_grid((unsigned)std::min(64, (pad_per_plane + 255) / 256), (unsigned)std::min(4 * lv->nz, 65535));
-        float *buf[2] = {static_cast<float *>(lv->state), static_cast<float *>(lv->work)};
+        float *buf[2] = {static_cast<float *>(lv->state),
+                         static_cast<float *>(r.out_state != nullptr ? r.out_state : lv->work)};
         LevelFusedMaps maps[2];
         int rc;
         for (int b = 0; b < 2; ++b)
@@ -250,6 +254,8 @@ struct TileConfigEntry {
 };
 
 static const TileConfigEntry kF32Configs[] = {
+    // the default: the fastest FP32 step at 512^3 (two sweeps where it does not apply)
+    {"f32 fused 32x16 ring6 t640", &FusedConfig<32, 16, 6, 640>::run},
     {"f32 v2 64x8 ring8", &SweepConfig<float, 2, 64, 8, 8, 2>::run},
     {"f32 v2 32x16 ring8", &SweepConfig<float, 2, 32, 16, 8, 2>::run},
     {"f32 v4 32x16 ring8", &SweepConfig<float, 4, 32, 16, 8, 2>::run},
@@ -267,7 +273,6 @@ static const TileConfigEntry kF32Configs[] = {
     // one-pass fused step (level_fused.cuh)
     {"f32 fused 32x16 ring6", &FusedConfig<32, 16, 6>::run},
     {"f32 fused 32x16 ring7", &FusedConfig<32, 16, 7>::run},
-    {"f32 fused 32x16 ring6 t640", &FusedConfig<32, 16, 6, 640>::run},
     {"f32 fused 32x16 ring7 t640", &FusedConfig<32, 16, 7, 640>::run},
 };
 static const TileConfigEntry kF64Configs[] = {
@@ -297,7 +302,7 @@ static int run_sweeps(const axs_level *lv, const LevelGeom &g, const axs_backgro
     const TileConfigEntry *cfg = config_for(lv->dtype, lv->tile_config);
     AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "tile_config %d out of range (0..%d)", lv->tile_config,
                 config_count(lv->dtype));
-    SweepRunArgs r{lv, &g, bg, tau_i, t0, dt, nsteps, mask, st};
+    SweepRunArgs r{lv, &g, bg, tau_i, t0, dt, nsteps, mask, st, nullptr};
     return cfg->run(r);
 }
 
@@ -430,6 +435,33 @@ int axs_level_rk4_sweep(const axs_level *lv, const axs_background *bg, double ta
     AXS_REQUIRE(sweep == 0 || sweep == 1, AXS_ERR_INVALID_ARGUMENT, "sweep must be 0 (A) or 1 (B)");
     AXS_REQUIRE(std::isfinite(dt) && dt > 0.0, AXS_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
     return run_sweeps(lv, g, bg, tau_i, t, dt, 1, sweep == 0 ? 1 : 2, (cudaStream_t)stream);
+}
+
+int axs_level_rk4_step_to(const axs_level *lv, void *dst_state, const axs_background *bg, double tau_i, double t,
+                          double dt, void *stream)
+{
+    LevelGeom g;
+    int rc = validate_level(lv, g);
+    if (rc) return rc;
+    AXS_REQUIRE(bg != nullptr, AXS_ERR_INVALID_ARGUMENT, "null background");
+    AXS_REQUIRE(std::isfinite(dt) && dt > 0.0, AXS_ERR_INVALID_ARGUMENT, "dt must be positive and finite");
+    AXS_REQUIRE(dst_state != nullptr, AXS_ERR_INVALID_ARGUMENT, "null destination state");
+    AXS_REQUIRE(((uintptr_t)dst_state % 128) == 0, AXS_ERR_ALIGNMENT, "destination state must be 128-byte aligned");
+    const size_t bytes = 4 * (size_t)g.cs * dtype_size(lv->dtype);
+    const char *d = static_cast<const char *>(dst_state), *s0 = static_cast<const char *>(lv->state),
+               *w0 = static_cast<const char *>(lv->work);
+    AXS_REQUIRE(d + bytes <= s0 || d >= s0 + bytes, AXS_ERR_INVALID_ARGUMENT, "destination overlaps the state");
+    AXS_REQUIRE(d + bytes <= w0 || d >= w0 + 8 * (size_t)g.cs * dtype_size(lv->dtype) + 256, AXS_ERR_INVALID_ARGUMENT,
+                "destination overlaps the work buffer");
+    if (bg->kind == AXS_BG_EXPANDING) {
+        AXS_REQUIRE(bg->a_inv > 1.0, AXS_ERR_INVALID_ARGUMENT, "a_inv must exceed 1");
+        AXS_REQUIRE(tau_i + t > 0.0, AXS_ERR_INVALID_ARGUMENT, "conformal time must stay positive");
+    }
+    const TileConfigEntry *cfg = config_for(lv->dtype, lv->tile_config);
+    AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "tile_config %d out of range (0..%d)", lv->tile_config,
+                config_count(lv->dtype));
+    SweepRunArgs r{lv, &g, bg, tau_i, t, dt, 1, 3, (cudaStream_t)stream, dst_state};
+    return cfg->run(r);
 }
 
 int axs_level_device_status(const axs_level *lv, void *stream)

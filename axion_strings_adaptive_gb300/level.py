@@ -249,6 +249,25 @@ class PeriodicLevel:
         L.call("axs_level_rk4_advance", C.byref(self.c), C.byref(bg.to_c()), float(tau_i), float(t0), float(dt),
                int(nsteps), _stream_ptr(stream))
 
+    def step_to(self, dst: torch.Tensor, bg: Background, tau_i: float, t: float, dt: float, stream=None) -> None:
+        """One RK4 step from t written into `dst` (a tensor like ``state``); the
+        level's state is unchanged (axs_level_rk4_step_to); asynchronous."""
+        if dst.shape != self.state.shape or dst.dtype != self.dtype or dst.device != self.state.device or \
+                not dst.is_contiguous():
+            raise ValueError("step_to needs a contiguous tensor of the state's shape, dtype and device")
+        L.call("axs_level_rk4_step_to", C.byref(self.c), dst.data_ptr(), C.byref(bg.to_c()), float(tau_i), float(t),
+               float(dt), _stream_ptr(stream))
+
+    def swap_state(self, other: torch.Tensor) -> torch.Tensor:
+        """Make `other` (a tensor like ``state``) the level's state and return the
+        previous state tensor; no data moves."""
+        if other.shape != self.state.shape or other.dtype != self.dtype or other.device != self.state.device or \
+                not other.is_contiguous():
+            raise ValueError("swap_state needs a contiguous tensor of the state's shape, dtype and device")
+        old, self.state = self.state, other
+        self.c.state = self.state.data_ptr()
+        return old
+
     def sweep(self, bg: Background, tau_i: float, t: float, dt: float, which: int, stream=None) -> None:
         """Sweep A (0) or B (1) of the step starting at t; A then B is one RK4 step."""
         L.call("axs_level_rk4_sweep", C.byref(self.c), C.byref(bg.to_c()), float(tau_i), float(t), float(dt),

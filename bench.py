@@ -493,7 +493,9 @@ def scale_report(A, dev, hbm_peak, n=512, steps=20, block=16, kdiv=64, regrid_ev
     p = two.patches
     parts = {}
     if p is not None:
-        parts["coarse_step"] = ev_ms(lambda: coarse.advance(bg, TAU_I, tau, DT, 1))[0]
+        # as TwoLevel.advance takes it: one step into the spare buffer (the timing
+        # leaves the new state there; the fills timed next only read it)
+        parts["coarse_step"] = ev_ms(lambda: coarse.step_to(two.old_state, bg, TAU_I, tau, DT))[0]
         for name, theta in (("ring_fill_theta0", 0.0), ("ring_fill_theta_half", 0.5)):
             parts[name] = ev_ms(lambda: L.call("axs_patches_fill", C.byref(p.c), C.byref(two._map()),
                                                C.byref(two.old_c), C.byref(coarse.c), theta, DT, 0, None))[0]
@@ -604,7 +606,9 @@ def run_native(args):
         return ms, per, clocks
 
     def level_config_name(level):
-        return dict(level.tile_configs())[level.tile_config] if level.tile_config else "default"
+        # tile_config 0 is the table's first entry (the default tiling)
+        return A._lib.lib().axs_level_tile_config_name(A._lib.AXS_F32 if level.dtype == torch.float32
+                                                       else A._lib.AXS_F64, level.tile_config).decode()
 
     # algorithmic words per site and launch (read + write, each compulsory word once)
     WORDS = {"rk4_sweep_A": 12, "rk4_sweep_B": 16, "rk4_fused_level": 8}

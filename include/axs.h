@@ -237,6 +237,15 @@ int axs_level_download(const axs_level *lv, void *host_state, void *stream);
 int axs_level_rk4_advance(const axs_level *lv, const axs_background *bg, double tau_i, double t0,
                           double dt, int32_t nsteps, void *stream);
 
+/* One axs_level_rk4_advance step from time t written into dst_state (a buffer
+ * of the level's state layout, axs_level_layout.state_bytes, 128-byte aligned,
+ * overlapping neither the state nor the work buffer), padding included; the
+ * level's state is left as it was. A subcycling driver that needs the coarse
+ * state at both ends of a step keeps the two buffers and swaps them, instead of
+ * copying the state before an in-place step. */
+int axs_level_rk4_step_to(const axs_level *lv, void *dst_state, const axs_background *bg, double tau_i, double t,
+                          double dt, void *stream);
+
 /* One of the two sweeps of the step starting at time t (sweep 0 = A: reads the
  * state, writes the between-sweep components; sweep 1 = B: reads those, writes
  * the state). Sweep A then sweep B equals one axs_level_rk4_advance step; this

@@ -230,3 +230,19 @@ def test_diagnostics_rejects_small_scratch_without_gpu(L):
     rc = lib.axs_diagnostics(C.byref(f), C.byref(p), None, C.c_void_p(8192), None, 0, C.c_void_p(16384), 16, None)
     assert rc == L.AXS_ERR_WORKSPACE
     assert b"scratch too small" in lib.axs_last_error()
+
+
+def test_step_to_validates_its_destination_without_gpu(L):
+    lib = L.lib()
+    lv = L.LevelC(C.c_void_p(4096), C.c_void_p(1 << 20), L.AXS_F32, 8, 8, 8, 0.5, 0)
+    bg = L.BackgroundC(0, 0, 2.0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0)
+    assert lib.axs_level_rk4_step_to(C.byref(lv), None, C.byref(bg), 1.0, 0.0, 0.1, None) == \
+        L.AXS_ERR_INVALID_ARGUMENT
+    assert lib.axs_level_rk4_step_to(C.byref(lv), C.c_void_p(4096), C.byref(bg), 1.0, 0.0, 0.1, None) == \
+        L.AXS_ERR_INVALID_ARGUMENT
+    assert b"overlaps the state" in lib.axs_last_error()
+    assert lib.axs_level_rk4_step_to(C.byref(lv), C.c_void_p((1 << 20) + 128), C.byref(bg), 1.0, 0.0, 0.1, None) == \
+        L.AXS_ERR_INVALID_ARGUMENT
+    assert b"overlaps the work" in lib.axs_last_error()
+    assert lib.axs_level_rk4_step_to(C.byref(lv), C.c_void_p((1 << 24) + 16), C.byref(bg), 1.0, 0.0, 0.1, None) == \
+        L.AXS_ERR_ALIGNMENT

@@ -24,6 +24,7 @@ def _state(n, seed, dtype):
 
 
 @pytest.mark.parametrize("dtype,tiling", [(torch.float32, "f32 v2 64x8 ring8"),
+                                          (torch.float32, "f32 fused 32x16 ring6 t640"),
                                           (torch.float32, "f32 fused 32x16 ring7 t640"),
                                           (torch.float64, None)])
 def test_expired_waits_are_reported_and_the_level_recovers(axs, dtype, tiling):

@@ -111,3 +111,46 @@ def test_fp32_step_vs_oracle_fp32_and_fp64_builds(axs, orc):
         e_gpu = _rel_max(got, ref64)
         assert e_gpu <= e_float_build and e_gpu < 1e-5, (name, e_gpu, e_float_build)
         assert _rel_max(got, ref32) <= e_gpu + e_float_build
+
+
+@pytest.mark.parametrize("cfg", [None, "f32 v2 32x8 ring8 l2", "f32 fused 32x16 ring6 t640"])
+@pytest.mark.parametrize("shape", [(64, 64, 64), (96, 48, 40), (32, 16, 5)])
+def test_step_to_equals_an_in_place_step(axs, cfg, shape):
+    """axs_level_rk4_step_to writes the in-place step's whole padded state into
+    another buffer and leaves the level's state as it was."""
+    v = _state(shape, 3 + sum(shape))
+    bg = axs.Background.expanding(1.5, 1.0, lambda0=2.0)
+    ref = _run(axs, shape, cfg, v, 1, bg)
+    lv = axs.PeriodicLevel(shape, 0.5, dtype=torch.float32)
+    if cfg is not None:
+        lv.tile_config = _config_id(lv, cfg)
+    lv.set_state(v.cuda())
+    before = lv.state.clone()
+    dst = torch.zeros_like(lv.state)
+    lv.step_to(dst, bg, 1.0, 0.0, 0.1)
+    lv.device_status()
+    torch.cuda.synchronize()
+    assert torch.equal(lv.state, before)
+    assert torch.equal(dst, ref.state)
+    old = lv.swap_state(dst)
+    assert torch.equal(old, before) and lv.state.data_ptr() == dst.data_ptr()
+    lv.advance(bg, 1.0, 0.1, 0.1, 1)  # the swapped-in buffer steps like any state
+    ref.advance(bg, 1.0, 0.1, 0.1, 1)
+    torch.cuda.synchronize()
+    assert torch.equal(lv.state, ref.state)
+
+
+def test_step_to_fp64(axs):
+    shape = (48, 40, 24)
+    rng = np.random.default_rng(5)
+    v = torch.from_numpy(rng.standard_normal((4, shape[2], shape[1], shape[0])) + 1.5)
+    bg = axs.Background.flat(1.0)
+    a = axs.PeriodicLevel(shape, 0.5, dtype=torch.float64)
+    a.set_state(v.cuda())
+    b = axs.PeriodicLevel(shape, 0.5, dtype=torch.float64)
+    b.set_state(v.cuda())
+    dst = torch.zeros_like(b.state)
+    a.advance(bg, 1.0, 0.0, 0.05, 1)
+    b.step_to(dst, bg, 1.0, 0.0, 0.05)
+    torch.cuda.synchronize()
+    assert torch.equal(dst, a.state)
