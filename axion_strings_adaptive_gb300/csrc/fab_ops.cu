@@ -91,14 +91,22 @@ __global__ void eval_rhs_f64_kernel(const axs_fab s, const axs_fab r, double one
 // planes ahead of the plane the block computes: every stencil operand then
 // comes from shared memory, each staged value is read from global memory once
 // per block, and a thread keeps about 5 D copies in flight.
-template <int TY, int ZC, int D>
+// W16: FABs whose psi tile rows start 16-byte aligned (ng = 2 mod 4, strides
+// multiples of 4 elements, a 16-byte aligned base) and whose extents are
+// multiples of the block tile (nx of 32, ny of TY): the tile's rows are copied
+// in 16-byte pieces (9 per 36-column row), Pi over the same 36-column rows, and
+// no piece leaves the ghost region, so no zero-fill is needed.
+template <int TY, int ZC, int D, bool W16>
 __global__ void __launch_bounds__(32 * TY) eval_rhs_f32_zmarch_kernel(const axs_fab s, const axs_fab r,
                                                                       float one_over_dx2, float kappa, float lambda,
                                                                       float R2)
 {
-    constexpr int SX = 36, SY = TY + 4, PSI = SX * SY, NT = 32 * TY, PI = NT, SLOT = 2 * PSI + 2 * PI;
-    constexpr int NSLOT = D + 5, NPS = (2 * PSI + NT - 1) / NT;
-    __shared__ float sh[NSLOT * SLOT];
+    constexpr int SX = 36, SY = TY + 4, PSI = SX * SY, NT = 32 * TY;
+    constexpr int PI = W16 ? TY * SX : NT;  // one Pi component of a slot
+    constexpr int SLOT = 2 * PSI + 2 * PI, NSLOT = D + 5;
+    constexpr int NPS = W16 ? (2 * SY * 9 + 2 * TY * 9 + NT - 1) / NT : (2 * PSI + NT - 1) / NT;
+    static_assert(!W16 || (SLOT % 4 == 0 && PSI % 4 == 0 && PI % 4 == 0), "16-byte pieces land 16-byte aligned");
+    __shared__ __align__(16) float sh[NSLOT * SLOT];
     const float *__restrict__ sp = static_cast<const float *>(s.data);
     float *__restrict__ rp = static_cast<float *>(r.data);
     const float wf = 8.33333333333333333333e-2f, wn = 1.33333333333333333333e+0f, wl = 2.5f;
@@ -108,37 +116,64 @@ __global__ void __launch_bounds__(32 * TY) eval_rhs_f32_zmarch_kernel(const axs_
     const int i = x0 + tx, j = y0 + ty;
     const bool in = i < s.nx && j < s.ny;
     const int64_t o0 = fab_off(s, in ? i : 0, in ? j : 0, 0), ro0 = fab_off(r, in ? i : 0, in ? j : 0, 0);
-    // This thread's staged psi cells: plane-0 global offset, and whether the cell
-    // lies within the FAB's 2 ghost layers (else it is zero-filled, and no
-    // computed cell reads it).
-    int64_t psi_off[NPS];
-    bool psi_ok[NPS];
+    // This thread's staging tasks: plane-0 global offset, shared offset within a
+    // slot, and whether the task copies (W16: 16-byte pieces of psi rows, then of
+    // Pi rows; else psi cells, zero-filled outside the FAB's 2 ghost layers).
+    int64_t st_off[NPS];
+    int st_sh[NPS];
+    bool st_ok[NPS];
 #pragma unroll
     for (int q = 0; q < NPS; ++q) {
         const int e = tid + q * NT;
-        const int c = e >= PSI, rem = e - c * PSI, yy = rem / SX, xx = rem - yy * SX;
-        const int gi = x0 - 2 + xx, gj = y0 - 2 + yy;
-        psi_ok[q] = e < 2 * PSI && gi < s.nx + 2 && gj < s.ny + 2;
-        psi_off[q] = psi_ok[q] ? c * s.cstride + fab_off(s, gi, gj, 0) : 0;
+        if constexpr (W16) {
+            const int npsi = 2 * SY * 9, e2 = e - npsi;
+            const bool is_psi = e < npsi;
+            const int rows = is_psi ? SY : TY, ee = is_psi ? e : e2;
+            const int c = ee / (rows * 9), rem = ee - c * rows * 9, row = rem / 9, k = rem - row * 9;
+            st_ok[q] = is_psi || e2 < 2 * TY * 9;
+            const int gj = is_psi ? y0 - 2 + row : y0 + row;
+            st_off[q] = st_ok[q] ? (is_psi ? c : 2 + c) * s.cstride + fab_off(s, x0 - 2 + 4 * k, gj, 0) : 0;
+            st_sh[q] = (is_psi ? c * PSI : 2 * PSI + c * PI) + row * SX + 4 * k;
+        } else {
+            const int c = e >= PSI, rem = e - c * PSI, yy = rem / SX, xx = rem - yy * SX;
+            const int gi = x0 - 2 + xx, gj = y0 - 2 + yy;
+            st_ok[q] = e < 2 * PSI && gi < s.nx + 2 && gj < s.ny + 2;
+            st_off[q] = st_ok[q] ? c * s.cstride + fab_off(s, gi, gj, 0) : 0;
+            st_sh[q] = e;
+        }
     }
     auto slot = [&](int p) { return sh + ((p - z0 + 2) % NSLOT) * SLOT; };
     auto issue = [&](int p) {
         if (p > z1 + 1) return;  // beyond the last plane a computed cell reads
         float *dst = slot(p);
         const int64_t po = (int64_t)p * s.kstride;
+        if constexpr (W16) {
+            // psi pieces for every staged plane; Pi pieces only for the computed planes
 #pragma unroll
-        for (int q = 0; q < NPS; ++q)
-            if (tid + q * NT < 2 * PSI) cp_async_elem(dst + tid + q * NT, sp + psi_off[q] + po, psi_ok[q], sp);
-        if (p >= z0 && p < z1) {
-            cp_async_elem(dst + 2 * PSI + tid, sp + 2 * s.cstride + o0 + po, in, sp);
-            cp_async_elem(dst + 2 * PSI + PI + tid, sp + 3 * s.cstride + o0 + po, in, sp);
+            for (int q = 0; q < NPS; ++q) {
+                const bool pi_piece = st_sh[q] >= 2 * PSI;
+                if (st_ok[q] && (!pi_piece || (p >= z0 && p < z1))) {
+                    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + st_sh[q]);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(sp + st_off[q] + po)
+                                 : "memory");
+                }
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < NPS; ++q)
+                if (tid + q * NT < 2 * PSI) cp_async_elem(dst + st_sh[q], sp + st_off[q] + po, st_ok[q], sp);
+            if (p >= z0 && p < z1) {
+                cp_async_elem(dst + 2 * PSI + tid, sp + 2 * s.cstride + o0 + po, in, sp);
+                cp_async_elem(dst + 2 * PSI + PI + tid, sp + 3 * s.cstride + o0 + po, in, sp);
+            }
         }
     };
     for (int p = z0 - 2; p <= z0 + 1 + D; ++p) {
         issue(p);
         cp_async_commit();
     }
-    const int c0 = (ty + 2) * SX + tx + 2;  // this thread's cell in a plane's psi tile
+    const int c0 = (ty + 2) * SX + tx + 2;                    // this thread's cell in a plane's psi tile
+    const int pi0 = 2 * PSI + (W16 ? ty * SX + tx + 2 : tid);  // ... and in its Pi tile
     for (int z = z0; z < z1; ++z) {
         cp_async_wait<D - 1>();  // planes up to z + 2 have landed (this thread's copies)
         __syncthreads();         // ... and everyone's; the slot of plane z - 3 is free
@@ -161,8 +196,8 @@ __global__ void __launch_bounds__(32 * TY) eval_rhs_f32_zmarch_kernel(const axs_
             const int64_t ro = ro0 + (int64_t)z * r.kstride;
             const float psi1 = t[c0], psi2 = t[PSI + c0];
             const float pc = 0.5f * lambda * (psi1 * psi1 + psi2 * psi2 - R2);
-            rp[ro] = t[2 * PSI + tid];
-            rp[r.cstride + ro] = t[2 * PSI + PI + tid];
+            rp[ro] = t[pi0];
+            rp[r.cstride + ro] = t[pi0 + PI];
             rp[2 * r.cstride + ro] = lap[0] + kappa * psi1 - pc * psi1;
             rp[3 * r.cstride + ro] = lap[1] + kappa * psi2 - pc * psi2;
         }
@@ -579,10 +614,19 @@ int axs_eval_rhs(const axs_fab *soln, const axs_fab *rhs, double dx, const axs_r
     cudaStream_t st = (cudaStream_t)stream;
     if (soln->dtype == AXS_F64)
         eval_rhs_f64_kernel<<<g, 256, 0, st>>>(*soln, *rhs, one_over_dx2, c->kappa, c->lambda, c->R2);
-    else
-        eval_rhs_f32_zmarch_kernel<8, 64, 2><<<dim3((soln->nx + 31) / 32, (soln->ny + 7) / 8, (soln->nz + 63) / 64),
-                                            dim3(32, 8), 0, st>>>(*soln, *rhs, (float)one_over_dx2, (float)c->kappa,
-                                                                  (float)c->lambda, (float)c->R2);
+    else {
+        const dim3 grid((soln->nx + 31) / 32, (soln->ny + 7) / 8, (soln->nz + 63) / 64), block(32, 8);
+        const bool w16 = soln->ng % 4 == 2 && soln->jstride % 4 == 0 && soln->kstride % 4 == 0 &&
+                         soln->cstride % 4 == 0 && (uintptr_t)soln->data % 16 == 0 && soln->nx % 32 == 0 &&
+                         soln->ny % 8 == 0;
+        const float k = (float)c->kappa, l = (float)c->lambda, r2 = (float)c->R2;
+        if (w16)
+            eval_rhs_f32_zmarch_kernel<8, 64, 2, true><<<grid, block, 0, st>>>(*soln, *rhs, (float)one_over_dx2, k, l,
+                                                                               r2);
+        else
+            eval_rhs_f32_zmarch_kernel<8, 64, 2, false><<<grid, block, 0, st>>>(*soln, *rhs, (float)one_over_dx2, k, l,
+                                                                                r2);
+    }
     return launch_status("eval_rhs");
 }
 

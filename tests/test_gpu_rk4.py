@@ -228,3 +228,23 @@ def test_fused_rk4_f64_512cubed_matches_oracle(axs, orc):
     ref = orc.from_fab(fab, 2)
     del fab
     assert _rel_max(got, ref) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(64, 16, 40), (32, 8, 5), (96, 24, 70)])
+def test_eval_rhs_f32_wide_staging_equals_cell_staging(axs, shape):
+    """FP32 drop-in RHS: FABs with ng = 2 and tile-multiple extents stage their
+    rows in 16-byte pieces, others cell by cell; same arithmetic, same bits."""
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx + ny + nz)
+    v = torch.from_numpy(rng.standard_normal((4, nz, ny, nx)) + 1.0).float().cuda()
+    c = axs.Background.expanding(2.0, 2.0, lambda0=2.0).rhs_coeffs(1.7)
+    out = []
+    for ng in (2, 3):
+        s = axs.new_fab((nx, ny, nz), ng, dtype=torch.float32)
+        axs.valid(s, ng).copy_(v)
+        axs.fill_periodic_ghosts(s, ng)
+        r = axs.new_fab((nx, ny, nz), 0, dtype=torch.float32)
+        axs.eval_rhs(s, r, ng, 0, 0.5, c)
+        out.append(axs.valid(r, 0).clone())
+    torch.cuda.synchronize()
+    assert torch.equal(out[0], out[1])
