@@ -25,6 +25,7 @@ AXS_ERR_CAPACITY = 7
 AXS_DEFAULT_WAIT_POLLS = 4194304
 
 AXS_F32, AXS_F64 = 1, 2
+LEVEL_COMPENSATED_FP32 = 1  # axs_level.flags
 BG_EXPANDING, BG_FLAT, BG_PRE_EVOLUTION = 0, 1, 2
 MASK_NONE, MASK_A, MASK_B = 0, 1, 2
 BOUNDARY_GHOSTS, BOUNDARY_PERIODIC = 0, 1
@@ -58,7 +59,7 @@ class LevelLayout(C.Structure):
 
 class LevelC(C.Structure):
     _fields_ = [("state", _ptr), ("work", _ptr), ("dtype", _i32), ("nx", _i32), ("ny", _i32), ("nz", _i32),
-                ("dx", _dbl), ("tile_config", _i32)]
+                ("dx", _dbl), ("tile_config", _i32), ("flags", _i32)]
 
 
 class DiagParams(C.Structure):
@@ -218,7 +219,7 @@ def lib():
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
-        if L.axs_abi_version() != 1:
+        if L.axs_abi_version() != 2:
             raise RuntimeError("libaxs_gb300.so ABI version mismatch")
         _lib = L
     return _lib

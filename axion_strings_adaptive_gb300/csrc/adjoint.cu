@@ -40,6 +40,7 @@ int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const Leve
 struct AdjointB {
     static constexpr int kPointwise = 6;
     static constexpr bool kLambdaGrad = true;
+    static constexpr bool kComp = false;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
                                  const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam,
@@ -85,6 +86,7 @@ struct AdjointB {
 struct AdjointA {
     static constexpr int kPointwise = 12;
     static constexpr bool kLambdaGrad = true;
+    static constexpr bool kComp = false;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
                                  const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam,

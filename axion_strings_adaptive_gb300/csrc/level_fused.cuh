@@ -38,8 +38,9 @@
 
 namespace axs {
 
-template <int TX_, int TY_, int NS_, int THREADS_ = 512> struct LevelFusedShape {
+template <int TX_, int TY_, int NS_, int THREADS_ = 512, bool COMP_ = false> struct LevelFusedShape {
     using T = float;
+    static constexpr bool COMP = COMP_;  // the compensated FP32 step (stage_a in rk4_ops.cuh)
     static constexpr int V = 2, TX = TX_, TY = TY_, NS = NS_;
     // sweep A units run on the first NA threads and sweep B units on the last NB:
     // with 640 threads no thread runs both, so sweep B of one plane overlaps sweep
@@ -84,28 +85,27 @@ template <int OFF> __device__ __forceinline__ void sts2(uint32_t addr, float x, 
 // Laplacian and centre of two sites of one component: p[d] = shared address of
 // the first site in planes z-2 .. z+2, RB the row length in bytes, CO the
 // component's byte offset. The arithmetic is lap_pair's, as in every FP32 sweep.
-template <int RB, int CO>
+template <int RB, int CO, bool COMP>
 __device__ __forceinline__ void star_pair_sh(const SweepArgs<float> &a, const uint32_t (&p)[5], float (&lap)[2],
                                              float (&ctr)[2])
 {
     const float2 a0 = lds2<CO - 8>(p[2]), a1 = lds2<CO>(p[2]), a2 = lds2<CO + 8>(p[2]);
     const float r[6] = {a0.x, a0.y, a1.x, a1.y, a2.x, a2.y};
-    lap_pair(a.wA, a.wB, r, lds2<CO - RB>(p[2]), lds2<CO + RB>(p[2]), lds2<CO - 2 * RB>(p[2]),
-             lds2<CO + 2 * RB>(p[2]), lds2<CO>(p[1]), lds2<CO>(p[3]), lds2<CO>(p[0]), lds2<CO>(p[4]), lap[0],
-             lap[1]);
+    lap_pair<COMP>(a, r, lds2<CO - RB>(p[2]), lds2<CO + RB>(p[2]), lds2<CO - 2 * RB>(p[2]), lds2<CO + 2 * RB>(p[2]),
+                   lds2<CO>(p[1]), lds2<CO>(p[3]), lds2<CO>(p[0]), lds2<CO>(p[4]), lap[0], lap[1]);
     ctr[0] = a1.x;
     ctr[1] = a1.y;
 }
 
 // the same for the four components, CS bytes apart
-template <int RB, int CS>
+template <int RB, int CS, bool COMP>
 __device__ __forceinline__ void star4_sh(const SweepArgs<float> &a, const uint32_t (&p)[5], float (&lap)[4][2],
                                          float (&ctr)[4][2])
 {
-    star_pair_sh<RB, 0 * CS>(a, p, lap[0], ctr[0]);
-    star_pair_sh<RB, 1 * CS>(a, p, lap[1], ctr[1]);
-    star_pair_sh<RB, 2 * CS>(a, p, lap[2], ctr[2]);
-    star_pair_sh<RB, 3 * CS>(a, p, lap[3], ctr[3]);
+    star_pair_sh<RB, 0 * CS, COMP>(a, p, lap[0], ctr[0]);
+    star_pair_sh<RB, 1 * CS, COMP>(a, p, lap[1], ctr[1]);
+    star_pair_sh<RB, 2 * CS, COMP>(a, p, lap[2], ctr[2]);
+    star_pair_sh<RB, 3 * CS, COMP>(a, p, lap[3], ctr[3]);
 }
 
 // The three tensor maps over one state buffer: the whole box (interior tile
@@ -258,9 +258,9 @@ __global__ void __launch_bounds__(S::THREADS, 1)
 #pragma unroll
                 for (int d = 0; d < 5; ++d) pa[d] = pl[d] + a_at;
                 T lap[4][V], ctr[4][V];
-                star4_sh<BX * 4, BX * BY * 4>(a, pa, lap, ctr);
+                star4_sh<BX * 4, BX * BY * 4, S::COMP>(a, pa, lap, ctr);
                 T o[8][V];
-                stage_a<T, V>(a, lap, ctr, o);
+                stage_a<T, V, S::COMP>(a, lap, ctr, o);
                 const uint32_t sz = swin_sh + (uint32_t)s0 * (uint32_t)(S::SWIN * 4) + a_so;  // d3, d4 of plane za
                 sts2<0 * AX * AY * 4>(sz, o[0][0], o[0][1]);
                 sts2<1 * AX * AY * 4>(sz, o[1][0], o[1][1]);
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
                 }
                 const uint32_t ez = eqw_sh + (uint32_t)(e0 ^ 2) * (uint32_t)(S::EQW * 4) + b_eo;  // E, Q of plane zb
                 T lap[4][V], ctr[4][V], o[4][V], pq[8][V];
-                star4_sh<AX * 4, AX * AY * 4>(a, sp, lap, ctr);
+                star4_sh<AX * 4, AX * AY * 4, S::COMP>(a, sp, lap, ctr);
                 const float2 e[4] = {lds2<0 * TX * TY * 4>(ez), lds2<1 * TX * TY * 4>(ez), lds2<2 * TX * TY * 4>(ez),
                                      lds2<3 * TX * TY * 4>(ez)};
 #pragma unroll
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
                     pq[4 + c][0] = pn[c].x;
                     pq[4 + c][1] = pn[c].y;
                 }
-                stage_b<T, V>(a, lap, ctr, pq, o);
+                stage_b<T, V, decltype(pq), S::COMP>(a, lap, ctr, pq, o);
                 const int x = x0 + bxl, y = y0 + byl;
                 const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + oy) * a.js + (int64_t)zb * a.ks;
 #pragma unroll

@@ -68,6 +68,8 @@ static int validate_level(const axs_level *lv, LevelGeom &g)
     int rc = level_geom(lv->dtype, lv->nx, lv->ny, lv->nz, g);
     if (rc) return rc;
     AXS_REQUIRE(lv->dx > 0.0, AXS_ERR_INVALID_ARGUMENT, "dx must be positive");
+    AXS_REQUIRE((lv->flags & ~AXS_LEVEL_COMPENSATED_FP32) == 0, AXS_ERR_INVALID_ARGUMENT, "unknown level flags 0x%x",
+                lv->flags);
     AXS_REQUIRE(((uintptr_t)lv->state % 128) == 0 && ((uintptr_t)lv->work % 128) == 0, AXS_ERR_ALIGNMENT,
                 "level buffers must be 128-byte aligned");
     return AXS_OK;
@@ -110,9 +112,10 @@ int make_level_map(CUtensorMap *map, const void *base, int32_t dtype, const Leve
                               4);
 }
 
-template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false> struct SweepConfig {
-    using LA = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardA, SingleLevel, HINT>;
-    using LB = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardB, SingleLevel, HINT>;
+template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false, bool COMP = false>
+struct SweepConfig {
+    using LA = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardAT<COMP>, SingleLevel, HINT>;
+    using LB = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardBT<COMP>, SingleLevel, HINT>;
 
     static int run(const SweepRunArgs &r)
     {
@@ -163,9 +166,9 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
 // the first 4 component planes of its work buffer (same layout); each step is
 // the fused launch and the padding launch. An odd step count runs its first
 // step as the two sweeps, which step the state in place.
-template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
-    using S = LevelFusedShape<TX, TY, NS, THREADS>;
-    using Fallback = SweepConfig<float, 2, 32, 8, 8, 3, true>;  // the fastest two-sweep tiling at 512^3
+template <int TX, int TY, int NS, int THREADS = 512, bool COMP = false> struct FusedConfig {
+    using S = LevelFusedShape<TX, TY, NS, THREADS, COMP>;
+    using Fallback = SweepConfig<float, 2, 32, 8, 8, 3, true, COMP>;  // the fastest two-sweep tiling at 512^3
 
     static bool applies(const axs_level *lv)
     {
@@ -247,15 +250,18 @@ template <int TX, int TY, int NS, int THREADS = 512> struct FusedConfig {
 };
 
 // Tile configurations (vector width, tile, ring depth, expected blocks/SM).
-// Entry 0 of each table is the default (tile_config = 0).
+// Entry 0 of each table is the default (tile_config = 0). run_comp: the
+// compensated FP32 step (AXS_LEVEL_COMPENSATED_FP32) of the same tiling, where
+// one is compiled; other tilings run the default entry's.
 struct TileConfigEntry {
     const char *name;
     int (*run)(const SweepRunArgs &);
+    int (*run_comp)(const SweepRunArgs &);
 };
 
 static const TileConfigEntry kF32Configs[] = {
     // the default: the fastest FP32 step at 512^3 (two sweeps where it does not apply)
-    {"f32 fused 32x16 ring6 t640", &FusedConfig<32, 16, 6, 640>::run},
+    {"f32 fused 32x16 ring6 t640", &FusedConfig<32, 16, 6, 640>::run, &FusedConfig<32, 16, 6, 640, true>::run},
     {"f32 v2 64x8 ring8", &SweepConfig<float, 2, 64, 8, 8, 2>::run},
     {"f32 v2 32x16 ring8", &SweepConfig<float, 2, 32, 16, 8, 2>::run},
     {"f32 v4 32x16 ring8", &SweepConfig<float, 4, 32, 16, 8, 2>::run},
@@ -268,7 +274,8 @@ static const TileConfigEntry kF32Configs[] = {
     // L2 policies: stencil planes evict-last, pointwise inputs and outputs evict-first
     {"f32 v2 64x8 ring8 l2", &SweepConfig<float, 2, 64, 8, 8, 2, true>::run},
     {"f32 v2 32x16 ring8 l2", &SweepConfig<float, 2, 32, 16, 8, 2, true>::run},
-    {"f32 v2 32x8 ring8 l2", &SweepConfig<float, 2, 32, 8, 8, 3, true>::run},
+    {"f32 v2 32x8 ring8 l2", &SweepConfig<float, 2, 32, 8, 8, 3, true>::run,
+     &SweepConfig<float, 2, 32, 8, 8, 3, true, true>::run},
     {"f32 v4 64x16 ring6 l2", &SweepConfig<float, 4, 64, 16, 6, 1, true>::run},
     // one-pass fused step (level_fused.cuh)
     {"f32 fused 32x16 ring6", &FusedConfig<32, 16, 6>::run},
@@ -296,6 +303,16 @@ static const TileConfigEntry *config_for(int32_t dtype, int32_t id)
     return &tab[id == 0 ? 0 : id - 1];
 }
 
+// The level's runner: its tiling, or the compensated FP32 step when the level
+// asks for it (FP64 levels have no compensated form: the flag changes nothing).
+using Runner = int (*)(const SweepRunArgs &);
+static Runner runner_for(const axs_level *lv, const TileConfigEntry *cfg)
+{
+    if (lv->dtype == AXS_F32 && (lv->flags & AXS_LEVEL_COMPENSATED_FP32))
+        return cfg->run_comp != nullptr ? cfg->run_comp : kF32Configs[0].run_comp;
+    return cfg->run;
+}
+
 static int run_sweeps(const axs_level *lv, const LevelGeom &g, const axs_background *bg, double tau_i, double t0,
                       double dt, int nsteps, int mask, cudaStream_t st)
 {
@@ -303,7 +320,7 @@ static int run_sweeps(const axs_level *lv, const LevelGeom &g, const axs_backgro
     AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "tile_config %d out of range (0..%d)", lv->tile_config,
                 config_count(lv->dtype));
     SweepRunArgs r{lv, &g, bg, tau_i, t0, dt, nsteps, mask, st, nullptr};
-    return cfg->run(r);
+    return runner_for(lv, cfg)(r);
 }
 
 }  // namespace axs
@@ -461,7 +478,7 @@ int axs_level_rk4_step_to(const axs_level *lv, void *dst_state, const axs_backgr
     AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "tile_config %d out of range (0..%d)", lv->tile_config,
                 config_count(lv->dtype));
     SweepRunArgs r{lv, &g, bg, tau_i, t, dt, 1, 3, (cudaStream_t)stream, dst_state};
-    return cfg->run(r);
+    return runner_for(lv, cfg)(r);
 }
 
 int axs_level_device_status(const axs_level *lv, void *stream)

@@ -45,6 +45,9 @@ template <typename T> struct SweepArgs {
     T wA, wB, wC;                // lap = wA*S1 + wB*S2 + wC*f0 (S1/S2: sums of +-1 / +-2 neighbours)
     StageCoef<T> c1, c2, c4;     // stage coefficients at t, t + h/2, t + h
     T h, h_half, h2_quarter, h2_half, h_sixth, h_third, h2_sixth;
+    // remainders of the FP32 weights and step fractions (exact value - FP32 value),
+    // used by the compensated FP32 step
+    T wA_lo, wB_lo, h_lo, h_half_lo, h2_quarter_lo, h2_half_lo, h_sixth_lo, h_third_lo, h2_sixth_lo;
     const T *pt[kMaxPointwise];  // pointwise input components (level layout)
     T *out[8];                   // output components (level layout)
     double inv_lambda0;          // adjoint: dlambda_s/dlambda0 = lambda_s / lambda0
@@ -222,17 +225,22 @@ __device__ __forceinline__ void rhs_adjoint_pair(const StageCoef<T> &c, T u1, T 
 // sum(f+-2 - f0): a neighbour within a factor 2 of f0 gives an exact
 // difference, so the -30 f0 term of the plain sum does not cancel against the
 // neighbours. f - f0 is formed as f + (-f0), the same IEEE result. Every FP32
-// sweep evaluates its stencils through this function.
-__device__ __forceinline__ void lap_pair(float wA, float wB, const float *r, float2 ym1, float2 yp1, float2 ym2,
-                                         float2 yp2, float2 zm1, float2 zp1, float2 zm2, float2 zp2, float &l0,
-                                         float &l1)
+// sweep evaluates its stencils through this function. COMP (the compensated
+// FP32 step) adds the weights' FP32 remainders times d1, d2: FP32 rounds 16/3
+// and -1/3 in the same direction for every site, a bias that the plain form
+// carries into every step.
+template <bool COMP = false>
+__device__ __forceinline__ void lap_pair(const SweepArgs<float> &a, const float *r, float2 ym1, float2 yp1,
+                                         float2 ym2, float2 yp2, float2 zm1, float2 zp1, float2 zm2, float2 zp2,
+                                         float &l0, float &l1)
 {
     const F2 m0(-r[2], -r[3]);
     const F2 d1 = ((F2(r[1], r[2]) + m0) + (F2(r[3], r[4]) + m0)) + ((F2(ym1) + m0) + (F2(yp1) + m0)) +
                   ((F2(zm1) + m0) + (F2(zp1) + m0));
     const F2 d2 = ((F2(r[0], r[1]) + m0) + (F2(r[4], r[5]) + m0)) + ((F2(ym2) + m0) + (F2(yp2) + m0)) +
                   ((F2(zm2) + m0) + (F2(zp2) + m0));
-    const F2 l = fma(F2(wA), d1, F2(wB) * d2);
+    F2 l = fma(F2(a.wA), d1, F2(a.wB) * d2);
+    if constexpr (COMP) l = fma(F2(a.wA_lo), d1, fma(F2(a.wB_lo), d2, l));  // the weights' FP32 remainders
     l0 = l.v.x;
     l1 = l.v.y;
 }
@@ -246,7 +254,7 @@ __device__ __forceinline__ void lap_pair(float wA, float wB, const float *r, flo
 // does not cancel against the neighbour sums: lap = wA sum(f+-1 - f0) +
 // wB sum(f+-2 - f0), two sites per packed instruction where V is even. FP64:
 // the plain weighted sums.
-template <typename T, int V>
+template <typename T, int V, bool COMP = false>
 __device__ __forceinline__ void star_laplacian(const SweepArgs<T> &a, const T *zm2p, const T *zm1p, const T *P0,
                                                const T *zp1p, const T *zp2p, int at, int bx, T (&lap)[V],
                                                T (&ctr)[V])
@@ -267,7 +275,7 @@ __device__ __forceinline__ void star_laplacian(const SweepArgs<T> &a, const T *z
 #pragma unroll
         for (int v = 0; v < V; v += 2) {
             const int ci = PRE * V + v;
-            lap_pair(a.wA, a.wB, row + ci - 2, make_float2(ym1[v], ym1[v + 1]), make_float2(yp1[v], yp1[v + 1]),
+            lap_pair<COMP>(a, row + ci - 2, make_float2(ym1[v], ym1[v + 1]), make_float2(yp1[v], yp1[v + 1]),
                      make_float2(ym2[v], ym2[v + 1]), make_float2(yp2[v], yp2[v + 1]), make_float2(zm1[v], zm1[v + 1]),
                      make_float2(zp1[v], zp1[v + 1]), make_float2(zm2[v], zm2[v + 1]), make_float2(zp2[v], zp2[v + 1]),
                      lap[v], lap[v + 1]);
@@ -285,6 +293,7 @@ __device__ __forceinline__ void star_laplacian(const SweepArgs<T> &a, const T *z
                 const T d2 = ((row[ci - 2] - f0) + (row[ci + 2] - f0)) + ((ym2[v] - f0) + (yp2[v] - f0)) +
                              ((zm2[v] - f0) + (zp2[v] - f0));
                 lap[v] = fma(a.wA, d1, a.wB * d2);
+                if constexpr (COMP) lap[v] = fma(a.wA_lo, d1, fma(a.wB_lo, d2, lap[v]));
             } else {
                 const T s1 = (row[ci - 1] + row[ci + 1]) + (ym1[v] + yp1[v]) + (zm1[v] + zp1[v]);
                 const T s2 = (row[ci - 2] + row[ci + 2]) + (ym2[v] + yp2[v]) + (zm2[v] + zp2[v]);
@@ -444,7 +453,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                 T lap[4][V], ctr[4][V];
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    star_laplacian<T, V>(a, sl[0] + c * S::TILE, sl[1] + c * S::TILE, sl[2] + c * S::TILE,
+                    star_laplacian<T, V, Op::kComp>(a, sl[0] + c * S::TILE, sl[1] + c * S::TILE, sl[2] + c * S::TILE,
                                          sl[3] + c * S::TILE, sl[4] + c * S::TILE, yl * S::BX + xl, S::BX, lap[c],
                                          ctr[c]);
                 Op::template apply<T, V, HINT>(a, b, lap, ctr, pq, off + a.dox_out, x, y, lam_acc, pol_first);

@@ -195,6 +195,16 @@ class PeriodicLevel:
     def tile_config(self, v: int) -> None:
         self.c.tile_config = int(v)
 
+    @property
+    def compensated(self) -> bool:
+        """FP32 steps with the FP32 remainders of the Laplacian weights and the
+        step fractions applied (AXS_LEVEL_COMPENSATED_FP32; no effect in FP64)."""
+        return bool(self.c.flags & L.LEVEL_COMPENSATED_FP32)
+
+    @compensated.setter
+    def compensated(self, on: bool) -> None:
+        self.c.flags = (self.c.flags | L.LEVEL_COMPENSATED_FP32) if on else (self.c.flags & ~L.LEVEL_COMPENSATED_FP32)
+
     def tile_configs(self) -> list:
         """(id, name) of every sweep tiling compiled for this level's dtype."""
         lib = L.lib()

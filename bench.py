@@ -770,26 +770,35 @@ def run_native(args):
         ps = args.precision_steps
         marks = sorted({min(40, ps), ps})
         # fp64_fp32_storage: FP64 arithmetic with the state rounded to FP32 after every step
-        # (FP32 storage alone, without FP32 arithmetic)
-        legs = (("fp64", torch.float64, ic64, False), ("fp32", torch.float32, ic64.float(), False),
-                ("fp64_rounded_ic", torch.float64, ic64.float().double(), False),
-                ("fp64_fp32_storage", torch.float64, ic64.float().double(), True))
-        out = {}
-        for name, dt_, s0, round_state in legs:
+        # (FP32 storage alone, without FP32 arithmetic); fp32_compensated: the FP32 step with
+        # the FP32 remainders of its constants applied (AXS_LEVEL_COMPENSATED_FP32)
+        legs = (("fp64", torch.float64, ic64, False, False), ("fp32", torch.float32, ic64.float(), False, False),
+                ("fp32_compensated", torch.float32, ic64.float(), False, True),
+                ("fp64_rounded_ic", torch.float64, ic64.float().double(), False, False),
+                ("fp64_fp32_storage", torch.float64, ic64.float().double(), True, False))
+        out, step_ms = {}, {}
+        for name, dt_, s0, round_state, comp in legs:
             lv = A.PeriodicLevel(n, DX, dtype=dt_, device=dev, pierced_capacity=3 * n ** 3 // 8)
+            lv.compensated = comp
             lv.set_state(s0.to(dt_))
-            done = 0
+            done, t_ms = 0, 0.0
             for mk in marks:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
                 if round_state:
                     for s_ in range(done, mk):
                         lv.advance(bg, TAU_I, s_ * DT, DT, 1)
                         lv.state.copy_(lv.state.float())
                 else:
                     lv.advance(bg, TAU_I, done * DT, DT, mk - done)
+                e1.record()
+                torch.cuda.synchronize()
+                t_ms += e0.elapsed_time(e1)
                 done = mk
                 lv.device_status()
                 d = lv.diagnostics(bg, TAU_I + mk * DT, want_list=True)
                 out[(name, mk)] = (d, torch.sort(d.pierced.to(torch.int64))[0])
+            step_ms[name] = t_ms / done
             del lv
             torch.cuda.empty_cache()
 
@@ -811,8 +820,12 @@ def run_native(args):
             precision["by_step"][str(mk)] = {
                 "tau": TAU_I + mk * DT, "xi_fp64": ref[0].xi_plain, "n_p_fp64": ref[0].n_p_plain,
                 "fp32_vs_fp64": compare(ref, out[("fp32", mk)]),
+                "fp32_compensated_vs_fp64": compare(ref, out[("fp32_compensated", mk)]),
                 "fp64_rounded_ic_vs_fp64": compare(ref, out[("fp64_rounded_ic", mk)]),
                 "fp64_fp32_storage_vs_fp64": compare(ref, out[("fp64_fp32_storage", mk)])}
+        # step times of the legs (the 400-step advance, diagnostics excluded; FP32 levels on
+        # the default tiling, odd first segments on its two-sweep fallback)
+        precision["ms_per_step"] = {k: step_ms[k] for k in ("fp32", "fp32_compensated", "fp64")}
         fin = precision["by_step"][str(ps)]["fp32_vs_fp64"]
         precision["total_energy_rel_err"] = fin["total_energy_rel_err"]
         precision["max_energy_rel_err"] = fin["max_energy_rel_err"]

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define AXS_ABI_VERSION 1
+#define AXS_ABI_VERSION 2
 
 typedef enum axs_status {
     AXS_OK = 0,
@@ -200,7 +200,17 @@ typedef struct axs_level {
     int32_t nx, ny, nz;
     double dx;
     int32_t tile_config; /* 0 = default sweep tiling for the dtype; 1..N = axs_level_tile_config_name(dtype, id) */
+    int32_t flags;       /* AXS_LEVEL_* bits, 0 = none */
 } axs_level;
+
+/* axs_level.flags: FP32 steps with the FP32 remainders of the Laplacian weights
+ * and the RK4 step fractions (h, h/2, h^2/4, ...) applied as second FMAs. FP32
+ * rounds each of those constants once for the whole run and in the same
+ * direction at every site; the plain step integrates that bias (at 512^3 over
+ * 400 steps it is most of the FP32 run's departure from FP64 beyond FP32
+ * storage rounding). The same state layout and entry points; about 7 % slower.
+ * Ignored for FP64 levels. */
+#define AXS_LEVEL_COMPENSATED_FP32 1
 
 int axs_level_layout_for(int32_t dtype, int32_t nx, int32_t ny, int32_t nz, axs_level_layout *out);
 

@@ -38,7 +38,7 @@ def test_every_declared_symbol_is_exported(L):
 
 def test_abi_version_and_status_strings(L):
     lib = L.lib()
-    assert lib.axs_abi_version() == 1
+    assert lib.axs_abi_version() == 2
     for s in range(8):
         assert lib.axs_status_string(s)
 
@@ -246,3 +246,13 @@ def test_step_to_validates_its_destination_without_gpu(L):
     assert b"overlaps the work" in lib.axs_last_error()
     assert lib.axs_level_rk4_step_to(C.byref(lv), C.c_void_p((1 << 24) + 16), C.byref(bg), 1.0, 0.0, 0.1, None) == \
         L.AXS_ERR_ALIGNMENT
+
+
+def test_level_flags_are_checked_without_gpu(L):
+    lib = L.lib()
+    bg = L.BackgroundC(0, 0, 2.0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0)
+    lv = L.LevelC(C.c_void_p(4096), C.c_void_p(8192), L.AXS_F32, 8, 8, 8, 0.5, 0, 4)
+    assert lib.axs_level_rk4_advance(C.byref(lv), C.byref(bg), 1.0, 0.0, 0.1, 1, None) == L.AXS_ERR_INVALID_ARGUMENT
+    assert b"unknown level flags" in lib.axs_last_error()
+    lv.flags = L.LEVEL_COMPENSATED_FP32
+    assert lib.axs_level_rk4_advance(C.byref(lv), C.byref(bg), 1.0, 0.0, 0.1, 0, None) == L.AXS_OK  # no-op
