@@ -98,6 +98,11 @@ public:
     double time() const { return time_; }
     const axs_level &level() const { return lv_; }
     void set_tile_config(int32_t id) { lv_.tile_config = id; }
+    // the compensated FP32 step (AXS_LEVEL_COMPENSATED_FP32; no effect in FP64)
+    void set_compensated(bool on)
+    {
+        lv_.flags = on ? (lv_.flags | AXS_LEVEL_COMPENSATED_FP32) : (lv_.flags & ~AXS_LEVEL_COMPENSATED_FP32);
+    }
 
     // Valid cells (4, nz, ny, nx) of the level's dtype from / to host memory.
     void set_state(const void *host)

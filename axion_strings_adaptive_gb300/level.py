@@ -362,13 +362,16 @@ class AxionStringsLevel:
     """
 
     def __init__(self, n, dx: float, background: Background, tau_i: float = 1.0, dtype=torch.float32,
-                 masking_scheme: int = L.MASK_A, masking_threshold: float = 0.8, device="cuda"):
+                 masking_scheme: int = L.MASK_A, masking_threshold: float = 0.8, device="cuda",
+                 compensated: bool = False):
+        """compensated: the compensated FP32 step (PeriodicLevel.compensated)."""
         self.bg = background
         self.tau_i = float(tau_i)
         self.time = 0.0
         self.masking_scheme = masking_scheme
         self.masking_threshold = masking_threshold
         self.level = PeriodicLevel(n, dx, dtype=dtype, device=device)
+        self.level.compensated = compensated
 
     @property
     def tau(self) -> float:
