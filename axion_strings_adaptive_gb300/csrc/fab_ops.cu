@@ -218,7 +218,7 @@ template <typename T>
 __global__ void fill_periodic_kernel(const axs_fab f, int with_z)
 {
     T *p = static_cast<T *>(f.data) + blockIdx.y * f.cstride;
-    const int ng = f.ng, gx = f.nx + 2 * ng, gy = f.ny + 2 * ng, lane = threadIdx.x & 31;
+    const int ng = f.ng, gy = f.ny + 2 * ng, lane = threadIdx.x & 31;
     const int zrows = with_z ? 2 * ng * gy : 0, rows = zrows + f.nz * 2 * ng;
     for (int r = row_warp(); r < rows; r += row_warps()) {
         int j, k;

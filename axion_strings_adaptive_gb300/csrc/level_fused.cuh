@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
     __shared__ uint64_t full[NS];
     __shared__ int abort_flag;
     const int tid = threadIdx.x;
-    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int ny = a.ny, nz = a.nz;
     constexpr int oy = 2;  // padded row of y = 0 in the level layout
 
     if (tid == 0) {

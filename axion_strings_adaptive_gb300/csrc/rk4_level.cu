@@ -262,32 +262,32 @@ struct TileConfigEntry {
 static const TileConfigEntry kF32Configs[] = {
     // the default: the fastest FP32 step at 512^3 (two sweeps where it does not apply)
     {"f32 fused 32x16 ring6 t640", &FusedConfig<32, 16, 6, 640>::run, &FusedConfig<32, 16, 6, 640, true>::run},
-    {"f32 v2 64x8 ring8", &SweepConfig<float, 2, 64, 8, 8, 2>::run},
-    {"f32 v2 32x16 ring8", &SweepConfig<float, 2, 32, 16, 8, 2>::run},
-    {"f32 v4 32x16 ring8", &SweepConfig<float, 4, 32, 16, 8, 2>::run},
-    {"f32 v2 32x8 ring8", &SweepConfig<float, 2, 32, 8, 8, 3>::run},
-    {"f32 v1 32x8 ring8", &SweepConfig<float, 1, 32, 8, 8, 3>::run},
-    {"f32 v2 64x8 ring10", &SweepConfig<float, 2, 64, 8, 10, 1>::run},
-    {"f32 v4 64x16 ring6", &SweepConfig<float, 4, 64, 16, 6, 1>::run},
-    {"f32 v2 32x16 ring6", &SweepConfig<float, 2, 32, 16, 6, 2>::run},
-    {"f32 v1 32x16 ring7", &SweepConfig<float, 1, 32, 16, 7, 2>::run},
+    {"f32 v2 64x8 ring8", &SweepConfig<float, 2, 64, 8, 8, 2>::run, nullptr},
+    {"f32 v2 32x16 ring8", &SweepConfig<float, 2, 32, 16, 8, 2>::run, nullptr},
+    {"f32 v4 32x16 ring8", &SweepConfig<float, 4, 32, 16, 8, 2>::run, nullptr},
+    {"f32 v2 32x8 ring8", &SweepConfig<float, 2, 32, 8, 8, 3>::run, nullptr},
+    {"f32 v1 32x8 ring8", &SweepConfig<float, 1, 32, 8, 8, 3>::run, nullptr},
+    {"f32 v2 64x8 ring10", &SweepConfig<float, 2, 64, 8, 10, 1>::run, nullptr},
+    {"f32 v4 64x16 ring6", &SweepConfig<float, 4, 64, 16, 6, 1>::run, nullptr},
+    {"f32 v2 32x16 ring6", &SweepConfig<float, 2, 32, 16, 6, 2>::run, nullptr},
+    {"f32 v1 32x16 ring7", &SweepConfig<float, 1, 32, 16, 7, 2>::run, nullptr},
     // L2 policies: stencil planes evict-last, pointwise inputs and outputs evict-first
-    {"f32 v2 64x8 ring8 l2", &SweepConfig<float, 2, 64, 8, 8, 2, true>::run},
-    {"f32 v2 32x16 ring8 l2", &SweepConfig<float, 2, 32, 16, 8, 2, true>::run},
+    {"f32 v2 64x8 ring8 l2", &SweepConfig<float, 2, 64, 8, 8, 2, true>::run, nullptr},
+    {"f32 v2 32x16 ring8 l2", &SweepConfig<float, 2, 32, 16, 8, 2, true>::run, nullptr},
     {"f32 v2 32x8 ring8 l2", &SweepConfig<float, 2, 32, 8, 8, 3, true>::run,
      &SweepConfig<float, 2, 32, 8, 8, 3, true, true>::run},
-    {"f32 v4 64x16 ring6 l2", &SweepConfig<float, 4, 64, 16, 6, 1, true>::run},
+    {"f32 v4 64x16 ring6 l2", &SweepConfig<float, 4, 64, 16, 6, 1, true>::run, nullptr},
     // one-pass fused step (level_fused.cuh)
-    {"f32 fused 32x16 ring6", &FusedConfig<32, 16, 6>::run},
-    {"f32 fused 32x16 ring7", &FusedConfig<32, 16, 7>::run},
-    {"f32 fused 32x16 ring7 t640", &FusedConfig<32, 16, 7, 640>::run},
+    {"f32 fused 32x16 ring6", &FusedConfig<32, 16, 6>::run, nullptr},
+    {"f32 fused 32x16 ring7", &FusedConfig<32, 16, 7>::run, nullptr},
+    {"f32 fused 32x16 ring7 t640", &FusedConfig<32, 16, 7, 640>::run, nullptr},
 };
 static const TileConfigEntry kF64Configs[] = {
-    {"f64 v1 32x8 ring6", &SweepConfig<double, 1, 32, 8, 6, 2>::run},
-    {"f64 v2 32x8 ring6", &SweepConfig<double, 2, 32, 8, 6, 2>::run},
-    {"f64 v2 32x16 ring6", &SweepConfig<double, 2, 32, 16, 6, 1>::run},
-    {"f64 v1 32x4 ring7", &SweepConfig<double, 1, 32, 4, 7, 3>::run},
-    {"f64 v1 32x8 ring6 l2", &SweepConfig<double, 1, 32, 8, 6, 2, true>::run},
+    {"f64 v1 32x8 ring6", &SweepConfig<double, 1, 32, 8, 6, 2>::run, nullptr},
+    {"f64 v2 32x8 ring6", &SweepConfig<double, 2, 32, 8, 6, 2>::run, nullptr},
+    {"f64 v2 32x16 ring6", &SweepConfig<double, 2, 32, 16, 6, 1>::run, nullptr},
+    {"f64 v1 32x4 ring7", &SweepConfig<double, 1, 32, 4, 7, 3>::run, nullptr},
+    {"f64 v1 32x8 ring6 l2", &SweepConfig<double, 1, 32, 8, 6, 2, true>::run, nullptr},
 };
 
 static int config_count(int32_t dtype)
