@@ -86,7 +86,7 @@ public:
         state_ = DeviceBuffer((size_t)layout_.state_bytes);
         work_ = DeviceBuffer((size_t)layout_.work_bytes);
         cuda_check(cudaMemset(work_.get(), 0, work_.bytes()), "cudaMemset");
-        lv_ = axs_level{state_.get(), work_.get(), dtype, nx, ny, nz, dx, 0};
+        lv_ = axs_level{state_.get(), work_.get(), dtype, nx, ny, nz, dx, 0, 0};
         staging_ = DeviceBuffer((size_t)4 * nx * ny * nz * es_);
         int64_t sb = 0;
         check(axs_diagnostics_scratch_bytes(nx, ny, nz, &sb));
