@@ -91,6 +91,34 @@ __device__ __forceinline__ double diff1_vals(double m2, double m1, double p1, do
     }
 }
 
+// float -> double without the conversion unit: GB300 issues FP32 <-> FP64
+// conversions at its FP64 rate (1/64 of FP32), and the FP64 per-cell pass
+// converts every stencil tap. Normal numbers and zeros by integer operations
+// (the same double the conversion gives), the rest by the conversion.
+__device__ __forceinline__ double f2d_exact(float x)
+{
+    const unsigned u = __float_as_uint(x), e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    if (e - 1u < 254u)
+        return __longlong_as_double(
+            (long long)(sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+    if ((u << 1) == 0u) return __longlong_as_double((long long)sgn);
+    return (double)x;
+}
+
+// diff1_vals for FP32 fields from float taps: the same operations; r32 is the
+// rounded float the reference squares, the return value its double.
+__device__ __forceinline__ double diff1_f32(float m2, float m1, float p1, float p2, double inv_dx, float &r32)
+{
+    const double wf = 8.33333333333333333333e-2, wn = 6.66666666666666666667e-1;
+    double r = __dmul_rn(wf, f2d_exact(m2));
+    r = __dsub_rn(r, __dmul_rn(wn, f2d_exact(m1)));
+    r = __dadd_rn(r, __dmul_rn(wn, f2d_exact(p1)));
+    r = __dsub_rn(r, __dmul_rn(wf, f2d_exact(p2)));
+    r32 = __double2float_rn(__dmul_rn(r, inv_dx));
+    return f2d_exact(r32);
+}
+
 // The seven per-cell energy terms (EnergyKernel.hpp:130-190) and the masking
 // weight (Masking.hpp:75-93) from psi, Pi and the six diff1 values, in math
 // type M: double as the reference computes them, or float for the
@@ -99,18 +127,22 @@ template <typename M> struct CellConst {
     M R2, inv_R, inv_R2, inv_R4, lambda, RpR, threshold;
 };
 
+// gt: the diff1 values in the field precision (the reference squares them there)
 template <typename M, typename T>
-__device__ __forceinline__ void cell_energy(const CellConst<M> &k, int scheme, M psi1, M psi2, M Pi1, M Pi2,
-                                            const M (&g)[2][3], M (&term)[6], M &wgt)
+__device__ __forceinline__ void cell_energy_g(const CellConst<M> &k, int scheme, M psi1, M psi2, M Pi1, M Pi2,
+                                              const M (&g)[2][3], const T (&gt)[2][3], M (&term)[6], M &wgt)
 {
     const M psi_sq = psi1 * psi1 + psi2 * psi2;
     M g1sq = 0, g2sq = 0, cross2 = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        if constexpr (sizeof(M) == 8) {
+        if constexpr (sizeof(M) == 8 && sizeof(T) == 4) {
             // the reference squares the float diff1 values in float
-            g1sq += (M)((T)g[0][d] * (T)g[0][d]);
-            g2sq += (M)((T)g[1][d] * (T)g[1][d]);
+            g1sq += f2d_exact(gt[0][d] * gt[0][d]);
+            g2sq += f2d_exact(gt[1][d] * gt[1][d]);
+        } else if constexpr (sizeof(M) == 8) {
+            g1sq += (M)(gt[0][d] * gt[0][d]);
+            g2sq += (M)(gt[1][d] * gt[1][d]);
         } else {
             g1sq += g[0][d] * g[0][d];
             g2sq += g[1][d] * g[1][d];
@@ -141,6 +173,18 @@ __device__ __forceinline__ void cell_energy(const CellConst<M> &k, int scheme, M
             wgt = f * f;
         }
     }
+}
+
+template <typename M, typename T>
+__device__ __forceinline__ void cell_energy(const CellConst<M> &k, int scheme, M psi1, M psi2, M Pi1, M Pi2,
+                                            const M (&g)[2][3], M (&term)[6], M &wgt)
+{
+    T gt[2][3];
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gt[c][d] = (T)g[c][d];
+    cell_energy_g<M, T>(k, scheme, psi1, psi2, Pi1, Pi2, g, gt, term, wgt);
 }
 
 // Tiled diagnostics pass. A block owns a DTX x DTY tile of cells and marches
@@ -410,18 +454,38 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                         }
                     }
                     if (!done) {
-                        double g[2][3];
+                        double g[2][3], term[6], wgt;
+                        if constexpr (sizeof(T) == 4) {
+                            // FP32 fields: taps widened by integer operations (f2d_exact)
+                            float gf[2][3];
 #pragma unroll
-                        for (int c = 0; c < 2; ++c) {
-                            g[c][0] = diff1_vals<T>(sm.ps[s0][c][hy][hx - 2], sm.ps[s0][c][hy][hx - 1],
-                                                    sm.ps[s0][c][hy][hx + 1], sm.ps[s0][c][hy][hx + 2], q.one_over_dx);
-                            g[c][1] = diff1_vals<T>(sm.ps[s0][c][hy - 2][hx], sm.ps[s0][c][hy - 1][hx],
-                                                    sm.ps[s0][c][hy + 1][hx], sm.ps[s0][c][hy + 2][hx], q.one_over_dx);
-                            g[c][2] = diff1_vals<T>(sm.ps[sm2][c][hy][hx], sm.ps[sm1][c][hy][hx],
-                                                    sm.ps[sp1][c][hy][hx], sm.ps[sp2][c][hy][hx], q.one_over_dx);
+                            for (int c = 0; c < 2; ++c) {
+                                g[c][0] = diff1_f32(sm.ps[s0][c][hy][hx - 2], sm.ps[s0][c][hy][hx - 1],
+                                                    sm.ps[s0][c][hy][hx + 1], sm.ps[s0][c][hy][hx + 2], q.one_over_dx,
+                                                    gf[c][0]);
+                                g[c][1] = diff1_f32(sm.ps[s0][c][hy - 2][hx], sm.ps[s0][c][hy - 1][hx],
+                                                    sm.ps[s0][c][hy + 1][hx], sm.ps[s0][c][hy + 2][hx], q.one_over_dx,
+                                                    gf[c][1]);
+                                g[c][2] = diff1_f32(sm.ps[sm2][c][hy][hx], sm.ps[sm1][c][hy][hx],
+                                                    sm.ps[sp1][c][hy][hx], sm.ps[sp2][c][hy][hx], q.one_over_dx,
+                                                    gf[c][2]);
+                            }
+                            cell_energy_g<double, float>(kd, q.scheme, f2d_exact(p1), f2d_exact(p2), f2d_exact(q1),
+                                                         f2d_exact(q2), g, gf, term, wgt);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 2; ++c) {
+                                g[c][0] = diff1_vals<T>(sm.ps[s0][c][hy][hx - 2], sm.ps[s0][c][hy][hx - 1],
+                                                        sm.ps[s0][c][hy][hx + 1], sm.ps[s0][c][hy][hx + 2],
+                                                        q.one_over_dx);
+                                g[c][1] = diff1_vals<T>(sm.ps[s0][c][hy - 2][hx], sm.ps[s0][c][hy - 1][hx],
+                                                        sm.ps[s0][c][hy + 1][hx], sm.ps[s0][c][hy + 2][hx],
+                                                        q.one_over_dx);
+                                g[c][2] = diff1_vals<T>(sm.ps[sm2][c][hy][hx], sm.ps[sm1][c][hy][hx],
+                                                        sm.ps[sp1][c][hy][hx], sm.ps[sp2][c][hy][hx], q.one_over_dx);
+                            }
+                            cell_energy<double, T>(kd, q.scheme, p1, p2, q1, q2, g, term, wgt);
                         }
-                        double term[6], wgt;
-                        cell_energy<double, T>(kd, q.scheme, p1, p2, q1, q2, g, term, wgt);
 #pragma unroll
                         for (int k = 0; k < 6; ++k) {
                             e[2 * k] += term[k];
