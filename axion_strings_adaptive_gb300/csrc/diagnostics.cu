@@ -106,6 +106,15 @@ __device__ __forceinline__ double f2d_exact(float x)
     return (double)x;
 }
 
+// a field value as double: FP32 widened by f2d_exact, FP64 as it is
+template <typename T> __device__ __forceinline__ double widen(T x)
+{
+    if constexpr (sizeof(T) == 4)
+        return f2d_exact(x);
+    else
+        return x;
+}
+
 // diff1_vals for FP32 fields from float taps: the same operations; r32 is the
 // rounded float the reference squares, the return value its double.
 __device__ __forceinline__ double diff1_f32(float m2, float m1, float p1, float p2, double inv_dx, float &r32)
@@ -371,7 +380,8 @@ __global__ void __launch_bounds__(kDiagThreads, 2) diag_kernel(const DiagView v,
                     const float re = phi1 * pd1 + phi2 * pd2;
                     sm.gv[ts][vy][vx] = pd_sq * q.f_vel_a * (1.f - q.f_vel_b * phi_sq) - q.f_vel_c * re * re;
                 } else if (q.want_vel) {
-                    const double psi1 = a, psi2 = b, Pi1 = sm.pi[ps_][0][vy][vx], Pi2 = sm.pi[ps_][1][vy][vx];
+                    const double psi1 = widen(a), psi2 = widen(b), Pi1 = widen(sm.pi[ps_][0][vy][vx]),
+                                 Pi2 = widen(sm.pi[ps_][1][vy][vx]);
                     const double phi1 = psi1 * q.inv_R, phi2 = psi2 * q.inv_R;
                     const double pd1 = (Pi1 - q.RpR * psi1) * q.inv_R2, pd2 = (Pi2 - q.RpR * psi2) * q.inv_R2;
                     const double phi_sq = phi1 * phi1 + phi2 * phi2;
