@@ -43,7 +43,7 @@ struct AdjointB {
     static constexpr bool kComp = false;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam,
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, LamAcc<T> &lam,
                                  uint64_t pol)
     {
         T fo[4][V], uo[4][V];
@@ -68,10 +68,10 @@ struct AdjointB {
             uo[1][v] = u3b2;
             uo[2][v] = u4b1;
             uo[3][v] = u4b2;
-            // lambda0 gradient: per-site term in T, accumulated in double
+            // lambda0 gradient: per-site term in T, compensated sum in T (LamAcc)
             const T m3 = fma(u31, u31, fma(u32, u32, -a.c2.R2));
             const T m4 = fma(u41, u41, fma(u42, u42, -a.c4.R2));
-            lam -= (double)(fma(a.c2.hlam * m3, fma(u31, f3b1, u32 * f3b2), a.c4.hlam * m4 * fma(u41, f4b1, u42 * f4b2)));
+            lam.add(-fma(a.c2.hlam * m3, fma(u31, f3b1, u32 * f3b2), a.c4.hlam * m4 * fma(u41, f4b1, u42 * f4b2)));
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c)
@@ -89,7 +89,7 @@ struct AdjointA {
     static constexpr bool kComp = false;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &lam,
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, LamAcc<T> &lam,
                                  uint64_t pol)
     {
         T o[4][V];
@@ -111,7 +111,7 @@ struct AdjointA {
             o[3][v] = fma(a.h, u4b2, fma(a.h_half, u2b2, fma(a.h, qb2, pb2)));
             const T m1 = fma(p1, p1, fma(p2, p2, -a.c1.R2));
             const T m2 = fma(u21, u21, fma(u22, u22, -a.c2.R2));
-            lam -= (double)(fma(a.c1.hlam * m1, fma(p1, f1b1, p2 * f1b2), a.c2.hlam * m2 * fma(u21, f2b1, u22 * f2b2)));
+            lam.add(-fma(a.c1.hlam * m1, fma(p1, f1b1, p2 * f1b2), a.c2.hlam * m2 * fma(u21, f2b1, u22 * f2b2)));
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c)

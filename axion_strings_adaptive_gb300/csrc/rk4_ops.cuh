@@ -165,7 +165,7 @@ template <bool COMP> struct ForwardAT {
     static constexpr bool kComp = COMP;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &, int64_t off, int x, int y, double &,
+                                 const T (&ctr)[4][V], const PQ &, int64_t off, int x, int y, LamAcc<T> &,
                                  uint64_t pol)
     {
         T o[8][V];
@@ -186,7 +186,7 @@ template <bool COMP> struct ForwardBT {
     static constexpr bool kComp = COMP;
     template <typename T, int V, bool HINT, typename PQ>
     __device__ static void apply(const SweepArgs<T> &a, const BoxGeom &b, const T (&lap)[4][V],
-                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, double &,
+                                 const T (&ctr)[4][V], const PQ &pq, int64_t off, int x, int y, LamAcc<T> &,
                                  uint64_t pol)
     {
         T o[4][V];

@@ -304,6 +304,20 @@ __device__ __forceinline__ void star_laplacian(const SweepArgs<T> &a, const T *z
     }
 }
 
+// The lambda0-gradient sum of an adjoint sweep: per thread in the field
+// precision with Neumaier compensation, widened to double once for the block
+// sum (a conversion and an FP64 add per site run at GB300's FP64 rate).
+template <typename T> struct LamAcc {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T x)
+    {
+        const T t = s + x;
+        c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 template <typename T, int V, int TX, int TY, int NS, int MINB, class Op, class Src = SingleLevel, bool HINT = false>
 __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     stencil_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const SweepArgs<T> a)
@@ -318,7 +332,7 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
 
     const int tid = threadIdx.x;
     const int tx = tid % S::NTX, ty = tid / S::NTX;
-    double lam_acc = 0.0;
+    LamAcc<T> lam_acc;
     // HINT: stencil planes (re-read by neighbouring tiles) evict-last in L2,
     // pointwise inputs and all outputs (touched once) evict-first
     const uint64_t pol_first = HINT ? l2_policy_evict_first() : 0, pol_last = HINT ? l2_policy_evict_last() : 0;
@@ -481,8 +495,9 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     }
     if constexpr (Op::kLambdaGrad) {
         // fixed-order block reduction of the lambda0-gradient contributions
-        for (int o = 16; o > 0; o >>= 1) lam_acc += __shfl_down_sync(0xffffffffu, lam_acc, o);
-        if ((tid & 31) == 0) lam_red[tid >> 5] = lam_acc;
+        double lv = lam_acc.value();
+        for (int o = 16; o > 0; o >>= 1) lv += __shfl_down_sync(0xffffffffu, lv, o);
+        if ((tid & 31) == 0) lam_red[tid >> 5] = lv;
         __syncthreads();
         if (tid == 0) {
             double s = 0.0;
