@@ -11,14 +11,23 @@
 //
 // Work: the (tile, z-chunk) items of all boxes form one list, ordered by
 // descending item cost (longest z-chunk first), box-major and tile-fastest
-// within a box. Each RK4 sweep is ONE persistent launch of the generic
-// TMA-staged sweep kernel (sweep.cuh) over that list with the BoxTable item
-// source: a block looks each item's box up in the device table and loads
-// planes through that box's own tensor map, also in the table.
+// within a box. A block looks each item's box up in the device table and
+// loads planes through that box's own tensor maps, also in the table. Two
+// kinds of tiling run over the list:
+//   - the one-pass fused step (level_fused.cuh, FusedBoxes item source): ONE
+//     persistent launch per RK4 step plus one launch for the boxes' periodic
+//     padding, 8 words per site; steps alternate between the state arena and
+//     the work arena's first four planes. Boxes need ny a multiple of the
+//     tile height and an even nx (a last, partial tile column is masked);
+//   - the two sweeps (sweep.cuh, BoxTable item source): one persistent launch
+//     per sweep, 28 words per site, any box shape.
 //
 // Device table (caller-owned, written once by axs_ensemble_init):
 //   [0, 128)                header: status word
-//   [128, 128 + 256 nboxes) two CUtensorMaps per box (state; stage increments d3, d4)
+//   [128, 128 + 768 nboxes) six CUtensorMaps per box: the two sweeps use maps
+//                           2b (state) and 2b + 1 (stage increments d3, d4);
+//                           the fused step maps 6b .. 6b + 2 (state) and
+//                           6b + 3 .. 6b + 5 (work arena)
 //   then                    EnsBoxDesc[nboxes], then uint32 work items
 #include <algorithm>
 #include <cmath>
@@ -28,7 +37,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "rk4_ops.cuh"
+#include "level_fused.cuh"
 
 namespace axs {
 
@@ -41,6 +50,7 @@ int diag_level_box(const void *data, int32_t dtype, int nx, int ny, int nz, cons
 int64_t diag_scratch_bytes_for(int64_t ncell);
 
 constexpr int64_t kEnsHeader = 128;
+constexpr int kEnsMapsPerBox = 6;
 constexpr int kEnsMinTX = 16, kEnsMinTY = 4;  // smallest tile of any configuration (item-count bound)
 constexpr int kEnsMaxBoxes = 1 << (32 - kEnsItemBits);
 
@@ -86,8 +96,8 @@ static int64_t ens_item_bound(int nboxes, const int32_t *dims)
 
 static int64_t ens_table_bytes(int nboxes, const int32_t *dims)
 {
-    return kEnsHeader + (int64_t)nboxes * 2 * sizeof(CUtensorMap) + (int64_t)nboxes * sizeof(EnsBoxDesc) +
-           4 * ens_item_bound(nboxes, dims);
+    return kEnsHeader + (int64_t)nboxes * kEnsMapsPerBox * sizeof(CUtensorMap) +
+           (int64_t)nboxes * sizeof(EnsBoxDesc) + 4 * ens_item_bound(nboxes, dims);
 }
 
 static uint64_t ens_key(const axs_ensemble *e, int32_t tile_config, int32_t z_chunk)
@@ -194,7 +204,20 @@ struct EnsTiling {
     uint32_t box_x, box_y;
     int (*caps)(int &cap_a, int &cap_b);  // resident blocks of each sweep on the device
     int (*run)(const EnsRun &);
+    bool fused;  // the one-pass fused step (tensor maps and box constraints of FusedBoxes)
 };
+
+// The launch arguments that point into the device table.
+template <typename T> static void table_args(SweepArgs<T> &a, const axs_ensemble *e, int64_t n_items)
+{
+    char *table = static_cast<char *>(e->table);
+    a.n_items = n_items;
+    a.status = reinterpret_cast<unsigned *>(table);
+    a.maps = reinterpret_cast<const CUtensorMap *>(table + kEnsHeader);
+    a.boxes = reinterpret_cast<const EnsBoxDesc *>(table + kEnsHeader +
+                                                   kEnsMapsPerBox * sizeof(CUtensorMap) * (size_t)e->nboxes);
+    a.items = reinterpret_cast<const uint32_t *>(a.boxes + e->nboxes);
+}
 
 template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false> struct EnsConfig {
     using LA = SweepLauncher<T, V, TX, TY, NS, MINB, ForwardA, BoxTable, HINT>;
@@ -217,15 +240,10 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
     {
         const axs_ensemble *e = r.e;
         const int64_t P = r.geo->plane;
-        char *table = static_cast<char *>(e->table);
         SweepArgs<T> a{};
         fill_step_constants(a, e->dx, r.dt);
         a.ox = r.geo->g[0].ox;
-        a.n_items = r.plan->n_items;
-        a.status = reinterpret_cast<unsigned *>(table);
-        a.maps = reinterpret_cast<const CUtensorMap *>(table + kEnsHeader);
-        a.boxes = reinterpret_cast<const EnsBoxDesc *>(table + kEnsHeader + 2 * sizeof(CUtensorMap) * e->nboxes);
-        a.items = reinterpret_cast<const uint32_t *>(a.boxes + e->nboxes);
+        table_args(a, e, r.plan->n_items);
         T *state = static_cast<T *>(e->state), *work = static_cast<T *>(e->work);
         CUtensorMap unused;  // the BoxTable source reads each box's map from the table
         std::memset(&unused, 0, sizeof(unused));
@@ -252,13 +270,111 @@ template <typename T, int V, int TX, int TY, int NS, int MINB, bool HINT = false
 
     static EnsTiling entry(const char *name)
     {
-        return EnsTiling{name, TX, TY, (uint32_t)(TX + 8), (uint32_t)(TY + 4), &caps, &run};
+        return EnsTiling{name, TX, TY, (uint32_t)(TX + 8), (uint32_t)(TY + 4), &caps, &run, false};
     }
 };
 
-// Entry 0 of each table is the default (the fastest on a mixed 32^3..128^3
-// ensemble on GB300). The 16-wide tiles leave no idle columns on boxes whose
-// width is a multiple of 16 but read 96-byte rows.
+// The one-pass fused step over every box: per RK4 step one launch of
+// level_fused_kernel<S, FusedBoxes> from one state buffer into the other and
+// one ens_pad_kernel for the periodic padding of the buffer written. An odd
+// step count first copies the state arena (padding included) to the work
+// arena, so that the last step writes the state arena.
+template <int TX, int TY, int NS, int THREADS> struct EnsFusedConfig {
+    using S = LevelFusedShape<TX, TY, NS, THREADS>;
+
+    static int prepare()
+    {
+        static int smem_set = 0;
+        if (!smem_set) {
+            AXS_CUDA_CHECK(cudaFuncSetAttribute(level_fused_kernel<S, FusedBoxes>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM));
+            smem_set = 1;
+        }
+        return AXS_OK;
+    }
+
+    static int caps(int &cap_a, int &cap_b)
+    {
+        int rc = prepare();
+        if (rc) return rc;
+        int bps = 0;
+        AXS_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, level_fused_kernel<S, FusedBoxes>,
+                                                                     S::THREADS, S::SMEM));
+        AXS_REQUIRE(bps > 0, AXS_ERR_UNSUPPORTED, "the fused ensemble step does not fit on this device");
+        const int sms = device_sm_count();
+        AXS_REQUIRE(sms > 0, AXS_ERR_CUDA, "no CUDA device");
+        cap_a = cap_b = bps * sms;
+        return AXS_OK;
+    }
+
+    static int run(const EnsRun &r)
+    {
+        const axs_ensemble *e = r.e;
+        const int64_t P = r.geo->plane;
+        int rc = prepare();
+        if (rc) return rc;
+        SweepArgs<float> a{};
+        fill_step_constants(a, e->dx, r.dt);
+        a.ox = r.geo->g[0].ox;
+        table_args(a, e, r.plan->n_items);
+        float *buf[2] = {static_cast<float *>(e->state), static_cast<float *>(e->work)};
+        LevelFusedMaps unused;  // FusedBoxes reads each box's maps from the table
+        std::memset(&unused, 0, sizeof(unused));
+        int max_nz = 1, max_row = 1;
+        for (int b = 0; b < e->nboxes; ++b) {
+            const int nx = e->dims[3 * b], ny = e->dims[3 * b + 1], nz = e->dims[3 * b + 2];
+            max_nz = std::max(max_nz, nz);
+            max_row = std::max(max_row, 16 * (ny + 4) + 4 * nx);
+        }
+        const dim3 pad_grid((unsigned)std::min(64, (max_row + 255) / 256), (unsigned)std::min(4 * max_nz, 65535),
+                            (unsigned)e->nboxes);
+        int first = 0;
+        if (r.nsteps & 1) {
+            AXS_CUDA_CHECK(cudaMemcpyAsync(buf[1], buf[0], (size_t)(4 * P) * sizeof(float), cudaMemcpyDeviceToDevice,
+                                           r.st));
+            first = 1;
+        }
+        for (int s = 0; s < r.nsteps; ++s) {
+            const double t = r.t0 + s * r.dt;
+            const int src = (s + first) & 1;
+            SweepArgs<float> as = a;
+            as.map_sel = src;
+            as.c1 = stage_coef<float>(*r.bg, r.tau_i + t);
+            as.c2 = stage_coef<float>(*r.bg, r.tau_i + t + 0.5 * r.dt);
+            as.c4 = stage_coef<float>(*r.bg, r.tau_i + t + r.dt);
+            float *dst = buf[src ^ 1];
+            for (int c = 0; c < 4; ++c) as.out[c] = dst + c * P;
+            level_fused_kernel<S, FusedBoxes><<<r.plan->grid_a, S::THREADS, S::SMEM, r.st>>>(unused, as);
+            if ((rc = launch_status("fused ensemble step"))) return rc;
+            ens_pad_kernel<float><<<pad_grid, 256, 0, r.st>>>(dst, a.boxes, P, a.ox);
+            if ((rc = launch_status("ensemble padding"))) return rc;
+        }
+        return AXS_OK;
+    }
+
+    static EnsTiling entry(const char *name)
+    {
+        return EnsTiling{name, TX, TY, (uint32_t)S::BX, (uint32_t)S::BY, &caps, &run, true};
+    }
+};
+
+// Whether every box suits a fused tiling of tile height ty: ny a multiple of
+// ty, nx even (the last tile column may be partial, its sites come in pairs).
+static bool fused_fits(const int32_t *dims, int nboxes, int ty)
+{
+    for (int b = 0; b < nboxes; ++b)
+        if (dims[3 * b] % 2 != 0 || dims[3 * b + 1] % ty != 0) return false;
+    return true;
+}
+
+// The default (tile_config 0) is the first entry of its table that suits
+// every box: the fastest two-sweep tiling on a mixed 32^3..128^3 ensemble on
+// GB300. The 16-wide tiles leave no idle columns on boxes whose width is a
+// multiple of 16 but read 96-byte rows. On that ensemble the fused step is
+// slower than the two sweeps (1.04 against 1.00 ms per step): a third of its
+// tiles touch a box's y edge and load each plane as 12 pieces, and small
+// boxes have more padding per site; the autotuner keeps it for boxes where it
+// wins.
 static const EnsTiling kEnsF32[] = {
     EnsConfig<float, 2, 64, 8, 8, 2>::entry("f32 v2 64x8 ring8"),
     EnsConfig<float, 2, 32, 8, 8, 3>::entry("f32 v2 32x8 ring8"),
@@ -268,6 +384,7 @@ static const EnsTiling kEnsF32[] = {
     EnsConfig<float, 1, 16, 8, 8, 4>::entry("f32 v1 16x8 ring8"),
     EnsConfig<float, 2, 64, 8, 8, 2, true>::entry("f32 v2 64x8 ring8 l2"),
     EnsConfig<float, 2, 32, 8, 8, 3, true>::entry("f32 v2 32x8 ring8 l2"),
+    EnsFusedConfig<32, 16, 6, 640>::entry("f32 fused 32x16 ring6 t640"),
 };
 static const EnsTiling kEnsF64[] = {
     EnsConfig<double, 1, 32, 8, 6, 2>::entry("f64 v1 32x8 ring6"),
@@ -288,6 +405,19 @@ static const EnsTiling *ens_config(int32_t dtype, int32_t id)
     if (n == 0 || id < 0 || id > n) return nullptr;
     const EnsTiling *tab = dtype == AXS_F64 ? kEnsF64 : kEnsF32;
     return &tab[id == 0 ? 0 : id - 1];
+}
+
+// The tiling an ensemble runs for tile_config id: id 0 resolves to the first
+// entry that suits its boxes.
+static const EnsTiling *ens_config_for(const axs_ensemble *e, int32_t id)
+{
+    if (id != 0) return ens_config(e->dtype, id);
+    const int n = ens_config_count(e->dtype);
+    for (int i = 1; i <= n; ++i) {
+        const EnsTiling *c = ens_config(e->dtype, i);
+        if (!c->fused || fused_fits(e->dims, e->nboxes, c->ty)) return c;
+    }
+    return nullptr;
 }
 
 // Chunk length for every box from one target length: each box splits its nz
@@ -375,9 +505,11 @@ int axs_ensemble_init(const axs_ensemble *e, axs_ensemble_plan *plan, void *stre
     int rc = validate_ensemble(e, geo);
     if (rc) return rc;
     AXS_REQUIRE(plan != nullptr, AXS_ERR_INVALID_ARGUMENT, "null plan");
-    const EnsTiling *cfg = ens_config(e->dtype, plan->tile_config);
+    const EnsTiling *cfg = ens_config_for(e, plan->tile_config);
     AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "tile_config %d out of range (0..%d)", plan->tile_config,
                 ens_config_count(e->dtype));
+    AXS_REQUIRE(!cfg->fused || fused_fits(e->dims, e->nboxes, cfg->ty), AXS_ERR_UNSUPPORTED,
+                "tiling '%s' needs every box's ny a multiple of %d and nx even", cfg->name, cfg->ty);
     AXS_REQUIRE(plan->z_chunk >= 0, AXS_ERR_INVALID_ARGUMENT, "negative z_chunk");
     int cap_a = 0, cap_b = 0;
     if ((rc = cfg->caps(cap_a, cap_b))) return rc;
@@ -418,16 +550,32 @@ int axs_ensemble_init(const axs_ensemble *e, axs_ensemble_plan *plan, void *stre
     AXS_REQUIRE((int64_t)items.size() <= ens_item_bound(nb, e->dims), AXS_ERR_WORKSPACE, "work list overflow");
 
     // table image: header, tensor maps, descriptors, items
-    const size_t maps_off = kEnsHeader, desc_off = maps_off + 2 * sizeof(CUtensorMap) * nb,
+    const size_t maps_off = kEnsHeader, desc_off = maps_off + kEnsMapsPerBox * sizeof(CUtensorMap) * nb,
                  items_off = desc_off + sizeof(EnsBoxDesc) * nb;
     std::vector<unsigned char> img(items_off + 4 * items.size(), 0);
     const int64_t es = (int64_t)dtype_size(e->dtype);
     for (int b = 0; b < nb; ++b) {
         const LevelGeom &g = geo.g[b];
         const int ny = e->dims[3 * b + 1], nz = e->dims[3 * b + 2];
-        auto *maps = reinterpret_cast<CUtensorMap *>(img.data() + maps_off) + 2 * b;
         const char *sbase = static_cast<const char *>(e->state) + geo.base[b] * es;
         const char *wbase = static_cast<const char *>(e->work) + geo.base[b] * es;
+        if (cfg->fused) {
+            // full box, TY + 4 rows of one component, 2 rows of one component (level_fused.cuh)
+            auto *maps = reinterpret_cast<CUtensorMap *>(img.data() + maps_off) + kEnsMapsPerBox * b;
+            for (int sel = 0; sel < 2; ++sel) {
+                const char *base = sel ? wbase : sbase;
+                CUtensorMap *m = maps + 3 * sel;
+                const uint64_t d0 = g.js, d1 = ny + 4, sj = g.js * es, sk = g.ks * es, sc = geo.plane * es;
+                if ((rc = make_tensor_map_4d(&m[0], base, e->dtype, d0, d1, nz, 4, sj, sk, sc, cfg->box_x, cfg->box_y,
+                                             1, 4)) ||
+                    (rc = make_tensor_map_4d(&m[1], base, e->dtype, d0, d1, nz, 4, sj, sk, sc, cfg->box_x,
+                                             (uint32_t)cfg->ty + 4, 1, 1)) ||
+                    (rc = make_tensor_map_4d(&m[2], base, e->dtype, d0, d1, nz, 4, sj, sk, sc, cfg->box_x, 2, 1, 1)))
+                    return rc;
+            }
+            continue;
+        }
+        auto *maps = reinterpret_cast<CUtensorMap *>(img.data() + maps_off) + 2 * b;
         if ((rc = make_tensor_map_4d(&maps[0], sbase, e->dtype, g.js, ny + 4, nz, 4, g.js * es, g.ks * es,
                                      geo.plane * es, cfg->box_x, cfg->box_y, 1, 4)))
             return rc;
@@ -483,7 +631,7 @@ int axs_ensemble_rk4_advance(const axs_ensemble *e, const axs_ensemble_plan *pla
         AXS_REQUIRE(tau_i + t0 > 0.0, AXS_ERR_INVALID_ARGUMENT, "conformal time must stay positive");
     }
     if (nsteps == 0) return AXS_OK;
-    const EnsTiling *cfg = ens_config(e->dtype, plan->tile_config);
+    const EnsTiling *cfg = ens_config_for(e, plan->tile_config);
     AXS_REQUIRE(cfg != nullptr, AXS_ERR_INVALID_ARGUMENT, "bad tile_config in plan");
     EnsRun r{e, &geo, plan, bg, tau_i, t0, dt, nsteps, (cudaStream_t)stream};
     return cfg->run(r);

@@ -114,7 +114,53 @@ struct LevelFusedMaps {
     CUtensorMap full, mid, rows2;
 };
 
-template <class S>
+// A work item of the fused step: a TX x TY tile over a chunk of z planes of
+// one periodic box, with the box's geometry and the three tensor maps of the
+// buffer the step reads.
+struct FusedItem {
+    int x0, y0, z0, len;
+    int nx, ny, nz;
+    int64_t js, ks, base;  // base: element offset of the box in every component plane
+    const CUtensorMap *full, *mid, *rows2;
+};
+
+// Work-item sources of the fused step.
+// One periodic level: geometry from the launch parameters, nx a multiple of TX.
+struct FusedLevel {
+    static constexpr bool kPartialX = false;
+    template <int TX, int TY>
+    __device__ __forceinline__ static FusedItem item(const SweepArgs<float> &a, const LevelFusedMaps &m, int64_t it)
+    {
+        const int tile = (int)(it % a.ntiles);
+        const int z0 = (int)(it / a.ntiles) * a.zchunk;
+        return FusedItem{(tile % a.tiles_x) * TX, (tile / a.tiles_x) * TY, z0, min(a.zchunk, a.nz - z0), a.nx, a.ny,
+                         a.nz, a.js, a.ks, 0, &m.full, &m.mid, &m.rows2};
+    }
+};
+// The boxes of an ensemble: the item list and box descriptors of a box table,
+// and per box six tensor maps in the table (full, mid, rows2 over each of the
+// two state buffers; map_sel picks the buffer read). ny is a multiple of TY.
+// The last tile column of a box whose width is not a multiple of TX runs past
+// the box: its stores are masked. Its sweep A sites up to nx + 1 read the
+// padding copies (8 columns) and feed the last valid sites; the ones further
+// right read zero-filled or unused columns and feed only masked sites.
+struct FusedBoxes {
+    static constexpr bool kPartialX = true;
+    template <int TX, int TY>
+    __device__ __forceinline__ static FusedItem item(const SweepArgs<float> &a, const LevelFusedMaps &, int64_t it)
+    {
+        const uint32_t e = __ldg(a.items + it);
+        const EnsBoxDesc &d = a.boxes[e >> kEnsItemBits];
+        const int local = (int)(e & ((1u << kEnsItemBits) - 1));
+        const int tile = local % d.ntiles;
+        const int z0 = (local / d.ntiles) * d.zchunk;
+        const CUtensorMap *m = a.maps + 3 * (2 * d.map_box + a.map_sel);
+        return FusedItem{(tile % d.tiles_x) * TX, (tile / d.tiles_x) * TY, z0, min(d.zchunk, d.nz - z0), d.nx, d.ny,
+                         d.nz, d.js, d.ks, d.base, m, m + 1, m + 2};
+    }
+};
+
+template <class S, class Src = FusedLevel>
 __global__ void __launch_bounds__(S::THREADS, 1)
     level_fused_kernel(const __grid_constant__ LevelFusedMaps maps, const SweepArgs<float> a)
 {
@@ -127,7 +173,6 @@ __global__ void __launch_bounds__(S::THREADS, 1)
     __shared__ uint64_t full[NS];
     __shared__ int abort_flag;
     const int tid = threadIdx.x;
-    const int ny = a.ny, nz = a.nz;
     constexpr int oy = 2;  // padded row of y = 0 in the level layout
 
     if (tid == 0) {
@@ -142,43 +187,40 @@ __global__ void __launch_bounds__(S::THREADS, 1)
 
     // ---- producer cursor (thread 0 only): planes z0 - 4 .. z0 + len + 3 of each item
     int64_t p_item = blockIdx.x;
-    int p_k = 0, p_len = 0, p_z0 = 0, p_x0 = 0, p_y0 = 0;
+    int p_k = 0;
+    FusedItem p{};
     bool p_edge = false;
     auto p_start = [&]() {
         if (p_item >= a.n_items) return;
-        const int tile = (int)(p_item % a.ntiles);
-        p_z0 = (int)(p_item / a.ntiles) * a.zchunk;
-        p_len = min(a.zchunk, nz - p_z0);
-        p_x0 = (tile % a.tiles_x) * TX;
-        p_y0 = (tile / a.tiles_x) * TY;
-        p_edge = p_y0 == 0 || p_y0 + TY == ny;  // rows y0 - 4, y0 - 3 or y0 + TY + 2, + 3 lie past the padding
+        p = Src::template item<TX, TY>(a, maps, p_item);
+        p_edge = p.y0 == 0 || p.y0 + TY == p.ny;  // rows y0 - 4, y0 - 3 or y0 + TY + 2, + 3 lie past the padding
     };
     int64_t q_issued = 0;
     int p_slot = 0;  // ring slot of plane q_issued
     auto issue_one = [&]() -> bool {
         if (p_item >= a.n_items) return false;
-        int zp = (p_z0 - 4 + p_k) % nz;
-        if (zp < 0) zp += nz;
+        int zp = (p.z0 - 4 + p_k) % p.nz;
+        if (zp < 0) zp += p.nz;
         const int slot = p_slot;
         if (++p_slot == NS) p_slot = 0;
         T *dst = ring + (size_t)slot * S::RING;
         mbar_arrive_expect_tx(&full[slot], S::SLOT_BYTES);
-        const int xc = a.ox - 8 + p_x0;  // padded column of the box's first column (16-byte aligned)
+        const int xc = a.ox - 8 + p.x0;  // padded column of the box's first column (16-byte aligned)
         if (!p_edge) {
-            tma_load_4d(dst, &maps.full, xc, p_y0 - 4 + oy, zp, 0, &full[slot]);
+            tma_load_4d(dst, p.full, xc, p.y0 - 4 + oy, zp, 0, &full[slot]);
         } else {
-            const int rt = ((p_y0 - 4) % ny + ny) % ny + oy;  // rows y0 - 4, y0 - 3 (wrapped)
-            const int rb = (p_y0 + TY + 2) % ny + oy;        // rows y0 + TY + 2, + 3 (wrapped)
+            const int rt = ((p.y0 - 4) % p.ny + p.ny) % p.ny + oy;  // rows y0 - 4, y0 - 3 (wrapped)
+            const int rb = (p.y0 + TY + 2) % p.ny + oy;            // rows y0 + TY + 2, + 3 (wrapped)
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 T *dc = dst + (size_t)c * BX * BY;
-                tma_load_4d(dc, &maps.rows2, xc, rt, zp, c, &full[slot]);
-                tma_load_4d(dc + 2 * BX, &maps.mid, xc, p_y0 - 2 + oy, zp, c, &full[slot]);
-                tma_load_4d(dc + (TY + 6) * BX, &maps.rows2, xc, rb, zp, c, &full[slot]);
+                tma_load_4d(dc, p.rows2, xc, rt, zp, c, &full[slot]);
+                tma_load_4d(dc + 2 * BX, p.mid, xc, p.y0 - 2 + oy, zp, c, &full[slot]);
+                tma_load_4d(dc + (TY + 6) * BX, p.rows2, xc, rb, zp, c, &full[slot]);
             }
         }
         ++q_issued;
-        if (++p_k == p_len + 8) {
+        if (++p_k == p.len + 8) {
             p_k = 0;
             p_item += gridDim.x;
             p_start();
@@ -227,10 +269,12 @@ __global__ void __launch_bounds__(S::THREADS, 1)
     int64_t q_waited = 0;
     bool aborted = false;
     for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-        const int tile = (int)(item % a.ntiles);
-        const int z0 = (int)(item / a.ntiles) * a.zchunk;
-        const int len = min(a.zchunk, nz - z0);
-        const int x0 = (tile % a.tiles_x) * TX, y0 = (tile / a.tiles_x) * TY;
+        const FusedItem w = Src::template item<TX, TY>(a, maps, item);
+        const int z0 = w.z0, len = w.len;
+        // this thread's sweep B sites: element offset of their row at z = 0, and
+        // whether they lie in the box
+        const int64_t b_row = w.base + (int64_t)(w.x0 + bxl + a.ox) + (int64_t)(w.y0 + byl + oy) * w.js;
+        const bool b_in = !Src::kPartialX || w.x0 + bxl < w.nx;
         // iteration i: sweep A at plane za = z0 - 2 + i (ring planes q_base + i .. + 4),
         // sweep B at zb = za - 2 = z0 - 4 + i for i >= 4
         for (int i = 0; i < len + 4; ++i) {
@@ -317,10 +361,11 @@ __global__ void __launch_bounds__(S::THREADS, 1)
                     pq[4 + c][1] = pn[c].y;
                 }
                 stage_b<T, V, decltype(pq), S::COMP>(a, lap, ctr, pq, o);
-                const int x = x0 + bxl, y = y0 + byl;
-                const int64_t off = (int64_t)(x + a.ox) + (int64_t)(y + oy) * a.js + (int64_t)zb * a.ks;
+                const int64_t off = b_row + (int64_t)zb * w.ks;
+                if (b_in) {
 #pragma unroll
-                for (int c = 0; c < 4; ++c) stv<T, V>(a.out[c] + off, o[c]);
+                    for (int c = 0; c < 4; ++c) stv<T, V>(a.out[c] + off, o[c]);
+                }
             }
             if (++r0 == NS) r0 = 0;
             if (++s0 == S::NSW) s0 = 0;
@@ -344,8 +389,8 @@ __global__ void __launch_bounds__(S::THREADS, 1)
 // rows are planes (z + nz c); within a plane, consecutive threads take
 // consecutive elements of a padding row.
 template <typename T>
-__global__ void level_pad_kernel(T *__restrict__ buf, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
-                                 int ox, int oy)
+__device__ __forceinline__ void pad_box(T *__restrict__ buf, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
+                                        int ox, int oy)
 {
     const int xpad = 16 * (ny + 4), per_plane = xpad + 4 * nx;
     for (int plane = blockIdx.y; plane < 4 * nz; plane += gridDim.y) {
@@ -365,6 +410,21 @@ __global__ void level_pad_kernel(T *__restrict__ buf, int nx, int ny, int nz, in
             p[x + (int64_t)y * js] = p[xs + (int64_t)ys * js];
         }
     }
+}
+
+template <typename T>
+__global__ void level_pad_kernel(T *__restrict__ buf, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
+                                 int ox, int oy)
+{
+    pad_box(buf, nx, ny, nz, js, ks, cs, ox, oy);
+}
+
+// The same for every box of an ensemble buffer, one box per blockIdx.z.
+template <typename T>
+__global__ void ens_pad_kernel(T *__restrict__ buf, const EnsBoxDesc *__restrict__ boxes, int64_t cs, int ox)
+{
+    const EnsBoxDesc &d = boxes[blockIdx.z];
+    pad_box(buf + d.base, d.nx, d.ny, d.nz, d.js, d.ks, cs, ox, d.oy);
 }
 
 }  // namespace axs

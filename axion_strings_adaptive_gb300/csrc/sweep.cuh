@@ -76,7 +76,8 @@ struct EnsBoxDesc {
     int xlo, ylo, zlo;
     int oy, oz;    // padded row / plane of valid y = 0 / z = 0
     int periodic;  // 1: wrap z, write periodic copies; 0: explicit ghost rings
-    int map_box;   // tensor maps 2*map_box (state) and 2*map_box + 1 (stage buffers)
+    int map_box;   // two-sweep tensor maps 2*map_box (state), 2*map_box + 1 (stage buffers);
+                   // an ensemble's fused step uses maps 6*map_box .. 6*map_box + 5
     int pad;
 };
 constexpr int kEnsItemBits = 16;  // work items per box < 2^16; boxes < 2^16

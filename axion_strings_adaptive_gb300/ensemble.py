@@ -2,8 +2,11 @@
 
 :class:`Ensemble` packs its boxes component-major in one state arena and one
 stage-buffer arena (the ``axs_ensemble`` layout of include/axs.h), builds the
-device table for one sweep tiling, and advances every box with two persistent
-launches per RK4 step. ``capture(...)`` records a whole run -- the steps plus
+device table for one tiling, and advances every box together: with two
+persistent sweep launches per RK4 step (any box shape; the default) or with
+the one-pass fused step (one persistent launch per step plus one for the
+periodic padding; boxes with ny a multiple of 16 and an even nx).
+``capture(...)`` records a whole run -- the steps plus
 per-box diagnostics -- as one CUDA graph; :meth:`Ensemble.autotune` times the
 compiled tilings and z-chunk targets (the work each block takes from a box) on
 the caller's boxes and keeps the fastest.
@@ -86,7 +89,7 @@ class Ensemble:
 
     # ------------------------------------------------------------------ evolution
     def advance(self, bg: Background, tau_i: float, t0: float, dt: float, nsteps: int, stream=None) -> None:
-        """nsteps RK4 steps of every box: two persistent launches per step; asynchronous."""
+        """nsteps RK4 steps of every box (the plan's tiling); asynchronous."""
         L.call("axs_ensemble_rk4_advance", C.byref(self.c), C.byref(self.plan), C.byref(bg.to_c()), float(tau_i),
                float(t0), float(dt), int(nsteps), _stream_ptr(stream))
 
@@ -146,13 +149,19 @@ class Ensemble:
     def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 3, repeats: int = 2,
                  z_chunks=(0, 8, 16, 32, 64)) -> dict:
         """Time every compiled tiling x z-chunk target on these boxes and keep the
-        fastest. The state is saved and restored. Returns {"name zN": ms/step}."""
+        fastest (tilings that do not suit every box are left out). The state is
+        saved and restored. Returns {"name zN": ms/step}."""
         saved = self.state.clone()
         timings = {}
         best = (float("inf"), self.plan.tile_config, self.plan.z_chunk)
         for cid, name in self.tile_configs():
             for zc in z_chunks:
-                self.init(cid, zc)
+                try:
+                    self.init(cid, zc)
+                except L.AxsError as err:
+                    if err.status != L.AXS_ERR_UNSUPPORTED:
+                        raise
+                    break
                 self.advance(bg, tau_i, 0.0, dt, 1)
                 ms = float("inf")
                 for _ in range(repeats):

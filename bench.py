@@ -305,10 +305,11 @@ def differentiation_report(A, ic, dev, n=128, nsteps=200, ndir=16):
 # ---------------------------------------------------------------- batching configuration
 def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 64, 96, 128)):
     """64 seeded boxes of sizes drawn uniformly from `sizes`, FP32, c0 = 1,
-    lambda0 = 2, IC |n| < N_box/4 (seed + box), 200 RK4 steps per box: one
-    persistent launch per sweep over all boxes, the whole run plus per-box
-    diagnostics captured as one CUDA graph; beside it the same boxes advanced
-    one level at a time."""
+    lambda0 = 2, IC |n| < N_box/4 (seed + box), 200 RK4 steps per box: the
+    autotuned tiling over all boxes at once (the fused step: one persistent
+    launch per RK4 step; a two-sweep tiling: one per sweep), the whole run plus
+    per-box diagnostics captured as one CUDA graph; beside it the same boxes
+    advanced one level at a time."""
     import numpy as np
     import torch
     rng = np.random.RandomState(SEED)
@@ -842,7 +843,7 @@ def run_native(args):
     if not args.no_differentiation:
         differentiation = differentiation_report(A, ic, dev, args.diff_n, args.diff_steps, args.diff_directions)
 
-    # ---------------- batching: 64 uneven boxes, one persistent launch per sweep, one CUDA graph
+    # ---------------- batching: 64 uneven boxes advanced together, one CUDA graph
     batching = None
     if not args.no_batching:
         batching = batching_report(A, ic, dev, hbm_peak)

@@ -1,8 +1,10 @@
 """Ensemble (batching) path through the C ABI: boxes of uneven sizes packed in
-one arena and advanced by one persistent launch per sweep evolve bit for bit
-as the same boxes advanced one level at a time, for every compiled tiling and
-z-chunk target; per-box diagnostics equal the level diagnostics; a captured
-CUDA graph replays the eager run exactly."""
+one arena and advanced together (one persistent launch per sweep, or one fused
+launch per step) evolve bit for bit as the same boxes advanced one level at a
+time, for every compiled tiling and z-chunk target and for even and odd step
+counts; the fused step's padding equals a ghost fill; per-box diagnostics
+equal the level diagnostics; a captured CUDA graph replays the eager run
+exactly."""
 import ctypes as C
 
 import pytest
@@ -11,6 +13,8 @@ import torch
 pytestmark = pytest.mark.gpu
 
 DIMS = [(32, 32, 32), (48, 40, 24), (64, 16, 36), (24, 28, 12), (16, 16, 8)]
+# boxes the fused step takes: ny a multiple of 16, nx even (48 and 16 leave a partial tile column)
+DIMS_FUSED = [(32, 32, 32), (48, 48, 24), (96, 16, 36), (16, 32, 12), (64, 16, 8)]
 
 
 def _box_ic(dims, seed, dtype):
@@ -43,21 +47,65 @@ def _ensemble(axs, dims, dtype):
     return e
 
 
+def _fused_id(e):
+    ids = [cid for cid, name in e.tile_configs() if "fused" in name]
+    assert len(ids) == 1
+    return ids[0]
+
+
+@pytest.mark.parametrize("dims,steps", [(DIMS, 4), (DIMS_FUSED, 4), (DIMS_FUSED, 3)], ids=["odd", "fused", "fused-odd"])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
-def test_ensemble_matches_levels_bitwise_every_tiling(axs, dtype):
+def test_ensemble_matches_levels_bitwise_every_tiling(axs, dtype, dims, steps):
+    from axion_strings_adaptive_gb300 import _lib as L
     bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
-    steps = 4
-    ref = [lv.get_state() for lv in _levels(axs, DIMS, dtype, bg, steps)]
-    e = _ensemble(axs, DIMS, dtype)
+    ref = [lv.get_state() for lv in _levels(axs, dims, dtype, bg, steps)]
+    e = _ensemble(axs, dims, dtype)
     init = e.state.clone()
-    for cid, name in e.tile_configs():
+    ran = []
+    for cid, name in [(0, "default")] + e.tile_configs():
         for zc in (0, 3, 7):
             e.state.copy_(init)
-            e.init(cid, zc)
+            try:
+                e.init(cid, zc)
+            except L.AxsError as err:
+                # only the fused tiling refuses boxes, and only boxes it cannot take
+                assert err.status == L.AXS_ERR_UNSUPPORTED and "fused" in name and dims is DIMS, (name, err)
+                break
             e.advance(bg, 1.0, 0.0, 0.1, steps)
             e.device_status()
-            for b in range(len(DIMS)):
+            for b in range(len(dims)):
                 assert torch.equal(e.get_box(b), ref[b]), (name, zc, b)
+            ran.append(name)
+    if dtype == torch.float32 and dims is DIMS_FUSED:
+        assert any("fused" in n for n in ran)
+
+
+@pytest.mark.parametrize("steps", [2, 5])
+def test_fused_ensemble_padding_equals_ghost_fill(axs, steps):
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    e = _ensemble(axs, DIMS_FUSED, torch.float32)
+    e.init(_fused_id(e), 0)
+    e.advance(bg, 1.0, 0.0, 0.1, steps)
+    e.device_status()
+    after = e.state.clone()
+    e.fill_ghosts()
+    assert torch.equal(e.state, after)
+
+
+@pytest.mark.parametrize("steps", [8, 7])
+def test_fused_graph_replay_equals_eager(axs, steps):
+    bg = axs.Background.expanding(2.0, 1.0, lambda0=2.0)
+    e = _ensemble(axs, DIMS_FUSED, torch.float32)
+    e.init(_fused_id(e), 0)
+    init = e.state.clone()
+    e.advance(bg, 1.0, 0.0, 0.1, steps)
+    eager_state = e.state.clone()
+    e.state.copy_(init)
+    g = e.capture(bg, 1.0, 0.0, 0.1, steps, diagnostics=False)
+    g.replay()
+    torch.cuda.synchronize()
+    e.device_status()
+    assert torch.equal(e.state, eager_state)
 
 
 def test_ensemble_diagnostics_match_levels(axs):
