@@ -202,18 +202,17 @@ def cpu_table():
 def dropin_report(A, ic, dev, n=512, steps=4, warmup=1):
     """The one-for-one replacement of specific_eval_rhs under a host RK driver
     (AxionStringsLevel.cpp:909-920, GRTeclyn's classic RK4): per step four
-    ghost fills + axs_eval_rhs on AMReX-layout FABs (ng = 2), three
-    axs_lincomb stage combinations and one axs_rk4_combine, in FP32 and FP64
-    on the headline box. Algorithmic words per site and step: eval_rhs 8
-    (4 read, 4 written) x 4, lincomb 12 x 3, rk4_combine 24: 92 (ghost fills
-    excluded)."""
+    ghost fills + axs_eval_rhs on AMReX-layout FABs, three axs_lincomb stage
+    combinations and one axs_rk4_combine, in FP32 and FP64 on the headline
+    box: ng = 2 (FP32 rows staged in 16-byte pieces) and, in FP32, ng = 3 (cell
+    by cell). Algorithmic words per site and step: eval_rhs 8 (4 read, 4
+    written) x 4, lincomb 12 x 3, rk4_combine 24: 92 (ghost fills excluded)."""
     import torch
     bg = A.Background.expanding(A_INV, C0, lambda0=LAMBDA0)
     out = {"words_per_site_step": 92, "kernels_per_step": ["fill_periodic x4", "eval_rhs x4", "lincomb x3",
                                                            "rk4_combine"]}
     s0 = ic.fourier_state(n, ic.strict_cutoff(n / 8), seed=SEED, dtype=torch.float64, device=dev)
-    for name, dt_ in (("f32", torch.float32), ("f64", torch.float64)):
-        ng = 2
+    for name, dt_, ng in (("f32", torch.float32, 2), ("f32_ng3", torch.float32, 3), ("f64", torch.float64, 2)):
         u = A.new_fab((n, n, n), ng, dtype=dt_, device=dev)
         A.valid(u, ng).copy_(s0)
         uold, us = torch.empty_like(u), torch.empty_like(u)
