@@ -124,15 +124,26 @@ struct FusedItem {
     const CUtensorMap *full, *mid, *rows2;
 };
 
-// Work-item sources of the fused step.
-// One periodic level: geometry from the launch parameters, nx a multiple of TX.
+// A block's walk over its work items (the producer thread and the consumers
+// each keep one).
+struct FusedCursor {
+    int64_t pos, end;
+};
+
+// Work-item sources of the fused step: begin / valid / item / next.
+// One periodic level in (tile, z-chunk) items, taken by blocks in turn;
+// geometry from the launch parameters, nx a multiple of TX.
 struct FusedLevel {
     static constexpr bool kPartialX = false;
+    __device__ __forceinline__ static FusedCursor begin(const SweepArgs<float> &a) { return {blockIdx.x, a.n_items}; }
+    __device__ __forceinline__ static bool valid(const FusedCursor &c) { return c.pos < c.end; }
+    __device__ __forceinline__ static void next(FusedCursor &c, int) { c.pos += gridDim.x; }
     template <int TX, int TY>
-    __device__ __forceinline__ static FusedItem item(const SweepArgs<float> &a, const LevelFusedMaps &m, int64_t it)
+    __device__ __forceinline__ static FusedItem item(const SweepArgs<float> &a, const LevelFusedMaps &m,
+                                                     const FusedCursor &c)
     {
-        const int tile = (int)(it % a.ntiles);
-        const int z0 = (int)(it / a.ntiles) * a.zchunk;
+        const int tile = (int)(c.pos % a.ntiles);
+        const int z0 = (int)(c.pos / a.ntiles) * a.zchunk;
         return FusedItem{(tile % a.tiles_x) * TX, (tile / a.tiles_x) * TY, z0, min(a.zchunk, a.nz - z0), a.nx, a.ny,
                          a.nz, a.js, a.ks, 0, &m.full, &m.mid, &m.rows2};
     }
@@ -146,10 +157,14 @@ struct FusedLevel {
 // right read zero-filled or unused columns and feed only masked sites.
 struct FusedBoxes {
     static constexpr bool kPartialX = true;
+    __device__ __forceinline__ static FusedCursor begin(const SweepArgs<float> &a) { return {blockIdx.x, a.n_items}; }
+    __device__ __forceinline__ static bool valid(const FusedCursor &c) { return c.pos < c.end; }
+    __device__ __forceinline__ static void next(FusedCursor &c, int) { c.pos += gridDim.x; }
     template <int TX, int TY>
-    __device__ __forceinline__ static FusedItem item(const SweepArgs<float> &a, const LevelFusedMaps &, int64_t it)
+    __device__ __forceinline__ static FusedItem item(const SweepArgs<float> &a, const LevelFusedMaps &,
+                                                     const FusedCursor &c)
     {
-        const uint32_t e = __ldg(a.items + it);
+        const uint32_t e = __ldg(a.items + c.pos);
         const EnsBoxDesc &d = a.boxes[e >> kEnsItemBits];
         const int local = (int)(e & ((1u << kEnsItemBits) - 1));
         const int tile = local % d.ntiles;
@@ -186,19 +201,19 @@ __global__ void __launch_bounds__(S::THREADS, 1)
     __syncthreads();
 
     // ---- producer cursor (thread 0 only): planes z0 - 4 .. z0 + len + 3 of each item
-    int64_t p_item = blockIdx.x;
+    FusedCursor p_cur = Src::begin(a);
     int p_k = 0;
     FusedItem p{};
     bool p_edge = false;
     auto p_start = [&]() {
-        if (p_item >= a.n_items) return;
-        p = Src::template item<TX, TY>(a, maps, p_item);
+        if (!Src::valid(p_cur)) return;
+        p = Src::template item<TX, TY>(a, maps, p_cur);
         p_edge = p.y0 == 0 || p.y0 + TY == p.ny;  // rows y0 - 4, y0 - 3 or y0 + TY + 2, + 3 lie past the padding
     };
     int64_t q_issued = 0;
     int p_slot = 0;  // ring slot of plane q_issued
     auto issue_one = [&]() -> bool {
-        if (p_item >= a.n_items) return false;
+        if (!Src::valid(p_cur)) return false;
         int zp = (p.z0 - 4 + p_k) % p.nz;
         if (zp < 0) zp += p.nz;
         const int slot = p_slot;
@@ -222,7 +237,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
         ++q_issued;
         if (++p_k == p.len + 8) {
             p_k = 0;
-            p_item += gridDim.x;
+            Src::next(p_cur, p.len);
             p_start();
         }
         return true;
@@ -268,8 +283,8 @@ __global__ void __launch_bounds__(S::THREADS, 1)
     int s0 = 0, e0 = 0;           // d3, d4 slot and E, Q slot of sweep A's plane
     int64_t q_waited = 0;
     bool aborted = false;
-    for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-        const FusedItem w = Src::template item<TX, TY>(a, maps, item);
+    for (FusedCursor cur = Src::begin(a); Src::valid(cur);) {
+        const FusedItem w = Src::template item<TX, TY>(a, maps, cur);
         const int z0 = w.z0, len = w.len;
         // this thread's sweep B sites: element offset of their row at z = 0, and
         // whether they lie in the box
@@ -375,6 +390,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
         // the next item's window starts 4 planes past this item's last window start + 1
         r0 += 4;
         if (r0 >= NS) r0 -= NS;
+        Src::next(cur, len);
     }
     // A wait expired: make sure no bulk copy is still landing in shared memory
     // before the block exits (bounded as well).
