@@ -326,8 +326,8 @@ template <int TX, int TY, int NS, int THREADS> struct EnsFusedConfig {
             max_nz = std::max(max_nz, nz);
             max_row = std::max(max_row, 16 * (ny + 4) + 4 * nx);
         }
-        const dim3 pad_grid((unsigned)std::min(64, (max_row + 255) / 256), (unsigned)std::min(4 * max_nz, 65535),
-                            (unsigned)e->nboxes);
+        const dim3 pad_grid((unsigned)std::min(64, (max_row + 256 * kPadUnroll - 1) / (256 * kPadUnroll)),
+                            (unsigned)std::min(4 * max_nz, 65535), (unsigned)e->nboxes);
         int first = 0;
         if (r.nsteps & 1) {
             AXS_CUDA_CHECK(cudaMemcpyAsync(buf[1], buf[0], (size_t)(4 * P) * sizeof(float), cudaMemcpyDeviceToDevice,

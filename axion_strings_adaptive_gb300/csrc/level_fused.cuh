@@ -403,27 +403,45 @@ __global__ void __launch_bounds__(S::THREADS, 1)
 // x = -8 .. -1 and nx .. nx+7 of rows y = -2 .. ny+1, and rows y = -2, -1, ny,
 // ny+1 of columns 0 .. nx-1, each a copy of the valid cell it wraps to. Grid
 // rows are planes (z + nz c); within a plane, consecutive threads take
-// consecutive elements of a padding row.
+// consecutive elements of a padding row, and each thread copies kPadUnroll
+// elements a grid-row stride apart, all loads before the stores (sources are
+// valid cells, destinations padding: no copy reads another's destination).
+constexpr int kPadUnroll = 4;
 template <typename T>
 __device__ __forceinline__ void pad_box(T *__restrict__ buf, int nx, int ny, int nz, int64_t js, int64_t ks, int64_t cs,
                                         int ox, int oy)
 {
     const int xpad = 16 * (ny + 4), per_plane = xpad + 4 * nx;
+    const int stride = gridDim.x * blockDim.x;
     for (int plane = blockIdx.y; plane < 4 * nz; plane += gridDim.y) {
         T *p = buf + (int64_t)(plane / nz) * cs + (int64_t)(plane % nz) * ks + ox + (int64_t)oy * js;
-        for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < per_plane; r += gridDim.x * blockDim.x) {
-            int x, y;
-            if (r < xpad) {  // x padding: 16 columns of every padded row
-                const int k = r & 15;
-                x = k < 8 ? k - 8 : nx + (k - 8);
-                y = (r >> 4) - 2;
-            } else {  // y padding: 4 rows of the valid columns
-                const int rr = r - xpad, k = rr / nx;
-                x = rr - k * nx;
-                y = k < 2 ? k - 2 : ny + (k - 2);
+        for (int r0 = blockIdx.x * blockDim.x + threadIdx.x; r0 < per_plane; r0 += kPadUnroll * stride) {
+            int64_t dst[kPadUnroll], src[kPadUnroll];
+            bool on[kPadUnroll];
+#pragma unroll
+            for (int u = 0; u < kPadUnroll; ++u) {
+                const int r = r0 + u * stride;
+                int x, y;
+                if (r < xpad) {  // x padding: 16 columns of every padded row
+                    const int k = r & 15;
+                    x = k < 8 ? k - 8 : nx + (k - 8);
+                    y = (r >> 4) - 2;
+                } else {  // y padding: 4 rows of the valid columns
+                    const int rr = r - xpad, k = rr / nx;
+                    x = rr - k * nx;
+                    y = k < 2 ? k - 2 : ny + (k - 2);
+                }
+                const int xs = x < 0 ? x + nx : (x >= nx ? x - nx : x), ys = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+                on[u] = r < per_plane;
+                dst[u] = x + (int64_t)y * js;
+                src[u] = on[u] ? xs + (int64_t)ys * js : 0;
             }
-            const int xs = x < 0 ? x + nx : (x >= nx ? x - nx : x), ys = y < 0 ? y + ny : (y >= ny ? y - ny : y);
-            p[x + (int64_t)y * js] = p[xs + (int64_t)ys * js];
+            T v[kPadUnroll];
+#pragma unroll
+            for (int u = 0; u < kPadUnroll; ++u) v[u] = p[src[u]];
+#pragma unroll
+            for (int u = 0; u < kPadUnroll; ++u)
+                if (on[u]) p[dst[u]] = v[u];
         }
     }
 }

@@ -230,7 +230,8 @@ template <int TX, int TY, int NS, int THREADS = 512, bool COMP = false> struct F
         plan_chunks(a.ntiles, lv->nz, sms, a.zchunk, a.n_items, grid);
         fill_level_constants(a, lv, g, r.dt);
         const int pad_per_plane = 16 * (lv->ny + 4) + 4 * lv->nx;
-        const dim3 pad_grid((unsigned)std::min(64, (pad_per_plane + 255) / 256), (unsigned)std::min(4 * lv->nz, 65535));
+        const dim3 pad_grid((unsigned)std::min(64, (pad_per_plane + 256 * kPadUnroll - 1) / (256 * kPadUnroll)),
+                            (unsigned)std::min(4 * lv->nz, 65535));
         float *buf[2] = {static_cast<float *>(lv->state),
                          static_cast<float *>(r.out_state != nullptr ? r.out_state : lv->work)};
         LevelFusedMaps maps[2];
