@@ -368,14 +368,12 @@ static bool fused_fits(const int32_t *dims, int nboxes, int ty)
 }
 
 // The default (tile_config 0) is the first entry of its table that suits
-// every box: the fastest two-sweep tiling on a mixed 32^3..128^3 ensemble on
-// GB300. The 16-wide tiles leave no idle columns on boxes whose width is a
-// multiple of 16 but read 96-byte rows. On that ensemble the fused step is
-// slower than the two sweeps (1.04 against 1.00 ms per step): a third of its
-// tiles touch a box's y edge and load each plane as 12 pieces, and small
-// boxes have more padding per site; the autotuner keeps it for boxes where it
-// wins.
+// every box: the fused step (0.91 ms per step on a mixed 32^3..128^3
+// ensemble on GB300), else the fastest two-sweep tiling there (1.01 ms). The
+// 16-wide tiles leave no idle columns on boxes whose width is a multiple of
+// 16 but read 96-byte rows.
 static const EnsTiling kEnsF32[] = {
+    EnsFusedConfig<32, 16, 6, 640>::entry("f32 fused 32x16 ring6 t640"),
     EnsConfig<float, 2, 64, 8, 8, 2>::entry("f32 v2 64x8 ring8"),
     EnsConfig<float, 2, 32, 8, 8, 3>::entry("f32 v2 32x8 ring8"),
     EnsConfig<float, 1, 32, 8, 8, 3>::entry("f32 v1 32x8 ring8"),
@@ -384,7 +382,6 @@ static const EnsTiling kEnsF32[] = {
     EnsConfig<float, 1, 16, 8, 8, 4>::entry("f32 v1 16x8 ring8"),
     EnsConfig<float, 2, 64, 8, 8, 2, true>::entry("f32 v2 64x8 ring8 l2"),
     EnsConfig<float, 2, 32, 8, 8, 3, true>::entry("f32 v2 32x8 ring8 l2"),
-    EnsFusedConfig<32, 16, 6, 640>::entry("f32 fused 32x16 ring6 t640"),
 };
 static const EnsTiling kEnsF64[] = {
     EnsConfig<double, 1, 32, 8, 6, 2>::entry("f64 v1 32x8 ring6"),
@@ -425,8 +422,10 @@ static const EnsTiling *ens_config_for(const axs_ensemble *e, int32_t id)
 static int box_zchunk(int nz, int target) { return (nz + (nz + target - 1) / target - 1) / ((nz + target - 1) / target); }
 
 // Automatic target: the candidate whose item list best fills the persistent
-// grid (last-wave fill x warm-up overhead of 4 planes per chunk).
-static int auto_ztarget(const int32_t *dims, int nboxes, int tx, int ty, int cap)
+// grid (last-wave fill x warm-up overhead of `warm` planes per chunk: 4 for the
+// two sweeps; 8 for the fused step, whose chunks restart with 4 planes of
+// sweep A alone and 8 extra plane loads).
+static int auto_ztarget(const int32_t *dims, int nboxes, int tx, int ty, int cap, double warm)
 {
     static const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256};
     double best = -1.0;
@@ -440,9 +439,9 @@ static int auto_ztarget(const int32_t *dims, int nboxes, int tx, int ty, int cap
             const int zc = box_zchunk(nz, std::min(zt, nz));
             const int nch = (nz + zc - 1) / zc;
             items += ntiles * nch;
-            work += (double)ntiles * (nz + 4.0 * nch);
+            work += (double)ntiles * (nz + warm * nch);
             useful += (double)ntiles * nz;
-            longest = std::max(longest, (double)zc + 4.0);
+            longest = std::max(longest, (double)zc + warm);
         }
         const int64_t g = std::min<int64_t>(items, cap);
         // greedy bound on the makespan: average load per block plus one longest item
@@ -514,7 +513,9 @@ int axs_ensemble_init(const axs_ensemble *e, axs_ensemble_plan *plan, void *stre
     int cap_a = 0, cap_b = 0;
     if ((rc = cfg->caps(cap_a, cap_b))) return rc;
     const int nb = e->nboxes;
-    const int zt = plan->z_chunk > 0 ? plan->z_chunk : auto_ztarget(e->dims, nb, cfg->tx, cfg->ty, std::min(cap_a, cap_b));
+    const int zt = plan->z_chunk > 0 ? plan->z_chunk
+                                     : auto_ztarget(e->dims, nb, cfg->tx, cfg->ty, std::min(cap_a, cap_b),
+                                                    cfg->fused ? 8.0 : 4.0);
 
     // box descriptors
     std::vector<EnsBoxDesc> desc(nb);

@@ -186,14 +186,12 @@ __global__ void __launch_bounds__(S::THREADS, 1)
     T *swin = ring + (size_t)NS * S::RING;
     T *eqw = swin + (size_t)S::NSW * S::SWIN;
     __shared__ uint64_t full[NS];
-    __shared__ int abort_flag;
     const int tid = threadIdx.x;
     constexpr int oy = 2;  // padded row of y = 0 in the level layout
 
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         fence_mbar_init();
-        abort_flag = 0;
         prefetch_tensormap(&maps.full);
         prefetch_tensormap(&maps.mid);
         prefetch_tensormap(&maps.rows2);
@@ -295,10 +293,11 @@ __global__ void __launch_bounds__(S::THREADS, 1)
         for (int i = 0; i < len + 4; ++i) {
             // planes up to q_base + i + 4 must have landed: the first iteration of an
             // item waits for five, every later one for one more
+            bool late = false;  // this thread's wait expired
             for (int need = i == 0 ? 5 : 1; need > 0; --need) {
                 if (!mbar_wait_bounded(&full[w_slot], (uint32_t)w_phase, a.wait_polls)) {
                     atomicOr(a.status, kDevTimeout);
-                    abort_flag = 1;
+                    late = true;
                 }
                 ++q_waited;
                 if (++w_slot == NS) {
@@ -312,7 +311,7 @@ __global__ void __launch_bounds__(S::THREADS, 1)
                 const int sd = r0 + d < NS ? r0 + d : r0 + d - NS;
                 pl[d] = ring_sh + (uint32_t)sd * (uint32_t)(S::RING * 4);
             }
-            if (has_a && !abort_flag) {
+            if (has_a) {
                 uint32_t pa[5];
 #pragma unroll
                 for (int d = 0; d < 5; ++d) pa[d] = pl[d] + a_at;
@@ -335,15 +334,20 @@ __global__ void __launch_bounds__(S::THREADS, 1)
             }
             // sweep B's psi_n, Pi_n at plane zb: ring plane q_base + i, refilled after the barrier
             float2 pn[4];
-            if (has_b && i >= 4 && !abort_flag) {
+            if (has_b && i >= 4) {
                 const uint32_t r0p = pl[0] + b_ro;
                 pn[0] = lds2<0 * BX * BY * 4>(r0p);
                 pn[1] = lds2<1 * BX * BY * 4>(r0p);
                 pn[2] = lds2<2 * BX * BY * 4>(r0p);
                 pn[3] = lds2<3 * BX * BY * 4>(r0p);
             }
-            __syncthreads();  // d3, d4, E, Q of plane za are in place; ring plane q_base + i is read no more
-            if (abort_flag) {
+            // d3, d4, E, Q of plane za are in place; ring plane q_base + i is read no
+            // more. The barrier also ORs the threads' expired waits: a thread whose
+            // wait expired ran its sweeps on a slot that may still be landing, and
+            // the block drops those results here, before any global store (one
+            // block-wide flag in shared memory, read three times a plane, cost
+            // 1.4 % of the step).
+            if (__syncthreads_or(late)) {
                 aborted = true;
                 break;
             }

@@ -328,7 +328,6 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *ring = reinterpret_cast<T *>(smem_raw);
     __shared__ uint64_t full[NS];
-    __shared__ int abort_flag;
     __shared__ double lam_red[(S::NT + 31) / 32];
 
     const int tid = threadIdx.x;
@@ -341,7 +340,6 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
     if (tid == 0) {
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         fence_mbar_init();
-        abort_flag = 0;
         if constexpr (std::is_same<Src, SingleLevel>::value) prefetch_tensormap(&tmap);
     }
     __syncthreads();
@@ -451,11 +449,12 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
             }
 
             const int64_t need = q_base + m + 4;
+            bool late = false;  // this thread's wait expired
             while (q_waited <= need) {
                 const int slot = (int)(q_waited % NS);
                 if (!mbar_wait_bounded(&full[slot], (uint32_t)((q_waited / NS) & 1), a.wait_polls)) {
                     atomicOr(a.status, kDevTimeout);
-                    abort_flag = 1;
+                    late = true;
                 }
                 ++q_waited;
             }
@@ -474,8 +473,9 @@ __global__ void __launch_bounds__(SweepShape<T, V, TX, TY>::NT, MINB)
                 Op::template apply<T, V, HINT>(a, b, lap, ctr, pq, off + a.dox_out, x, y, lam_acc, pol_first);
             }
 
-            __syncthreads();  // everyone is done with the oldest plane of this window
-            if (abort_flag) {
+            // everyone is done with the oldest plane of this window; the barrier
+            // also ORs the threads' expired waits (the block stops after this plane)
+            if (__syncthreads_or(late)) {
                 aborted = true;
                 break;
             }

@@ -2,10 +2,10 @@
 
 :class:`Ensemble` packs its boxes component-major in one state arena and one
 stage-buffer arena (the ``axs_ensemble`` layout of include/axs.h), builds the
-device table for one tiling, and advances every box together: with two
-persistent sweep launches per RK4 step (any box shape; the default) or with
-the one-pass fused step (one persistent launch per step plus one for the
-periodic padding; boxes with ny a multiple of 16 and an even nx).
+device table for one tiling, and advances every box together: with the
+one-pass fused step (one persistent launch per RK4 step plus one for the
+periodic padding; the default for boxes with ny a multiple of 16 and an even
+nx) or with two persistent sweep launches per step (any box shape).
 ``capture(...)`` records a whole run -- the steps plus
 per-box diagnostics -- as one CUDA graph; :meth:`Ensemble.autotune` times the
 compiled tilings and z-chunk targets (the work each block takes from a box) on
@@ -146,11 +146,13 @@ class Ensemble:
                 self.diagnostics_async(bg, tau_i + t0 + nsteps * dt, per_cell_fp32=per_cell_fp32, stream=s)
         return g
 
-    def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 3, repeats: int = 2,
+    def autotune(self, bg: Background, tau_i: float, dt: float, steps: int = 4, repeats: int = 2,
                  z_chunks=(0, 8, 16, 32, 64)) -> dict:
         """Time every compiled tiling x z-chunk target on these boxes and keep the
         fastest (tilings that do not suit every box are left out). The state is
-        saved and restored. Returns {"name zN": ms/step}."""
+        saved and restored. `steps` is rounded up to an even count: the fused
+        step copies the state once on an odd count. Returns {"name zN": ms/step}."""
+        steps += steps & 1
         saved = self.state.clone()
         timings = {}
         best = (float("inf"), self.plan.tile_config, self.plan.z_chunk)

@@ -322,7 +322,7 @@ def batching_report(A, ic, dev, hbm_peak, nboxes=64, nsteps=200, sizes=(32, 48, 
         ens.set_box(b, s0)
         ics.append(s0)
     ens.fill_ghosts()
-    tune = ens.autotune(bg, TAU_I, DT, steps=3, repeats=1)
+    tune = ens.autotune(bg, TAU_I, DT, steps=4, repeats=1)
     init = ens.state.clone()
     sites = ens.n_sites
 
