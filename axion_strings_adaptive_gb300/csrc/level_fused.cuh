@@ -135,6 +135,7 @@ struct FusedCursor {
 // geometry from the launch parameters, nx a multiple of TX.
 struct FusedLevel {
     static constexpr bool kPartialX = false;
+    static constexpr bool kMapsInTable = false;  // maps by value in the launch parameters
     __device__ __forceinline__ static FusedCursor begin(const SweepArgs<float> &a) { return {blockIdx.x, a.n_items}; }
     __device__ __forceinline__ static bool valid(const FusedCursor &c) { return c.pos < c.end; }
     __device__ __forceinline__ static void next(FusedCursor &c, int) { c.pos += gridDim.x; }
@@ -157,6 +158,7 @@ struct FusedLevel {
 // right read zero-filled or unused columns and feed only masked sites.
 struct FusedBoxes {
     static constexpr bool kPartialX = true;
+    static constexpr bool kMapsInTable = true;  // written by a host copy: acquired before use
     __device__ __forceinline__ static FusedCursor begin(const SweepArgs<float> &a) { return {blockIdx.x, a.n_items}; }
     __device__ __forceinline__ static bool valid(const FusedCursor &c) { return c.pos < c.end; }
     __device__ __forceinline__ static void next(FusedCursor &c, int) { c.pos += gridDim.x; }
@@ -207,6 +209,11 @@ __global__ void __launch_bounds__(S::THREADS, 1)
         if (!Src::valid(p_cur)) return;
         p = Src::template item<TX, TY>(a, maps, p_cur);
         p_edge = p.y0 == 0 || p.y0 + TY == p.ny;  // rows y0 - 4, y0 - 3 or y0 + TY + 2, + 3 lie past the padding
+        if constexpr (Src::kMapsInTable) {
+            fence_tensormap_acquire(p.full);
+            fence_tensormap_acquire(p.mid);
+            fence_tensormap_acquire(p.rows2);
+        }
     };
     int64_t q_issued = 0;
     int p_slot = 0;  // ring slot of plane q_issued
