@@ -18,6 +18,10 @@
  *     written to caller-provided DEVICE memory.
  *   - Arguments are validated on the host before anything is launched; a
  *     failed validation launches nothing.
+ *   - One CUDA device per process: kernels' shared-memory limits and
+ *     occupancy figures are set up on the first call that launches them and
+ *     assumed for every later call. Make that first call outside stream
+ *     capture.
  *
  * Each declaration names the reference interface it replaces (paths relative
  * to the reference project root).
