@@ -120,6 +120,33 @@ class CompositeDiagnostics:
     refined_fraction: float
 
 
+def in_place_slots(old_q: np.ndarray, n_new: int):
+    """The slot plan of a regrid inside the same arena.
+
+    old_q[i] is the patch slot that block i of the new set held before (-1: the
+    block is newly refined). Kept patches whose slot lies below n_new stay
+    there; kept patches at or above n_new move into the free slots below it, in
+    order; new patches take the slots left. Returns (slot of each block,
+    src_of_dst per slot for axs_patches_copy_boxes: PATCH_KEEP where the patch
+    stays, the old slot it is copied from, or -1 for a new patch, and the slots
+    of the new patches)."""
+    old_q = np.asarray(old_q, dtype=np.int64)
+    slot = np.full(n_new, -1, dtype=np.int64)
+    stay = (old_q >= 0) & (old_q < n_new)
+    slot[stay] = old_q[stay]
+    used = np.zeros(n_new, dtype=bool)
+    used[old_q[stay]] = True
+    holes = np.nonzero(~used)[0]
+    movers = np.nonzero(old_q >= n_new)[0]
+    fresh = np.nonzero(old_q < 0)[0]
+    slot[movers] = holes[:len(movers)]
+    slot[fresh] = holes[len(movers):]
+    src_of_dst = np.full(n_new, L.PATCH_KEEP, dtype=np.int32)
+    src_of_dst[slot[movers]] = old_q[movers]
+    src_of_dst[slot[fresh]] = -1
+    return slot, src_of_dst, slot[fresh].astype(np.int32)
+
+
 class TwoLevel:
     """A periodic coarse level plus 2x-refined patches on tagged block^3 blocks."""
 
@@ -182,22 +209,9 @@ class TwoLevel:
             old_q = np.full(n_new, -1, dtype=np.int64)
         in_place = old_patches is not None and n_new <= old_patches.capacity
         if in_place:
-            slot = np.full(n_new, -1, dtype=np.int64)
-            stay = (old_q >= 0) & (old_q < n_new)
-            slot[stay] = old_q[stay]
-            used = np.zeros(n_new, dtype=bool)
-            used[old_q[stay]] = True
-            holes = np.nonzero(~used)[0]
-            movers = np.nonzero(old_q >= n_new)[0]
-            fresh = np.nonzero(old_q < 0)[0]
-            slot[movers] = holes[:len(movers)]
-            slot[fresh] = holes[len(movers):]
-            src_of_dst = np.full(n_new, L.PATCH_KEEP, dtype=np.int32)
-            src_of_dst[slot[movers]] = old_q[movers]
-            src_of_dst[slot[fresh]] = -1
+            slot, src_of_dst, new_slots = in_place_slots(old_q, n_new)
             order = np.argsort(slot)  # patch q holds block order[q]
             blocks = blocks[order]
-            new_slots = slot[fresh].astype(np.int32)
             storage, cap = old_patches.storage, old_patches.capacity
         else:
             src_of_dst = old_q.astype(np.int32)  # -1: newly refined (cleared, then interpolated)
