@@ -549,8 +549,14 @@ int axs_level_tag_cells(const axs_level *lv, const axs_tag_params *p, uint8_t *t
  * y_offset, jstride, kstride as axs_level_layout_for reports). The state arena
  * holds 4 planes, the work arena 8; both and the table are caller-owned device
  * memory, 128-byte aligned. axs_ensemble_init writes the device table (box
- * descriptors, work items, two TMA descriptors per box) for one tiling; every
- * RK4 sweep is then ONE persistent launch over the work items of all boxes.
+ * descriptors, work items, six TMA descriptor slots per box) for one tiling.
+ * A two-sweep tiling runs every RK4 sweep as ONE persistent launch over the
+ * work items of all boxes. The fused tiling runs every RK4 step as one launch
+ * (plus one for the boxes' periodic padding), with the work arena's first 4
+ * planes as the second state buffer; it takes boxes whose ny is a multiple of
+ * 16 and whose nx is even. tile_config 0 is the first tiling (by id) that
+ * suits every box: the fused one where it fits. After every advance the result
+ * and its padding are in the state arena.
  * ------------------------------------------------------------------------- */
 typedef struct axs_ensemble {
     int32_t dtype;
@@ -570,7 +576,7 @@ typedef struct axs_ensemble_box {
 } axs_ensemble_box;
 
 typedef struct axs_ensemble_plan {
-    int32_t tile_config; /* in: index from axs_ensemble_tile_config_name, 0 = default */
+    int32_t tile_config; /* in: index from axs_ensemble_tile_config_name (1..count), 0 = the first that suits */
     int32_t z_chunk;     /* in: target z planes per work item, 0 = automatic */
     int64_t n_items;     /* out: work items of one sweep (all boxes) */
     int32_t grid_a;      /* out: persistent grid of sweep A */
